@@ -1,0 +1,204 @@
+/*
+ * asteriy_gb300.h - C ABI of the GB300-native explicit r-z finite-volume step.
+ *
+ * The reference (Asteriy_2d) has no library interface: its operator is the
+ * step kernel
+ *     Kernel_TVD(double2* s, double2* u, double2* s2, double2* u2,
+ *                double* T, double* T_do, double* TT, int method)
+ * (kernel.cu:2513), the first-order variants add2 (kernel.cu:1928) and
+ * add_MK (kernel.cu:2293), and the scalar kernel funk_time (kernel.cu:1525)
+ * that shifts the lagged time step.  Grid, gamma, CFL and boundary rules are
+ * compile-time macros (Header.h:6-47) and hard-coded branches.  This header
+ * turns all of that into a runtime configuration and a small set of entry
+ * points with status-code returns.
+ *
+ * Conventions kept from the reference:
+ *   - state layout at the boundary: two arrays of K = N*M pairs,
+ *     s[k] = (rho, p) and u[k] = (v_z, v_r), k = m*N + n, n along z (the
+ *     reference's x), m along r (the reference's y)  (kernel.cu:2515-2517);
+ *   - cell centres z = x_min + n*dx with dx = (x_max - x_min)/(N-1) and
+ *     r = y_min + m*dy with dy = y_max/M, y_min = dy/2   (Header.h:11-16);
+ *   - lagged time step: a step uses T_do, the step size computed during the
+ *     previous step; the first step uses dt_first (1e-9, kernel.cu:3322);
+ *     after each step T_do <- new dt, TT += T_do, step += 1
+ *     (funk_time, kernel.cu:1525-1536).
+ *
+ * All functions return AST_OK (0) or a negative AST_ERR_* code.
+ * Pointers are host pointers unless a parameter says otherwise.
+ */
+#ifndef ASTERIY_GB300_H
+#define ASTERIY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AST_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define AST_OK               0
+#define AST_ERR_INVALID     -1  /* bad argument or configuration           */
+#define AST_ERR_CUDA        -2  /* a CUDA runtime call failed               */
+#define AST_ERR_NOMEM       -3  /* device or host allocation failed         */
+#define AST_ERR_IO          -4  /* file could not be read or written        */
+#define AST_ERR_UNSUPPORTED -5  /* valid request this build does not serve  */
+#define AST_ERR_NUMERIC     -6  /* non-finite values appeared in the state  */
+
+/* ---- device status bits (ast_stats.status) ----------------------------- */
+#define AST_ST_RHO_FLOOR    0x01u /* rho' <= 0: old density kept (kernel.cu:3060-3064) */
+#define AST_ST_P_FLOOR      0x02u /* p' <= 0: set to p_floor (kernel.cu:3070-3073)     */
+#define AST_ST_NEWTON_CAP   0x04u /* two-shock Newton hit riemann_max_iter             */
+#define AST_ST_BISECT_CAP   0x08u /* shock-rarefaction bisection hit its cap           */
+#define AST_ST_NONFINITE    0x10u /* a wave speed or state became NaN/Inf              */
+#define AST_ST_VACUUM       0x20u /* exact solver met the vacuum pattern               */
+#define AST_ST_MLP_FALLBACK 0x40u /* learned guess rejected, PVRS guess used           */
+
+/* ---- enumerations ------------------------------------------------------ */
+enum ast_flux   { AST_FLUX_HLL = 0, AST_FLUX_HLLC = 1, AST_FLUX_GODUNOV = 2 };
+enum ast_recon  { AST_RECON_NONE = 0, AST_RECON_MINMOD = 1 };
+enum ast_geom   { AST_GEOM_PLANAR = 0, AST_GEOM_AXISYM = 1 };
+enum ast_prec   { AST_PREC_FP64 = 0, AST_PREC_FP32 = 1 };
+enum ast_guess  { AST_GUESS_PVRS = 0, AST_GUESS_MLP = 1 };
+enum ast_side   { AST_Z_LO = 0, AST_Z_HI = 1, AST_R_LO = 2, AST_R_HI = 3 };
+/*
+ * Boundary kinds.  Each side has two ghost layers, j = 0 next to the
+ * boundary cell b0, j = 1 beyond it (the reference's first and second
+ * neighbours, kernel.cu:2549-2619 and 2638-2698):
+ *   REFLECT  ghost j = mirror of interior cell j, normal velocity negated
+ *            (axis and wall rules, kernel.cu:2564-2569, 2609-2614, 2661-2698);
+ *   OUTFLOW  ghost j = b0 (zero gradient, kernel.cu:2549-2553, 2639-2643);
+ *   FIXED    ghost j = the side's (rho, p, vz, vr) (kernel.cu:2577-2580);
+ *   SUCTION  ghost j = b0 with the normal velocity limited: on a low side
+ *            v_n = min(v_n, limit), on a high side v_n = max(v_n, limit),
+ *            limit = the side's vz (z sides) or vr (r sides)
+ *            (add_MK, kernel.cu:2340-2354).
+ */
+enum ast_bc_kind { AST_BC_REFLECT = 0, AST_BC_OUTFLOW = 1, AST_BC_FIXED = 2, AST_BC_SUCTION = 3 };
+
+typedef struct ast_bc {
+    int32_t kind;
+    int32_t pad_;
+    double rho, p, vz, vr;
+} ast_bc;
+
+/*
+ * Runtime configuration.  Defaults from ast_config_default() reproduce the
+ * reference macros (Header.h) where they exist.
+ */
+typedef struct ast_config {
+    int32_t N, M;                 /* cells along z and r (Header.h:8-10)             */
+    double  x_min, x_max, y_max;  /* domain (Header.h:11-13)                          */
+    double  gamma;                /* ratio of specific heats, ggg (Header.h:17)       */
+    double  cfl;                  /* krit (Header.h:47)                               */
+    int32_t flux;                 /* enum ast_flux                                    */
+    int32_t recon;                /* enum ast_recon                                   */
+    int32_t geom;                 /* enum ast_geom                                    */
+    int32_t precision;            /* enum ast_prec                                    */
+    int32_t grad_p;               /* 1: reconstruct p too (grad_p, Header.h:31)       */
+    int32_t guess;                /* enum ast_guess (exact solver's p* start)         */
+    ast_bc  bc[4];                /* indexed by enum ast_side                         */
+    /* cells with (z-fixed_zc)^2/fixed_az^2 + r^2/fixed_ar^2 < 1 keep their state
+       (add_MK, kernel.cu:2317-2324); 0 disables                                     */
+    int32_t fixed_region;
+    int32_t region_select;        /* 1: high-order flux only on faces whose z
+                                     position lies in (region_lo, region_hi), first-
+                                     order HLL elsewhere (kernel.cu:2799-2857)        */
+    double  fixed_zc, fixed_az, fixed_ar;
+    double  region_lo, region_hi;
+    /* body force Q2 = -amp*rho (r >= body_rsplit) / +amp*rho (r < body_rsplit)
+       in v_r for body_lo < z < body_hi (kernel.cu:3039-3056); 0 disables           */
+    int32_t body_force;
+    int32_t riemann_max_iter;     /* cap for Newton / bisection (reference: none)     */
+    double  body_lo, body_hi, body_rsplit, body_amp;
+    double  dt_first;             /* T_do of the first step (kernel.cu:3322): 1e-9    */
+    double  dt_cap;               /* per-cell tmin start (kernel.cu:2530): 1000       */
+    double  p_floor;              /* pressure floor (kernel.cu:3072): 1e-6            */
+    double  riemann_tol;          /* Newton/bisection tolerance, eps (Header.h:62)    */
+    int32_t collect_stats;        /* 1: count Riemann iterations in ast_stats         */
+    int32_t reserved_i[7];
+    double  reserved_d[8];
+} ast_config;
+
+typedef struct ast_stats {
+    uint32_t status;              /* OR of AST_ST_* bits since the last reset         */
+    uint32_t newton_max_iters;    /* largest iteration count of one Newton solve      */
+    uint64_t rho_floor;           /* cells that hit the density floor                 */
+    uint64_t p_floor;             /* cells that hit the pressure floor                */
+    uint64_t newton_calls, newton_iters;
+    uint64_t bisect_calls, bisect_iters;
+    uint64_t mlp_fallback;        /* learned guesses replaced by the PVRS guess       */
+    uint64_t reserved[4];
+} ast_stats;
+
+typedef struct ast_solver ast_solver;
+
+/* ---- library ----------------------------------------------------------- */
+int         ast_abi_version(void);
+const char* ast_strerror(int code);
+/* Fills *cfg with the reference's macro values: gamma 5/3, CFL 0.05,
+   HLL + minmod, planar, FP64, reflect on r sides, outflow on z sides,
+   dt_first 1e-9, dt_cap 1000, p_floor 1e-6, riemann_tol 1e-9. */
+void        ast_config_default(ast_config* cfg);
+int         ast_config_check(const ast_config* cfg);
+
+/* ---- solver object (replaces main's allocation + time loop,
+        kernel.cu:3283-3298 and 3868-3947) ------------------------------- */
+int ast_create(const ast_config* cfg, ast_solver** out);
+int ast_destroy(ast_solver* solver);
+/* Runs on the given cudaStream_t (NULL = the legacy default stream). */
+int ast_set_stream(ast_solver* solver, void* cuda_stream);
+/* s, u: K (rho,p) and K (v_z,v_r) pairs; on_device=1 means device pointers. */
+int ast_set_state(ast_solver* solver, const double* s, const double* u, int on_device);
+int ast_get_state(ast_solver* solver, double* s, double* u, int on_device);
+int ast_set_clock(ast_solver* solver, double T_do, double TT, int64_t step);
+int ast_get_clock(ast_solver* solver, double* T_do, double* TT, int64_t* step);
+/* Enqueues nsteps steps (ping-pong, lagged dt) on the solver's stream and
+   returns without waiting; ast_synchronize waits and reports errors. */
+int ast_step(ast_solver* solver, int nsteps);
+int ast_synchronize(ast_solver* solver);
+int ast_get_stats(ast_solver* solver, ast_stats* out, int reset);
+
+/* ---- kernel-level drop-in ----------------------------------------------
+ * One step on reference-layout device arrays, the replacement for
+ *   Kernel_TVD<<<K/256,256>>>(s, u, s2, u2, T, T_do, TT, method)
+ * (kernel.cu:2513, launched at kernel.cu:3874).  Reads s, u and *T_do,
+ * writes s2, u2 and lowers *T to min(*T, new dt) exactly (the reference's
+ * racy write, kernel.cu:3013-3017, becomes an atomic min).  method is kept
+ * for signature compatibility and ignored: cfg->flux selects the flux.
+ * All pointers are device pointers; cuda_stream may be NULL.
+ */
+int ast_step_raw(const double* s, const double* u, double* s2, double* u2,
+                 double* T, const double* T_do, const double* TT, int method,
+                 const ast_config* cfg, void* cuda_stream);
+/* Replacement for funk_time<<<1,1>>>(T, T_do, TT, i) (kernel.cu:1525-1536):
+   T_do = T; TT += T_do; T = 1e7; i += 1.  Device pointers. */
+int ast_funk_time(double* T, double* T_do, double* TT, int* i, void* cuda_stream);
+
+/* ---- problem set-up and files (host) ------------------------------------ */
+/* Axisymmetric blast: rho=1, v=0, p=p_in for z^2+r^2 < radius^2, else p_out. */
+int ast_fill_blast(const ast_config* cfg, double p_in, double p_out, double radius,
+                   double* s, double* u);
+/* Wind-counterflow: counterflow (rho_inf, p_inf, v_inf along z) with uniform
+   density noise in [-noise, noise] (one std::mt19937_64 draw per cell in k
+   order, u = (draw >> 11) * 2^-53, factor 1 + noise*(2u-1)); inside the wind
+   sphere R < r_w: rho = rho_w (r_w/R)^2, radial speed v_w,
+   p = rho_w v_w^2/(gamma mach_w^2) (r_w/R)^(2 gamma). */
+int ast_fill_wind(const ast_config* cfg, double r_w, double rho_w, double v_w, double mach_w,
+                  double rho_inf, double p_inf, double v_inf, double noise, uint64_t seed,
+                  double* s, double* u);
+/* 6 doubles per cell (x, y, rho, p, vx, vy), k order (kernel.cu:4111-4148;
+   read side kernel.cu:3414-3436). */
+int ast_write_bin(const ast_config* cfg, const double* s, const double* u, const char* path);
+int ast_read_bin(const ast_config* cfg, double* s, double* u, const char* path);
+/* Tecplot FEPOINT quadrilateral file, every stride-th cell, variables
+   X Y Ro P Vx Vy Mach omega (print_file_mini, kernel.cu:3109-3173). */
+int ast_write_tecplot(const ast_config* cfg, const double* s, const double* u,
+                      int stride, double soltime, const char* path);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ASTERIY_GB300_H */

@@ -1,0 +1,161 @@
+"""ctypes wrapper of the CPU oracle (oracle/ast_oracle.c) and of the host-
+compiled reference functions (oracle/_ref/libastref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+the cpu_baseline / reference legs of bench.py, never by the package.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "libastoracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libastref.so")
+
+_dp = C.POINTER(C.c_double)
+_i64p = C.POINTER(C.c_int64)
+
+
+def build_oracle(cc="gcc"):
+    """Compile the C restatement (a few seconds)."""
+    cmd = [cc, "-O2", "-std=c99", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+           os.path.join(HERE, "ast_oracle.c"), "-lm", "-o", ORACLE_SO]
+    subprocess.run(cmd, check=True)
+    return ORACLE_SO
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build_oracle()
+        L = C.CDLL(ORACLE_SO)
+        L.ora_minmod.restype = C.c_double
+        L.ora_minmod.argtypes = [C.c_double, C.c_double]
+        L.ora_linear.restype = C.c_double
+        L.ora_linear.argtypes = [C.c_double] * 7
+        L.ora_linear2.restype = None
+        L.ora_linear2.argtypes = [C.c_double] * 8 + [_dp, _dp]
+        L.ora_face.restype = C.c_double
+        L.ora_face.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                               _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_double, _dp, _i64p]
+        L.ora_step.restype = C.c_double
+        L.ora_step.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_int, _i64p]
+        L.ora_run.restype = C.c_int
+        L.ora_run.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _i64p, C.c_int, _i64p]
+        L.ora_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def have_ref():
+    return os.path.exists(REF_SO)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        R = C.CDLL(REF_SO)
+        R.ref_set_params.restype = None
+        R.ref_set_params.argtypes = [C.c_int, C.c_int] + [C.c_double] * 5
+        R.ref_face.restype = C.c_double
+        R.ref_face.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_double, _dp]
+        R.ref_minmod.restype = C.c_double
+        R.ref_minmod.argtypes = [C.c_double, C.c_double]
+        R.ref_linear.restype = C.c_double
+        R.ref_linear.argtypes = [C.c_double] * 7
+        R.ref_linear2.restype = None
+        R.ref_linear2.argtypes = [C.c_double] * 8 + [_dp, _dp]
+        R.ref_kernel_step.restype = C.c_double
+        R.ref_kernel_step.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, C.c_int]
+        R.ref_kernel_run.restype = C.c_int
+        R.ref_kernel_run.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_int, _dp, _dp,
+                                     C.POINTER(C.c_longlong), C.c_int]
+        R.ref_diag_count.restype = C.c_longlong
+        R.ref_max_threads.restype = C.c_int
+        _ref = R
+    return _ref
+
+
+# ---------------------------------------------------------------- oracle
+
+FACE_HLL, FACE_HLLC, FACE_GODUNOV = 0, 1, 2
+
+
+def face(flux, sL, uL, sR, uR, n1, n2, rad, gamma=5.0 / 3.0, cfl=0.05, tol=10e-10, max_iter=200):
+    """One face flux.  Returns (dt, out[4] = mass, mom_z, mom_r, energy, counters[7])."""
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (sL, uL, sR, uR)]
+    out = np.zeros(4)
+    cnt = np.zeros(7, dtype=np.int64)
+    t = lib().ora_face(flux, gamma, cfl, tol, max_iter, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(a[3]),
+                       n1, n2, rad, _ptr(out), cnt.ctypes.data_as(_i64p))
+    return t, out, cnt
+
+
+def step(cfg, s, u, T_do, nthreads=1):
+    """One step; s, u: (K, 2) float64.  Returns (s2, u2, new_dt, counters[10])."""
+    s = np.ascontiguousarray(s, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    s2 = np.empty_like(s)
+    u2 = np.empty_like(u)
+    cnt = np.zeros(10, dtype=np.int64)
+    T = lib().ora_step(C.byref(cfg), _ptr(s), _ptr(u), _ptr(s2), _ptr(u2), T_do, nthreads,
+                       cnt.ctypes.data_as(_i64p))
+    return s2, u2, T, cnt
+
+
+def run(cfg, s, u, nsteps, T_do=None, TT=0.0, step_no=0, nthreads=1):
+    """nsteps steps with the lagged-dt protocol.  Returns (s, u, T_do, TT, step, counters)."""
+    s = np.array(s, dtype=np.float64, order="C")
+    u = np.array(u, dtype=np.float64, order="C")
+    tdo = C.c_double(cfg.dt_first if T_do is None else T_do)
+    tt = C.c_double(TT)
+    st = C.c_int64(step_no)
+    cnt = np.zeros(10, dtype=np.int64)
+    rc = lib().ora_run(C.byref(cfg), _ptr(s), _ptr(u), nsteps, C.byref(tdo), C.byref(tt),
+                       C.byref(st), nthreads, cnt.ctypes.data_as(_i64p))
+    if rc != 0:
+        raise RuntimeError(f"ora_run failed: {rc}")
+    return s, u, tdo.value, tt.value, st.value, cnt
+
+
+def max_threads():
+    return lib().ora_max_threads()
+
+
+# ---------------------------------------------------------------- reference
+
+REF_KERNEL_TVD, REF_ADD_MK, REF_ADD2 = 0, 1, 2
+
+
+def ref_set(cfg):
+    ref().ref_set_params(cfg.N, cfg.M, cfg.x_min, cfg.x_max, cfg.y_max, cfg.gamma, cfg.cfl)
+
+
+def ref_face(which, sL, uL, sR, uR, n1, n2, rad):
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (sL, uL, sR, uR)]
+    out = np.zeros(4)
+    t = ref().ref_face(which, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(a[3]), n1, n2, rad, _ptr(out))
+    return t, out
+
+
+def ref_run(kernel, cfg, s, u, nsteps, method=0, nthreads=1):
+    ref_set(cfg)
+    s = np.array(s, dtype=np.float64, order="C")
+    u = np.array(u, dtype=np.float64, order="C")
+    tdo = C.c_double(cfg.dt_first)
+    tt = C.c_double(0.0)
+    st = C.c_longlong(0)
+    ref().ref_kernel_run(kernel, _ptr(s), _ptr(u), nsteps, method, C.byref(tdo), C.byref(tt),
+                         C.byref(st), nthreads)
+    return s, u, tdo.value, tt.value, st.value

@@ -1,0 +1,98 @@
+"""Generate the golden vectors in tests/golden/ from the reference's own code.
+
+Runs only where the reference sources exist: it builds oracle/_ref/libastref.so
+(oracle/make_ref.py, the reference's functions compiled for the host) and
+records their outputs on seeded inputs:
+
+  faces.npz      HLL, HLLC and exact-Godunov fluxes + dt on 1024 random
+                 states and on hand-picked states that reach every wave
+                 pattern of the exact solver (two shocks, shock-rarefaction,
+                 two rarefactions, vacuum) and the uniform-state case of the
+                 reference's `test` kernel (kernel.cu:3095-3107);
+  step_tvd.npz   20 launches of Kernel_TVD (kernel.cu:2513) + funk_time on a
+                 96x12 grid with a random state;
+  step_mk_hll.npz, step_mk_god.npz
+                 20 launches of add_MK (kernel.cu:2293), method 0 (HLL) and
+                 method 2 (exact Godunov), on a 48x24 axisymmetric grid.
+
+The configurations that reproduce those kernels live in golden_configs.py so
+the tests use exactly the same ones.  Usage:  python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, HERE)
+
+import make_ref  # noqa: E402
+import pyoracle as O  # noqa: E402
+import golden_configs as G  # noqa: E402
+
+
+def face_cases(rng):
+    cases = []
+    for _ in range(1024):
+        sL = [rng.uniform(0.1, 5.0), rng.uniform(0.05, 20.0)]
+        sR = [rng.uniform(0.1, 5.0), rng.uniform(0.05, 20.0)]
+        uL = list(rng.uniform(-5.0, 5.0, 2))
+        uR = list(rng.uniform(-5.0, 5.0, 2))
+        cases.append(sL + uL + sR + uR)
+    # exact-solver wave patterns, normal along +z
+    cases += [
+        [1.0, 1.0, 2.0, 0.0, 1.0, 1.0, -2.0, 0.0],        # two shocks (colliding)
+        [4.0, 10.0, 3.0, 0.5, 1.0, 1.0, -1.0, -0.5],      # two shocks, unequal
+        [1.0, 1.0, 0.0, 0.0, 0.125, 0.1, 0.0, 0.0],       # Sod: shock + rarefaction
+        [1.0, 0.4, -2.0, 0.0, 1.0, 0.4, 2.0, 0.0],        # 123 problem: two rarefactions
+        [1.0, 0.1, -10.0, 0.3, 1.0, 0.1, 10.0, -0.3],     # vacuum generation
+        [1.0, 0.0666666, -1.0, 0.0, 1.0, 0.0666666, -1.0, 0.0],  # `test` kernel state
+        [1.0, 10.0, 0.0, 0.0, 1.0, 0.1, 0.0, 0.0],        # blast interface
+        [2.0, 3.0, 0.7, 0.2, 2.0, 3.0, 0.7, 0.2],         # identical states
+    ]
+    return np.array(cases)
+
+
+def make_faces(rng):
+    cfg = G.face_config()
+    O.ref_set(cfg)
+    X = face_cases(rng)
+    normals = [(1.0, 0.0), (-1.0, 0.0), (0.0, 1.0), (0.0, -1.0)]
+    n = np.array([normals[i % 4] for i in range(len(X))])
+    n[-8:] = (1.0, 0.0)
+    rad = np.where(n[:, 0] != 0, 0.01, 0.02)
+    out = {}
+    for name, which in (("hll", 0), ("hllc", 1), ("godunov", 2)):
+        F = np.zeros((len(X), 4))
+        T = np.zeros(len(X))
+        for i, row in enumerate(X):
+            T[i], F[i] = O.ref_face(which, row[0:2], row[2:4], row[4:6], row[6:8], n[i, 0], n[i, 1], rad[i])
+        out[name + "_flux"] = F
+        out[name + "_dt"] = T
+    np.savez_compressed(os.path.join(HERE, "faces.npz"), states=X, normals=n, rad=rad,
+                        gamma=cfg.gamma, cfl=cfg.cfl, **out)
+
+
+def make_step(fname, cfg, kernel, method, nsteps, rng):
+    K = cfg.N * cfg.M
+    s, u = G.random_state(K, rng)
+    s1, u1, tdo, tt, st = O.ref_run(kernel, cfg, s, u, nsteps, method=method)
+    np.savez_compressed(os.path.join(HERE, fname), s0=s, u0=u, s=s1, u=u1, T_do=tdo, TT=tt,
+                        steps=st, nsteps=nsteps)
+
+
+def main():
+    make_ref.main([])
+    rng = np.random.default_rng(20261203)
+    make_faces(rng)
+    make_step("step_tvd.npz", G.tvd_config(), O.REF_KERNEL_TVD, 1, 20, rng)
+    make_step("step_mk_hll.npz", G.add_mk_config(0), O.REF_ADD_MK, 0, 20, rng)
+    make_step("step_mk_god.npz", G.add_mk_config(2), O.REF_ADD_MK, 2, 20, rng)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
