@@ -1,0 +1,457 @@
+// api.cu - the C ABI of include/asteriy_gb300.h on top of the step kernel.
+//
+// The solver object replaces the reference's main(): allocation
+// (kernel.cu:3283-3298), host->device copies (kernel.cu:3444-3455), the
+// ping-pong time loop with its funk_time launches and synchronisations
+// (kernel.cu:3868-3947) and the final device->host copies
+// (kernel.cu:4075-4080).  Steps are queued on one stream; the dt shift runs
+// on the device inside the step kernel, so nsteps steps cost nsteps launches
+// and no host synchronisation.  Repeated step counts are replayed from a
+// captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/asteriy_gb300.h"
+#include "launch.cuh"
+
+using namespace ast;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+#define AST_CUDA(call)                                      \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+int fail(int code, const char* msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+// ---------------------------------------------------------------- layout conversion
+template <typename R>
+__global__ void aos_to_soa(const double2* __restrict__ s, const double2* __restrict__ u, R* __restrict__ q,
+                           int N, int M, long long ld, long long plane)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (long long)N * M) return;
+    int m = (int)(k / N), n = (int)(k - (long long)m * N);
+    long long o = (long long)m * ld + n;
+    double2 a = s[k], b = u[k];
+    q[o] = (R)a.x; q[o + plane] = (R)a.y; q[o + 2 * plane] = (R)b.x; q[o + 3 * plane] = (R)b.y;
+}
+
+template <typename R>
+__global__ void soa_to_aos(const R* __restrict__ q, double2* __restrict__ s, double2* __restrict__ u, int N,
+                           int M, long long ld, long long plane)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (long long)N * M) return;
+    int m = (int)(k / N), n = (int)(k - (long long)m * N);
+    long long o = (long long)m * ld + n;
+    s[k] = make_double2((double)q[o], (double)q[o + plane]);
+    u[k] = make_double2((double)q[o + 2 * plane], (double)q[o + 3 * plane]);
+}
+
+__global__ void funk_time_kernel(double* T, double* T_do, double* TT, int* i)
+{
+    *T_do = *T;
+    *TT = *TT + *T_do;
+    *T = 10000000;
+    *i = *i + 1;
+}
+
+void fill_params(StepParams& P, const ast_config& c)
+{
+    std::memset(&P, 0, sizeof P);
+    P.N = c.N;
+    P.M = c.M;
+    P.x_min = c.x_min;
+    P.dx = (c.x_max - c.x_min) / (c.N - 1);
+    P.dy = (c.y_max) / (c.M);
+    P.y_min = (c.y_max / (2.0 * c.M));
+    P.krit_dx = c.cfl * P.dx;
+    P.krit_dy = c.cfl * P.dy;
+    P.dt_cap = c.dt_cap;
+    P.p_floor = c.p_floor;
+    P.gamma = c.gamma;
+    P.tol = c.riemann_tol;
+    P.max_iter = c.riemann_max_iter;
+    P.geom = c.geom;
+    P.grad_p = c.grad_p;
+    P.collect_stats = c.collect_stats;
+    for (int sd = 0; sd < 4; sd++) {
+        P.bc_kind[sd] = c.bc[sd].kind;
+        P.bc_val[sd][0] = c.bc[sd].rho;
+        P.bc_val[sd][1] = c.bc[sd].p;
+        P.bc_val[sd][2] = c.bc[sd].vz;
+        P.bc_val[sd][3] = c.bc[sd].vr;
+    }
+    P.fixed_region = c.fixed_region;
+    P.fixed_zc = c.fixed_zc;
+    P.fixed_az2 = c.fixed_az * c.fixed_az;
+    P.fixed_ar2 = c.fixed_ar * c.fixed_ar;
+    P.region_select = c.region_select;
+    P.region_lo = c.region_lo;
+    P.region_hi = c.region_hi;
+    P.body_force = c.body_force;
+    P.body_lo = c.body_lo;
+    P.body_hi = c.body_hi;
+    P.body_rsplit = c.body_rsplit;
+    P.body_amp = c.body_amp;
+}
+
+}  // namespace
+
+int ast::cuda_fail(cudaError_t e, const char* what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return AST_ERR_CUDA;
+}
+
+// ==================================================================== solver
+struct ast_solver {
+    ast_config cfg;
+    StepParams P;
+    cudaStream_t stream = nullptr;
+    size_t elem = 8;                 // bytes per state value
+    long long ld = 0, plane = 0;
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    DevClock* clock = nullptr;
+    double* stage_s = nullptr;       // device AoS staging for set/get
+    double* stage_u = nullptr;
+    cudaGraphExec_t graph = nullptr; // captured block of graph_steps steps
+    int graph_steps = 0;
+    int graph_cur = -1;              // buffer index the graph starts from
+};
+
+extern "C" {
+
+int ast_abi_version(void) { return AST_ABI_VERSION; }
+
+const char* ast_last_error(void) { return g_last_error.c_str(); }
+
+const char* ast_strerror(int code)
+{
+    switch (code) {
+    case AST_OK: return "ok";
+    case AST_ERR_INVALID: return "invalid argument or configuration";
+    case AST_ERR_CUDA: return "CUDA runtime error";
+    case AST_ERR_NOMEM: return "out of memory";
+    case AST_ERR_IO: return "file I/O error";
+    case AST_ERR_UNSUPPORTED: return "unsupported request";
+    case AST_ERR_NUMERIC: return "non-finite values in the state";
+    default: return "unknown error";
+    }
+}
+
+size_t ast_sizeof_config(void) { return sizeof(ast_config); }
+size_t ast_sizeof_stats(void) { return sizeof(ast_stats); }
+
+int ast_create(const ast_config* cfg, ast_solver** out)
+{
+    if (!cfg || !out) return fail(AST_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int rc = ast_config_check(cfg);
+    if (rc != AST_OK) return rc;
+    ast_solver* S = new (std::nothrow) ast_solver();
+    if (!S) return fail(AST_ERR_NOMEM, "host allocation");
+    S->cfg = *cfg;
+    S->elem = (cfg->precision == AST_PREC_FP32) ? 4 : 8;
+    // rows padded to 128 bytes: aligned, coalesced row starts
+    const long long align = 128 / (long long)S->elem;
+    S->ld = ((long long)cfg->N + align - 1) / align * align;
+    S->plane = S->ld * cfg->M;
+    const size_t bytes = (size_t)S->plane * 4 * S->elem;
+    const size_t K = (size_t)cfg->N * cfg->M;
+    cudaError_t e;
+    if ((e = cudaMalloc(&S->buf[0], bytes)) != cudaSuccess || (e = cudaMalloc(&S->buf[1], bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&S->clock, sizeof(DevClock))) != cudaSuccess ||
+        (e = cudaMalloc(&S->stage_s, K * 2 * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&S->stage_u, K * 2 * sizeof(double))) != cudaSuccess) {
+        ast_destroy(S);
+        g_last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return AST_ERR_NOMEM;
+    }
+    cudaMemset(S->buf[0], 0, bytes);
+    cudaMemset(S->buf[1], 0, bytes);
+    fill_params(S->P, *cfg);
+    S->P.ld = S->ld;
+    S->P.plane = S->plane;
+    S->P.clock = S->clock;
+    DevClock c0;
+    std::memset(&c0, 0, sizeof c0);
+    c0.T_do = cfg->dt_first;
+    if ((e = cudaMemcpy(S->clock, &c0, sizeof c0, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        ast_destroy(S);
+        return cuda_fail(e, "cudaMemcpy clock");
+    }
+    rc = (S->elem == 8) ? launch_step_r<double, kSoA>(S->P, cfg->flux, cfg->recon, nullptr, false)
+                        : launch_step_r<float, kSoA>(S->P, cfg->flux, cfg->recon, nullptr, false);
+    if (rc != AST_OK) {
+        ast_destroy(S);
+        return rc;
+    }
+    *out = S;
+    return AST_OK;
+}
+
+int ast_destroy(ast_solver* S)
+{
+    if (!S) return AST_OK;
+    if (S->graph) cudaGraphExecDestroy(S->graph);
+    cudaFree(S->buf[0]);
+    cudaFree(S->buf[1]);
+    cudaFree(S->clock);
+    cudaFree(S->stage_s);
+    cudaFree(S->stage_u);
+    delete S;
+    return AST_OK;
+}
+
+int ast_set_stream(ast_solver* S, void* stream)
+{
+    if (!S) return fail(AST_ERR_INVALID, "null solver");
+    S->stream = (cudaStream_t)stream;
+    if (S->graph) {
+        cudaGraphExecDestroy(S->graph);
+        S->graph = nullptr;
+    }
+    return AST_OK;
+}
+
+static int convert_in(ast_solver* S, const double* s, const double* u)
+{
+    const long long K = (long long)S->cfg.N * S->cfg.M;
+    const int nb = (int)((K + 255) / 256);
+    void* dst = S->buf[S->cur];
+    if (S->elem == 8)
+        aos_to_soa<double><<<nb, 256, 0, S->stream>>>((const double2*)s, (const double2*)u, (double*)dst, S->cfg.N,
+                                                      S->cfg.M, S->ld, S->plane);
+    else
+        aos_to_soa<float><<<nb, 256, 0, S->stream>>>((const double2*)s, (const double2*)u, (float*)dst, S->cfg.N,
+                                                     S->cfg.M, S->ld, S->plane);
+    AST_CUDA(cudaGetLastError());
+    return AST_OK;
+}
+
+int ast_set_state(ast_solver* S, const double* s, const double* u, int on_device)
+{
+    if (!S || !s || !u) return fail(AST_ERR_INVALID, "null argument");
+    const size_t bytes = (size_t)S->cfg.N * S->cfg.M * 2 * sizeof(double);
+    if (on_device) return convert_in(S, s, u);
+    AST_CUDA(cudaMemcpyAsync(S->stage_s, s, bytes, cudaMemcpyHostToDevice, S->stream));
+    AST_CUDA(cudaMemcpyAsync(S->stage_u, u, bytes, cudaMemcpyHostToDevice, S->stream));
+    int rc = convert_in(S, S->stage_s, S->stage_u);
+    if (rc != AST_OK) return rc;
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    return AST_OK;
+}
+
+int ast_get_state(ast_solver* S, double* s, double* u, int on_device)
+{
+    if (!S || !s || !u) return fail(AST_ERR_INVALID, "null argument");
+    const long long K = (long long)S->cfg.N * S->cfg.M;
+    const int nb = (int)((K + 255) / 256);
+    double* ds = on_device ? s : S->stage_s;
+    double* du = on_device ? u : S->stage_u;
+    const void* src = S->buf[S->cur];
+    if (S->elem == 8)
+        soa_to_aos<double><<<nb, 256, 0, S->stream>>>((const double*)src, (double2*)ds, (double2*)du, S->cfg.N,
+                                                      S->cfg.M, S->ld, S->plane);
+    else
+        soa_to_aos<float><<<nb, 256, 0, S->stream>>>((const float*)src, (double2*)ds, (double2*)du, S->cfg.N,
+                                                     S->cfg.M, S->ld, S->plane);
+    AST_CUDA(cudaGetLastError());
+    if (!on_device) {
+        const size_t bytes = (size_t)K * 2 * sizeof(double);
+        AST_CUDA(cudaMemcpyAsync(s, ds, bytes, cudaMemcpyDeviceToHost, S->stream));
+        AST_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, S->stream));
+        AST_CUDA(cudaStreamSynchronize(S->stream));
+    }
+    return AST_OK;
+}
+
+int ast_set_clock(ast_solver* S, double T_do, double TT, int64_t step)
+{
+    if (!S) return fail(AST_ERR_INVALID, "null solver");
+    DevClock c;
+    AST_CUDA(cudaMemcpyAsync(&c, S->clock, sizeof c, cudaMemcpyDeviceToHost, S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    c.T_do = T_do;
+    c.TT = TT;
+    c.step = step;
+    c.smax_z = c.smax_r = 0;
+    c.done = 0;
+    AST_CUDA(cudaMemcpyAsync(S->clock, &c, sizeof c, cudaMemcpyHostToDevice, S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    return AST_OK;
+}
+
+int ast_get_clock(ast_solver* S, double* T_do, double* TT, int64_t* step)
+{
+    if (!S) return fail(AST_ERR_INVALID, "null solver");
+    DevClock c;
+    AST_CUDA(cudaMemcpyAsync(&c, S->clock, sizeof c, cudaMemcpyDeviceToHost, S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    if (T_do) *T_do = c.T_do;
+    if (TT) *TT = c.TT;
+    if (step) *step = c.step;
+    return AST_OK;
+}
+
+static int enqueue_one(ast_solver* S)
+{
+    StepParams P = S->P;
+    P.in = S->buf[S->cur];
+    P.out = S->buf[S->cur ^ 1];
+    int rc = (S->elem == 8) ? launch_step_r<double, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true)
+                            : launch_step_r<float, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true);
+    if (rc == AST_OK) S->cur ^= 1;
+    return rc;
+}
+
+// Captures `count` consecutive steps starting from buffer `cur` into a graph.
+static int capture_block(ast_solver* S, int count)
+{
+    if (S->graph) {
+        cudaGraphExecDestroy(S->graph);
+        S->graph = nullptr;
+    }
+    cudaStream_t cs;
+    AST_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaStream_t saved = S->stream;
+    const int cur0 = S->cur;
+    S->stream = cs;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    int rc = AST_OK;
+    if (e == cudaSuccess) {
+        for (int i = 0; i < count && rc == AST_OK; i++) rc = enqueue_one(S);
+        e = cudaStreamEndCapture(cs, &graph);
+    }
+    S->stream = saved;
+    S->cur = cur0;
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+    if (rc != AST_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    e = cudaGraphInstantiate(&S->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    S->graph_steps = count;
+    S->graph_cur = cur0;
+    return AST_OK;
+}
+
+int ast_step(ast_solver* S, int nsteps)
+{
+    if (!S || nsteps < 0) return fail(AST_ERR_INVALID, "bad argument");
+    // a captured block of an even number of steps returns to the same
+    // buffer, so it can be replayed back to back
+    const int block = 16;
+    while (nsteps >= block) {
+        if (!S->graph || S->graph_steps != block || S->graph_cur != S->cur) {
+            int rc = capture_block(S, block);
+            if (rc != AST_OK) return rc;
+        }
+        AST_CUDA(cudaGraphLaunch(S->graph, S->stream));
+        nsteps -= block;
+    }
+    for (int i = 0; i < nsteps; i++) {
+        int rc = enqueue_one(S);
+        if (rc != AST_OK) return rc;
+    }
+    return AST_OK;
+}
+
+int ast_synchronize(ast_solver* S)
+{
+    if (!S) return fail(AST_ERR_INVALID, "null solver");
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    unsigned int status = 0;
+    AST_CUDA(cudaMemcpy(&status, &S->clock->status, sizeof status, cudaMemcpyDeviceToHost));
+    if (status & AST_ST_NONFINITE) return fail(AST_ERR_NUMERIC, "non-finite wave speed");
+    return AST_OK;
+}
+
+int ast_get_stats(ast_solver* S, ast_stats* out, int reset)
+{
+    if (!S || !out) return fail(AST_ERR_INVALID, "null argument");
+    DevClock c;
+    AST_CUDA(cudaMemcpyAsync(&c, S->clock, sizeof c, cudaMemcpyDeviceToHost, S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    std::memset(out, 0, sizeof *out);
+    out->status = c.status;
+    out->rho_floor = c.cnt[0];
+    out->p_floor = c.cnt[1];
+    out->newton_calls = c.cnt[2];
+    out->newton_iters = c.cnt[3];
+    out->bisect_calls = c.cnt[4];
+    out->bisect_iters = c.cnt[5];
+    out->mlp_fallback = c.cnt[6];
+    out->newton_max_iters = (uint32_t)c.cnt[7];
+    if (reset) {
+        c.status = 0;
+        std::memset(c.cnt, 0, sizeof c.cnt);
+        AST_CUDA(cudaMemcpyAsync(S->clock, &c, sizeof c, cudaMemcpyHostToDevice, S->stream));
+        AST_CUDA(cudaStreamSynchronize(S->stream));
+    }
+    return AST_OK;
+}
+
+int ast_device_state(ast_solver* S, void** planes, int64_t* ld, int* elem_bytes)
+{
+    if (!S) return fail(AST_ERR_INVALID, "null solver");
+    if (planes) *planes = S->buf[S->cur];
+    if (ld) *ld = S->ld;
+    if (elem_bytes) *elem_bytes = (int)S->elem;
+    return AST_OK;
+}
+
+// ==================================================================== kernel-level drop-in
+int ast_step_raw(const double* s, const double* u, double* s2, double* u2, double* T, const double* T_do,
+                 const double* TT, int method, const ast_config* cfg, void* stream)
+{
+    (void)TT;
+    (void)method;
+    if (!s || !u || !s2 || !u2 || !T || !T_do || !cfg) return fail(AST_ERR_INVALID, "null argument");
+    int rc = ast_config_check(cfg);
+    if (rc != AST_OK) return rc;
+    if (cfg->precision != AST_PREC_FP64) return fail(AST_ERR_UNSUPPORTED, "raw step is FP64 (reference layout)");
+    StepParams P;
+    fill_params(P, *cfg);
+    P.in = s;
+    P.in_u = u;
+    P.out = s2;
+    P.out_u = u2;
+    P.clock = nullptr;
+    P.T_min = T;
+    P.T_do_ptr = T_do;
+    P.collect_stats = 0;
+    rc = launch_step_r<double, kAoS>(P, cfg->flux, cfg->recon, (cudaStream_t)stream, false);
+    if (rc != AST_OK) return rc;
+    return launch_step_r<double, kAoS>(P, cfg->flux, cfg->recon, (cudaStream_t)stream, true);
+}
+
+int ast_funk_time(double* T, double* T_do, double* TT, int* i, void* stream)
+{
+    if (!T || !T_do || !TT || !i) return fail(AST_ERR_INVALID, "null argument");
+    funk_time_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(T, T_do, TT, i);
+    AST_CUDA(cudaGetLastError());
+    return AST_OK;
+}
+
+}  // extern "C"

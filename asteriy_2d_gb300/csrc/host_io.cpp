@@ -1,0 +1,198 @@
+// host_io.cpp - configuration, initial conditions and the reference's file
+// formats (host code of the C ABI).
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <random>
+#include <string>
+
+#include "../../include/asteriy_gb300.h"
+
+namespace {
+
+// cell centres as the reference's writers compute them (kernel.cu:3127-3128,
+// 4136-4137): x_min + n*(x_max-x_min)/(N-1), y_min + m*y_max/M
+inline double out_x(const ast_config* c, int n) { return c->x_min + n * (c->x_max - c->x_min) / (c->N - 1); }
+inline double out_y(const ast_config* c, int m)
+{
+    return (c->y_max / (2.0 * c->M)) + m * (c->y_max) / (c->M);
+}
+// cell centres as the kernels and the initial-condition loop compute them
+// (kernel.cu:3345-3346): x_min + n*dx, y_min + m*dy
+inline double cell_x(const ast_config* c, int n) { return c->x_min + n * ((c->x_max - c->x_min) / (c->N - 1)); }
+inline double cell_y(const ast_config* c, int m) { return (c->y_max / (2.0 * c->M)) + m * ((c->y_max) / (c->M)); }
+
+}  // namespace
+
+extern "C" {
+
+void ast_config_default(ast_config* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof *c);
+    c->N = 32000;                       // Header.h:8
+    c->M = 400;                         // Header.h:9
+    c->x_min = 0.0;                     // Header.h:11
+    c->x_max = 80.0;                    // Header.h:12
+    c->y_max = 1.0;                     // Header.h:13
+    c->gamma = 5.0 / 3.0;               // Header.h:17
+    c->cfl = 0.05;                      // Header.h:47
+    c->flux = AST_FLUX_HLL;
+    c->recon = AST_RECON_MINMOD;
+    c->geom = AST_GEOM_PLANAR;
+    c->precision = AST_PREC_FP64;
+    c->grad_p = 1;                      // Header.h:31
+    c->guess = AST_GUESS_PVRS;
+    c->bc[AST_Z_LO].kind = AST_BC_OUTFLOW;
+    c->bc[AST_Z_HI].kind = AST_BC_OUTFLOW;
+    c->bc[AST_R_LO].kind = AST_BC_REFLECT;
+    c->bc[AST_R_HI].kind = AST_BC_REFLECT;
+    c->fixed_az = c->fixed_ar = 1.0;
+    c->riemann_max_iter = 200;
+    c->dt_first = 0.000000001;          // kernel.cu:3322
+    c->dt_cap = 1000;                   // kernel.cu:2530
+    c->p_floor = 0.000001;              // kernel.cu:3072
+    c->riemann_tol = 10e-10;            // Header.h:62
+}
+
+int ast_config_check(const ast_config* c)
+{
+    if (!c) return AST_ERR_INVALID;
+    if (c->N < 4 || c->M < 4 || (long long)c->N * c->M > (1LL << 31) - 1) return AST_ERR_INVALID;
+    if (c->M > 65535 * 16) return AST_ERR_INVALID;
+    if (!(c->x_max > c->x_min) || !(c->y_max > 0.0)) return AST_ERR_INVALID;
+    if (!(c->gamma > 1.0) || !(c->cfl > 0.0)) return AST_ERR_INVALID;
+    if (c->flux < AST_FLUX_HLL || c->flux > AST_FLUX_GODUNOV) return AST_ERR_INVALID;
+    if (c->recon < AST_RECON_NONE || c->recon > AST_RECON_MINMOD) return AST_ERR_INVALID;
+    if (c->geom < AST_GEOM_PLANAR || c->geom > AST_GEOM_AXISYM) return AST_ERR_INVALID;
+    if (c->precision < AST_PREC_FP64 || c->precision > AST_PREC_FP32) return AST_ERR_INVALID;
+    if (c->guess < AST_GUESS_PVRS || c->guess > AST_GUESS_MLP) return AST_ERR_INVALID;
+    for (int s = 0; s < 4; s++) {
+        if (c->bc[s].kind < AST_BC_REFLECT || c->bc[s].kind > AST_BC_SUCTION) return AST_ERR_INVALID;
+        if (c->bc[s].kind == AST_BC_FIXED && !(c->bc[s].rho > 0.0 && c->bc[s].p > 0.0)) return AST_ERR_INVALID;
+    }
+    if (c->fixed_region && !(c->fixed_az > 0.0 && c->fixed_ar > 0.0)) return AST_ERR_INVALID;
+    if (c->riemann_max_iter < 1 || !(c->riemann_tol > 0.0)) return AST_ERR_INVALID;
+    if (!(c->dt_first > 0.0) || !(c->dt_cap > 0.0) || !(c->p_floor > 0.0)) return AST_ERR_INVALID;
+    return AST_OK;
+}
+
+int ast_fill_blast(const ast_config* c, double p_in, double p_out, double radius, double* s, double* u)
+{
+    if (!c || !s || !u || ast_config_check(c) != AST_OK) return AST_ERR_INVALID;
+    for (int m = 0; m < c->M; m++) {
+        for (int n = 0; n < c->N; n++) {
+            const long long k = (long long)m * c->N + n;
+            const double x = cell_x(c, n), y = cell_y(c, m);
+            const double dist = std::sqrt(x * x + y * y);
+            s[2 * k] = 1.0;
+            s[2 * k + 1] = (dist < radius) ? p_in : p_out;
+            u[2 * k] = 0.0;
+            u[2 * k + 1] = 0.0;
+        }
+    }
+    return AST_OK;
+}
+
+int ast_fill_wind(const ast_config* c, double r_w, double rho_w, double v_w, double mach_w, double rho_inf,
+                  double p_inf, double v_inf, double noise, uint64_t seed, double* s, double* u)
+{
+    if (!c || !s || !u || ast_config_check(c) != AST_OK || !(r_w > 0.0)) return AST_ERR_INVALID;
+    std::mt19937_64 gen(seed);
+    const double p_w = rho_w * v_w * v_w / (c->gamma * mach_w * mach_w);
+    for (int m = 0; m < c->M; m++) {
+        for (int n = 0; n < c->N; n++) {
+            const long long k = (long long)m * c->N + n;
+            const double x = cell_x(c, n), y = cell_y(c, m);
+            const double uni = (double)(gen() >> 11) * 0x1.0p-53;
+            const double dist = std::sqrt(x * x + y * y);
+            if (dist < r_w) {
+                const double q = r_w / dist;
+                s[2 * k] = rho_w * q * q;
+                s[2 * k + 1] = p_w * std::pow(q, 2.0 * c->gamma);
+                u[2 * k] = v_w * x / dist;
+                u[2 * k + 1] = v_w * y / dist;
+            } else {
+                s[2 * k] = rho_inf * (1.0 + noise * (2.0 * uni - 1.0));
+                s[2 * k + 1] = p_inf;
+                u[2 * k] = v_inf;
+                u[2 * k + 1] = 0.0;
+            }
+        }
+    }
+    return AST_OK;
+}
+
+int ast_write_bin(const ast_config* c, const double* s, const double* u, const char* path)
+{
+    if (!c || !s || !u || !path || ast_config_check(c) != AST_OK) return AST_ERR_INVALID;
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return AST_ERR_IO;
+    for (int m = 0; m < c->M; m++) {
+        for (int n = 0; n < c->N; n++) {
+            const long long k = (long long)m * c->N + n;
+            const double rec[6] = {out_x(c, n), out_y(c, m), s[2 * k], s[2 * k + 1], u[2 * k], u[2 * k + 1]};
+            f.write(reinterpret_cast<const char*>(rec), sizeof rec);
+        }
+    }
+    return f.good() ? AST_OK : AST_ERR_IO;
+}
+
+int ast_read_bin(const ast_config* c, double* s, double* u, const char* path)
+{
+    if (!c || !s || !u || !path || ast_config_check(c) != AST_OK) return AST_ERR_INVALID;
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return AST_ERR_IO;
+    const long long K = (long long)c->N * c->M;
+    for (long long k = 0; k < K; k++) {
+        double rec[6];
+        f.read(reinterpret_cast<char*>(rec), sizeof rec);
+        if (!f) return AST_ERR_IO;  // truncated file
+        s[2 * k] = rec[2];
+        s[2 * k + 1] = rec[3];
+        u[2 * k] = rec[4];
+        u[2 * k + 1] = rec[5];
+    }
+    return AST_OK;
+}
+
+int ast_write_tecplot(const ast_config* c, const double* s, const double* u, int stride, double soltime,
+                      const char* path)
+{
+    if (!c || !s || !u || !path || stride < 1 || ast_config_check(c) != AST_OK) return AST_ERR_INVALID;
+    std::ofstream f(path);
+    if (!f) return AST_ERR_IO;
+    const int N = c->N, M = c->M;
+    const long long K = (long long)N * M;
+    const double dx = (c->x_max - c->x_min) / (N - 1), dy = c->y_max / M;
+    const int nn = (N + stride - 1) / stride, mm = (M + stride - 1) / stride;
+    f << "TITLE = \"HP\"  VARIABLES = \"X\", \"Y\", \"Ro\", \"P\", \"Vx\", \"Vy\", \"Mach\", \"omega\", ZONE T = \"HP\", "
+         "SOLUTIONTIME = "
+      << soltime << ", N = " << nn * mm << " , E = " << (long long)(nn - 1) * (mm - 1)
+      << ", F = FEPOINT, ET = quadrilateral" << std::endl;
+    for (long long k = 0; k < K; k++) {
+        const int n = (int)(k % N), m = (int)(k / N);
+        if ((n % stride != 0) || (m % stride != 0)) continue;
+        // neighbour indices as print_file_mini forms them (kernel.cu:3143-3152)
+        const long long k2 = (long long)m * N + (n + 1), k3 = (long long)(m - 1) * N + n;
+        const long long k4 = (long long)m * N + (n - 1), k5 = (long long)(m + 1) * N + n;
+        double dvx = 0.0, dvy = 0.0, mach = 0.0;
+        if (k3 >= 0 && k3 < K && k5 >= 0 && k5 < K) dvx = (u[2 * k5] - u[2 * k3]) / (2.0 * dy);
+        if (k2 >= 0 && k2 < K && k4 >= 0 && k4 < K) dvy = (u[2 * k2 + 1] - u[2 * k4 + 1]) / (2.0 * dx);
+        if (s[2 * k] > 0.0)
+            mach = std::sqrt((u[2 * k] * u[2 * k] + u[2 * k + 1] * u[2 * k + 1]) / (c->gamma * s[2 * k + 1] / s[2 * k]));
+        f << out_x(c, n) << " " << out_y(c, m) << " " << s[2 * k] << " " << s[2 * k + 1] << " " << u[2 * k] << " "
+          << u[2 * k + 1] << " " << mach << " " << (dvy - dvx) / 2.0 << std::endl;
+    }
+    for (long long k = 0; k < (long long)nn * mm; k++) {
+        const long long n = k % nn, m = k / nn;
+        if ((m < mm - 1) && (n < nn - 1))
+            f << m * nn + n + 1 << " " << m * nn + n + 2 << " " << (m + 1) * nn + n + 2 << " " << (m + 1) * nn + n + 1
+              << std::endl;
+    }
+    return f.good() ? AST_OK : AST_ERR_IO;
+}
+
+}  // extern "C"

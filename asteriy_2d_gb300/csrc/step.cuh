@@ -1,0 +1,406 @@
+// step.cuh - the fused explicit r-z step: one kernel per time step.
+//
+// A CTA owns a TZ x TR tile of cells.  It stages the tile plus a two-cell
+// halo of (rho, p, v_z, v_r) in shared memory, filling halo cells outside
+// the domain with the side's ghost rule; evaluates every z face and every r
+// face of the tile once (minmod reconstruction + the configured flux);
+// updates each cell from its four faces with the planar (Kernel_TVD,
+// kernel.cu:3027-3073) or axisymmetric (add_MK, kernel.cu:2480-2509)
+// conservative update; and reduces the largest wave speed per direction.
+// The last CTA to finish turns the two maxima into the next dt and performs
+// the reference's funk_time shift (kernel.cu:1525-1536) on the device, so a
+// sequence of steps needs no host round trip.
+#pragma once
+
+#include "physics.cuh"
+
+namespace ast {
+
+constexpr int kThreads = 256;
+
+// device-resident clock and counters of a solver (one per solver)
+struct DevClock {
+    double T_do;                   // dt the next step uses
+    double TT;                     // accumulated time
+    long long step;                // steps taken
+    unsigned long long smax_z;     // bits of the largest z-face wave speed (>= 0)
+    unsigned long long smax_r;     // same for r faces
+    unsigned int done;             // CTAs of the current step that finished
+    unsigned int status;           // OR of AST_ST_* bits
+    unsigned long long cnt[8];     // rho_floor, p_floor, newton_calls, newton_iters,
+                                   // bisect_calls, bisect_iters, mlp_fallback, newton_max
+};
+
+enum Layout { kSoA = 0, kAoS = 1 };
+
+struct StepParams {
+    int N, M;
+    long long ld;                  // SoA row pitch in elements
+    long long plane;               // SoA plane size in elements
+    double x_min, dx, y_min, dy;
+    double krit_dx, krit_dy;       // cfl*dx and cfl*dy
+    double dt_cap, p_floor;
+    double gamma, tol;
+    int max_iter;
+    int geom, grad_p, collect_stats;
+    int bc_kind[4];
+    double bc_val[4][4];           // rho, p, vz, vr of FIXED sides; vz/vr limit of SUCTION
+    int fixed_region;
+    double fixed_zc, fixed_az2, fixed_ar2;
+    int region_select;
+    double region_lo, region_hi;
+    int body_force;
+    double body_lo, body_hi, body_rsplit, body_amp;
+    // state: SoA planes (in/out) or reference AoS (s, u, s2, u2)
+    const void* in;
+    void* out;
+    const double* in_u;
+    double* out_u;
+    DevClock* clock;               // solver mode
+    double* T_min;                 // raw mode: *T_min = min(*T_min, dt), atomic
+    const double* T_do_ptr;        // raw mode: the step's dt
+    unsigned int* status_ptr;      // raw mode: status bits (may be null)
+};
+
+// ------------------------------------------------------------------ loads
+template <typename R, int LAYOUT>
+__device__ __forceinline__ void read_cell(const StepParams& P, int n, int m, R v[4])
+{
+    if (LAYOUT == kSoA) {
+        const R* q = (const R*)P.in;
+        long long k = (long long)m * P.ld + n;
+        v[0] = q[k];
+        v[1] = q[k + P.plane];
+        v[2] = q[k + 2 * P.plane];
+        v[3] = q[k + 3 * P.plane];
+    } else {
+        long long k = (long long)m * P.N + n;
+        double2 s = ((const double2*)P.in)[k];
+        double2 u = ((const double2*)P.in_u)[k];
+        v[0] = (R)s.x; v[1] = (R)s.y; v[2] = (R)u.x; v[3] = (R)u.y;
+    }
+}
+
+// state of cell (n, m) where at most one of n, m may lie outside the domain;
+// outside cells follow their side's ghost rule (include/asteriy_gb300.h)
+template <typename R, int LAYOUT>
+__device__ __forceinline__ void fetch_cell(const StepParams& P, int n, int m, R v[4])
+{
+    const int N = P.N, M = P.M;
+    if (n >= 0 && n < N && m >= 0 && m < M) {
+        read_cell<R, LAYOUT>(P, n, m, v);
+        return;
+    }
+    int side, j, bn, bm, mn, mm;
+    bool low;
+    if (n < 0)       { side = 0; j = -1 - n; low = true;  bn = 0;     bm = m; mn = j;         mm = m; }
+    else if (n >= N) { side = 1; j = n - N;  low = false; bn = N - 1; bm = m; mn = N - 1 - j; mm = m; }
+    else if (m < 0)  { side = 2; j = -1 - m; low = true;  bn = n; bm = 0;     mn = n; mm = j; }
+    else             { side = 3; j = m - M;  low = false; bn = n; bm = M - 1; mn = n; mm = M - 1 - j; }
+    // only ghost layers 0 and 1 feed valid faces; deeper ones (partial
+    // tiles) are clamped to stay inside the arrays
+    mn = min(max(mn, 0), N - 1);
+    mm = min(max(mm, 0), M - 1);
+    bm = min(max(bm, 0), M - 1);
+    bn = min(max(bn, 0), N - 1);
+    const int kind = P.bc_kind[side];
+    const bool zside = side < 2;
+    if (kind == 0) {            // REFLECT
+        read_cell<R, LAYOUT>(P, mn, mm, v);
+        if (zside) v[2] = -v[2]; else v[3] = -v[3];
+    } else if (kind == 2) {     // FIXED
+        v[0] = (R)P.bc_val[side][0]; v[1] = (R)P.bc_val[side][1];
+        v[2] = (R)P.bc_val[side][2]; v[3] = (R)P.bc_val[side][3];
+    } else {                    // OUTFLOW, SUCTION
+        read_cell<R, LAYOUT>(P, bn, bm, v);
+        if (kind == 3) {
+            R lim = (R)(zside ? P.bc_val[side][2] : P.bc_val[side][3]);
+            R& vn = zside ? v[2] : v[3];
+            if (low) { if (vn > lim) vn = lim; }
+            else     { if (vn < lim) vn = lim; }
+        }
+    }
+}
+
+__device__ __forceinline__ bool cell_fixed(const StepParams& P, double x, double y)
+{
+    double xz = x - P.fixed_zc;
+    return (xz * xz) / P.fixed_az2 + (y * y) / P.fixed_ar2 < 1.0;
+}
+
+// ------------------------------------------------------------------ reductions
+__device__ __forceinline__ float warp_max(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+// ------------------------------------------------------------------ the kernel
+template <typename R, int TZ, int TR>
+struct TileSmem {
+    static constexpr int HZ = TZ + 4, HR = TR + 4;
+    R q[4][HR][HZ];              // staged state with a two-cell halo
+    R Fz[4][TR][TZ + 1];         // z-face flux: mass, mom_z, mom_r, energy
+    R Fr[4][TR + 1][TZ];         // r-face flux
+    unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
+};
+
+template <typename R, int TZ, int TR>
+constexpr size_t tile_smem_bytes() { return sizeof(TileSmem<R, TZ, TR>); }
+
+// All faces of one orientation in the tile, one thread per face.  ZF: z
+// faces (between tile columns c-1 and c of a row), else r faces (between
+// tile rows a-1 and a of a column).  Writes the flux, in (mass, mom_z,
+// mom_r, energy) order, to sm.Fz / sm.Fr and raises smax to the largest wave
+// speed of the faces that belong to at least one updated cell.
+template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF>
+__device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
+                                          int m0, RiemannCount& rc, R& smax)
+{
+    constexpr int NF = ZF ? TR * (TZ + 1) : (TR + 1) * TZ;
+    constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
+    constexpr int NN = ZF ? 2 : 3;           // normal velocity component
+    constexpr int TT = ZF ? 3 : 2;           // tangential velocity component
+    constexpr int DJ = ZF ? 0 : 1, DI = ZF ? 1 : 0;
+    for (int f = threadIdx.x; f < NF; f += kThreads) {
+        const int a = f / W, c = f - a * W;
+        // smem indices of the lower (l) and upper (u) cell of the face
+        const int jl = ZF ? a + 2 : a + 1, il = ZF ? c + 1 : c + 2;
+        const int ju = a + 2, iu = c + 2;
+        const int nl = n0 + il - 2, ml = m0 + jl - 2, nu = n0 + iu - 2, mu = m0 + ju - 2;
+        const bool lval = nl >= 0 && nl < P.N && ml >= 0 && ml < P.M;
+        const bool uval = nu >= 0 && nu < P.N && mu >= 0 && mu < P.M;
+        bool active = lval || uval;
+        if (active && P.fixed_region) active = (lval && !sm.fx[jl][il]) || (uval && !sm.fx[ju][iu]);
+        bool hi = true;
+        if (P.region_select) {
+            // the face's z position as the reference's lower cell sees it
+            const double xl = P.x_min + nl * P.dx;
+            const double xf = ZF ? xl + P.dx / 2.0 : xl;
+            hi = (xf > P.region_lo && xf < P.region_hi);
+        }
+        R L[4], U[4], F[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const R tl = sm.q[k][jl][il], tu = sm.q[k][ju][iu];
+            L[k] = tl;
+            U[k] = tu;
+            if (RECON && hi) {
+                const R tll = sm.q[k][jl - DJ][il - DI], tuu = sm.q[k][ju + DJ][iu + DI];
+                R x0, x1;
+                recon_pair(tll, tl, tu, x0, x1);
+                L[k] = x1;                  // right/top value of the lower cell
+                recon_pair(tl, tu, tuu, x0, x1);
+                U[k] = x0;                  // left/bottom value of the upper cell
+                // positivity of the reconstructed rho and p (kernel.cu:2706-2743)
+                if (k == 0) {
+                    if (L[0] <= R(0)) L[0] = tl;
+                    if (U[0] <= R(0)) U[0] = tu;
+                } else if (k == 1) {
+                    if (L[1] <= R(0) || !P.grad_p) L[1] = tl;
+                    if (U[1] <= R(0) || !P.grad_p) U[1] = tu;
+                }
+            }
+        }
+        R Sp;
+        if (hi) {
+            if (FLUX == 0) Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+            else if (FLUX == 1) Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+            else Sp = flux_godunov(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F, rc);
+        } else {
+            Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+        }
+        if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
+        if (ZF) {
+            sm.Fz[0][a][c] = F[0]; sm.Fz[1][a][c] = F[1]; sm.Fz[2][a][c] = F[2]; sm.Fz[3][a][c] = F[3];
+        } else {
+            // r face: the normal momentum is mom_r, the tangential one mom_z
+            sm.Fr[0][a][c] = F[0]; sm.Fr[1][a][c] = F[2]; sm.Fr[2][a][c] = F[1]; sm.Fr[3][a][c] = F[3];
+        }
+        if (active) smax = fmax(smax, Sp);
+    }
+}
+
+template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
+__global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
+{
+    using S = TileSmem<R, TZ, TR>;
+    constexpr int HZ = S::HZ, HR = S::HR;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    S& sm = *reinterpret_cast<S*>(smem_raw);
+    __shared__ double red_d[2][kThreads / 32];
+    __shared__ int red_i[3][kThreads / 32];
+    __shared__ int s_last;
+
+    const int tid = threadIdx.x;
+    const int n0 = blockIdx.x * TZ, m0 = blockIdx.y * TR;
+    const Gas<R> g = make_gas<R>(P.gamma, P.tol, P.max_iter);
+    const double T_do = (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr;
+
+    // ---- stage tile + halo; the corners are never read by the cross stencil
+    for (int idx = tid; idx < HR * HZ; idx += kThreads) {
+        const int j = idx / HZ, i = idx - j * HZ;
+        const bool rin = (j >= 2 && j < TR + 2), cin = (i >= 2 && i < TZ + 2);
+        if (!rin && !cin) continue;
+        const int n = n0 - 2 + i, m = m0 - 2 + j;
+        R v[4];
+        fetch_cell<R, LAYOUT>(P, n, m, v);
+        sm.q[0][j][i] = v[0]; sm.q[1][j][i] = v[1]; sm.q[2][j][i] = v[2]; sm.q[3][j][i] = v[3];
+        if (P.fixed_region) {
+            const bool inside = (n >= 0 && n < P.N && m >= 0 && m < P.M);
+            sm.fx[j][i] = inside ? (unsigned char)cell_fixed(P, P.x_min + n * P.dx, P.y_min + m * P.dy) : 0;
+        }
+    }
+    __syncthreads();
+
+    RiemannCount rc;
+    rc.clear();
+    R smz = R(0), smr = R(0);
+
+    // ---- every face of the tile once: z faces, then r faces
+    face_pass<R, FLUX, RECON, TZ, TR, true>(P, sm, g, n0, m0, rc, smz);
+    face_pass<R, FLUX, RECON, TZ, TR, false>(P, sm, g, n0, m0, rc, smr);
+    __syncthreads();
+
+    // ---- conservative update of the tile's cells
+    int nrho = 0, np = 0;
+    const double dx = P.dx, dy = P.dy, dV = dx * dy;
+    const R tdv = (R)(T_do / dV);
+    for (int cidx = tid; cidx < TZ * TR; cidx += kThreads) {
+        const int row = cidx / TZ, col = cidx - row * TZ;
+        const int n = n0 + col, m = m0 + row;
+        if (n >= P.N || m >= P.M) continue;
+        const int j = row + 2, i = col + 2;
+        const R r1 = sm.q[0][j][i], p1 = sm.q[1][j][i], vz1 = sm.q[2][j][i], vr1 = sm.q[3][j][i];
+        R o0, o1, o2, o3;
+        if (P.fixed_region && sm.fx[j][i]) {
+            o0 = r1; o1 = p1; o2 = vz1; o3 = vr1;
+        } else {
+            const double x = P.x_min + n * dx, y = P.y_min + m * dy;
+            R Q2 = R(0);
+            if (P.body_force && x > P.body_lo && x < P.body_hi)
+                Q2 = (y >= P.body_rsplit) ? -(R)P.body_amp * r1 : (R)P.body_amp * r1;
+            const R Q3 = Q2 * vr1;
+            R ps[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                // outward face fluxes: +right, -left, -bottom, +top
+                const R f12 = sm.Fz[k][row][col + 1], f14 = -sm.Fz[k][row][col];
+                const R f13 = -sm.Fr[k][row][col], f15 = sm.Fr[k][row + 1][col];
+                if (P.geom == 1) ps[k] = (f12 + f14) * (R)dy + (f13 + f15) * (R)dx;
+                else ps[k] = f12 * (R)dy + f13 * (R)dx + f14 * (R)dy + f15 * (R)dx;
+            }
+            const R ke1 = r1 * (vz1 * vz1 + vr1 * vr1) * R(0.5);
+            R rho2, mz, mr, E2;
+            if (P.geom == 1) {
+                const R ty = (R)(T_do / y);
+                rho2 = r1 - tdv * ps[0] - ty * r1 * vr1;
+                if (rho2 <= R(0)) { nrho++; rho2 = r1; }
+                mz = r1 * vz1 - tdv * ps[1] - ty * r1 * vr1 * vz1;
+                mr = r1 * vr1 - tdv * ps[2] - ty * r1 * vr1 * vr1 + (R)T_do * Q2;
+                E2 = (p1 * g.inv_g1 + ke1) - tdv * ps[3] - ty * vr1 * (g.ga * p1 * g.inv_g1 + ke1) + (R)T_do * Q3;
+            } else {
+                rho2 = r1 - tdv * ps[0];
+                if (rho2 <= R(0)) { nrho++; rho2 = r1; }
+                mz = r1 * vz1 - tdv * ps[1];
+                mr = r1 * vr1 - tdv * ps[2] + (R)T_do * Q2;
+                E2 = (p1 * g.inv_g1 + ke1) - tdv * ps[3] + (R)T_do * Q3;
+            }
+            const R irho = R(1) / rho2;
+            o0 = rho2;
+            o2 = mz * irho;
+            o3 = mr * irho;
+            o1 = (E2 - R(0.5) * rho2 * (o2 * o2 + o3 * o3)) * g.g1;
+            if (o1 <= R(0)) { np++; o1 = (R)P.p_floor; }
+        }
+        if (LAYOUT == kSoA) {
+            R* out = (R*)P.out;
+            const long long k = (long long)m * P.ld + n;
+            out[k] = o0; out[k + P.plane] = o1; out[k + 2 * P.plane] = o2; out[k + 3 * P.plane] = o3;
+        } else {
+            const long long k = (long long)m * P.N + n;
+            ((double2*)P.out)[k] = make_double2((double)o0, (double)o1);
+            ((double2*)P.out_u)[k] = make_double2((double)o2, (double)o3);
+        }
+    }
+
+    // ---- block reductions and the step epilogue
+    const int lane = tid & 31, wid = tid >> 5;
+    {
+        const double a = warp_max((double)smz), b = warp_max((double)smr);
+        const int c0 = __reduce_add_sync(0xffffffffu, nrho), c1 = __reduce_add_sync(0xffffffffu, np);
+        const unsigned st = __reduce_or_sync(0xffffffffu, rc.status);
+        if (lane == 0) {
+            red_d[0][wid] = a; red_d[1][wid] = b;
+            red_i[0][wid] = c0; red_i[1][wid] = c1; red_i[2][wid] = (int)st;
+        }
+        if (P.collect_stats && P.clock != nullptr) {
+            const int n1 = __reduce_add_sync(0xffffffffu, rc.newton_calls);
+            const int n2 = __reduce_add_sync(0xffffffffu, rc.newton_iters);
+            const int b1 = __reduce_add_sync(0xffffffffu, rc.bisect_calls);
+            const int b2 = __reduce_add_sync(0xffffffffu, rc.bisect_iters);
+            const unsigned nm = __reduce_max_sync(0xffffffffu, (unsigned)rc.newton_max);
+            if (lane == 0) {
+                if (n1) atomicAdd(&P.clock->cnt[2], (unsigned long long)n1);
+                if (n2) atomicAdd(&P.clock->cnt[3], (unsigned long long)n2);
+                if (b1) atomicAdd(&P.clock->cnt[4], (unsigned long long)b1);
+                if (b2) atomicAdd(&P.clock->cnt[5], (unsigned long long)b2);
+                if (nm) atomicMax(&P.clock->cnt[7], (unsigned long long)nm);
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0.0, b = 0.0;
+        int c0 = 0, c1 = 0;
+        unsigned st = 0;
+        for (int w = 0; w < kThreads / 32; w++) {
+            a = fmax(a, red_d[0][w]); b = fmax(b, red_d[1][w]);
+            c0 += red_i[0][w]; c1 += red_i[1][w]; st |= (unsigned)red_i[2][w];
+        }
+        if (c0) st |= 0x01u;
+        if (c1) st |= 0x02u;
+        if (P.clock != nullptr) {
+            DevClock* C = P.clock;
+            if (a > 0.0) atomicMax(&C->smax_z, (unsigned long long)__double_as_longlong(a));
+            if (b > 0.0) atomicMax(&C->smax_r, (unsigned long long)__double_as_longlong(b));
+            if (c0) atomicAdd(&C->cnt[0], (unsigned long long)c0);
+            if (c1) atomicAdd(&C->cnt[1], (unsigned long long)c1);
+            if (st) atomicOr(&C->status, st);
+            __threadfence();
+            const unsigned int total = gridDim.x * gridDim.y;
+            const unsigned int ticket = atomicAdd(&C->done, 1u);
+            s_last = (ticket == total - 1) ? 1 : 0;
+        } else {
+            // raw mode: this CTA's dt candidate, min-reduced into *T_min
+            double dt = P.dt_cap;
+            if (a > 0.0) dt = fmin(dt, P.krit_dx / a);
+            if (b > 0.0) dt = fmin(dt, P.krit_dy / b);
+            atomicMin((unsigned long long*)P.T_min, (unsigned long long)__double_as_longlong(dt));
+            if (st && P.status_ptr) atomicOr(P.status_ptr, st);
+            s_last = 0;
+        }
+    }
+    __syncthreads();
+    if (s_last && tid == 0) {
+        // funk_time (kernel.cu:1525-1536): T_do <- min dt, TT += T_do, i++
+        __threadfence();
+        DevClock* C = P.clock;
+        const double a = __longlong_as_double((long long)atomicExch(&C->smax_z, 0ull));
+        const double b = __longlong_as_double((long long)atomicExch(&C->smax_r, 0ull));
+        double dt = P.dt_cap;
+        if (a > 0.0) dt = fmin(dt, P.krit_dx / a);
+        if (b > 0.0) dt = fmin(dt, P.krit_dy / b);
+        C->T_do = dt;
+        C->TT = C->TT + dt;
+        C->step = C->step + 1;
+        C->done = 0u;
+        __threadfence();
+    }
+}
+
+}  // namespace ast

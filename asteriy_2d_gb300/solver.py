@@ -1,0 +1,209 @@
+"""Python binding of libasteriy_gb300.so (the C ABI in include/asteriy_gb300.h).
+
+The library is the product: every step runs in its CUDA kernels.  There is
+no CPU path; loading fails loudly when the library has not been built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi as A
+
+_lib = None
+_dp = C.POINTER(C.c_double)
+
+# every entry point of include/asteriy_gb300.h with (restype, argtypes)
+SIGNATURES = {
+    "ast_abi_version": (C.c_int, []),
+    "ast_strerror": (C.c_char_p, [C.c_int]),
+    "ast_last_error": (C.c_char_p, []),
+    "ast_sizeof_config": (C.c_size_t, []),
+    "ast_sizeof_stats": (C.c_size_t, []),
+    "ast_config_default": (None, [C.POINTER(A.ast_config)]),
+    "ast_config_check": (C.c_int, [C.POINTER(A.ast_config)]),
+    "ast_create": (C.c_int, [C.POINTER(A.ast_config), C.POINTER(C.c_void_p)]),
+    "ast_destroy": (C.c_int, [C.c_void_p]),
+    "ast_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ast_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "ast_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "ast_set_clock": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int64]),
+    "ast_get_clock": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int64)]),
+    "ast_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "ast_synchronize": (C.c_int, [C.c_void_p]),
+    "ast_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.ast_stats), C.c_int]),
+    "ast_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+    "ast_step_raw": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_int, C.POINTER(A.ast_config), C.c_void_p]),
+    "ast_funk_time": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ast_fill_blast": (C.c_int, [C.POINTER(A.ast_config), C.c_double, C.c_double, C.c_double, _dp, _dp]),
+    "ast_fill_wind": (C.c_int, [C.POINTER(A.ast_config), C.c_double, C.c_double, C.c_double, C.c_double,
+                                C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint64, _dp, _dp]),
+    "ast_write_bin": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
+    "ast_read_bin": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
+    "ast_write_tecplot": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_int, C.c_double, C.c_char_p]),
+}
+
+
+class AstError(RuntimeError):
+    def __init__(self, code, where):
+        lib = load()
+        msg = lib.ast_strerror(code).decode()
+        detail = lib.ast_last_error().decode()
+        super().__init__(f"{where}: {msg} ({code}) {detail}")
+        self.code = code
+
+
+def load(path=None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or A.LIB_PATH
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc, where):
+    if rc != A.AST_OK:
+        raise AstError(rc, where)
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def fill_blast(cfg, p_in=10.0, p_out=0.1, radius=0.2):
+    K = cfg.N * cfg.M
+    s = np.empty((K, 2))
+    u = np.empty((K, 2))
+    check(load().ast_fill_blast(C.byref(cfg), p_in, p_out, radius, _dptr(s), _dptr(u)), "ast_fill_blast")
+    return s, u
+
+
+def fill_wind(cfg, r_w=0.05, rho_w=1.0, v_w=10.0, mach_w=10.0, rho_inf=1.0, p_inf=None, v_inf=-2.0,
+              noise=0.01, seed=20261203):
+    K = cfg.N * cfg.M
+    s = np.empty((K, 2))
+    u = np.empty((K, 2))
+    if p_inf is None:
+        p_inf = 1.0 / cfg.gamma
+    check(load().ast_fill_wind(C.byref(cfg), r_w, rho_w, v_w, mach_w, rho_inf, p_inf, v_inf, noise, seed,
+                               _dptr(s), _dptr(u)), "ast_fill_wind")
+    return s, u
+
+
+def write_bin(cfg, s, u, path):
+    check(load().ast_write_bin(C.byref(cfg), _dptr(np.ascontiguousarray(s)), _dptr(np.ascontiguousarray(u)),
+                               os.fsencode(path)), "ast_write_bin")
+
+
+def read_bin(cfg, path):
+    K = cfg.N * cfg.M
+    s = np.empty((K, 2))
+    u = np.empty((K, 2))
+    check(load().ast_read_bin(C.byref(cfg), _dptr(s), _dptr(u), os.fsencode(path)), "ast_read_bin")
+    return s, u
+
+
+def write_tecplot(cfg, s, u, path, stride=2, soltime=0.0):
+    check(load().ast_write_tecplot(C.byref(cfg), _dptr(np.ascontiguousarray(s)), _dptr(np.ascontiguousarray(u)),
+                                   stride, soltime, os.fsencode(path)), "ast_write_tecplot")
+
+
+class Solver:
+    """One r-z problem resident on the GPU (the ast_solver object)."""
+
+    def __init__(self, cfg, stream=None):
+        self.lib = load()
+        self.cfg = cfg.copy()
+        h = C.c_void_p()
+        check(self.lib.ast_create(C.byref(self.cfg), C.byref(h)), "ast_create")
+        self.h = h
+        if stream is not None:
+            check(self.lib.ast_set_stream(self.h, C.c_void_p(stream)), "ast_set_stream")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ast_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def K(self):
+        return self.cfg.N * self.cfg.M
+
+    def set_state(self, s, u):
+        s = np.ascontiguousarray(s, dtype=np.float64)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        assert s.shape == (self.K, 2) and u.shape == (self.K, 2)
+        check(self.lib.ast_set_state(self.h, s.ctypes.data, u.ctypes.data, 0), "ast_set_state")
+
+    def set_state_device(self, s_ptr, u_ptr):
+        check(self.lib.ast_set_state(self.h, C.c_void_p(s_ptr), C.c_void_p(u_ptr), 1), "ast_set_state")
+
+    def get_state(self):
+        s = np.empty((self.K, 2))
+        u = np.empty((self.K, 2))
+        check(self.lib.ast_get_state(self.h, s.ctypes.data, u.ctypes.data, 0), "ast_get_state")
+        return s, u
+
+    def get_state_device(self, s_ptr, u_ptr):
+        check(self.lib.ast_get_state(self.h, C.c_void_p(s_ptr), C.c_void_p(u_ptr), 1), "ast_get_state")
+
+    def set_clock(self, T_do, TT=0.0, step=0):
+        check(self.lib.ast_set_clock(self.h, T_do, TT, step), "ast_set_clock")
+
+    def clock(self):
+        a, b, c = C.c_double(), C.c_double(), C.c_int64()
+        check(self.lib.ast_get_clock(self.h, C.byref(a), C.byref(b), C.byref(c)), "ast_get_clock")
+        return a.value, b.value, c.value
+
+    def step(self, n=1, sync=True):
+        check(self.lib.ast_step(self.h, n), "ast_step")
+        if sync:
+            self.synchronize()
+
+    def synchronize(self):
+        check(self.lib.ast_synchronize(self.h), "ast_synchronize")
+
+    def stats(self, reset=False):
+        st = A.ast_stats()
+        check(self.lib.ast_get_stats(self.h, C.byref(st), int(reset)), "ast_get_stats")
+        return {name: getattr(st, name) for name, _ in st._fields_ if name != "reserved"}
+
+    def device_state(self):
+        p, ld, el = C.c_void_p(), C.c_int64(), C.c_int()
+        check(self.lib.ast_device_state(self.h, C.byref(p), C.byref(ld), C.byref(el)), "ast_device_state")
+        return p.value, ld.value, el.value
+
+
+def step_raw(s, u, s2, u2, T, T_do, TT, cfg, method=1, stream=None):
+    """ast_step_raw on device pointers (ints), the Kernel_TVD drop-in."""
+    check(load().ast_step_raw(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), C.c_void_p(T),
+                              C.c_void_p(T_do), C.c_void_p(TT), method, C.byref(cfg),
+                              C.c_void_p(stream) if stream else None), "ast_step_raw")
+
+
+def funk_time(T, T_do, TT, i, stream=None):
+    check(load().ast_funk_time(C.c_void_p(T), C.c_void_p(T_do), C.c_void_p(TT), C.c_void_p(i),
+                               C.c_void_p(stream) if stream else None), "ast_funk_time")

@@ -1,0 +1,286 @@
+"""Benchmark of the explicit r-z step on GB300.
+
+Workload (the metric of the reference's target): the axisymmetric blast at
+4096 x 2048 cells (z in [-1,1], r in [0,1], gamma 5/3, CFL 0.4, rho=1, v=0,
+p=10 inside radius 0.2, 0.1 outside; reflecting axis, outflow elsewhere) with
+the exact-Godunov flux and minmod reconstruction.  A step is one time step
+over the whole grid; the metric is cell-updates/s = N*M*steps / time.
+
+Forms measured (each from the same initial state, warm-up steps first):
+  fp64_godunov   plain FP64 path (the oracle-comparable form)
+  fp32_godunov   precision form: FP32 state and fluxes
+The headline `value` is the form named in config.form.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) each rank advances an independent replica (the path
+is not decomposed across GPUs); value is the sum over ranks of the work over
+the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_Z, M_R = 4096, 2048
+BYTES_PER_CELL = {"fp64": 64, "fp32": 32}   # one read + one write of 4 state values
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_config(form):
+    from asteriy_2d_gb300 import abi as A
+    from asteriy_2d_gb300 import problems
+    prec = A.PREC_FP64 if form.startswith("fp64") else A.PREC_FP32
+    return problems.blast_config(N_Z, M_R, flux=A.FLUX_GODUNOV, precision=prec)
+
+
+def time_form(form, s0, u0, steps, warmup, torch):
+    """Device-timed steps of one form: inputs resident in HBM, CUDA events on
+    the solver's stream.  Returns (seconds, ms per step)."""
+    from asteriy_2d_gb300 import solver
+    cfg = make_config(form)
+    stream = torch.cuda.Stream()
+    with solver.Solver(cfg, stream=stream.cuda_stream) as S:
+        S.set_state(s0, u0)
+        S.step(warmup)
+        S.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        S.step(steps, sync=False)
+        e1.record(stream)
+        S.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+    return ms / 1e3, ms / steps
+
+
+def time_e2e(form, s0, u0, steps, torch):
+    """Through the public API with host buffers: every step copies the state
+    in from pinned host memory, steps once and reads the result back."""
+    from asteriy_2d_gb300 import solver
+    cfg = make_config(form)
+    K = cfg.N * cfg.M
+    hs = torch.empty((K, 2), dtype=torch.float64, pin_memory=True)
+    hu = torch.empty((K, 2), dtype=torch.float64, pin_memory=True)
+    hs.numpy()[:] = s0
+    hu.numpy()[:] = u0
+    lib = solver.load()
+    with solver.Solver(cfg) as S:
+        def one():
+            solver.check(lib.ast_set_state(S.h, hs.data_ptr(), hu.data_ptr(), 0), "set_state")
+            S.step(1, sync=False)
+            solver.check(lib.ast_get_state(S.h, hs.data_ptr(), hu.data_ptr(), 0), "get_state")
+        one()
+        hs.numpy()[:] = s0
+        hu.numpy()[:] = u0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            one()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    return dt, 2 * K * 16, 2 * K * 16
+
+
+def cpu_baseline(cfg, s0, u0, nsteps):
+    """The reference's face functions compiled for the host (oracle/_ref) in
+    the oracle's step loop, on all host threads; the oracle port if the
+    reference build is absent."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    nt = os.cpu_count() or 1
+    if O.have_ref():
+        kind = "reference"
+        fn = lambda: O.ref_run_composed(cfg, s0, u0, nsteps, nthreads=nt)  # noqa: E731
+    else:
+        kind = "port"
+        fn = lambda: O.run(cfg, s0, u0, nsteps, nthreads=nt)  # noqa: E731
+    t0 = time.perf_counter()
+    fn()
+    dt = time.perf_counter() - t0
+    cells = cfg.N * cfg.M * nsteps
+    return {"value": cells / dt, "unit": "cell-updates/s", "cores": nt, "kind": kind,
+            "sample": f"{nsteps} step(s) of the full {cfg.N}x{cfg.M} grid from the initial state, FP64"}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="fp64_godunov", choices=["fp64_godunov", "fp32_godunov"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    from asteriy_2d_gb300 import solver
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        cfg = make_config("fp64_godunov")
+        s0, u0 = solver.fill_blast(cfg)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as O
+        nt = os.cpu_count() or 1
+        kind = "reference" if O.have_ref() else "port"
+        run = (lambda n: O.ref_run_composed(cfg, s0, u0, n, nthreads=nt)) if kind == "reference" else \
+            (lambda n: O.run(cfg, s0, u0, n, nthreads=nt))
+        if args.warmup:
+            run(1)
+        t0 = time.perf_counter()
+        run(args.steps)
+        dt = time.perf_counter() - t0
+        v = cfg.N * cfg.M * args.steps / dt
+        line = {"impl": "reference", "metric": "cell-updates/s", "value": v, "unit": "cell-updates/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": 1 if args.warmup else 0,
+                "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "dtype": "f64",
+                "data": "synthetic", "scaling": "weak", "vs_baseline": None,
+                "config": {"workload": f"blast {N_Z}x{M_R}, exact Godunov + minmod, axisymmetric",
+                           "form": "fp64_godunov", "parallelism": "host threads"},
+                "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nt, "kind": kind,
+                                 "sample": f"{args.steps} full steps of the {N_Z}x{M_R} grid"},
+                "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    cfg = make_config(args.form)
+    s0, u0 = solver.fill_blast(cfg)
+    # the other forms, for the side-by-side table
+    forms = {}
+    for form in ("fp64_godunov", "fp32_godunov"):
+        if form == args.form:
+            continue
+        sec, ms = time_form(form, s0, u0, max(2, args.steps // 2), 2, torch)
+        forms[form] = {"value": cfg.N * cfg.M * max(2, args.steps // 2) / sec, "ms_per_step": ms}
+
+    if ws > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    sec, ms = time_form(args.form, s0, u0, args.steps, args.warmup, torch)
+    clocks = sampler.stop()
+    if ws > 1:
+        t = torch.tensor([sec], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sec = t.item()
+    cells = cfg.N * cfg.M
+    value = ws * cells * args.steps / sec
+    forms[args.form] = {"value": cells * args.steps / sec, "ms_per_step": sec * 1e3 / args.steps}
+
+    e2e_steps = max(3, args.steps // 4)
+    esec, bi, bo = time_e2e(args.form, s0, u0, e2e_steps, torch)
+    hbm, src = peaks()
+    prec = "fp64" if args.form.startswith("fp64") else "fp32"
+    achieved = BYTES_PER_CELL[prec] * cells / (sec / args.steps) / 1e9
+    line = {
+        "metric": "cell-updates/s at 4096x2048 (exact Godunov + minmod)",
+        "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
+        "config": {"workload": f"blast {N_Z}x{M_R}, exact Godunov + minmod, axisymmetric, CFL 0.4",
+                   "form": args.form, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (state ping-pong 2x%d MB)" % (cells * BYTES_PER_CELL[prec] // 2 // 2**20)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": src, "traffic": None,
+                     "note": "algorithmic bytes = %d B/cell-update (one state read + one write)" % BYTES_PER_CELL[prec]},
+        "forms": forms,
+        "e2e": {"value": cells * e2e_steps / esec, "unit": "cell-updates/s", "h2d_bytes_per_step": bi,
+                "d2h_bytes_per_step": bo,
+                "note": "per step: ast_set_state from pinned host, ast_step(1), ast_get_state to pinned host"},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(make_config("fp64_godunov"), s0, u0, 1)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -138,6 +138,12 @@ typedef struct ast_solver ast_solver;
 /* ---- library ----------------------------------------------------------- */
 int         ast_abi_version(void);
 const char* ast_strerror(int code);
+/* Text of the last failure on the calling thread ("" if none). */
+const char* ast_last_error(void);
+/* sizeof(ast_config) and sizeof(ast_stats) as compiled into the library,
+   for bindings that mirror the structures. */
+size_t      ast_sizeof_config(void);
+size_t      ast_sizeof_stats(void);
 /* Fills *cfg with the reference's macro values: gamma 5/3, CFL 0.05,
    HLL + minmod, planar, FP64, reflect on r sides, outflow on z sides,
    dt_first 1e-9, dt_cap 1000, p_floor 1e-6, riemann_tol 1e-9. */
@@ -160,6 +166,10 @@ int ast_get_clock(ast_solver* solver, double* T_do, double* TT, int64_t* step);
 int ast_step(ast_solver* solver, int nsteps);
 int ast_synchronize(ast_solver* solver);
 int ast_get_stats(ast_solver* solver, ast_stats* out, int reset);
+/* Device view of the current state: four planes rho, p, v_z, v_r of M rows
+   with row pitch *ld elements of *elem_bytes bytes (8 = FP64, 4 = FP32),
+   plane stride ld*M.  Valid until the next ast_step / ast_set_state. */
+int ast_device_state(ast_solver* solver, void** planes, int64_t* ld, int* elem_bytes);
 
 /* ---- kernel-level drop-in ----------------------------------------------
  * One step on reference-layout device arrays, the replacement for

@@ -560,9 +560,25 @@ static void ora_get(const ora_grid* g, const ast_config* c, const d2* s, const d
     }
 }
 
+#ifdef ORA_WITH_REF
+/* Built into oracle/_ref/libastref.so: every face is evaluated by the
+   reference's own function (HLL kernel.cu:1399, HLLC_2d_Korolkov
+   Gas_Dinamic.cu:1814, Godunov_Solver_Alexashov kernel.cu:128), compiled for
+   the host by oracle/ref_driver.cpp; gamma and CFL come from ref_set_params. */
+double ref_face(int which, const double* sL, const double* uL, const double* sR, const double* uR,
+                double n1, double n2, double rad, double* out);
+#endif
+
 static double ora_flux(int flux, const ora_phys* ph, ora_stats* st, d2 Ls, d2 Lu, d2 Rs, d2 Ru,
                        double n1, double n2, d2* Ps, d2* Pu, double rad)
 {
+#ifdef ORA_WITH_REF
+    (void)ph; (void)st;
+    double sl[2] = {Ls.x, Ls.y}, ul[2] = {Lu.x, Lu.y}, sr[2] = {Rs.x, Rs.y}, ur[2] = {Ru.x, Ru.y}, out[4];
+    double t = ref_face(flux, sl, ul, sr, ur, n1, n2, rad, out);
+    Ps->x = out[0]; Pu->x = out[1]; Pu->y = out[2]; Ps->y = out[3];
+    return t;
+#endif
     if (flux == AST_FLUX_HLLC) return hllc(ph, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad, 0);
     if (flux == AST_FLUX_GODUNOV) return godunov(ph, st, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
     return hll(ph, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
@@ -669,7 +685,7 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
             t = ora_flux(c->flux, ph, st, s_1, u_1, s_2, u_2, 1, 0, &Ps12, &Pu12, dx);
         }
     } else {
-        t = hll(ph, s_1, u_1, s_2, u_2, 1, 0, &Ps12, &Pu12, dx);
+        t = ora_flux(AST_FLUX_HLL, ph, st, s_1, u_1, s_2, u_2, 1, 0, &Ps12, &Pu12, dx);
     }
     tmin = fmin(tmin, t);
     /* faces 13 (-r) and 15 (+r), rad dy (kernel.cu:2816-2840) */
@@ -688,9 +704,9 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
             tmin = fmin(tmin, t);
         }
     } else {
-        t = hll(ph, s_1, u_1, s_3, u_3, 0, -1, &Ps13, &Pu13, dy);
+        t = ora_flux(AST_FLUX_HLL, ph, st, s_1, u_1, s_3, u_3, 0, -1, &Ps13, &Pu13, dy);
         tmin = fmin(tmin, t);
-        t = hll(ph, s_1, u_1, s_5, u_5, 0, 1, &Ps15, &Pu15, dy);
+        t = ora_flux(AST_FLUX_HLL, ph, st, s_1, u_1, s_5, u_5, 0, 1, &Ps15, &Pu15, dy);
         tmin = fmin(tmin, t);
     }
     /* face 14: -z, rad dx (kernel.cu:2843-2857) */
@@ -702,7 +718,7 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
             t = ora_flux(c->flux, ph, st, s_1, u_1, s_4, u_4, -1, 0, &Ps14, &Pu14, dx);
         }
     } else {
-        t = hll(ph, s_1, u_1, s_4, u_4, -1, 0, &Ps14, &Pu14, dx);
+        t = ora_flux(AST_FLUX_HLL, ph, st, s_1, u_1, s_4, u_4, -1, 0, &Ps14, &Pu14, dx);
     }
     tmin = fmin(tmin, t);
 

@@ -5,7 +5,10 @@ TEST INFRASTRUCTURE ONLY.  Recipe:
      oracle/_ref/ref_extract.inc (each range preceded by a #line directive
      naming its origin, and checked against the function it must start with);
   2. compile oracle/ref_driver.cpp, which includes oracle/ref_shim.h and that
-     file, with g++ -fopenmp -ffp-contract=off into oracle/_ref/libastref.so.
+     file, with g++ -fopenmp -ffp-contract=off into oracle/_ref/libastref.so,
+     together with the oracle's step loop (oracle/ast_oracle.c built with
+     -DORA_WITH_REF) so that any configuration can be stepped with the
+     reference's own face functions (the CPU baseline of the benchmark).
 
 oracle/_ref/ is git-ignored.  The reference cannot be built as a binary
 unmodified (kernel.cu:20 declares an add2 overload that is never defined and
@@ -66,8 +69,12 @@ def compile_ref(cxx="g++"):
     if not os.path.exists(inc):
         raise FileNotFoundError(inc)
     so = os.path.join(OUT, "libastref.so")
+    obj = os.path.join(OUT, "ast_oracle_ref.o")
+    # the oracle's step loop, with every face evaluated by the reference's functions
+    subprocess.run(["gcc", "-O2", "-std=c99", "-fopenmp", "-ffp-contract=off", "-fPIC", "-DORA_WITH_REF", "-c",
+                    os.path.join(HERE, "ast_oracle.c"), "-o", obj], check=True)
     cmd = [cxx, "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-w",
-           "-I", HERE, os.path.join(HERE, "ref_driver.cpp"), "-o", so]
+           "-I", HERE, os.path.join(HERE, "ref_driver.cpp"), obj, "-o", so]
     subprocess.run(cmd, check=True)
     return so
 

@@ -81,6 +81,8 @@ def ref():
         R.ref_kernel_run.restype = C.c_int
         R.ref_kernel_run.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_int, _dp, _dp,
                                      C.POINTER(C.c_longlong), C.c_int]
+        R.ora_run.restype = C.c_int
+        R.ora_run.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _i64p, C.c_int, _i64p]
         R.ref_diag_count.restype = C.c_longlong
         R.ref_max_threads.restype = C.c_int
         _ref = R
@@ -159,3 +161,20 @@ def ref_run(kernel, cfg, s, u, nsteps, method=0, nthreads=1):
     ref().ref_kernel_run(kernel, _ptr(s), _ptr(u), nsteps, method, C.byref(tdo), C.byref(tt),
                          C.byref(st), nthreads)
     return s, u, tdo.value, tt.value, st.value
+
+
+def ref_run_composed(cfg, s, u, nsteps, nthreads=1):
+    """The oracle's step loop with every face evaluated by the reference's own
+    HLL / HLLC / Godunov functions (any configuration).  Returns like run()."""
+    ref_set(cfg)
+    s = np.array(s, dtype=np.float64, order="C")
+    u = np.array(u, dtype=np.float64, order="C")
+    tdo = C.c_double(cfg.dt_first)
+    tt = C.c_double(0.0)
+    st = C.c_int64(0)
+    cnt = np.zeros(10, dtype=np.int64)
+    rc = ref().ora_run(C.byref(cfg), _ptr(s), _ptr(u), nsteps, C.byref(tdo), C.byref(tt), C.byref(st),
+                       nthreads, cnt.ctypes.data_as(_i64p))
+    if rc != 0:
+        raise RuntimeError(f"ora_run failed: {rc}")
+    return s, u, tdo.value, tt.value, st.value, cnt

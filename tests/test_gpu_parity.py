@@ -1,0 +1,170 @@
+"""Parity of the CUDA step with the oracle (and through it, the reference).
+
+FP64 bar: relative L-infinity error <= 1e-10 per variable after 100 steps
+(max |gpu - oracle| / max |oracle|), shock positions identical to the cell,
+and the clock (T_do, TT, step) equal to the oracle's to 1e-12 relative.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import golden_configs as G
+import pyoracle as O
+from asteriy_2d_gb300 import abi as A
+from asteriy_2d_gb300 import problems, solver
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+NT = os.cpu_count() or 1
+
+
+def rel_linf(a, b):
+    return np.max(np.abs(a - b), axis=0) / np.maximum(np.max(np.abs(b), axis=0), 1e-300)
+
+
+def run_gpu(cfg, s0, u0, nsteps):
+    with solver.Solver(cfg) as S:
+        S.set_state(s0, u0)
+        S.step(nsteps)
+        s, u = S.get_state()
+        clk = S.clock()
+        st = S.stats()
+    return s, u, clk, st
+
+
+def assert_parity(cfg, s0, u0, nsteps, tol=TOL):
+    s, u, (tdo, tt, step), _ = run_gpu(cfg, s0, u0, nsteps)
+    os_, ou, otdo, ott, ost, _ = O.run(cfg, s0, u0, nsteps, nthreads=NT)
+    es, eu = rel_linf(s, os_), rel_linf(u, ou)
+    assert np.all(es <= tol) and np.all(eu <= tol), (es, eu)
+    assert step == ost
+    assert abs(tdo - otdo) <= 1e-12 * otdo and abs(tt - ott) <= 1e-12 * ott, (tdo, otdo, tt, ott)
+    return s, u, os_, ou
+
+
+def shock_cells(s, cfg):
+    rho = s[:, 0].reshape(cfg.M, cfg.N)
+    return np.argmax(np.abs(np.diff(rho, axis=1)), axis=1)
+
+
+def test_blast_hll_minmod_fp64_256x128_100_steps():
+    cfg = problems.blast_config(256, 128)
+    s0, u0 = solver.fill_blast(cfg)
+    s, u, os_, ou = assert_parity(cfg, s0, u0, 100)
+    assert np.array_equal(shock_cells(s, cfg), shock_cells(os_, cfg))
+
+
+@pytest.mark.parametrize("flux", [A.FLUX_HLLC, A.FLUX_GODUNOV])
+def test_blast_other_fluxes(flux):
+    cfg = problems.blast_config(128, 64, flux=flux)
+    s0, u0 = solver.fill_blast(cfg)
+    s, u, os_, ou = assert_parity(cfg, s0, u0, 100)
+    assert np.array_equal(shock_cells(s, cfg), shock_cells(os_, cfg))
+
+
+def test_wind_counterflow_hllc_fixed_sphere():
+    cfg = problems.wind_config(128, 64)
+    s0, u0 = solver.fill_wind(cfg)
+    assert_parity(cfg, s0, u0, 60)
+
+
+@pytest.mark.parametrize("fname,cfg", [
+    ("step_tvd.npz", G.tvd_config()),
+    ("step_mk_hll.npz", G.add_mk_config(0)),
+    ("step_mk_god.npz", G.add_mk_config(2)),
+])
+def test_reference_kernel_fixtures(fname, cfg):
+    """Kernel_TVD and add_MK outputs recorded from the reference itself."""
+    d = golden(fname)
+    s, u, (tdo, tt, step), _ = run_gpu(cfg, d["s0"], d["u0"], int(d["nsteps"]))
+    assert np.all(rel_linf(s, d["s"]) <= TOL) and np.all(rel_linf(u, d["u"]) <= TOL)
+    assert step == int(d["steps"]) and abs(tdo - float(d["T_do"])) <= 1e-12 * float(d["T_do"])
+
+
+@pytest.mark.parametrize("N,M", [(37, 21), (4, 4), (33, 17), (65, 5)])
+def test_ragged_and_minimal_grids(N, M):
+    cfg = problems.blast_config(N, M, flux=A.FLUX_HLLC)
+    rng = np.random.default_rng(N * 100 + M)
+    s0, u0 = G.random_state(N * M, rng)
+    assert_parity(cfg, s0, u0, 20)
+
+
+@pytest.mark.parametrize("geom", [A.GEOM_PLANAR, A.GEOM_AXISYM])
+@pytest.mark.parametrize("kinds", [(A.BC_REFLECT,) * 4, (A.BC_SUCTION, A.BC_FIXED, A.BC_REFLECT, A.BC_OUTFLOW)])
+def test_boundary_kinds(geom, kinds):
+    cfg = problems.blast_config(48, 24, flux=A.FLUX_GODUNOV)
+    cfg.geom = geom
+    for side, kind in enumerate(kinds):
+        A.set_bc(cfg, side, kind, 1.2, 3.0, -0.7, 0.1)
+    rng = np.random.default_rng(7)
+    s0, u0 = G.random_state(48 * 24, rng)
+    assert_parity(cfg, s0, u0, 20)
+
+
+def test_raw_drop_in_matches_oracle_over_steps():
+    """ast_step_raw + ast_funk_time replace Kernel_TVD + funk_time in the
+    reference's host loop (kernel.cu:3868-3947)."""
+    import torch
+    cfg = G.tvd_config()
+    d = golden("step_tvd.npz")
+    dev = torch.device("cuda:0")
+    bufs = [torch.tensor(d["s0"], device=dev), torch.tensor(d["u0"], device=dev)]
+    bufs2 = [torch.empty_like(bufs[0]), torch.empty_like(bufs[1])]
+    T = torch.tensor([1e7], dtype=torch.float64, device=dev)
+    T_do = torch.tensor([cfg.dt_first], dtype=torch.float64, device=dev)
+    TT = torch.zeros(1, dtype=torch.float64, device=dev)
+    i = torch.zeros(1, dtype=torch.int32, device=dev)
+    for _ in range(int(d["nsteps"])):
+        solver.step_raw(bufs[0].data_ptr(), bufs[1].data_ptr(), bufs2[0].data_ptr(), bufs2[1].data_ptr(),
+                        T.data_ptr(), T_do.data_ptr(), TT.data_ptr(), cfg)
+        solver.funk_time(T.data_ptr(), T_do.data_ptr(), TT.data_ptr(), i.data_ptr())
+        bufs, bufs2 = bufs2, bufs
+    torch.cuda.synchronize()
+    s, u = bufs[0].cpu().numpy(), bufs[1].cpu().numpy()
+    assert np.all(rel_linf(s, d["s"]) <= TOL) and np.all(rel_linf(u, d["u"]) <= TOL)
+    assert int(i.item()) == int(d["steps"]) and T.item() == 1e7
+    assert abs(T_do.item() - float(d["T_do"])) <= 1e-12 * float(d["T_do"])
+
+
+def test_deterministic_bitwise():
+    cfg = problems.blast_config(96, 48, flux=A.FLUX_GODUNOV)
+    s0, u0 = solver.fill_blast(cfg)
+    a = run_gpu(cfg, s0, u0, 30)
+    b = run_gpu(cfg, s0, u0, 30)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
+
+
+def test_mass_conserved_in_closed_planar_box():
+    cfg = problems.blast_config(64, 64, flux=A.FLUX_HLLC)
+    cfg.geom = A.GEOM_PLANAR
+    for side in range(4):
+        A.set_bc(cfg, side, A.BC_REFLECT)
+    s0, u0 = solver.fill_blast(cfg)
+    s, u, _, _ = run_gpu(cfg, s0, u0, 200)
+    assert abs(s[:, 0].sum() - s0[:, 0].sum()) <= 1e-12 * s0[:, 0].sum()
+
+
+def test_graph_block_and_single_steps_agree():
+    cfg = problems.blast_config(64, 32)
+    s0, u0 = solver.fill_blast(cfg)
+    with solver.Solver(cfg) as S:
+        S.set_state(s0, u0)
+        S.step(37)
+        a = S.get_state()
+    with solver.Solver(cfg) as S:
+        S.set_state(s0, u0)
+        for _ in range(37):
+            S.step(1)
+        b = S.get_state()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_stats_count_riemann_work():
+    cfg = problems.blast_config(64, 32, flux=A.FLUX_GODUNOV)
+    cfg.collect_stats = 1
+    s0, u0 = solver.fill_blast(cfg)
+    _, _, _, st = run_gpu(cfg, s0, u0, 20)
+    assert st["newton_calls"] + st["bisect_calls"] > 0 and st["newton_max_iters"] >= 1
+    assert st["status"] & A.AST_ST_NONFINITE == 0

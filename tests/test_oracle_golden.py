@@ -81,3 +81,19 @@ def test_oracle_matches_live_reference_on_fresh_inputs():
     o = O.run(cfg, s, u, 8)
     np.testing.assert_array_equal(r[0], o[0])
     np.testing.assert_array_equal(r[1], o[1])
+
+
+@pytest.mark.skipif(not O.have_ref(), reason="reference functions not built here")
+@pytest.mark.parametrize("flux", [O.FACE_HLL, O.FACE_HLLC, O.FACE_GODUNOV])
+def test_composed_step_with_reference_faces_is_bitwise(flux):
+    """Blast problem (axisymmetric, minmod) stepped with the reference's own
+    face functions equals the oracle bit for bit."""
+    from asteriy_2d_gb300 import problems
+    cfg = problems.blast_config(64, 32, flux=flux)
+    s0 = np.stack([np.ones(64 * 32), np.where(np.arange(64 * 32) % 7 == 0, 10.0, 0.1)], 1)
+    u0 = np.zeros((64 * 32, 2))
+    a = O.run(cfg, s0, u0, 15)
+    b = O.ref_run_composed(cfg, s0, u0, 15)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    assert a[2] == b[2]
