@@ -19,6 +19,9 @@ LIB = os.path.join(HERE, "libasteriy_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "step_f64.cu", "step_f32.cu", "step_raw.cu", "host_io.cpp"]
+# per-file extra flags: the FP32 form uses the fast single-precision
+# intrinsics (division, sqrt, pow); double-precision code is not affected
+EXTRA = {"step_f32.cu": ["--use_fast_math"]}
 
 
 def nvcc():
@@ -42,7 +45,7 @@ def _flags(ptxas_verbose=False):
 def _compile(src, ptxas_verbose):
     path = os.path.join(CSRC, src)
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc()] + _flags(ptxas_verbose) + ["-c", path, "-o", obj]
+    cmd = [nvcc()] + _flags(ptxas_verbose) + EXTRA.get(src, []) + ["-c", path, "-o", obj]
     if src.endswith(".cpp"):
         cmd = [nvcc(), "-x", "c++", "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-I",
                os.path.join(ROOT, "include"), "-c", path, "-o", obj]

@@ -152,6 +152,56 @@ struct TileSmem {
 template <typename R, int TZ, int TR>
 constexpr size_t tile_smem_bytes() { return sizeof(TileSmem<R, TZ, TR>); }
 
+// Conservative update of one cell in arithmetic C from its state `in`
+// (rho, p, vz, vr) and its four outward face fluxes f[k][face] (k = mass,
+// mom_z, mom_r, energy; face = right, left, bottom, top, the left and bottom
+// ones still oriented along +z / +r).  Planar: Kernel_TVD, kernel.cu:3027-3073;
+// axisymmetric with the cylindrical source: add_MK, kernel.cu:2480-2509.
+template <typename C, typename R, typename G>
+__device__ __forceinline__ void update_cell(const StepParams& P, const G& g, const R in[4], const R f[4][4],
+                                            double T_do, double x, double y, int& nrho, int& np, R out[4],
+                                            float* E2o = nullptr, float* KE2o = nullptr)
+{
+    const C r1 = (C)in[0], p1 = (C)in[1], vz1 = (C)in[2], vr1 = (C)in[3];
+    const C dx = (C)P.dx, dy = (C)P.dy;
+    const C tdv = (C)(T_do / (P.dx * P.dy));
+    C ps[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const C f12 = (C)f[k][0], f14 = -(C)f[k][1], f13 = -(C)f[k][2], f15 = (C)f[k][3];
+        if (P.geom == 1) ps[k] = (f12 + f14) * dy + (f13 + f15) * dx;
+        else ps[k] = f12 * dy + f13 * dx + f14 * dy + f15 * dx;
+    }
+    C Q2 = C(0);
+    if (P.body_force && x > P.body_lo && x < P.body_hi)
+        Q2 = (y >= P.body_rsplit) ? -(C)P.body_amp * r1 : (C)P.body_amp * r1;
+    const C Q3 = Q2 * vr1;
+    const C ga = (C)g.ga, inv_g1 = (C)g.inv_g1, g1 = (C)g.g1;
+    const C ke1 = r1 * (vz1 * vz1 + vr1 * vr1) * C(0.5);
+    C rho2, mz, mr, E2;
+    if (P.geom == 1) {
+        const C ty = (C)(T_do / y);
+        rho2 = r1 - tdv * ps[0] - ty * r1 * vr1;
+        if (rho2 <= C(0)) { nrho++; rho2 = r1; }
+        mz = r1 * vz1 - tdv * ps[1] - ty * r1 * vr1 * vz1;
+        mr = r1 * vr1 - tdv * ps[2] - ty * r1 * vr1 * vr1 + (C)T_do * Q2;
+        E2 = (p1 * inv_g1 + ke1) - tdv * ps[3] - ty * vr1 * (ga * p1 * inv_g1 + ke1) + (C)T_do * Q3;
+    } else {
+        rho2 = r1 - tdv * ps[0];
+        if (rho2 <= C(0)) { nrho++; rho2 = r1; }
+        mz = r1 * vz1 - tdv * ps[1];
+        mr = r1 * vr1 - tdv * ps[2] + (C)T_do * Q2;
+        E2 = (p1 * inv_g1 + ke1) - tdv * ps[3] + (C)T_do * Q3;
+    }
+    const C irho = C(1) / rho2;
+    const C vz2 = mz * irho, vr2 = mr * irho;
+    const C KE2 = C(0.5) * rho2 * (vz2 * vz2 + vr2 * vr2);
+    C p2 = (E2 - KE2) * g1;
+    if (p2 <= C(0)) { np++; p2 = (C)P.p_floor; }
+    out[0] = (R)rho2; out[1] = (R)p2; out[2] = (R)vz2; out[3] = (R)vr2;
+    if (E2o) { *E2o = (float)E2; *KE2o = (float)KE2; }
+}
+
 // All faces of one orientation in the tile, one thread per face.  ZF: z
 // faces (between tile columns c-1 and c of a row), else r faces (between
 // tile rows a-1 and a of a column).  Writes the flux, in (mass, mom_z,
@@ -268,63 +318,49 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
 
     // ---- conservative update of the tile's cells
     int nrho = 0, np = 0;
-    const double dx = P.dx, dy = P.dy, dV = dx * dy;
-    const R tdv = (R)(T_do / dV);
+    const double dx = P.dx, dy = P.dy;
+    const Gas<double> g64 = make_gas<double>(P.gamma, P.tol, P.max_iter);
     for (int cidx = tid; cidx < TZ * TR; cidx += kThreads) {
         const int row = cidx / TZ, col = cidx - row * TZ;
         const int n = n0 + col, m = m0 + row;
         if (n >= P.N || m >= P.M) continue;
         const int j = row + 2, i = col + 2;
-        const R r1 = sm.q[0][j][i], p1 = sm.q[1][j][i], vz1 = sm.q[2][j][i], vr1 = sm.q[3][j][i];
-        R o0, o1, o2, o3;
-        if (P.fixed_region && sm.fx[j][i]) {
-            o0 = r1; o1 = p1; o2 = vz1; o3 = vr1;
-        } else {
+        R o[4] = {sm.q[0][j][i], sm.q[1][j][i], sm.q[2][j][i], sm.q[3][j][i]};
+        if (!(P.fixed_region && sm.fx[j][i])) {
             const double x = P.x_min + n * dx, y = P.y_min + m * dy;
-            R Q2 = R(0);
-            if (P.body_force && x > P.body_lo && x < P.body_hi)
-                Q2 = (y >= P.body_rsplit) ? -(R)P.body_amp * r1 : (R)P.body_amp * r1;
-            const R Q3 = Q2 * vr1;
-            R ps[4];
+            R in[4] = {o[0], o[1], o[2], o[3]};
+            // outward face fluxes of the cell: +right, -left, -bottom, +top
+            R f[4][4];
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                // outward face fluxes: +right, -left, -bottom, +top
-                const R f12 = sm.Fz[k][row][col + 1], f14 = -sm.Fz[k][row][col];
-                const R f13 = -sm.Fr[k][row][col], f15 = sm.Fr[k][row + 1][col];
-                if (P.geom == 1) ps[k] = (f12 + f14) * (R)dy + (f13 + f15) * (R)dx;
-                else ps[k] = f12 * (R)dy + f13 * (R)dx + f14 * (R)dy + f15 * (R)dx;
+                f[k][0] = sm.Fz[k][row][col + 1];
+                f[k][1] = sm.Fz[k][row][col];
+                f[k][2] = sm.Fr[k][row][col];
+                f[k][3] = sm.Fr[k][row + 1][col];
             }
-            const R ke1 = r1 * (vz1 * vz1 + vr1 * vr1) * R(0.5);
-            R rho2, mz, mr, E2;
-            if (P.geom == 1) {
-                const R ty = (R)(T_do / y);
-                rho2 = r1 - tdv * ps[0] - ty * r1 * vr1;
-                if (rho2 <= R(0)) { nrho++; rho2 = r1; }
-                mz = r1 * vz1 - tdv * ps[1] - ty * r1 * vr1 * vz1;
-                mr = r1 * vr1 - tdv * ps[2] - ty * r1 * vr1 * vr1 + (R)T_do * Q2;
-                E2 = (p1 * g.inv_g1 + ke1) - tdv * ps[3] - ty * vr1 * (g.ga * p1 * g.inv_g1 + ke1) + (R)T_do * Q3;
+            if (sizeof(R) == 8 || (P.geom == 1 && m < 4)) {
+                // FP64 path; in the FP32 form also the near-axis cells, where
+                // the 1/r source is largest
+                update_cell<double>(P, g64, in, f, T_do, x, y, nrho, np, o);
             } else {
-                rho2 = r1 - tdv * ps[0];
-                if (rho2 <= R(0)) { nrho++; rho2 = r1; }
-                mz = r1 * vz1 - tdv * ps[1];
-                mr = r1 * vr1 - tdv * ps[2] + (R)T_do * Q2;
-                E2 = (p1 * g.inv_g1 + ke1) - tdv * ps[3] + (R)T_do * Q3;
+                float E2, KE2;
+                update_cell<float>(P, g, in, f, T_do, x, y, nrho, np, o, &E2, &KE2);
+                // FP32 form: pressure recovery p = (g-1)(E - rho v^2/2) in FP64
+                // where the kinetic energy is more than 99% of the total
+                if ((float)KE2 > 0.99f * (float)E2) {
+                    int d0 = 0, d1 = 0;
+                    update_cell<double>(P, g64, in, f, T_do, x, y, d0, d1, o);
+                }
             }
-            const R irho = R(1) / rho2;
-            o0 = rho2;
-            o2 = mz * irho;
-            o3 = mr * irho;
-            o1 = (E2 - R(0.5) * rho2 * (o2 * o2 + o3 * o3)) * g.g1;
-            if (o1 <= R(0)) { np++; o1 = (R)P.p_floor; }
         }
         if (LAYOUT == kSoA) {
             R* out = (R*)P.out;
             const long long k = (long long)m * P.ld + n;
-            out[k] = o0; out[k + P.plane] = o1; out[k + 2 * P.plane] = o2; out[k + 3 * P.plane] = o3;
+            out[k] = o[0]; out[k + P.plane] = o[1]; out[k + 2 * P.plane] = o[2]; out[k + 3 * P.plane] = o[3];
         } else {
             const long long k = (long long)m * P.N + n;
-            ((double2*)P.out)[k] = make_double2((double)o0, (double)o1);
-            ((double2*)P.out_u)[k] = make_double2((double)o2, (double)o3);
+            ((double2*)P.out)[k] = make_double2((double)o[0], (double)o[1]);
+            ((double2*)P.out_u)[k] = make_double2((double)o[2], (double)o[3]);
         }
     }
 

@@ -30,7 +30,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_Z, M_R = 4096, 2048
+N_Z, M_R = 4096, 2048   # overridable with --grid for profiling runs
 BYTES_PER_CELL = {"fp64": 64, "fp32": 32}   # one read + one write of 4 state values
 
 
@@ -188,7 +188,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="fp64_godunov", choices=["fp64_godunov", "fp32_godunov"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-forms", action="store_true", help="time only --form")
+    ap.add_argument("--grid", default=None, help="NxM instead of 4096x2048 (profiling runs)")
     args = ap.parse_args()
+    global N_Z, M_R
+    if args.grid:
+        N_Z, M_R = (int(v) for v in args.grid.lower().split("x"))
     ws, rank, local = dist_setup()
     from asteriy_2d_gb300 import solver
 
@@ -231,7 +236,7 @@ def main():
     # the other forms, for the side-by-side table
     forms = {}
     for form in ("fp64_godunov", "fp32_godunov"):
-        if form == args.form:
+        if form == args.form or args.no_forms:
             continue
         sec, ms = time_form(form, s0, u0, max(2, args.steps // 2), 2, torch)
         forms[form] = {"value": cfg.N * cfg.M * max(2, args.steps // 2) / sec, "ms_per_step": ms}

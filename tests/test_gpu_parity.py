@@ -45,8 +45,12 @@ def assert_parity(cfg, s0, u0, nsteps, tol=TOL):
 
 
 def shock_cells(s, cfg):
+    """Per row of cells (fixed r), the z index of the largest density jump in
+    each half of the domain: the blast has one shock on either side of z=0."""
     rho = s[:, 0].reshape(cfg.M, cfg.N)
-    return np.argmax(np.abs(np.diff(rho, axis=1)), axis=1)
+    jump = np.abs(np.diff(rho, axis=1))
+    h = jump.shape[1] // 2
+    return np.stack([np.argmax(jump[:, :h], axis=1), h + np.argmax(jump[:, h:], axis=1)], 1)
 
 
 def test_blast_hll_minmod_fp64_256x128_100_steps():
@@ -56,11 +60,28 @@ def test_blast_hll_minmod_fp64_256x128_100_steps():
     assert np.array_equal(shock_cells(s, cfg), shock_cells(os_, cfg))
 
 
-@pytest.mark.parametrize("flux", [A.FLUX_HLLC, A.FLUX_GODUNOV])
-def test_blast_other_fluxes(flux):
-    cfg = problems.blast_config(128, 64, flux=flux)
+def test_blast_hllc():
+    cfg = problems.blast_config(128, 64, flux=A.FLUX_HLLC)
     s0, u0 = solver.fill_blast(cfg)
     s, u, os_, ou = assert_parity(cfg, s0, u0, 100)
+    assert np.array_equal(shock_cells(s, cfg), shock_cells(os_, cfg))
+
+
+# The exact solver's shock-rarefaction bisection stops on an absolute
+# residual of 10e-10 (devtwo, kernel.cu:685): which bisection iterate first
+# meets it depends on the last bits of pow(), which differ between CUDA and
+# glibc, so p* itself agrees only to about 1e-9 relative.  With the
+# reference's tolerance the step agrees to TOL_GODUNOV; with a tight
+# tolerance the same comparison meets the 1e-10 bar.
+TOL_GODUNOV = 1e-9
+
+
+@pytest.mark.parametrize("riemann_tol,tol", [(10e-10, TOL_GODUNOV), (1e-13, TOL)])
+def test_blast_godunov(riemann_tol, tol):
+    cfg = problems.blast_config(128, 64, flux=A.FLUX_GODUNOV)
+    cfg.riemann_tol = riemann_tol
+    s0, u0 = solver.fill_blast(cfg)
+    s, u, os_, ou = assert_parity(cfg, s0, u0, 100, tol=tol)
     assert np.array_equal(shock_cells(s, cfg), shock_cells(os_, cfg))
 
 
@@ -95,6 +116,7 @@ def test_ragged_and_minimal_grids(N, M):
 @pytest.mark.parametrize("kinds", [(A.BC_REFLECT,) * 4, (A.BC_SUCTION, A.BC_FIXED, A.BC_REFLECT, A.BC_OUTFLOW)])
 def test_boundary_kinds(geom, kinds):
     cfg = problems.blast_config(48, 24, flux=A.FLUX_GODUNOV)
+    cfg.riemann_tol = 1e-13
     cfg.geom = geom
     for side, kind in enumerate(kinds):
         A.set_bc(cfg, side, kind, 1.2, 3.0, -0.7, 0.1)
@@ -168,3 +190,19 @@ def test_stats_count_riemann_work():
     _, _, _, st = run_gpu(cfg, s0, u0, 20)
     assert st["newton_calls"] + st["bisect_calls"] > 0 and st["newton_max_iters"] >= 1
     assert st["status"] & A.AST_ST_NONFINITE == 0
+
+
+@pytest.mark.parametrize("flux", [A.FLUX_HLL, A.FLUX_GODUNOV])
+def test_fp32_form_error_against_fp64_oracle(flux):
+    """Precision form: FP32 state and fluxes, FP64 in the near-axis update,
+    in high-Mach pressure recovery and in the dt reduction.  Density L1
+    error relative to the FP64 oracle stays below 1e-4 after 100 steps."""
+    cfg = problems.blast_config(256, 128, flux=flux, precision=A.PREC_FP32)
+    s0, u0 = solver.fill_blast(cfg)
+    s, u, (tdo, tt, step), _ = run_gpu(cfg, s0, u0, 100)
+    ref = problems.blast_config(256, 128, flux=flux)
+    os_, ou, otdo, ott, ost, _ = O.run(ref, s0, u0, 100, nthreads=NT)
+    l1_rho = np.sum(np.abs(s[:, 0] - os_[:, 0])) / np.sum(np.abs(os_[:, 0]))
+    l1_p = np.sum(np.abs(s[:, 1] - os_[:, 1])) / np.sum(np.abs(os_[:, 1]))
+    assert l1_rho < 1e-4 and l1_p < 1e-4, (l1_rho, l1_p)
+    assert step == ost and abs(tt - ott) < 1e-4 * ott
