@@ -24,6 +24,8 @@ AST_ST_BISECT_CAP = 0x08
 AST_ST_NONFINITE = 0x10
 AST_ST_VACUUM = 0x20
 AST_ST_MLP_FALLBACK = 0x40
+AST_MLP_NPARAM = 1325
+AST_RECORD_FLOATS = 10
 
 FLUX_HLL, FLUX_HLLC, FLUX_GODUNOV = 0, 1, 2
 RECON_NONE, RECON_MINMOD = 0, 1
@@ -55,7 +57,7 @@ class ast_config(C.Structure):
         ("body_rsplit", C.c_double), ("body_amp", C.c_double),
         ("dt_first", C.c_double), ("dt_cap", C.c_double), ("p_floor", C.c_double),
         ("riemann_tol", C.c_double),
-        ("collect_stats", C.c_int32), ("reserved_i", C.c_int32 * 7),
+        ("collect_stats", C.c_int32), ("riemann_newton", C.c_int32), ("reserved_i", C.c_int32 * 6),
         ("reserved_d", C.c_double * 8),
     ]
 

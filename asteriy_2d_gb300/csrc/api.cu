@@ -89,6 +89,11 @@ void fill_params(StepParams& P, const ast_config& c)
     P.geom = c.geom;
     P.grad_p = c.grad_p;
     P.collect_stats = c.collect_stats;
+    // the FP32 form always iterates with the safeguarded Newton: the
+    // reference's absolute bisection tolerance is below FP32 resolution
+    P.riemann_newton = (c.riemann_newton || c.precision == AST_PREC_FP32) ? 1 : 0;
+    P.guess = c.guess;
+    P.rec_every = 1;
     for (int sd = 0; sd < 4; sd++) {
         P.bc_kind[sd] = c.bc[sd].kind;
         P.bc_val[sd][0] = c.bc[sd].rho;
@@ -133,6 +138,10 @@ struct ast_solver {
     cudaGraphExec_t graph = nullptr; // captured block of graph_steps steps
     int graph_steps = 0;
     int graph_cur = -1;              // buffer index the graph starts from
+    float* mlp = nullptr;            // learned start value parameters (device)
+    float* rec = nullptr;            // face recorder buffer (device)
+    unsigned long long* rec_n = nullptr;
+    long long rec_cap = 0;
 };
 
 extern "C" {
@@ -215,6 +224,9 @@ int ast_destroy(ast_solver* S)
     cudaFree(S->clock);
     cudaFree(S->stage_s);
     cudaFree(S->stage_u);
+    cudaFree(S->mlp);
+    cudaFree(S->rec);
+    cudaFree(S->rec_n);
     delete S;
     return AST_OK;
 }
@@ -359,6 +371,8 @@ static int capture_block(ast_solver* S, int count)
 int ast_step(ast_solver* S, int nsteps)
 {
     if (!S || nsteps < 0) return fail(AST_ERR_INVALID, "bad argument");
+    if (S->cfg.flux == AST_FLUX_GODUNOV && S->cfg.guess == AST_GUESS_MLP && S->P.riemann_newton && !S->mlp)
+        return fail(AST_ERR_INVALID, "guess == MLP needs ast_set_mlp first");
     // a captured block of an even number of steps returns to the same
     // buffer, so it can be replayed back to back
     const int block = 16;
@@ -412,6 +426,69 @@ int ast_get_stats(ast_solver* S, ast_stats* out, int reset)
     return AST_OK;
 }
 
+static void drop_graph(ast_solver* S)
+{
+    if (S->graph) {
+        cudaGraphExecDestroy(S->graph);
+        S->graph = nullptr;
+    }
+}
+
+int ast_set_mlp(ast_solver* S, const float* params)
+{
+    if (!S || !params) return fail(AST_ERR_INVALID, "null argument");
+    if (!S->mlp) AST_CUDA(cudaMalloc(&S->mlp, sizeof(float) * AST_MLP_NPARAM));
+    AST_CUDA(cudaMemcpyAsync(S->mlp, params, sizeof(float) * AST_MLP_NPARAM, cudaMemcpyHostToDevice, S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    S->P.mlp = S->mlp;
+    drop_graph(S);
+    return AST_OK;
+}
+
+int ast_record_start(ast_solver* S, int64_t capacity, int every)
+{
+    if (!S || capacity < 1 || every < 1) return fail(AST_ERR_INVALID, "bad argument");
+    if (S->cfg.flux != AST_FLUX_GODUNOV) return fail(AST_ERR_UNSUPPORTED, "the recorder needs the exact solver");
+    cudaFree(S->rec);
+    S->rec = nullptr;
+    if (!S->rec_n) AST_CUDA(cudaMalloc(&S->rec_n, sizeof(unsigned long long)));
+    cudaError_t e = cudaMalloc(&S->rec, sizeof(float) * AST_RECORD_FLOATS * (size_t)capacity);
+    if (e != cudaSuccess) return fail(AST_ERR_NOMEM, "recorder buffer");
+    AST_CUDA(cudaMemsetAsync(S->rec_n, 0, sizeof(unsigned long long), S->stream));
+    S->rec_cap = capacity;
+    S->P.rec = S->rec;
+    S->P.rec_n = S->rec_n;
+    S->P.rec_cap = capacity;
+    S->P.rec_every = every;
+    drop_graph(S);
+    return AST_OK;
+}
+
+int ast_record_stop(ast_solver* S, int64_t* offered)
+{
+    if (!S) return fail(AST_ERR_INVALID, "null solver");
+    unsigned long long n = 0;
+    if (S->rec_n) {
+        AST_CUDA(cudaMemcpyAsync(&n, S->rec_n, sizeof n, cudaMemcpyDeviceToHost, S->stream));
+        AST_CUDA(cudaStreamSynchronize(S->stream));
+    }
+    if (offered) *offered = (int64_t)n;
+    S->P.rec = nullptr;
+    drop_graph(S);
+    return AST_OK;
+}
+
+int ast_record_read(ast_solver* S, float* out, int64_t n)
+{
+    if (!S || !out || n < 0) return fail(AST_ERR_INVALID, "bad argument");
+    if (!S->rec) return fail(AST_ERR_INVALID, "no recorder buffer");
+    n = n < S->rec_cap ? n : S->rec_cap;
+    AST_CUDA(cudaMemcpyAsync(out, S->rec, sizeof(float) * AST_RECORD_FLOATS * (size_t)n, cudaMemcpyDeviceToHost,
+                             S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    return AST_OK;
+}
+
 int ast_device_state(ast_solver* S, void** planes, int64_t* ld, int* elem_bytes)
 {
     if (!S) return fail(AST_ERR_INVALID, "null solver");
@@ -431,6 +508,7 @@ int ast_step_raw(const double* s, const double* u, double* s2, double* u2, doubl
     int rc = ast_config_check(cfg);
     if (rc != AST_OK) return rc;
     if (cfg->precision != AST_PREC_FP64) return fail(AST_ERR_UNSUPPORTED, "raw step is FP64 (reference layout)");
+    if (cfg->guess == AST_GUESS_MLP) return fail(AST_ERR_UNSUPPORTED, "raw step has no learned start value");
     StepParams P;
     fill_params(P, *cfg);
     P.in = s;

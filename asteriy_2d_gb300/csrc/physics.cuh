@@ -225,36 +225,171 @@ __device__ R newton_p(const Gas<R>& g, R enI, R pI, R rI, R cI, R enII, R pII, R
     return pn;
 }
 
-// Exact Godunov flux, sampled at w = 0 (Godunov_Solver_Alexashov,
-// kernel.cu:128-570).  Returns the dt wave speed: max(UU, eps8) with UU the
-// largest wave speed magnitude of the pattern.
+// The exact Riemann problem of one face in the reference's frame, where
+// the side with the lower pressure is side I (kernel.cu:144-184), with the
+// wave-pattern thresholds of kernel.cu:186-231:
+//   pattern 0  vacuum (Udf < Uvk)
+//           1  two rarefactions (Uvk <= Udf <= Urz), p* in closed form
+//           2  shock on side I, rarefaction on side II (Urz < Udf <= Uud),
+//              p* in [pI, pII] (bisection in the reference)
+//           3  two shocks (Udf > Uud), p* > pII (Newton in the reference)
+//           4  no pattern (NaN input)
 template <typename R>
-__device__ R flux_godunov(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR, R unR, R utR, R F[4],
-                          RiemannCount& rc)
+struct RPre {
+    R enI, teI, pI, rI, cI, enII, teII, pII, rII, cII;
+    R Udf, Urz, Uvk;
+    bool swap;
+    int pattern;
+};
+
+template <typename R>
+__device__ __forceinline__ RPre<R> godunov_pre(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR, R unR,
+                                               R utR)
 {
-    R enI = unL, teI = utL, enII = unR, teII = utR;
-    R pI = pL, pII = pR, rI = rL, rII = rR;
-    const bool swap = pI > pII;
-    if (swap) {
-        enI = -unR; teI = utR; pI = pR; rI = rR;
-        enII = -unL; teII = utL; pII = pL; rII = rL;
+    RPre<R> q;
+    q.swap = pL > pR;
+    if (q.swap) {
+        q.enI = -unR; q.teI = utR; q.pI = pR; q.rI = rR;
+        q.enII = -unL; q.teII = utL; q.pII = pL; q.rII = rL;
+    } else {
+        q.enI = unL; q.teI = utL; q.pI = pL; q.rI = rL;
+        q.enII = unR; q.teII = utR; q.pII = pR; q.rII = rR;
     }
-    R cI = (rI != R(0)) ? sqrt(g.ga * pI / rI) : R(0);
-    R cII = (rII != R(0)) ? sqrt(g.ga * pII / rII) : R(0);
-    R a = sqrt(rI * (g.g2 * pII + g.g1 * pI) / R(2));
-    R Uud = (pII - pI) / a;
-    R Urz = R(-2) * cII / g.g1 * (R(1) - pow(pI / pII, g.gm));
-    R Uvk = R(-2) * (cII + cI) / g.g1;
-    R Udf = enI - enII;
-    R en, p, r, te, UU;
-    // Sampling at w = 0.  The reference tests the fan intervals with
-    // independent ifs (kernel.cu:322-363, 419-476, 502-543), so a later
-    // interval overrides an earlier one; the same order is kept here.
+    q.cI = (q.rI != R(0)) ? sqrt(g.ga * q.pI / q.rI) : R(0);
+    q.cII = (q.rII != R(0)) ? sqrt(g.ga * q.pII / q.rII) : R(0);
+    const R a = sqrt(q.rI * (g.g2 * q.pII + g.g1 * q.pI) / R(2));
+    const R Uud = (q.pII - q.pI) / a;
+    q.Urz = R(-2) * q.cII / g.g1 * (R(1) - pow(q.pI / q.pII, g.gm));
+    q.Uvk = R(-2) * (q.cII + q.cI) / g.g1;
+    q.Udf = q.enI - q.enII;
+    if (q.Udf < q.Uvk) q.pattern = 0;
+    else if (q.Udf <= q.Urz) q.pattern = 1;
+    else if (q.Udf <= Uud) q.pattern = 2;
+    else if (q.Udf > Uud) q.pattern = 3;
+    else q.pattern = 4;
+    return q;
+}
+
+// p* of patterns 2 and 3 as the reference finds it: bisection on [pI, pII]
+// or Newton from the acoustic start value (kernel.cu:220-231, 641-642)
+template <typename R>
+__device__ __forceinline__ R solve_p_reference(const Gas<R>& g, const RPre<R>& q, RiemannCount& rc)
+{
+    if (q.pattern == 2) return bisect_p(g, q.enI, q.pI, q.rI, q.cI, q.enII, q.pII, q.cII, rc);
+    const R p0 = (q.pI * q.rII * q.cII + q.pII * q.rI * q.cI + (q.enI - q.enII) * q.rI * q.cI * q.rII * q.cII) /
+                 (q.rI * q.cI + q.rII * q.cII);
+    return newton_p(g, q.enI, q.pI, q.rI, q.cI, q.enII, q.pII, q.rII, q.cII, p0, rc);
+}
+
+// The acoustic (PVRS-type) start value of the reference, kept inside the
+// pattern's bracket: [pI, pII] for pattern 2, above pII for pattern 3.
+template <typename R>
+__device__ __forceinline__ R pvrs_guess(const RPre<R>& q)
+{
+    R p0 = (q.pI * q.rII * q.cII + q.pII * q.rI * q.cI + (q.enI - q.enII) * q.rI * q.cI * q.rII * q.cII) /
+           (q.rI * q.cI + q.rII * q.cII);
+    if (q.pattern == 2) p0 = fmin(fmax(p0, q.pI), q.pII);
+    else p0 = fmax(p0, q.pII);
+    return p0;
+}
+
+// true when p0 can start the Newton iteration of the pattern: finite and
+// inside the pattern's bracket
+template <typename R>
+__device__ __forceinline__ bool in_basin(const RPre<R>& q, R p0)
+{
+    if (!(p0 == p0) || !(p0 > R(0))) return false;
+    if (q.pattern == 2) return p0 >= q.pI && p0 <= q.pII;
+    return p0 >= q.pII && p0 < R(1e30);
+}
+
+// Safeguarded Newton on the full pressure function
+//   f(p) = f_I(p) + f_II(p) - (enI - enII),
+// f_K the shock branch (kernel.cu:656-662) for p > p_K and the rarefaction
+// branch (lev, kernel.cu:759) for p <= p_K, from start value p0 to the
+// relative change tol.  An iterate that leaves the bracket of the root is
+// replaced by a bisection step.
+template <typename R>
+__device__ R solve_p_newton(const Gas<R>& g, const RPre<R>& q, R p0, R tol, RiemannCount& rc)
+{
+    R lo = (q.pattern == 2) ? q.pI : q.pII;
+    R hi = (q.pattern == 2) ? q.pII : R(INFINITY);
+    const R dU = q.enI - q.enII;
+    const R b = R(3) * g.ga - R(1);
+    R p = p0;
+    int k = 0;
+    for (;;) {
+        k++;
+        R f = -dU, df = R(0);
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+            const R pK = side ? q.pII : q.pI, rK = side ? q.rII : q.rI, cK = side ? q.cII : q.cI;
+            if (p > pK) {
+                const R qq = g.gp * p / pK + g.gm, sq = sqrt(qq);
+                f += (p - pK) / (rK * cK * sq);
+                df += ((g.ga + R(1)) * p / pK + b) / (R(4) * g.ga * rK * cK * qq * sq);
+            } else {
+                const R t = pow(p / pK, g.gm);
+                f += R(2) / g.g1 * cK * (t - R(1));
+                df += t / (rK * cK) * (pK / p);
+            }
+        }
+        if (f < R(0)) lo = p; else hi = p;
+        R pn = p - f / df;
+        if (!(pn > lo && pn < hi)) pn = (hi < R(INFINITY)) ? R(0.5) * (lo + hi) : R(2) * p;
+        const bool done = fabs(pn - p) <= tol * p;
+        p = pn;
+        if (done) break;
+        if (k >= g.max_iter) { rc.status |= 0x04u; break; }
+    }
+    rc.newton_calls++;
+    rc.newton_iters += k;
+    if (k > rc.newton_max) rc.newton_max = k;
+    return p;
+}
+
+// Mass-flux coefficient of a rarefaction, g_m rho c (1 - x)/(1 - x^g_m) with
+// x = p/p_K, as the reference forms it (kernel.cu:297-304, 371-389): the
+// limit rho c when |p - p_K| < eps.  In FP32 the quotient cancels
+// catastrophically near x = 1, so there the three-term series in d = 1 - x
+// (d/(1-(1-d)^g) expanded about d = 0) is used for |d| < 0.02.
+template <typename R>
+__device__ __forceinline__ R rare_coef(const Gas<R>& g, R rK, R cK, R p, R pK)
+{
+    return (fabs(p - pK) < g.eps) ? rK * cK : g.gm * rK * cK * (R(1) - p / pK) / (R(1) - pow(p / pK, g.gm));
+}
+
+template <>
+__device__ __forceinline__ float rare_coef<float>(const Gas<float>& g, float rK, float cK, float p, float pK)
+{
+    const float d = 1.0f - p / pK;
+    if (fabsf(d) < 0.02f) {
+        const float a = 0.5f * (g.gm - 1.0f);
+        const float b = (g.gm - 1.0f) * (g.gm - 2.0f) * (1.0f / 6.0f);
+        const float c = (g.gm - 1.0f) * (g.gm - 2.0f) * (g.gm - 3.0f) * (1.0f / 24.0f);
+        return rK * cK * (1.0f + d * (a + d * ((a * a - b) + d * (a * a * a - 2.0f * a * b + c))));
+    }
+    return g.gm * rK * cK * d / (1.0f - powf(1.0f - d, g.gm));
+}
+
+// Sampling of the solution at w = 0 and the face flux (kernel.cu:233-568).
+// p: the solved p* for patterns 2 and 3 (ignored otherwise).  Returns the dt
+// wave speed max(UU, eps8), UU the largest wave speed of the pattern.
+template <typename R>
+__device__ R godunov_sample(const Gas<R>& g, const RPre<R>& q, R p, R F[4], RiemannCount& rc)
+{
+    const R enI = q.enI, teI = q.teI, pI = q.pI, rI = q.rI, cI = q.cI;
+    const R enII = q.enII, teII = q.teII, pII = q.pII, rII = q.rII, cII = q.cII;
+    R en, r, te, UU;
+    // The reference tests the fan intervals with independent ifs
+    // (kernel.cu:322-363, 419-476, 502-543), so a later interval overrides
+    // an earlier one; the same order is kept here.
     const R w = R(0);
-    en = p = r = te = UU = R(0);
-    if (Udf < Uvk) {
+    en = r = te = UU = R(0);
+    if (q.pattern == 0) {
         // vacuum between two rarefactions
         rc.status |= 0x20u;
+        p = R(0);
         R dI = enI - cI, ddI = enI + R(2) / g.g1 * cI;
         R dII = enII + cII, ddII = enII - R(2) / g.g1 * cII;
         UU = fmax(fmax(fabs(dI), fabs(dII)), fmax(fabs(ddII), fabs(ddI)));
@@ -269,12 +404,11 @@ __device__ R flux_godunov(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR,
             en = w - ce; p = pII * pow(ce / cII, R(1) / g.gm); r = g.ga * p / ce / ce; te = teII;
         }
         if (w >= dII) { en = enII; p = pII; r = rII; te = teII; }
-    } else if (Udf <= Urz) {
+    } else if (q.pattern == 1) {
         // two rarefactions, closed form
-        p = pI * pow((Udf - Uvk) / (Urz - Uvk), R(1) / g.gm);
-        R aI = (fabs(p - pI) < g.eps) ? rI * cI : g.gm * rI * cI * (R(1) - p / pI) / (R(1) - pow(p / pI, g.gm));
-        R aII = (fabs(p - pII) < g.eps) ? rII * cII
-                                        : g.gm * rII * cII * (R(1) - p / pII) / (R(1) - pow(p / pII, g.gm));
+        p = pI * pow((q.Udf - q.Uvk) / (q.Urz - q.Uvk), R(1) / g.gm);
+        R aI = rare_coef(g, rI, cI, p, pI);
+        R aII = rare_coef(g, rII, cII, p, pII);
         R u = (aI * enI + aII * enII + pI - pII) / (aI + aII);
         R dI = enI - cI;
         R ddI = u - cI - g.g1 * (enI - u) / R(2);
@@ -299,12 +433,10 @@ __device__ R flux_godunov(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR,
             en = w - ce; p = pII * pow(ce / cII, R(1) / g.gm); r = g.ga * p / ce / ce; te = teII;
         }
         if (w >= dII) { en = enII; p = pII; r = rII; te = teII; }
-    } else if (Udf <= Uud) {
-        // left shock, right rarefaction
-        p = bisect_p(g, enI, pI, rI, cI, enII, pII, cII, rc);
+    } else if (q.pattern == 2) {
+        // shock on side I, rarefaction on side II
         R aI = sqrt(rI * (g.g2 / R(2) * p + g.g1 / R(2) * pI));
-        R aII = (fabs(p - pII) < g.eps) ? rII * cII
-                                        : g.gm * rII * cII * (R(1) - p / pII) / (R(1) - pow(p / pII, g.gm));
+        R aII = rare_coef(g, rII, cII, p, pII);
         R u = (aI * enI + aII * enII + pI - pII) / (aI + aII);
         R dI = enI - aI / rI;
         R dII = enII + cII;
@@ -321,10 +453,8 @@ __device__ R flux_godunov(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR,
             en = w - ce; p = pII * pow(ce / cII, R(1) / g.gm); r = g.ga * p / ce / ce; te = teII;
         }
         if (w >= dII) { en = enII; p = pII; r = rII; te = teII; }
-    } else if (Udf > Uud) {
-        // two shocks; acoustic start value (kernel.cu:641-642)
-        R p0 = (pI * rII * cII + pII * rI * cI + (enI - enII) * rI * cI * rII * cII) / (rI * cI + rII * cII);
-        p = newton_p(g, enI, pI, rI, cI, enII, pII, rII, cII, p0, rc);
+    } else if (q.pattern == 3) {
+        // two shocks
         R aI = sqrt(rI * (g.g2 / R(2) * p + g.g1 / R(2) * pI));
         R aII = sqrt(rII * (g.g2 / R(2) * p + g.g1 / R(2) * pII));
         R u = (aI * enI + aII * enII + pI - pII) / (aI + aII);
@@ -336,11 +466,10 @@ __device__ R flux_godunov(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR,
         else if (w < dII) { en = u; r = rII * aII / (aII + rII * (enII - u)); te = teII; }
         else { en = enII; p = pII; r = rII; te = teII; }
     } else {
-        // NaN input: no pattern
         rc.status |= 0x10u;
         en = p = r = te = UU = R(NAN);
     }
-    if (swap) en = -en;
+    if (q.swap) en = -en;
     R e = p * g.inv_g1 + R(0.5) * r * (en * en + te * te);
     R m = r * en;
     F[0] = m;
@@ -348,6 +477,18 @@ __device__ R flux_godunov(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR,
     F[2] = m * te;
     F[3] = en * (e + p);
     return (UU > g.eps8) ? UU : g.eps8;
+}
+
+// Exact Godunov flux of one face with the reference's solver
+// (Godunov_Solver_Alexashov, kernel.cu:128-570).
+template <typename R>
+__device__ R flux_godunov(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR, R unR, R utR, R F[4],
+                          RiemannCount& rc)
+{
+    const RPre<R> q = godunov_pre(g, rL, pL, unL, utL, rR, pR, unR, utR);
+    R p = R(0);
+    if (q.pattern == 2 || q.pattern == 3) p = solve_p_reference(g, q, rc);
+    return godunov_sample(g, q, p, F, rc);
 }
 
 }  // namespace ast

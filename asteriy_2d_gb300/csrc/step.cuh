@@ -10,13 +10,21 @@
 // The last CTA to finish turns the two maxima into the next dt and performs
 // the reference's funk_time shift (kernel.cu:1525-1536) on the device, so a
 // sequence of steps needs no host round trip.
+//
+// Exact-Godunov faces are processed in two phases: every face is classified
+// (godunov_pre) and the closed-form patterns are finished at once, while the
+// faces that need an iterative p* solve are pushed to a shared-memory queue
+// and solved afterwards by all threads of the CTA, so that the iterations
+// run in full warps instead of in one or two lanes of many warps.
 #pragma once
 
+#include "mlp.cuh"
 #include "physics.cuh"
 
 namespace ast {
 
 constexpr int kThreads = 256;
+constexpr int kQueueCap = 256;   // queued exact-solver faces per tile
 
 // device-resident clock and counters of a solver (one per solver)
 struct DevClock {
@@ -43,6 +51,7 @@ struct StepParams {
     double gamma, tol;
     int max_iter;
     int geom, grad_p, collect_stats;
+    int riemann_newton, guess;     // exact solver: p* iteration and its start value
     int bc_kind[4];
     double bc_val[4][4];           // rho, p, vz, vr of FIXED sides; vz/vr limit of SUCTION
     int fixed_region;
@@ -60,6 +69,11 @@ struct StepParams {
     double* T_min;                 // raw mode: *T_min = min(*T_min, dt), atomic
     const double* T_do_ptr;        // raw mode: the step's dt
     unsigned int* status_ptr;      // raw mode: status bits (may be null)
+    const float* mlp;              // AST_MLP_NPARAM floats (guess == MLP)
+    float* rec;                    // face recorder: AST_RECORD_FLOATS per record, or null
+    unsigned long long* rec_n;     // records written (may exceed rec_cap)
+    long long rec_cap;
+    int rec_every;                 // record on steps with step % rec_every == 0
 };
 
 // ------------------------------------------------------------------ loads
@@ -81,8 +95,10 @@ __device__ __forceinline__ void read_cell(const StepParams& P, int n, int m, R v
     }
 }
 
-// state of cell (n, m) where at most one of n, m may lie outside the domain;
-// outside cells follow their side's ghost rule (include/asteriy_gb300.h)
+// state of cell (n, m); a cell outside the domain follows the ghost rule of
+// the side it lies beyond (include/asteriy_gb300.h).  Every index is clamped
+// into the arrays, so deeper ghost layers (partial tiles, corners) read
+// valid memory; they never feed a face that is used.
 template <typename R, int LAYOUT>
 __device__ __forceinline__ void fetch_cell(const StepParams& P, int n, int m, R v[4])
 {
@@ -97,8 +113,6 @@ __device__ __forceinline__ void fetch_cell(const StepParams& P, int n, int m, R 
     else if (n >= N) { side = 1; j = n - N;  low = false; bn = N - 1; bm = m; mn = N - 1 - j; mm = m; }
     else if (m < 0)  { side = 2; j = -1 - m; low = true;  bn = n; bm = 0;     mn = n; mm = j; }
     else             { side = 3; j = m - M;  low = false; bn = n; bm = M - 1; mn = n; mm = M - 1 - j; }
-    // only ghost layers 0 and 1 feed valid faces; deeper ones (partial
-    // tiles) are clamped to stay inside the arrays
     mn = min(max(mn, 0), N - 1);
     mm = min(max(mm, 0), M - 1);
     bm = min(max(bm, 0), M - 1);
@@ -129,42 +143,41 @@ __device__ __forceinline__ bool cell_fixed(const StepParams& P, double x, double
 }
 
 // ------------------------------------------------------------------ reductions
-__device__ __forceinline__ float warp_max(float v)
-{
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
 __device__ __forceinline__ double warp_max(double v)
 {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-// ------------------------------------------------------------------ the kernel
+
+// ------------------------------------------------------------------ shared memory of a tile
 template <typename R, int TZ, int TR>
 struct TileSmem {
     static constexpr int HZ = TZ + 4, HR = TR + 4;
     R q[4][HR][HZ];              // staged state with a two-cell halo
     R Fz[4][TR][TZ + 1];         // z-face flux: mass, mom_z, mom_r, energy
     R Fr[4][TR + 1][TZ];         // r-face flux
+    R qv[10][kQueueCap];         // queued exact-solver faces: enI teI pI rI cI enII teII pII rII cII
+    int qcode[kQueueCap];        // face code | active << 12 | swap << 13 | pattern << 14
+    float mlp[kMlpParams];       // learned start value (guess == MLP)
     unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
+    int nq;                      // queued faces (beyond kQueueCap they are solved in place)
 };
 
 template <typename R, int TZ, int TR>
 constexpr size_t tile_smem_bytes() { return sizeof(TileSmem<R, TZ, TR>); }
 
+// ------------------------------------------------------------------ cell update
 // Conservative update of one cell in arithmetic C from its state `in`
-// (rho, p, vz, vr) and its four outward face fluxes f[k][face] (k = mass,
-// mom_z, mom_r, energy; face = right, left, bottom, top, the left and bottom
-// ones still oriented along +z / +r).  Planar: Kernel_TVD, kernel.cu:3027-3073;
+// (rho, p, vz, vr) and its four face fluxes f[k][face] (k = mass, mom_z,
+// mom_r, energy; face = right, left, bottom, top, all oriented along +z/+r).
+// tdv = T_do/(dx dy), ty = T_do/r.  Planar: Kernel_TVD, kernel.cu:3027-3073;
 // axisymmetric with the cylindrical source: add_MK, kernel.cu:2480-2509.
-template <typename C, typename R, typename G>
-__device__ __forceinline__ void update_cell(const StepParams& P, const G& g, const R in[4], const R f[4][4],
-                                            double T_do, double x, double y, int& nrho, int& np, R out[4],
-                                            float* E2o = nullptr, float* KE2o = nullptr)
+template <typename C, typename R>
+__device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C inv_g1, const R in[4],
+                                            const R f[4][4], C T_do, C tdv, C ty, C dx, C dy, C Q2, int& nrho,
+                                            int& np, R out[4], C* E2o = nullptr, C* KE2o = nullptr)
 {
     const C r1 = (C)in[0], p1 = (C)in[1], vz1 = (C)in[2], vr1 = (C)in[3];
-    const C dx = (C)P.dx, dy = (C)P.dy;
-    const C tdv = (C)(T_do / (P.dx * P.dy));
     C ps[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -172,26 +185,21 @@ __device__ __forceinline__ void update_cell(const StepParams& P, const G& g, con
         if (P.geom == 1) ps[k] = (f12 + f14) * dy + (f13 + f15) * dx;
         else ps[k] = f12 * dy + f13 * dx + f14 * dy + f15 * dx;
     }
-    C Q2 = C(0);
-    if (P.body_force && x > P.body_lo && x < P.body_hi)
-        Q2 = (y >= P.body_rsplit) ? -(C)P.body_amp * r1 : (C)P.body_amp * r1;
     const C Q3 = Q2 * vr1;
-    const C ga = (C)g.ga, inv_g1 = (C)g.inv_g1, g1 = (C)g.g1;
     const C ke1 = r1 * (vz1 * vz1 + vr1 * vr1) * C(0.5);
     C rho2, mz, mr, E2;
     if (P.geom == 1) {
-        const C ty = (C)(T_do / y);
         rho2 = r1 - tdv * ps[0] - ty * r1 * vr1;
         if (rho2 <= C(0)) { nrho++; rho2 = r1; }
         mz = r1 * vz1 - tdv * ps[1] - ty * r1 * vr1 * vz1;
-        mr = r1 * vr1 - tdv * ps[2] - ty * r1 * vr1 * vr1 + (C)T_do * Q2;
-        E2 = (p1 * inv_g1 + ke1) - tdv * ps[3] - ty * vr1 * (ga * p1 * inv_g1 + ke1) + (C)T_do * Q3;
+        mr = r1 * vr1 - tdv * ps[2] - ty * r1 * vr1 * vr1 + T_do * Q2;
+        E2 = (p1 * inv_g1 + ke1) - tdv * ps[3] - ty * vr1 * (ga * p1 * inv_g1 + ke1) + T_do * Q3;
     } else {
         rho2 = r1 - tdv * ps[0];
         if (rho2 <= C(0)) { nrho++; rho2 = r1; }
         mz = r1 * vz1 - tdv * ps[1];
-        mr = r1 * vr1 - tdv * ps[2] + (C)T_do * Q2;
-        E2 = (p1 * inv_g1 + ke1) - tdv * ps[3] + (C)T_do * Q3;
+        mr = r1 * vr1 - tdv * ps[2] + T_do * Q2;
+        E2 = (p1 * inv_g1 + ke1) - tdv * ps[3] + T_do * Q3;
     }
     const C irho = C(1) / rho2;
     const C vz2 = mz * irho, vr2 = mr * irho;
@@ -199,19 +207,75 @@ __device__ __forceinline__ void update_cell(const StepParams& P, const G& g, con
     C p2 = (E2 - KE2) * g1;
     if (p2 <= C(0)) { np++; p2 = (C)P.p_floor; }
     out[0] = (R)rho2; out[1] = (R)p2; out[2] = (R)vz2; out[3] = (R)vr2;
-    if (E2o) { *E2o = (float)E2; *KE2o = (float)KE2; }
+    if (E2o) { *E2o = E2; *KE2o = KE2; }
 }
 
+// ------------------------------------------------------------------ exact solver helpers
+// p* of a queued (pattern 2 or 3) face: the reference's iteration, or the
+// safeguarded Newton from the PVRS-type or the learned start value.
+template <typename R>
+__device__ __forceinline__ R solve_queued(const StepParams& P, const Gas<R>& g, const RPre<R>& q, const float* W,
+                                          RiemannCount& rc, int& fallback)
+{
+    if (!P.riemann_newton) return solve_p_reference(g, q, rc);
+    R p0;
+    if (P.guess == 1) {
+        // the face's own left/right states (before the solver's side swap)
+        const R rL = q.swap ? q.rII : q.rI, pL = q.swap ? q.pII : q.pI, cL = q.swap ? q.cII : q.cI;
+        const R uL = q.swap ? -q.enII : q.enI;
+        const R rR = q.swap ? q.rI : q.rII, pR = q.swap ? q.pI : q.pII, cR = q.swap ? q.cI : q.cII;
+        const R uR = q.swap ? -q.enI : q.enII;
+        float x[kMlpIn];
+        mlp_features((float)g.ga, (float)rL, (float)pL, (float)uL, (float)cL, (float)rR, (float)pR, (float)uR,
+                     (float)cR, x);
+        p0 = pL * (R)__expf(mlp_forward(W, x));
+        if (!in_basin(q, p0)) {
+            fallback++;
+            p0 = pvrs_guess(q);
+        }
+    } else {
+        p0 = pvrs_guess(q);
+    }
+    return solve_p_newton(g, q, p0, g.tol, rc);
+}
+
+// one training record of a solved face (recorder enabled)
+template <typename R>
+__device__ __forceinline__ void record_face(const StepParams& P, const Gas<R>& g, const RPre<R>& q, R p, int step,
+                                            int face_id)
+{
+    const R rL = q.swap ? q.rII : q.rI, pL = q.swap ? q.pII : q.pI, cL = q.swap ? q.cII : q.cI;
+    const R uL = q.swap ? -q.enII : q.enI;
+    const R rR = q.swap ? q.rI : q.rII, pR = q.swap ? q.pI : q.pII, cR = q.swap ? q.cI : q.cII;
+    const R uR = q.swap ? -q.enI : q.enII;
+    const unsigned long long slot = atomicAdd(P.rec_n, 1ull);
+    if ((long long)slot >= P.rec_cap) return;
+    float* r = P.rec + slot * AST_RECORD_FLOATS;
+    r[0] = (float)(rR / rL);
+    r[1] = (float)(pR / pL);
+    r[2] = (float)((uR - uL) / cL);
+    r[3] = (float)(cR / cL);
+    r[4] = (float)g.ga;
+    r[5] = (float)log(pL);
+    r[6] = (float)log(p / pL);
+    r[7] = __int_as_float(step);
+    r[8] = __int_as_float(face_id);
+    r[9] = __int_as_float(q.pattern);
+}
+
+// ------------------------------------------------------------------ face passes
 // All faces of one orientation in the tile, one thread per face.  ZF: z
 // faces (between tile columns c-1 and c of a row), else r faces (between
 // tile rows a-1 and a of a column).  Writes the flux, in (mass, mom_z,
 // mom_r, energy) order, to sm.Fz / sm.Fr and raises smax to the largest wave
-// speed of the faces that belong to at least one updated cell.
+// speed of the faces that belong to at least one updated cell.  Exact-solver
+// faces of patterns 2 and 3 go to the queue instead.
 template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF>
 __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
-                                          int m0, RiemannCount& rc, R& smax)
+                                          int m0, int step, RiemannCount& rc, int& fallback, R& smax)
 {
     constexpr int NF = ZF ? TR * (TZ + 1) : (TR + 1) * TZ;
+    constexpr int NFZ = TR * (TZ + 1);
     constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
     constexpr int NN = ZF ? 2 : 3;           // normal velocity component
     constexpr int TT = ZF ? 3 : 2;           // tangential velocity component
@@ -257,10 +321,28 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
             }
         }
         R Sp;
-        if (hi) {
-            if (FLUX == 0) Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
-            else if (FLUX == 1) Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
-            else Sp = flux_godunov(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F, rc);
+        if (FLUX == 2 && hi) {
+            const RPre<R> q = godunov_pre(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT]);
+            R p = R(0);
+            if (q.pattern == 2 || q.pattern == 3) {
+                const int slot = atomicAdd(&sm.nq, 1);
+                if (slot < kQueueCap) {
+                    sm.qv[0][slot] = q.enI; sm.qv[1][slot] = q.teI; sm.qv[2][slot] = q.pI;
+                    sm.qv[3][slot] = q.rI; sm.qv[4][slot] = q.cI; sm.qv[5][slot] = q.enII;
+                    sm.qv[6][slot] = q.teII; sm.qv[7][slot] = q.pII; sm.qv[8][slot] = q.rII;
+                    sm.qv[9][slot] = q.cII;
+                    sm.qcode[slot] = (ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.swap ? 1 << 13 : 0) |
+                                     (q.pattern << 14);
+                    continue;
+                }
+                // queue full: solve in place
+                p = solve_queued(P, g, q, sm.mlp, rc, fallback);
+                if (P.rec && step % P.rec_every == 0)
+                    record_face(P, g, q, p, step, 2 * (mu * P.N + nu) + (ZF ? 0 : 1));
+            }
+            Sp = godunov_sample(g, q, p, F, rc);
+        } else if (FLUX == 1 && hi) {
+            Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         } else {
             Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         }
@@ -275,6 +357,46 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
     }
 }
 
+// the queued exact-solver faces, solved by all threads of the CTA
+template <typename R, int TZ, int TR>
+__device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
+                                           int m0, int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
+{
+    constexpr int NFZ = TR * (TZ + 1);
+    const int nq = min(sm.nq, kQueueCap);
+    for (int i = threadIdx.x; i < nq; i += kThreads) {
+        RPre<R> q;
+        q.enI = sm.qv[0][i]; q.teI = sm.qv[1][i]; q.pI = sm.qv[2][i]; q.rI = sm.qv[3][i]; q.cI = sm.qv[4][i];
+        q.enII = sm.qv[5][i]; q.teII = sm.qv[6][i]; q.pII = sm.qv[7][i]; q.rII = sm.qv[8][i];
+        q.cII = sm.qv[9][i];
+        const int code = sm.qcode[i];
+        q.swap = (code >> 13) & 1;
+        q.pattern = code >> 14;
+        q.Udf = q.enI - q.enII;
+        q.Urz = q.Uvk = R(0);   // only the closed-form patterns read these
+        const bool active = (code >> 12) & 1;
+        const int fc = code & 0xfff;
+        const R p = solve_queued(P, g, q, sm.mlp, rc, fallback);
+        R F[4];
+        R Sp = godunov_sample(g, q, p, F, rc);
+        if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
+        if (fc < NFZ) {
+            const int a = fc / (TZ + 1), c = fc - a * (TZ + 1);
+            sm.Fz[0][a][c] = F[0]; sm.Fz[1][a][c] = F[1]; sm.Fz[2][a][c] = F[2]; sm.Fz[3][a][c] = F[3];
+            if (active) smz = fmax(smz, Sp);
+            if (P.rec && step % P.rec_every == 0)
+                record_face(P, g, q, p, step, 2 * ((m0 + a) * P.N + (n0 + c)) + 0);
+        } else {
+            const int f2 = fc - NFZ, a = f2 / TZ, c = f2 - a * TZ;
+            sm.Fr[0][a][c] = F[0]; sm.Fr[1][a][c] = F[2]; sm.Fr[2][a][c] = F[1]; sm.Fr[3][a][c] = F[3];
+            if (active) smr = fmax(smr, Sp);
+            if (P.rec && step % P.rec_every == 0)
+                record_face(P, g, q, p, step, 2 * ((m0 + a) * P.N + (n0 + c)) + 1);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ the kernel
 template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
 __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
 {
@@ -283,13 +405,17 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     S& sm = *reinterpret_cast<S*>(smem_raw);
     __shared__ double red_d[2][kThreads / 32];
-    __shared__ int red_i[3][kThreads / 32];
+    __shared__ int red_i[4][kThreads / 32];
     __shared__ int s_last;
 
     const int tid = threadIdx.x;
     const int n0 = blockIdx.x * TZ, m0 = blockIdx.y * TR;
     const Gas<R> g = make_gas<R>(P.gamma, P.tol, P.max_iter);
     const double T_do = (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr;
+    const int step = (P.clock != nullptr) ? (int)P.clock->step : 0;
+    if (tid == 0) sm.nq = 0;
+    if (FLUX == 2 && P.guess == 1 && P.mlp != nullptr)
+        for (int i = tid; i < kMlpParams; i += kThreads) sm.mlp[i] = P.mlp[i];
 
     // ---- stage tile + halo; the corners are never read by the cross stencil
     for (int idx = tid; idx < HR * HZ; idx += kThreads) {
@@ -309,17 +435,24 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
 
     RiemannCount rc;
     rc.clear();
+    int fallback = 0;
     R smz = R(0), smr = R(0);
 
-    // ---- every face of the tile once: z faces, then r faces
-    face_pass<R, FLUX, RECON, TZ, TR, true>(P, sm, g, n0, m0, rc, smz);
-    face_pass<R, FLUX, RECON, TZ, TR, false>(P, sm, g, n0, m0, rc, smr);
+    // ---- every face of the tile once: z faces, then r faces, then the queue
+    face_pass<R, FLUX, RECON, TZ, TR, true>(P, sm, g, n0, m0, step, rc, fallback, smz);
+    face_pass<R, FLUX, RECON, TZ, TR, false>(P, sm, g, n0, m0, step, rc, fallback, smr);
     __syncthreads();
+    if (FLUX == 2) {
+        queue_pass<R, TZ, TR>(P, sm, g, n0, m0, step, rc, fallback, smz, smr);
+        __syncthreads();
+    }
 
     // ---- conservative update of the tile's cells
     int nrho = 0, np = 0;
-    const double dx = P.dx, dy = P.dy;
-    const Gas<double> g64 = make_gas<double>(P.gamma, P.tol, P.max_iter);
+    const double tdv_d = T_do / (P.dx * P.dy);
+    const float tdv_f = (float)tdv_d, Tf = (float)T_do, dxf = (float)P.dx, dyf = (float)P.dy;
+    const float yminf = (float)P.y_min;
+    const float gaf = (float)P.gamma, g1f = (float)(P.gamma - 1.0), ig1f = (float)(1.0 / (P.gamma - 1.0));
     for (int cidx = tid; cidx < TZ * TR; cidx += kThreads) {
         const int row = cidx / TZ, col = cidx - row * TZ;
         const int n = n0 + col, m = m0 + row;
@@ -327,9 +460,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
         const int j = row + 2, i = col + 2;
         R o[4] = {sm.q[0][j][i], sm.q[1][j][i], sm.q[2][j][i], sm.q[3][j][i]};
         if (!(P.fixed_region && sm.fx[j][i])) {
-            const double x = P.x_min + n * dx, y = P.y_min + m * dy;
             R in[4] = {o[0], o[1], o[2], o[3]};
-            // outward face fluxes of the cell: +right, -left, -bottom, +top
             R f[4][4];
 #pragma unroll
             for (int k = 0; k < 4; k++) {
@@ -339,17 +470,39 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
                 f[k][3] = sm.Fr[k][row + 1][col];
             }
             if (sizeof(R) == 8 || (P.geom == 1 && m < 4)) {
-                // FP64 path; in the FP32 form also the near-axis cells, where
-                // the 1/r source is largest
-                update_cell<double>(P, g64, in, f, T_do, x, y, nrho, np, o);
+                // FP64; in the FP32 form also the four cell rows next to the
+                // axis, where the 1/r source is largest
+                const double y = P.y_min + m * P.dy;
+                double Q2 = 0.0;
+                if (P.body_force) {
+                    const double x = P.x_min + n * P.dx;
+                    if (x > P.body_lo && x < P.body_hi)
+                        Q2 = (y >= P.body_rsplit) ? -P.body_amp * (double)in[0] : P.body_amp * (double)in[0];
+                }
+                const double ty = (P.geom == 1) ? T_do / y : 0.0;
+                update_cell<double>(P, P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0), in, f, T_do, tdv_d, ty, P.dx,
+                                    P.dy, Q2, nrho, np, o);
             } else {
+                // FP32 form: float arithmetic only
+                const float y = yminf + (float)m * dyf;
+                float Q2 = 0.0f;
+                if (P.body_force) {
+                    const float x = (float)P.x_min + (float)n * dxf;
+                    if (x > (float)P.body_lo && x < (float)P.body_hi)
+                        Q2 = (y >= (float)P.body_rsplit) ? -(float)P.body_amp * (float)in[0]
+                                                         : (float)P.body_amp * (float)in[0];
+                }
+                const float ty = (P.geom == 1) ? Tf / y : 0.0f;
                 float E2, KE2;
-                update_cell<float>(P, g, in, f, T_do, x, y, nrho, np, o, &E2, &KE2);
-                // FP32 form: pressure recovery p = (g-1)(E - rho v^2/2) in FP64
-                // where the kinetic energy is more than 99% of the total
-                if ((float)KE2 > 0.99f * (float)E2) {
+                update_cell<float>(P, gaf, g1f, ig1f, in, f, Tf, tdv_f, ty, dxf, dyf, Q2, nrho, np, o, &E2, &KE2);
+                // pressure recovery p = (g-1)(E - rho v^2/2) in FP64 where the
+                // kinetic energy is more than 99% of the total
+                if (KE2 > 0.99f * E2) {
                     int d0 = 0, d1 = 0;
-                    update_cell<double>(P, g64, in, f, T_do, x, y, d0, d1, o);
+                    const double yd = P.y_min + m * P.dy;
+                    const double ty64 = (P.geom == 1) ? T_do / yd : 0.0;
+                    update_cell<double>(P, P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0), in, f, T_do, tdv_d, ty64,
+                                        P.dx, P.dy, (double)Q2, d0, d1, o);
                 }
             }
         }
@@ -369,10 +522,11 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
     {
         const double a = warp_max((double)smz), b = warp_max((double)smr);
         const int c0 = __reduce_add_sync(0xffffffffu, nrho), c1 = __reduce_add_sync(0xffffffffu, np);
+        const int c2 = __reduce_add_sync(0xffffffffu, fallback);
         const unsigned st = __reduce_or_sync(0xffffffffu, rc.status);
         if (lane == 0) {
             red_d[0][wid] = a; red_d[1][wid] = b;
-            red_i[0][wid] = c0; red_i[1][wid] = c1; red_i[2][wid] = (int)st;
+            red_i[0][wid] = c0; red_i[1][wid] = c1; red_i[2][wid] = (int)st; red_i[3][wid] = c2;
         }
         if (P.collect_stats && P.clock != nullptr) {
             const int n1 = __reduce_add_sync(0xffffffffu, rc.newton_calls);
@@ -392,20 +546,22 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
     __syncthreads();
     if (tid == 0) {
         double a = 0.0, b = 0.0;
-        int c0 = 0, c1 = 0;
+        int c0 = 0, c1 = 0, c2 = 0;
         unsigned st = 0;
         for (int w = 0; w < kThreads / 32; w++) {
             a = fmax(a, red_d[0][w]); b = fmax(b, red_d[1][w]);
-            c0 += red_i[0][w]; c1 += red_i[1][w]; st |= (unsigned)red_i[2][w];
+            c0 += red_i[0][w]; c1 += red_i[1][w]; st |= (unsigned)red_i[2][w]; c2 += red_i[3][w];
         }
         if (c0) st |= 0x01u;
         if (c1) st |= 0x02u;
+        if (c2) st |= 0x40u;
         if (P.clock != nullptr) {
             DevClock* C = P.clock;
             if (a > 0.0) atomicMax(&C->smax_z, (unsigned long long)__double_as_longlong(a));
             if (b > 0.0) atomicMax(&C->smax_r, (unsigned long long)__double_as_longlong(b));
             if (c0) atomicAdd(&C->cnt[0], (unsigned long long)c0);
             if (c1) atomicAdd(&C->cnt[1], (unsigned long long)c1);
+            if (c2) atomicAdd(&C->cnt[6], (unsigned long long)c2);
             if (st) atomicOr(&C->status, st);
             __threadfence();
             const unsigned int total = gridDim.x * gridDim.y;

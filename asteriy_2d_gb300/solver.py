@@ -12,6 +12,7 @@ from . import abi as A
 
 _lib = None
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 
 # every entry point of include/asteriy_gb300.h with (restype, argtypes)
 SIGNATURES = {
@@ -42,6 +43,14 @@ SIGNATURES = {
     "ast_write_bin": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
     "ast_read_bin": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
     "ast_write_tecplot": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_int, C.c_double, C.c_char_p]),
+    "ast_set_mlp": (C.c_int, [C.c_void_p, _fp]),
+    "ast_record_start": (C.c_int, [C.c_void_p, C.c_int64, C.c_int]),
+    "ast_record_stop": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "ast_record_read": (C.c_int, [C.c_void_p, _fp, C.c_int64]),
+    "ast_mlp_init": (C.c_int, [_fp, C.c_int64, C.c_uint64, _fp]),
+    "ast_mlp_grad": (C.c_int, [_fp, _fp, C.c_int64, _fp, _fp]),
+    "ast_mlp_forward": (C.c_int, [_fp, _fp, C.c_int64, C.c_int, _fp]),
+    "ast_mlp_train": (C.c_int, [_fp, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, _fp, _fp]),
 }
 
 
@@ -79,6 +88,49 @@ def check(rc, where):
 
 def _dptr(a):
     return a.ctypes.data_as(_dp)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(_fp)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+# ---------------------------------------------------------------- learned start value
+
+def mlp_init(samples, seed=7):
+    samples = _f32(samples)
+    params = np.zeros(A.AST_MLP_NPARAM, dtype=np.float32)
+    check(load().ast_mlp_init(_fptr(samples), len(samples), seed, _fptr(params)), "ast_mlp_init")
+    return params
+
+
+def mlp_grad(params, samples):
+    params, samples = _f32(params), _f32(samples)
+    grad = np.zeros(A.AST_MLP_NPARAM, dtype=np.float32)
+    loss = C.c_float()
+    check(load().ast_mlp_grad(_fptr(params), _fptr(samples), len(samples), _fptr(grad), C.byref(loss)),
+          "ast_mlp_grad")
+    return grad, loss.value
+
+
+def mlp_forward(params, x):
+    params = _f32(params)
+    x = _f32(x)
+    y = np.zeros(len(x), dtype=np.float32)
+    check(load().ast_mlp_forward(_fptr(params), _fptr(x), len(x), x.shape[1], _fptr(y)), "ast_mlp_forward")
+    return y
+
+
+def mlp_train(samples, params, epochs=10, batch=8192, lr=3e-3, seed=7):
+    samples = _f32(samples)
+    params = _f32(params).copy()
+    losses = np.zeros(epochs, dtype=np.float32)
+    check(load().ast_mlp_train(_fptr(samples), len(samples), epochs, batch, lr, seed, _fptr(params),
+                               _fptr(losses)), "ast_mlp_train")
+    return params, losses
 
 
 def fill_blast(cfg, p_in=10.0, p_out=0.1, radius=0.2):
@@ -190,6 +242,24 @@ class Solver:
         st = A.ast_stats()
         check(self.lib.ast_get_stats(self.h, C.byref(st), int(reset)), "ast_get_stats")
         return {name: getattr(st, name) for name, _ in st._fields_ if name != "reserved"}
+
+    def set_mlp(self, params):
+        params = _f32(params)
+        assert params.shape == (A.AST_MLP_NPARAM,)
+        check(self.lib.ast_set_mlp(self.h, _fptr(params)), "ast_set_mlp")
+
+    def record_start(self, capacity, every=1):
+        check(self.lib.ast_record_start(self.h, capacity, every), "ast_record_start")
+        self._rec_cap = capacity
+
+    def record_stop(self):
+        n = C.c_int64()
+        check(self.lib.ast_record_stop(self.h, C.byref(n)), "ast_record_stop")
+        stored = min(n.value, self._rec_cap)
+        out = np.zeros((stored, A.AST_RECORD_FLOATS), dtype=np.float32)
+        if stored:
+            check(self.lib.ast_record_read(self.h, _fptr(out), stored), "ast_record_read")
+        return out, n.value
 
     def device_state(self):
         p, ld, el = C.c_void_p(), C.c_int64(), C.c_int()

@@ -118,7 +118,14 @@ typedef struct ast_config {
     double  p_floor;              /* pressure floor (kernel.cu:3072): 1e-6            */
     double  riemann_tol;          /* Newton/bisection tolerance, eps (Header.h:62)    */
     int32_t collect_stats;        /* 1: count Riemann iterations in ast_stats         */
-    int32_t reserved_i[7];
+    /* p* iteration of the exact solver: 0 = the reference's (bisection for
+       shock-rarefaction, Newton from the acoustic value for two shocks,
+       kernel.cu:220-231); 1 = safeguarded Newton on the full pressure
+       function for both patterns, started from `guess`.  The FP32 form
+       always uses 1 (the reference's absolute tolerance is below FP32
+       resolution).                                                          */
+    int32_t riemann_newton;
+    int32_t reserved_i[6];
     double  reserved_d[8];
 } ast_config;
 
@@ -134,6 +141,15 @@ typedef struct ast_stats {
 } ast_stats;
 
 typedef struct ast_solver ast_solver;
+
+/* Learned start value of the exact solver: parameter block of the 6-32-32-1
+   SiLU network (feature shift[6], scale[6], W1[32][6], b1[32], W2[32][32],
+   b2[32], w3[32], b3). */
+#define AST_MLP_NPARAM 1325
+/* One recorded face of the exact solver (training data of the network):
+   features x[6], target log(p* / p_L), then step, face id and wave pattern
+   stored as int32 bit patterns. */
+#define AST_RECORD_FLOATS 10
 
 /* ---- library ----------------------------------------------------------- */
 int         ast_abi_version(void);
@@ -170,6 +186,29 @@ int ast_get_stats(ast_solver* solver, ast_stats* out, int reset);
    with row pitch *ld elements of *elem_bytes bytes (8 = FP64, 4 = FP32),
    plane stride ld*M.  Valid until the next ast_step / ast_set_state. */
 int ast_device_state(ast_solver* solver, void** planes, int64_t* ld, int* elem_bytes);
+
+/* ---- learned start value of the exact solver (no reference counterpart:
+        the reference always starts from the acoustic value, kernel.cu:641-642)
+   A solver created with guess == AST_GUESS_MLP and riemann_newton == 1 (or
+   FP32 precision) starts every iterative p* solve from the network's
+   prediction p_L exp(y) and falls back to the acoustic start value when the
+   prediction lies outside the pattern's bracket (counted in mlp_fallback). */
+int ast_set_mlp(ast_solver* solver, const float* params);  /* AST_MLP_NPARAM host floats */
+/* Face recorder: on the following steps with step % every == 0, every exact-
+   solver face that needs the iterative p* solve is written as one record of
+   AST_RECORD_FLOATS floats, up to `capacity` records (device buffer owned by
+   the solver).  ast_record_stop returns the number of faces offered, which
+   may exceed the capacity; ast_record_read copies min(n, stored) records. */
+int ast_record_start(ast_solver* solver, int64_t capacity, int every);
+int ast_record_stop(ast_solver* solver, int64_t* offered);
+int ast_record_read(ast_solver* solver, float* out, int64_t n);
+/* Training kernels (host arrays in and out, work on the current device).
+   samples: n records as written by the recorder (x[6], target, ...). */
+int ast_mlp_init(const float* samples, int64_t n, uint64_t seed, float* params);
+int ast_mlp_grad(const float* params, const float* samples, int64_t n, float* grad, float* loss);
+int ast_mlp_forward(const float* params, const float* x, int64_t n, int stride, float* y);
+int ast_mlp_train(const float* samples, int64_t n, int epochs, int batch, float lr, uint64_t seed,
+                  float* params, float* loss_per_epoch);
 
 /* ---- kernel-level drop-in ----------------------------------------------
  * One step on reference-layout device arrays, the replacement for

@@ -44,27 +44,37 @@ def assert_parity(cfg, s0, u0, nsteps, tol=TOL):
     return s, u, os_, ou
 
 
-def shock_cells(s, cfg):
-    """Per row of cells (fixed r), the z index of the largest density jump in
-    each half of the domain: the blast has one shock on either side of z=0."""
+def jumps(s, cfg):
     rho = s[:, 0].reshape(cfg.M, cfg.N)
-    jump = np.abs(np.diff(rho, axis=1))
-    h = jump.shape[1] // 2
-    return np.stack([np.argmax(jump[:, :h], axis=1), h + np.argmax(jump[:, h:], axis=1)], 1)
+    return np.abs(np.diff(rho, axis=1))
+
+
+def assert_same_shock_cells(s, o, cfg, tie=1e-8):
+    """Per row of cells (fixed r) and per half of the domain (the blast has
+    one shock on either side of z=0), the cell face with the largest density
+    jump in the GPU result is also the largest jump of the oracle's result,
+    up to ties within `tie` relative (two adjacent faces with equal jumps)."""
+    jg, jo = jumps(s, cfg), jumps(o, cfg)
+    h = jg.shape[1] // 2
+    for lo, hi in ((0, h), (h, jg.shape[1])):
+        ig = lo + np.argmax(jg[:, lo:hi], axis=1)
+        mo = np.max(jo[:, lo:hi], axis=1)
+        rows = np.arange(jg.shape[0])
+        assert np.all(jo[rows, ig] >= mo * (1 - tie)), np.nonzero(jo[rows, ig] < mo * (1 - tie))
 
 
 def test_blast_hll_minmod_fp64_256x128_100_steps():
     cfg = problems.blast_config(256, 128)
     s0, u0 = solver.fill_blast(cfg)
     s, u, os_, ou = assert_parity(cfg, s0, u0, 100)
-    assert np.array_equal(shock_cells(s, cfg), shock_cells(os_, cfg))
+    assert_same_shock_cells(s, os_, cfg)
 
 
 def test_blast_hllc():
     cfg = problems.blast_config(128, 64, flux=A.FLUX_HLLC)
     s0, u0 = solver.fill_blast(cfg)
     s, u, os_, ou = assert_parity(cfg, s0, u0, 100)
-    assert np.array_equal(shock_cells(s, cfg), shock_cells(os_, cfg))
+    assert_same_shock_cells(s, os_, cfg)
 
 
 # The exact solver's shock-rarefaction bisection stops on an absolute
@@ -82,7 +92,7 @@ def test_blast_godunov(riemann_tol, tol):
     cfg.riemann_tol = riemann_tol
     s0, u0 = solver.fill_blast(cfg)
     s, u, os_, ou = assert_parity(cfg, s0, u0, 100, tol=tol)
-    assert np.array_equal(shock_cells(s, cfg), shock_cells(os_, cfg))
+    assert_same_shock_cells(s, os_, cfg)
 
 
 def test_wind_counterflow_hllc_fixed_sphere():
@@ -190,6 +200,19 @@ def test_stats_count_riemann_work():
     _, _, _, st = run_gpu(cfg, s0, u0, 20)
     assert st["newton_calls"] + st["bisect_calls"] > 0 and st["newton_max_iters"] >= 1
     assert st["status"] & A.AST_ST_NONFINITE == 0
+
+
+def test_fp64_safeguarded_newton_matches_oracle():
+    """The Newton iteration used by the learned form, in FP64, converges to
+    the reference's p*: with tight tolerances the step agrees to 1e-10."""
+    cfg = problems.blast_config(128, 64, flux=A.FLUX_GODUNOV)
+    cfg.riemann_tol = 1e-13
+    gpu = cfg.copy()
+    gpu.riemann_newton = 1
+    s0, u0 = solver.fill_blast(cfg)
+    s, u, _, _ = run_gpu(gpu, s0, u0, 100)
+    os_, ou, *_ = O.run(cfg, s0, u0, 100, nthreads=NT)
+    assert np.all(rel_linf(s, os_) <= TOL) and np.all(rel_linf(u, ou) <= TOL)
 
 
 @pytest.mark.parametrize("flux", [A.FLUX_HLL, A.FLUX_GODUNOV])

@@ -1,0 +1,58 @@
+"""The learned start value end to end on the GPU: record exact-solver faces
+from the FP64 solver, train the network with the CUDA kernels, and compare
+the FP32 Godunov solver started from the network with the same solver
+started from the acoustic (PVRS-type) value at the same Newton tolerance."""
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle as O
+from asteriy_2d_gb300 import abi as A
+from asteriy_2d_gb300 import learned, problems, solver
+
+pytestmark = pytest.mark.gpu
+
+
+def fp32_run(cfg, s0, u0, nsteps, params=None):
+    c = cfg.copy()
+    c.precision = A.PREC_FP32
+    c.collect_stats = 1
+    c.riemann_tol = 1e-8
+    c.guess = A.GUESS_MLP if params is not None else A.GUESS_PVRS
+    with solver.Solver(c) as S:
+        if params is not None:
+            S.set_mlp(params)
+        S.set_state(s0, u0)
+        S.step(nsteps)
+        s, u = S.get_state()
+        st = S.stats()
+    return s, u, st
+
+
+def test_recorder_trainer_and_learned_guess():
+    cfg = problems.blast_config(128, 64, flux=A.FLUX_GODUNOV)
+    s0, u0 = solver.fill_blast(cfg)
+    rec, offered = learned.record_faces(cfg, s0, u0, 150, every=1, capacity=1 << 20)
+    assert offered == len(rec) > 1000
+    assert np.all(np.isfinite(rec[:, :7]))
+    pat = rec[:, 9].view(np.int32)
+    assert set(np.unique(pat)) <= {2, 3}
+    samples = learned.sample_records(rec, min(len(rec), 1 << 16), seed=7)
+    params, losses = learned.train_guess(samples, epochs=30, batch=2048, lr=3e-3, seed=7)
+    assert losses[-1] < 0.5 * losses[0]
+
+    # same problem, FP32 solver: learned vs acoustic start value
+    sp, up, st_p = fp32_run(cfg, s0, u0, 150)
+    sm, um, st_m = fp32_run(cfg, s0, u0, 150, params)
+    it_p = st_p["newton_iters"] / st_p["newton_calls"]
+    it_m = st_m["newton_iters"] / st_m["newton_calls"]
+    fb = st_m["mlp_fallback"] / st_m["newton_calls"]
+    print(f"mean Newton iterations: PVRS {it_p:.3f}, learned {it_m:.3f}; fallback rate {fb:.4f}")
+    assert it_m < it_p
+    assert fb < 0.2
+    # both stay within the FP32 form's error bound against the FP64 oracle
+    os_, ou, *_ = O.run(cfg, s0, u0, 150, nthreads=os.cpu_count() or 1)
+    for s in (sp, sm):
+        l1 = np.sum(np.abs(s[:, 0] - os_[:, 0])) / np.sum(np.abs(os_[:, 0]))
+        assert l1 < 1e-4, l1
