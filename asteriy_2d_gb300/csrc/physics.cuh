@@ -293,15 +293,28 @@ __device__ __forceinline__ R pvrs_guess(const RPre<R>& q)
     return p0;
 }
 
-// true when p0 can start the Newton iteration of the pattern: finite and
-// inside the pattern's bracket
+// true when p0 can start the safeguarded Newton iteration of the pattern:
+// finite and inside the pattern's bracket widened by a factor 2 on each
+// side (the pressure function is increasing and concave, and the iteration
+// keeps the original bracket as its safeguard, so a start just outside it
+// converges as fast as one just inside)
 template <typename R>
 __device__ __forceinline__ bool in_basin(const RPre<R>& q, R p0)
 {
     if (!(p0 == p0) || !(p0 > R(0))) return false;
-    if (q.pattern == 2) return p0 >= q.pI && p0 <= q.pII;
-    return p0 >= q.pII && p0 < R(1e30);
+    if (q.pattern == 2) return p0 >= R(0.5) * q.pI && p0 <= R(2) * q.pII;
+    return p0 >= R(0.5) * q.pII && p0 < R(1e30);
 }
+
+// convergence threshold of the relative Newton step: the requested
+// tolerance, but not below 4 ulps of the arithmetic (1e-8 is below FP32
+// resolution; the same clamp applies to every start value)
+template <typename R>
+__device__ __forceinline__ R newton_tol(R tol);
+template <>
+__device__ __forceinline__ double newton_tol<double>(double tol) { return tol; }
+template <>
+__device__ __forceinline__ float newton_tol<float>(float tol) { return fmaxf(tol, 4.0f * 1.1920929e-7f); }
 
 // Safeguarded Newton on the full pressure function
 //   f(p) = f_I(p) + f_II(p) - (enI - enII),
@@ -334,10 +347,10 @@ __device__ R solve_p_newton(const Gas<R>& g, const RPre<R>& q, R p0, R tol, Riem
                 df += t / (rK * cK) * (pK / p);
             }
         }
-        if (f < R(0)) lo = p; else hi = p;
+        if (f < R(0)) lo = fmax(lo, p); else hi = fmin(hi, p);
         R pn = p - f / df;
         if (!(pn > lo && pn < hi)) pn = (hi < R(INFINITY)) ? R(0.5) * (lo + hi) : R(2) * p;
-        const bool done = fabs(pn - p) <= tol * p;
+        const bool done = fabs(pn - p) <= newton_tol(tol) * p;
         p = pn;
         if (done) break;
         if (k >= g.max_iter) { rc.status |= 0x04u; break; }

@@ -32,12 +32,16 @@ def record_faces(cfg, s0, u0, nsteps, every=1, capacity=1 << 24):
     return rec[order], offered
 
 
-def sample_records(rec, k, seed=7):
-    if len(rec) <= k:
-        return rec.copy()
+def sample_indices(n, k, seed=7):
+    """Sorted indices of a uniform sample of min(k, n) of n records."""
+    if n <= k:
+        return np.arange(n)
     rng = np.random.Generator(np.random.PCG64(seed))
-    idx = np.sort(rng.choice(len(rec), size=k, replace=False))
-    return rec[idx]
+    return np.sort(rng.choice(n, size=k, replace=False))
+
+
+def sample_records(rec, k, seed=7):
+    return rec[sample_indices(len(rec), k, seed)]
 
 
 def train_guess(samples, epochs=20, batch=8192, lr=3e-3, seed=7):

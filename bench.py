@@ -7,9 +7,12 @@ the exact-Godunov flux and minmod reconstruction.  A step is one time step
 over the whole grid; the metric is cell-updates/s = N*M*steps / time.
 
 Forms measured (each from the same initial state, warm-up steps first):
-  fp64_godunov   plain FP64 path (the oracle-comparable form)
-  fp32_godunov   precision form: FP32 state and fluxes
-The headline `value` is the form named in config.form.
+  fp64_godunov   plain FP64 path (the reference's solver; the oracle-comparable form)
+  fp32_pvrs      FP32 form, Newton for p* from the acoustic (PVRS-type) start value
+  fp32_learned   FP32 form, Newton from the learned start value (the headline)
+The FP32 forms report their density and pressure L1 error against the FP64
+run after the same steps, and Newton statistics (mean/max iterations,
+fallback rate).  The headline `value` is the form named in config.form.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -95,20 +98,45 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# the measured forms: FP64 plain (the reference's solver), and the FP32 form
+# started from the acoustic value or from the learned network, both at the
+# Newton tolerance 1e-8 (clamped to 4 ulps of FP32)
+FORMS = ("fp64_godunov", "fp32_pvrs", "fp32_learned")
+
+
 def make_config(form):
     from asteriy_2d_gb300 import abi as A
     from asteriy_2d_gb300 import problems
     prec = A.PREC_FP64 if form.startswith("fp64") else A.PREC_FP32
-    return problems.blast_config(N_Z, M_R, flux=A.FLUX_GODUNOV, precision=prec)
+    cfg = problems.blast_config(N_Z, M_R, flux=A.FLUX_GODUNOV, precision=prec)
+    if prec == A.PREC_FP32:
+        cfg.riemann_tol = 1e-8
+        cfg.guess = A.GUESS_MLP if form == "fp32_learned" else A.GUESS_PVRS
+    return cfg
 
 
-def time_form(form, s0, u0, steps, warmup, torch):
+def learned_params(s0, u0):
+    """Trained parameters of the start-value network: the committed ones
+    (asteriy_2d_gb300/train_guess.py) or, when absent, a quick training on
+    faces recorded from 200 FP64 steps of this workload."""
+    from asteriy_2d_gb300 import learned
+    path = os.path.join(ROOT, "asteriy_2d_gb300", "data", "guess_blast.npy")
+    if os.path.exists(path):
+        return np.load(path), "asteriy_2d_gb300/data/guess_blast.npy"
+    rec, _ = learned.record_faces(make_config("fp64_godunov"), s0, u0, 200, every=20, capacity=1 << 24)
+    params, _ = learned.train_guess(learned.sample_records(rec, 1 << 20), epochs=10, batch=16384)
+    return params, "trained in this run on faces of 200 FP64 steps"
+
+
+def time_form(form, s0, u0, steps, warmup, torch, params=None, stats_steps=0):
     """Device-timed steps of one form: inputs resident in HBM, CUDA events on
-    the solver's stream.  Returns (seconds, ms per step)."""
+    the solver's stream.  Returns (seconds, final s, final u, stats)."""
     from asteriy_2d_gb300 import solver
     cfg = make_config(form)
     stream = torch.cuda.Stream()
     with solver.Solver(cfg, stream=stream.cuda_stream) as S:
+        if params is not None:
+            S.set_mlp(params)
         S.set_state(s0, u0)
         S.step(warmup)
         S.synchronize()
@@ -121,10 +149,22 @@ def time_form(form, s0, u0, steps, warmup, torch):
         S.synchronize()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-    return ms / 1e3, ms / steps
+        s, u = S.get_state()
+    st = None
+    if stats_steps:
+        # Newton statistics from a separate run with the counters on
+        c = cfg.copy()
+        c.collect_stats = 1
+        with solver.Solver(c) as S:
+            if params is not None:
+                S.set_mlp(params)
+            S.set_state(s0, u0)
+            S.step(warmup + stats_steps)
+            st = S.stats()
+    return ms / 1e3, s, u, st
 
 
-def time_e2e(form, s0, u0, steps, torch):
+def time_e2e(form, s0, u0, steps, torch, params=None):
     """Through the public API with host buffers: every step copies the state
     in from pinned host memory, steps once and reads the result back."""
     from asteriy_2d_gb300 import solver
@@ -136,6 +176,9 @@ def time_e2e(form, s0, u0, steps, torch):
     hu.numpy()[:] = u0
     lib = solver.load()
     with solver.Solver(cfg) as S:
+        if params is not None:
+            S.set_mlp(params)
+
         def one():
             solver.check(lib.ast_set_state(S.h, hs.data_ptr(), hu.data_ptr(), 0), "set_state")
             S.step(1, sync=False)
@@ -186,7 +229,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp64_godunov", choices=["fp64_godunov", "fp32_godunov"])
+    ap.add_argument("--form", default="fp32_learned", choices=list(FORMS))
+    ap.add_argument("--no-stats", action="store_true", help="skip the Newton-statistics runs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-forms", action="store_true", help="time only --form")
     ap.add_argument("--grid", default=None, help="NxM instead of 4096x2048 (profiling runs)")
@@ -233,30 +277,58 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     cfg = make_config(args.form)
     s0, u0 = solver.fill_blast(cfg)
-    # the other forms, for the side-by-side table
-    forms = {}
-    for form in ("fp64_godunov", "fp32_godunov"):
+    cells = cfg.N * cfg.M
+    params, params_src = (None, None)
+    if "fp32_learned" in ((args.form,) if args.no_forms else FORMS):
+        params, params_src = learned_params(s0, u0)
+
+    # side-by-side forms (same initial state, same step count); the headline
+    # form is timed last, under the clock sampler and the rank barrier
+    forms, finals = {}, {}
+    for form in FORMS:
         if form == args.form or args.no_forms:
             continue
-        sec, ms = time_form(form, s0, u0, max(2, args.steps // 2), 2, torch)
-        forms[form] = {"value": cfg.N * cfg.M * max(2, args.steps // 2) / sec, "ms_per_step": ms}
-
+        sec, s, u, st = time_form(form, s0, u0, args.steps, args.warmup, torch,
+                                  params if form == "fp32_learned" else None, stats_steps=0 if args.no_stats else 5)
+        forms[form] = {"value": cells * args.steps / sec, "ms_per_step": sec * 1e3 / args.steps}
+        finals[form] = s
+        if st and st["newton_calls"]:
+            forms[form]["newton"] = {"mean_iters": st["newton_iters"] / st["newton_calls"],
+                                     "max_iters": st["newton_max_iters"],
+                                     "fallback_rate": st["mlp_fallback"] / st["newton_calls"]}
     if ws > 1:
         torch.distributed.barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    sec, ms = time_form(args.form, s0, u0, args.steps, args.warmup, torch)
+    sec, s, u, st = time_form(args.form, s0, u0, args.steps, args.warmup, torch,
+                              params if args.form == "fp32_learned" else None,
+                              stats_steps=0 if args.no_stats else 5)
     clocks = sampler.stop()
     if ws > 1:
         t = torch.tensor([sec], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         sec = t.item()
-    cells = cfg.N * cfg.M
     value = ws * cells * args.steps / sec
     forms[args.form] = {"value": cells * args.steps / sec, "ms_per_step": sec * 1e3 / args.steps}
+    finals[args.form] = s
+    if st and st["newton_calls"]:
+        forms[args.form]["newton"] = {"mean_iters": st["newton_iters"] / st["newton_calls"],
+                                      "max_iters": st["newton_max_iters"],
+                                      "fallback_rate": st["mlp_fallback"] / st["newton_calls"]}
+    # density / pressure L1 error of the FP32 forms against the FP64 run after
+    # the same warmup + steps
+    if "fp64_godunov" in finals:
+        ref = finals["fp64_godunov"]
+        for form, sf in finals.items():
+            if form == "fp64_godunov":
+                continue
+            forms[form]["l1_rho_vs_fp64"] = float(np.sum(np.abs(sf[:, 0] - ref[:, 0])) / np.sum(np.abs(ref[:, 0])))
+            forms[form]["l1_p_vs_fp64"] = float(np.sum(np.abs(sf[:, 1] - ref[:, 1])) / np.sum(np.abs(ref[:, 1])))
+    if "fp64_godunov" in forms and args.form != "fp64_godunov":
+        forms[args.form]["speedup_vs_fp64"] = forms[args.form]["value"] / forms["fp64_godunov"]["value"]
 
     e2e_steps = max(3, args.steps // 4)
-    esec, bi, bo = time_e2e(args.form, s0, u0, e2e_steps, torch)
+    esec, bi, bo = time_e2e(args.form, s0, u0, e2e_steps, torch, params if args.form == "fp32_learned" else None)
     hbm, src = peaks()
     prec = "fp64" if args.form.startswith("fp64") else "fp32"
     achieved = BYTES_PER_CELL[prec] * cells / (sec / args.steps) / 1e9
@@ -267,6 +339,7 @@ def main():
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
         "config": {"workload": f"blast {N_Z}x{M_R}, exact Godunov + minmod, axisymmetric, CFL 0.4",
                    "form": args.form, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "mlp_params": params_src,
                    "l2": "inputs larger than L2 (state ping-pong 2x%d MB)" % (cells * BYTES_PER_CELL[prec] // 2 // 2**20)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": src, "traffic": None,
