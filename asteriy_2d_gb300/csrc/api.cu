@@ -70,51 +70,6 @@ __global__ void funk_time_kernel(double* T, double* T_do, double* TT, int* i)
     *i = *i + 1;
 }
 
-void fill_params(StepParams& P, const ast_config& c)
-{
-    std::memset(&P, 0, sizeof P);
-    P.N = c.N;
-    P.M = c.M;
-    P.x_min = c.x_min;
-    P.dx = (c.x_max - c.x_min) / (c.N - 1);
-    P.dy = (c.y_max) / (c.M);
-    P.y_min = (c.y_max / (2.0 * c.M));
-    P.krit_dx = c.cfl * P.dx;
-    P.krit_dy = c.cfl * P.dy;
-    P.dt_cap = c.dt_cap;
-    P.p_floor = c.p_floor;
-    P.gamma = c.gamma;
-    P.tol = c.riemann_tol;
-    P.max_iter = c.riemann_max_iter;
-    P.geom = c.geom;
-    P.grad_p = c.grad_p;
-    P.collect_stats = c.collect_stats;
-    // the FP32 form always iterates with the safeguarded Newton: the
-    // reference's absolute bisection tolerance is below FP32 resolution
-    P.riemann_newton = (c.riemann_newton || c.precision == AST_PREC_FP32) ? 1 : 0;
-    P.guess = c.guess;
-    P.rec_every = 1;
-    for (int sd = 0; sd < 4; sd++) {
-        P.bc_kind[sd] = c.bc[sd].kind;
-        P.bc_val[sd][0] = c.bc[sd].rho;
-        P.bc_val[sd][1] = c.bc[sd].p;
-        P.bc_val[sd][2] = c.bc[sd].vz;
-        P.bc_val[sd][3] = c.bc[sd].vr;
-    }
-    P.fixed_region = c.fixed_region;
-    P.fixed_zc = c.fixed_zc;
-    P.fixed_az2 = c.fixed_az * c.fixed_az;
-    P.fixed_ar2 = c.fixed_ar * c.fixed_ar;
-    P.region_select = c.region_select;
-    P.region_lo = c.region_lo;
-    P.region_hi = c.region_hi;
-    P.body_force = c.body_force;
-    P.body_lo = c.body_lo;
-    P.body_hi = c.body_hi;
-    P.body_rsplit = c.body_rsplit;
-    P.body_amp = c.body_amp;
-}
-
 }  // namespace
 
 int ast::cuda_fail(cudaError_t e, const char* what)
@@ -194,7 +149,7 @@ int ast_create(const ast_config* cfg, ast_solver** out)
     }
     cudaMemset(S->buf[0], 0, bytes);
     cudaMemset(S->buf[1], 0, bytes);
-    fill_params(S->P, *cfg);
+    fill_step_params(S->P, *cfg);
     S->P.ld = S->ld;
     S->P.plane = S->plane;
     S->P.clock = S->clock;
@@ -510,7 +465,7 @@ int ast_step_raw(const double* s, const double* u, double* s2, double* u2, doubl
     if (cfg->precision != AST_PREC_FP64) return fail(AST_ERR_UNSUPPORTED, "raw step is FP64 (reference layout)");
     if (cfg->guess == AST_GUESS_MLP) return fail(AST_ERR_UNSUPPORTED, "raw step has no learned start value");
     StepParams P;
-    fill_params(P, *cfg);
+    fill_step_params(P, *cfg);
     P.in = s;
     P.in_u = u;
     P.out = s2;

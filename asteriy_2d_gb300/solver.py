@@ -37,6 +37,8 @@ SIGNATURES = {
     "ast_step_raw": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_int, C.POINTER(A.ast_config), C.c_void_p]),
     "ast_funk_time": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ast_step_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.POINTER(A.ast_config), C.c_void_p]),
     "ast_fill_blast": (C.c_int, [C.POINTER(A.ast_config), C.c_double, C.c_double, C.c_double, _dp, _dp]),
     "ast_fill_wind": (C.c_int, [C.POINTER(A.ast_config), C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint64, _dp, _dp]),
@@ -277,3 +279,11 @@ def step_raw(s, u, s2, u2, T, T_do, TT, cfg, method=1, stream=None):
 def funk_time(T, T_do, TT, i, stream=None):
     check(load().ast_funk_time(C.c_void_p(T), C.c_void_p(T_do), C.c_void_p(TT), C.c_void_p(i),
                                C.c_void_p(stream) if stream else None), "ast_funk_time")
+
+
+def step_noalloc(s, u, s2, u2, T_do, TT, step, cfg, status=None, stream=None):
+    """ast_step_noalloc on device pointers (ints): one step plus the dt shift
+    in one launch, with no device allocation (static scratch)."""
+    check(load().ast_step_noalloc(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), C.c_void_p(T_do),
+                                  C.c_void_p(TT), C.c_void_p(step), C.c_void_p(status) if status else None,
+                                  C.byref(cfg), C.c_void_p(stream) if stream else None), "ast_step_noalloc")
