@@ -65,6 +65,8 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
     P.gamma = c.gamma;
     P.tol = c.riemann_tol;
     P.max_iter = c.riemann_max_iter;
+    P.gd = make_gas<double>(c.gamma, c.riemann_tol, c.riemann_max_iter);
+    P.gf = make_gas<float>(c.gamma, c.riemann_tol, c.riemann_max_iter);
     P.geom = c.geom;
     P.grad_p = c.grad_p;
     P.collect_stats = c.collect_stats;

@@ -10,6 +10,7 @@
 //   W2[32][32] at 236  b2[32] at 1260  w3[32] at 1292  b3 at 1324
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/asteriy_gb300.h"
@@ -65,5 +66,115 @@ __device__ __forceinline__ float mlp_forward(const float* __restrict__ W, const 
     }
     return y;
 }
+
+// ------------------------------------------------------------------ tensor-core inference
+// The same network evaluated for 16 faces at a time by one warp with
+// mma.sync.m16n8k16 (f16 operands, f32 accumulation): layer 1 is one k-block
+// (6 features padded to 16) times four n-tiles of 8 hidden units, layer 2 is
+// two k-blocks times four n-tiles; the layer-1 accumulators are re-used in
+// registers as layer 2's A operand (the m16n8 C fragments of n-tiles 2kb and
+// 2kb+1 form the m16k16 A fragment of k-block kb).  SiLU(z) = h (1 + tanh h),
+// h = z/2, with tanh.approx.f16x2.  B operands are pre-packed per lane.
+namespace tc {
+
+constexpr int kL1 = 4 * 32 * 2;          // packed words of W1: [n-tile][lane][reg]
+constexpr int kL2 = 2 * 4 * 32 * 2;      // packed words of W2: [k-block][n-tile][lane][reg]
+
+__device__ __forceinline__ unsigned pack_h2(float lo, float hi)
+{
+    __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<unsigned*>(&h);
+}
+
+__device__ __forceinline__ void mma16816(float c[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3, unsigned b0,
+                                         unsigned b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// SiLU of a pair of accumulators plus their biases, packed as f16x2
+__device__ __forceinline__ unsigned silu_h2(float z0, float z1)
+{
+    __half2 h = __floats2half2_rn(0.5f * z0, 0.5f * z1);
+    unsigned hu = *reinterpret_cast<unsigned*>(&h), t;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(hu));
+    __half2 th = *reinterpret_cast<__half2*>(&t);
+    __half2 r = __hfma2(h, th, h);   // h * (1 + tanh h)
+    return *reinterpret_cast<unsigned*>(&r);
+}
+
+// pack W1 and W2 of the float parameter block W into per-lane B fragments
+__device__ __forceinline__ void pack_weights(const float* W, unsigned* B1, unsigned* B2)
+{
+    for (int i = threadIdx.x; i < kL1 + kL2; i += blockDim.x) {
+        if (i < kL1) {
+            const int j = i / 64, lane = (i / 2) % 32, reg = i % 2;
+            const int g = lane >> 2, t = lane & 3, n = 8 * j + g, k = 2 * t + 8 * reg;
+            const float w0 = (k < kMlpIn) ? W[kOffW1 + n * kMlpIn + k] : 0.0f;
+            const float w1 = (k + 1 < kMlpIn) ? W[kOffW1 + n * kMlpIn + k + 1] : 0.0f;
+            B1[i] = pack_h2(w0, w1);
+        } else {
+            const int q = i - kL1, kb = q / 256, j = (q / 64) % 4, lane = (q / 2) % 32, reg = q % 2;
+            const int g = lane >> 2, t = lane & 3, n = 8 * j + g, k = 16 * kb + 2 * t + 8 * reg;
+            B2[q] = pack_h2(W[kOffW2 + n * kMlpH + k], W[kOffW2 + n * kMlpH + k + 1]);
+        }
+    }
+}
+
+// y for 16 faces whose standardised features sit in X[16][8] (f32, cols 6-7
+// zero); result for face r in y[r] (written by the lanes with t == 0)
+__device__ __forceinline__ void forward16(const float* W, const unsigned* B1, const unsigned* B2, const float (*X)[8],
+                                          float* y)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const unsigned a0 = pack_h2(X[g][2 * t], X[g][2 * t + 1]);
+    const unsigned a1 = pack_h2(X[g + 8][2 * t], X[g + 8][2 * t + 1]);
+    // layer 1
+    float c1[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const float b0 = W[kOffB1 + 8 * j + 2 * t], b1 = W[kOffB1 + 8 * j + 2 * t + 1];
+        c1[j][0] = b0; c1[j][1] = b1; c1[j][2] = b0; c1[j][3] = b1;
+        mma16816(c1[j], a0, a1, 0u, 0u, B1[(j * 32 + lane) * 2], B1[(j * 32 + lane) * 2 + 1]);
+    }
+    unsigned h[4][2];   // SiLU(layer 1), f16x2: [n-tile][row g / g+8]
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        h[j][0] = silu_h2(c1[j][0], c1[j][1]);
+        h[j][1] = silu_h2(c1[j][2], c1[j][3]);
+    }
+    // layer 2 and the output dot product
+    float yg = 0.0f, yg8 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const float b0 = W[kOffB2 + 8 * j + 2 * t], b1 = W[kOffB2 + 8 * j + 2 * t + 1];
+        float c[4] = {b0, b1, b0, b1};
+#pragma unroll
+        for (int kb = 0; kb < 2; kb++) {
+            const int idx = ((kb * 4 + j) * 32 + lane) * 2;
+            mma16816(c, h[2 * kb][0], h[2 * kb][1], h[2 * kb + 1][0], h[2 * kb + 1][1], B2[idx], B2[idx + 1]);
+        }
+        const float w0 = W[kOffW3 + 8 * j + 2 * t], w1 = W[kOffW3 + 8 * j + 2 * t + 1];
+        unsigned s0 = silu_h2(c[0], c[1]), s1 = silu_h2(c[2], c[3]);
+        const float2 v0 = __half22float2(*reinterpret_cast<__half2*>(&s0));
+        const float2 v1 = __half22float2(*reinterpret_cast<__half2*>(&s1));
+        yg = fmaf(w0, v0.x, fmaf(w1, v0.y, yg));
+        yg8 = fmaf(w0, v1.x, fmaf(w1, v1.y, yg8));
+    }
+    yg += __shfl_xor_sync(0xffffffffu, yg, 1);
+    yg += __shfl_xor_sync(0xffffffffu, yg, 2);
+    yg8 += __shfl_xor_sync(0xffffffffu, yg8, 1);
+    yg8 += __shfl_xor_sync(0xffffffffu, yg8, 2);
+    if (t == 0) {
+        y[g] = yg + W[kOffB3];
+        y[g + 8] = yg8 + W[kOffB3];
+    }
+}
+
+}  // namespace tc
 
 }  // namespace ast

@@ -330,6 +330,7 @@ __device__ R solve_p_newton(const Gas<R>& g, const RPre<R>& q, R p0, R tol, Riem
     const R dU = q.enI - q.enII;
     const R b = R(3) * g.ga - R(1);
     R p = p0;
+    R prev_step = R(INFINITY);
     int k = 0;
     for (;;) {
         k++;
@@ -349,8 +350,13 @@ __device__ R solve_p_newton(const Gas<R>& g, const RPre<R>& q, R p0, R tol, Riem
         }
         if (f < R(0)) lo = fmax(lo, p); else hi = fmin(hi, p);
         R pn = p - f / df;
-        if (!(pn > lo && pn < hi)) pn = (hi < R(INFINITY)) ? R(0.5) * (lo + hi) : R(2) * p;
-        const bool done = fabs(pn - p) <= newton_tol(tol) * p;
+        const bool newton_step = (pn > lo && pn < hi);
+        if (!newton_step) pn = (hi < R(INFINITY)) ? R(0.5) * (lo + hi) : R(2) * p;
+        const R step = fabs(pn - p);
+        // converged, or a Newton step no shorter than the previous one: the
+        // iteration has reached the rounding noise of f
+        const bool done = step <= newton_tol(tol) * p || (newton_step && k > 2 && step >= prev_step);
+        prev_step = step;
         p = pn;
         if (done) break;
         if (k >= g.max_iter) { rc.status |= 0x04u; break; }

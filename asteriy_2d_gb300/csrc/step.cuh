@@ -70,6 +70,8 @@ struct StepParams {
     const double* T_do_ptr;        // raw mode: the step's dt
     unsigned int* status_ptr;      // raw mode: status bits (may be null)
     const float* mlp;              // AST_MLP_NPARAM floats (guess == MLP)
+    Gas<double> gd;                // gas constants, precomputed on the host
+    Gas<float> gf;
     float* rec;                    // face recorder: AST_RECORD_FLOATS per record, or null
     unsigned long long* rec_n;     // records written (may exceed rec_cap)
     long long rec_cap;
@@ -143,7 +145,8 @@ __device__ __forceinline__ bool cell_fixed(const StepParams& P, double x, double
 }
 
 // ------------------------------------------------------------------ reductions
-__device__ __forceinline__ double warp_max(double v)
+template <typename T>
+__device__ __forceinline__ T warp_max(T v)
 {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
@@ -159,6 +162,11 @@ struct TileSmem {
     R qv[10][kQueueCap];         // queued exact-solver faces: enI teI pI rI cI enII teII pII rII cII
     int qcode[kQueueCap];        // face code | active << 12 | swap << 13 | pattern << 14
     float mlp[kMlpParams];       // learned start value (guess == MLP)
+    unsigned mB1[tc::kL1];       // its W1, W2 as per-lane f16 mma fragments
+    unsigned mB2[tc::kL2];
+    float mX[kThreads / 32][16][8];  // per warp: standardised features of 16 faces
+    float mY[kThreads / 32][16];     // per warp: network outputs
+    R qp0[kQueueCap];            // start value of each queued face
     unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
     int nq;                      // queued faces (beyond kQueueCap they are solved in place)
 };
@@ -211,24 +219,28 @@ __device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C i
 }
 
 // ------------------------------------------------------------------ exact solver helpers
-// p* of a queued (pattern 2 or 3) face: the reference's iteration, or the
-// safeguarded Newton from the PVRS-type or the learned start value.
+// the face's own left/right states (before the solver's side swap)
 template <typename R>
-__device__ __forceinline__ R solve_queued(const StepParams& P, const Gas<R>& g, const RPre<R>& q, const float* W,
+__device__ __forceinline__ void face_sides(const RPre<R>& q, R& rL, R& pL, R& uL, R& cL, R& rR, R& pR, R& uR, R& cR)
+{
+    rL = q.swap ? q.rII : q.rI; pL = q.swap ? q.pII : q.pI; cL = q.swap ? q.cII : q.cI;
+    uL = q.swap ? -q.enII : q.enI;
+    rR = q.swap ? q.rI : q.rII; pR = q.swap ? q.pI : q.pII; cR = q.swap ? q.cI : q.cII;
+    uR = q.swap ? -q.enI : q.enII;
+}
+
+// p* of a queued (pattern 2 or 3) face: the reference's iteration, or the
+// safeguarded Newton from the learned start value p0_mlp (when it lies in
+// the basin; otherwise the acoustic one, counted as a fallback) or from the
+// acoustic start value.
+template <typename R>
+__device__ __forceinline__ R solve_queued(const StepParams& P, const Gas<R>& g, const RPre<R>& q, R p0_mlp,
                                           RiemannCount& rc, int& fallback)
 {
     if (!P.riemann_newton) return solve_p_reference(g, q, rc);
     R p0;
     if (P.guess == 1) {
-        // the face's own left/right states (before the solver's side swap)
-        const R rL = q.swap ? q.rII : q.rI, pL = q.swap ? q.pII : q.pI, cL = q.swap ? q.cII : q.cI;
-        const R uL = q.swap ? -q.enII : q.enI;
-        const R rR = q.swap ? q.rI : q.rII, pR = q.swap ? q.pI : q.pII, cR = q.swap ? q.cI : q.cII;
-        const R uR = q.swap ? -q.enI : q.enII;
-        float x[kMlpIn];
-        mlp_features((float)g.ga, (float)rL, (float)pL, (float)uL, (float)cL, (float)rR, (float)pR, (float)uR,
-                     (float)cR, x);
-        p0 = pL * (R)__expf(mlp_forward(W, x));
+        p0 = p0_mlp;
         if (!in_basin(q, p0)) {
             fallback++;
             p0 = pvrs_guess(q);
@@ -335,8 +347,9 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
                                      (q.pattern << 14);
                     continue;
                 }
-                // queue full: solve in place
-                p = solve_queued(P, g, q, sm.mlp, rc, fallback);
+                // queue full (more than kQueueCap iterative faces in the tile):
+                // solve in place, from the acoustic start value
+                p = solve_queued(P, g, q, R(-1), rc, fallback);
                 if (P.rec && step % P.rec_every == 0)
                     record_face(P, g, q, p, step, 2 * (mu * P.N + nu) + (ZF ? 0 : 1));
             }
@@ -364,6 +377,39 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
 {
     constexpr int NFZ = TR * (TZ + 1);
     const int nq = min(sm.nq, kQueueCap);
+    if (P.riemann_newton && P.guess == 1) {
+        // phase 1: learned start values of the queued faces, 16 per warp
+        // tile on the tensor cores
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        for (int t0 = 16 * w; t0 < nq; t0 += 16 * (kThreads / 32)) {
+            const int i = t0 + (lane & 15);
+            R pL = R(1);
+            if (lane < 16) {
+                float x[kMlpIn] = {0, 0, 0, 0, 0, 0};
+                if (i < nq) {
+                    RPre<R> q;
+                    q.enI = sm.qv[0][i]; q.pI = sm.qv[2][i]; q.rI = sm.qv[3][i]; q.cI = sm.qv[4][i];
+                    q.enII = sm.qv[5][i]; q.pII = sm.qv[7][i]; q.rII = sm.qv[8][i]; q.cII = sm.qv[9][i];
+                    q.swap = (sm.qcode[i] >> 13) & 1;
+                    R rL, uL, cL, rR, pR, uR, cR;
+                    face_sides(q, rL, pL, uL, cL, rR, pR, uR, cR);
+                    mlp_features((float)g.ga, (float)rL, (float)pL, (float)uL, (float)cL, (float)rR, (float)pR,
+                                 (float)uR, (float)cR, x);
+                }
+#pragma unroll
+                for (int k = 0; k < kMlpIn; k++) sm.mX[w][lane][k] = (x[k] - sm.mlp[kOffShift + k]) * sm.mlp[kOffScale + k];
+                sm.mX[w][lane][6] = 0.0f;
+                sm.mX[w][lane][7] = 0.0f;
+            }
+            __syncwarp();
+            tc::forward16(sm.mlp, sm.mB1, sm.mB2, sm.mX[w], sm.mY[w]);
+            __syncwarp();
+            if (lane < 16 && i < nq) sm.qp0[i] = pL * (R)__expf(sm.mY[w][lane]);
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+    // phase 2: p* (iteration), sampling and the flux of each queued face
     for (int i = threadIdx.x; i < nq; i += kThreads) {
         RPre<R> q;
         q.enI = sm.qv[0][i]; q.teI = sm.qv[1][i]; q.pI = sm.qv[2][i]; q.rI = sm.qv[3][i]; q.cI = sm.qv[4][i];
@@ -376,7 +422,7 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
         q.Urz = q.Uvk = R(0);   // only the closed-form patterns read these
         const bool active = (code >> 12) & 1;
         const int fc = code & 0xfff;
-        const R p = solve_queued(P, g, q, sm.mlp, rc, fallback);
+        const R p = solve_queued(P, g, q, (P.riemann_newton && P.guess == 1) ? sm.qp0[i] : R(0), rc, fallback);
         R F[4];
         R Sp = godunov_sample(g, q, p, F, rc);
         if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
@@ -398,7 +444,7 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
 
 // ------------------------------------------------------------------ the kernel
 template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
-__global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
+__global__ void __launch_bounds__(kThreads, 2) step_kernel(StepParams P)
 {
     using S = TileSmem<R, TZ, TR>;
     constexpr int HZ = S::HZ, HR = S::HR;
@@ -407,13 +453,17 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
     __shared__ double red_d[2][kThreads / 32];
     __shared__ int red_i[4][kThreads / 32];
     __shared__ int s_last;
+    __shared__ double s_tdv;
 
     const int tid = threadIdx.x;
     const int n0 = blockIdx.x * TZ, m0 = blockIdx.y * TR;
-    const Gas<R> g = make_gas<R>(P.gamma, P.tol, P.max_iter);
+    const Gas<R>& g = *reinterpret_cast<const Gas<R>*>(sizeof(R) == 8 ? (const void*)&P.gd : (const void*)&P.gf);
     const double T_do = (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr;
     const int step = (P.clock != nullptr) ? (int)P.clock->step : 0;
-    if (tid == 0) sm.nq = 0;
+    if (tid == 0) {
+        sm.nq = 0;
+        s_tdv = T_do / (P.dx * P.dy);
+    }
     if (FLUX == 2 && P.guess == 1 && P.mlp != nullptr)
         for (int i = tid; i < kMlpParams; i += kThreads) sm.mlp[i] = P.mlp[i];
 
@@ -433,6 +483,8 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
     }
     __syncthreads();
 
+    if (FLUX == 2 && P.guess == 1 && P.mlp != nullptr) tc::pack_weights(sm.mlp, sm.mB1, sm.mB2);
+
     RiemannCount rc;
     rc.clear();
     int fallback = 0;
@@ -449,10 +501,10 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
 
     // ---- conservative update of the tile's cells
     int nrho = 0, np = 0;
-    const double tdv_d = T_do / (P.dx * P.dy);
+    const double tdv_d = s_tdv;
     const float tdv_f = (float)tdv_d, Tf = (float)T_do, dxf = (float)P.dx, dyf = (float)P.dy;
     const float yminf = (float)P.y_min;
-    const float gaf = (float)P.gamma, g1f = (float)(P.gamma - 1.0), ig1f = (float)(1.0 / (P.gamma - 1.0));
+    const float gaf = P.gf.ga, g1f = P.gf.g1, ig1f = P.gf.inv_g1;
     for (int cidx = tid; cidx < TZ * TR; cidx += kThreads) {
         const int row = cidx / TZ, col = cidx - row * TZ;
         const int n = n0 + col, m = m0 + row;
@@ -480,7 +532,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
                         Q2 = (y >= P.body_rsplit) ? -P.body_amp * (double)in[0] : P.body_amp * (double)in[0];
                 }
                 const double ty = (P.geom == 1) ? T_do / y : 0.0;
-                update_cell<double>(P, P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0), in, f, T_do, tdv_d, ty, P.dx,
+                update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty, P.dx,
                                     P.dy, Q2, nrho, np, o);
             } else {
                 // FP32 form: float arithmetic only
@@ -501,7 +553,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
                     int d0 = 0, d1 = 0;
                     const double yd = P.y_min + m * P.dy;
                     const double ty64 = (P.geom == 1) ? T_do / yd : 0.0;
-                    update_cell<double>(P, P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0), in, f, T_do, tdv_d, ty64,
+                    update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty64,
                                         P.dx, P.dy, (double)Q2, d0, d1, o);
                 }
             }
@@ -520,7 +572,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(StepParams P)
     // ---- block reductions and the step epilogue
     const int lane = tid & 31, wid = tid >> 5;
     {
-        const double a = warp_max((double)smz), b = warp_max((double)smr);
+        const double a = (double)warp_max(smz), b = (double)warp_max(smr);
         const int c0 = __reduce_add_sync(0xffffffffu, nrho), c1 = __reduce_add_sync(0xffffffffu, np);
         const int c2 = __reduce_add_sync(0xffffffffu, fallback);
         const unsigned st = __reduce_or_sync(0xffffffffu, rc.status);
