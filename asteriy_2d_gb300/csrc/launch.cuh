@@ -65,6 +65,15 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
     P.gamma = c.gamma;
     P.tol = c.riemann_tol;
     P.max_iter = c.riemann_max_iter;
+    P.x_minf = (float)P.x_min;
+    P.dxf = (float)P.dx;
+    P.y_minf = (float)P.y_min;
+    P.dyf = (float)P.dy;
+    P.p_floorf = (float)c.p_floor;
+    P.body_lof = (float)c.body_lo;
+    P.body_hif = (float)c.body_hi;
+    P.body_rsplitf = (float)c.body_rsplit;
+    P.body_ampf = (float)c.body_amp;
     P.gd = make_gas<double>(c.gamma, c.riemann_tol, c.riemann_max_iter);
     P.gf = make_gas<float>(c.gamma, c.riemann_tol, c.riemann_max_iter);
     P.geom = c.geom;

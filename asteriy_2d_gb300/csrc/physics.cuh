@@ -320,8 +320,9 @@ __device__ __forceinline__ float newton_tol<float>(float tol) { return fmaxf(tol
 //   f(p) = f_I(p) + f_II(p) - (enI - enII),
 // f_K the shock branch (kernel.cu:656-662) for p > p_K and the rarefaction
 // branch (lev, kernel.cu:759) for p <= p_K, from start value p0 to the
-// relative change tol.  An iterate that leaves the bracket of the root is
-// replaced by a bisection step.
+// relative change tol.  The bracket of the root ([pI, pII] or (pII, inf))
+// shrinks with the sign of f; an iterate that leaves it is replaced by the
+// bracket's upper edge (or, below it, by a bisection step).
 template <typename R>
 __device__ R solve_p_newton(const Gas<R>& g, const RPre<R>& q, R p0, R tol, RiemannCount& rc)
 {
@@ -350,8 +351,11 @@ __device__ R solve_p_newton(const Gas<R>& g, const RPre<R>& q, R p0, R tol, Riem
         }
         if (f < R(0)) lo = fmax(lo, p); else hi = fmin(hi, p);
         R pn = p - f / df;
+        // f is increasing and concave: from f < 0 a Newton step overshoots
+        // the root; an overshoot past the bracket restarts from its upper
+        // edge, from where the iteration descends monotonically
         const bool newton_step = (pn > lo && pn < hi);
-        if (!newton_step) pn = (hi < R(INFINITY)) ? R(0.5) * (lo + hi) : R(2) * p;
+        if (!newton_step) pn = (pn >= hi) ? hi : R(0.5) * (lo + fmin(hi, R(2) * p));
         const R step = fabs(pn - p);
         // converged, or a Newton step no shorter than the previous one: the
         // iteration has reached the rounding noise of f

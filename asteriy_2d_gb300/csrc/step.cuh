@@ -24,7 +24,11 @@
 namespace ast {
 
 constexpr int kThreads = 256;
-constexpr int kQueueCap = 256;   // queued exact-solver faces per tile
+// queued exact-solver faces per tile: every face of the tile in FP32 (the
+// queue never overflows), 256 in FP64 (shared memory; more iterative faces
+// than that in one tile are solved in place)
+template <typename R, int TZ, int TR>
+constexpr int queue_cap() { return sizeof(R) == 4 ? TR * (TZ + 1) + (TR + 1) * TZ : 256; }
 
 // device-resident clock and counters of a solver (one per solver)
 struct DevClock {
@@ -72,6 +76,9 @@ struct StepParams {
     const float* mlp;              // AST_MLP_NPARAM floats (guess == MLP)
     Gas<double> gd;                // gas constants, precomputed on the host
     Gas<float> gf;
+    // FP32 copies of the grid and source constants (conversions between
+    // double and float run on the FP64 pipe, 1/64 of the FP32 rate)
+    float x_minf, dxf, y_minf, dyf, p_floorf, body_lof, body_hif, body_rsplitf, body_ampf;
     float* rec;                    // face recorder: AST_RECORD_FLOATS per record, or null
     unsigned long long* rec_n;     // records written (may exceed rec_cap)
     long long rec_cap;
@@ -156,6 +163,7 @@ __device__ __forceinline__ T warp_max(T v)
 template <typename R, int TZ, int TR>
 struct TileSmem {
     static constexpr int HZ = TZ + 4, HR = TR + 4;
+    static constexpr int kQueueCap = queue_cap<R, TZ, TR>();
     R q[4][HR][HZ];              // staged state with a two-cell halo
     R Fz[4][TR][TZ + 1];         // z-face flux: mass, mom_z, mom_r, energy
     R Fr[4][TR + 1][TZ];         // r-face flux
@@ -213,7 +221,7 @@ __device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C i
     const C vz2 = mz * irho, vr2 = mr * irho;
     const C KE2 = C(0.5) * rho2 * (vz2 * vz2 + vr2 * vr2);
     C p2 = (E2 - KE2) * g1;
-    if (p2 <= C(0)) { np++; p2 = (C)P.p_floor; }
+    if (p2 <= C(0)) { np++; p2 = sizeof(C) == 4 ? (C)P.p_floorf : (C)P.p_floor; }
     out[0] = (R)rho2; out[1] = (R)p2; out[2] = (R)vz2; out[3] = (R)vr2;
     if (E2o) { *E2o = E2; *KE2o = KE2; }
 }
@@ -338,7 +346,7 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
             R p = R(0);
             if (q.pattern == 2 || q.pattern == 3) {
                 const int slot = atomicAdd(&sm.nq, 1);
-                if (slot < kQueueCap) {
+                if (slot < TileSmem<R, TZ, TR>::kQueueCap) {
                     sm.qv[0][slot] = q.enI; sm.qv[1][slot] = q.teI; sm.qv[2][slot] = q.pI;
                     sm.qv[3][slot] = q.rI; sm.qv[4][slot] = q.cI; sm.qv[5][slot] = q.enII;
                     sm.qv[6][slot] = q.teII; sm.qv[7][slot] = q.pII; sm.qv[8][slot] = q.rII;
@@ -376,7 +384,7 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
                                            int m0, int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
 {
     constexpr int NFZ = TR * (TZ + 1);
-    const int nq = min(sm.nq, kQueueCap);
+    const int nq = min(sm.nq, TileSmem<R, TZ, TR>::kQueueCap);
     if (P.riemann_newton && P.guess == 1) {
         // phase 1: learned start values of the queued faces, 16 per warp
         // tile on the tensor cores
@@ -450,10 +458,11 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(StepParams P)
     constexpr int HZ = S::HZ, HR = S::HR;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     S& sm = *reinterpret_cast<S*>(smem_raw);
-    __shared__ double red_d[2][kThreads / 32];
+    __shared__ R red_r[2][kThreads / 32];
     __shared__ int red_i[4][kThreads / 32];
     __shared__ int s_last;
     __shared__ double s_tdv;
+    __shared__ float s_tdv_f, s_T_f;
 
     const int tid = threadIdx.x;
     const int n0 = blockIdx.x * TZ, m0 = blockIdx.y * TR;
@@ -463,6 +472,8 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(StepParams P)
     if (tid == 0) {
         sm.nq = 0;
         s_tdv = T_do / (P.dx * P.dy);
+        s_tdv_f = (float)s_tdv;
+        s_T_f = (float)T_do;
     }
     if (FLUX == 2 && P.guess == 1 && P.mlp != nullptr)
         for (int i = tid; i < kMlpParams; i += kThreads) sm.mlp[i] = P.mlp[i];
@@ -502,8 +513,8 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(StepParams P)
     // ---- conservative update of the tile's cells
     int nrho = 0, np = 0;
     const double tdv_d = s_tdv;
-    const float tdv_f = (float)tdv_d, Tf = (float)T_do, dxf = (float)P.dx, dyf = (float)P.dy;
-    const float yminf = (float)P.y_min;
+    const float tdv_f = s_tdv_f, Tf = s_T_f, dxf = P.dxf, dyf = P.dyf;
+    const float yminf = P.y_minf;
     const float gaf = P.gf.ga, g1f = P.gf.g1, ig1f = P.gf.inv_g1;
     for (int cidx = tid; cidx < TZ * TR; cidx += kThreads) {
         const int row = cidx / TZ, col = cidx - row * TZ;
@@ -539,10 +550,9 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(StepParams P)
                 const float y = yminf + (float)m * dyf;
                 float Q2 = 0.0f;
                 if (P.body_force) {
-                    const float x = (float)P.x_min + (float)n * dxf;
-                    if (x > (float)P.body_lo && x < (float)P.body_hi)
-                        Q2 = (y >= (float)P.body_rsplit) ? -(float)P.body_amp * (float)in[0]
-                                                         : (float)P.body_amp * (float)in[0];
+                    const float x = P.x_minf + (float)n * dxf;
+                    if (x > P.body_lof && x < P.body_hif)
+                        Q2 = (y >= P.body_rsplitf) ? -P.body_ampf * (float)in[0] : P.body_ampf * (float)in[0];
                 }
                 const float ty = (P.geom == 1) ? Tf / y : 0.0f;
                 float E2, KE2;
@@ -572,12 +582,12 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(StepParams P)
     // ---- block reductions and the step epilogue
     const int lane = tid & 31, wid = tid >> 5;
     {
-        const double a = (double)warp_max(smz), b = (double)warp_max(smr);
+        const R a = warp_max(smz), b = warp_max(smr);
         const int c0 = __reduce_add_sync(0xffffffffu, nrho), c1 = __reduce_add_sync(0xffffffffu, np);
         const int c2 = __reduce_add_sync(0xffffffffu, fallback);
         const unsigned st = __reduce_or_sync(0xffffffffu, rc.status);
         if (lane == 0) {
-            red_d[0][wid] = a; red_d[1][wid] = b;
+            red_r[0][wid] = a; red_r[1][wid] = b;
             red_i[0][wid] = c0; red_i[1][wid] = c1; red_i[2][wid] = (int)st; red_i[3][wid] = c2;
         }
         if (P.collect_stats && P.clock != nullptr) {
@@ -597,16 +607,17 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(StepParams P)
     }
     __syncthreads();
     if (tid == 0) {
-        double a = 0.0, b = 0.0;
+        R ar = R(0), br = R(0);
         int c0 = 0, c1 = 0, c2 = 0;
         unsigned st = 0;
         for (int w = 0; w < kThreads / 32; w++) {
-            a = fmax(a, red_d[0][w]); b = fmax(b, red_d[1][w]);
+            ar = fmax(ar, red_r[0][w]); br = fmax(br, red_r[1][w]);
             c0 += red_i[0][w]; c1 += red_i[1][w]; st |= (unsigned)red_i[2][w]; c2 += red_i[3][w];
         }
         if (c0) st |= 0x01u;
         if (c1) st |= 0x02u;
         if (c2) st |= 0x40u;
+        const double a = (double)ar, b = (double)br;
         if (P.clock != nullptr) {
             DevClock* C = P.clock;
             if (a > 0.0) atomicMax(&C->smax_z, (unsigned long long)__double_as_longlong(a));

@@ -40,7 +40,8 @@ def assert_parity(cfg, s0, u0, nsteps, tol=TOL):
     es, eu = rel_linf(s, os_), rel_linf(u, ou)
     assert np.all(es <= tol) and np.all(eu <= tol), (es, eu)
     assert step == ost
-    assert abs(tdo - otdo) <= 1e-12 * otdo and abs(tt - ott) <= 1e-12 * ott, (tdo, otdo, tt, ott)
+    ctol = max(1e-12, 10 * tol if tol > TOL else 1e-12)
+    assert abs(tdo - otdo) <= ctol * otdo and abs(tt - ott) <= ctol * ott, (tdo, otdo, tt, ott)
     return s, u, os_, ou
 
 
