@@ -351,15 +351,20 @@ __device__ R solve_p_newton(const Gas<R>& g, const RPre<R>& q, R p0, R tol, Riem
         }
         if (f < R(0)) lo = fmax(lo, p); else hi = fmin(hi, p);
         R pn = p - f / df;
+        // converged: tested before the bracket, since at convergence the step
+        // may round onto the bracket's edge
+        if (fabs(pn - p) <= newton_tol(tol) * p) {
+            p = pn;
+            break;
+        }
         // f is increasing and concave: from f < 0 a Newton step overshoots
         // the root; an overshoot past the bracket restarts from its upper
         // edge, from where the iteration descends monotonically
-        const bool newton_step = (pn > lo && pn < hi);
-        if (!newton_step) pn = (pn >= hi) ? hi : R(0.5) * (lo + fmin(hi, R(2) * p));
+        if (!(pn > lo && pn < hi)) pn = (pn >= hi) ? hi : R(0.5) * (lo + fmin(hi, R(2) * p));
         const R step = fabs(pn - p);
-        // converged, or a Newton step no shorter than the previous one: the
-        // iteration has reached the rounding noise of f
-        const bool done = step <= newton_tol(tol) * p || (newton_step && k > 2 && step >= prev_step);
+        // a step no shorter than the previous one: the iteration has reached
+        // the rounding noise of f
+        const bool done = k > 2 && step >= prev_step;
         prev_step = step;
         p = pn;
         if (done) break;

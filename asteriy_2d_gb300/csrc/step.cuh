@@ -24,11 +24,11 @@
 namespace ast {
 
 constexpr int kThreads = 256;
-// queued exact-solver faces per tile: every face of the tile in FP32 (the
-// queue never overflows), 256 in FP64 (shared memory; more iterative faces
-// than that in one tile are solved in place)
+// queued exact-solver faces per tile (shared memory): 512 of the tile's 1072
+// faces in FP32, 256 in FP64; more iterative faces than that in one tile are
+// solved in place, from the acoustic start value
 template <typename R, int TZ, int TR>
-constexpr int queue_cap() { return sizeof(R) == 4 ? TR * (TZ + 1) + (TR + 1) * TZ : 256; }
+constexpr int queue_cap() { return sizeof(R) == 4 ? 512 : 256; }
 
 // device-resident clock and counters of a solver (one per solver)
 struct DevClock {
@@ -341,7 +341,20 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
             }
         }
         R Sp;
-        if (FLUX == 2 && hi) {
+        if (FLUX == 2 && hi && L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]) {
+            // identical states: the exact solution is that state (the
+            // reference reaches it through the two-rarefaction branch with
+            // p* = p, u* = u_n, up to rounding), its flux the physical flux
+            // and its largest wave speed |u_n| + c
+            const R r = L[0], p = L[1], un = L[NN], ut = L[TT];
+            const R c = sqrt(g.ga * p / r);
+            const R m = r * un;
+            F[0] = m;
+            F[1] = m * un + p;
+            F[2] = m * ut;
+            F[3] = un * (p * g.inv_g1 + R(0.5) * r * (un * un + ut * ut) + p);
+            Sp = fmax(fabs(un) + c, g.eps8);
+        } else if (FLUX == 2 && hi) {
             const RPre<R> q = godunov_pre(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT]);
             R p = R(0);
             if (q.pattern == 2 || q.pattern == 3) {
@@ -452,7 +465,7 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
 
 // ------------------------------------------------------------------ the kernel
 template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
-__global__ void __launch_bounds__(kThreads, 2) step_kernel(StepParams P)
+__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(StepParams P)
 {
     using S = TileSmem<R, TZ, TR>;
     constexpr int HZ = S::HZ, HR = S::HR;

@@ -128,16 +128,19 @@ def learned_params(s0, u0):
     return params, "trained in this run on faces of 200 FP64 steps"
 
 
-def time_form(form, s0, u0, steps, warmup, torch, params=None, stats_steps=0):
-    """Device-timed steps of one form: inputs resident in HBM, CUDA events on
-    the solver's stream.  Returns (seconds, final s, final u, stats)."""
+def time_form(form, start, steps, warmup, torch, params=None, stats_steps=0):
+    """Device-timed steps of one form from the start state `start` = (s, u,
+    (T_do, TT, step)): inputs resident in HBM, CUDA events on the solver's
+    stream.  Returns (seconds, final s, final u, stats)."""
     from asteriy_2d_gb300 import solver
+    s0, u0, clock = start
     cfg = make_config(form)
     stream = torch.cuda.Stream()
     with solver.Solver(cfg, stream=stream.cuda_stream) as S:
         if params is not None:
             S.set_mlp(params)
         S.set_state(s0, u0)
+        S.set_clock(*clock)
         S.step(warmup)
         S.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -159,15 +162,71 @@ def time_form(form, s0, u0, steps, warmup, torch, params=None, stats_steps=0):
             if params is not None:
                 S.set_mlp(params)
             S.set_state(s0, u0)
+            S.set_clock(*clock)
             S.step(warmup + stats_steps)
             st = S.stats()
     return ms / 1e3, s, u, st
 
 
-def time_e2e(form, s0, u0, steps, torch, params=None):
+def advance(form, s0, u0, nsteps, params=None):
+    """The blast advanced nsteps from t = 0 with one form: (s, u, clock)."""
+    from asteriy_2d_gb300 import solver
+    with solver.Solver(make_config(form)) as S:
+        if params is not None:
+            S.set_mlp(params)
+        S.set_state(s0, u0)
+        S.step(nsteps)
+        s, u = S.get_state()
+        clock = S.clock()
+    return s, u, clock
+
+
+def axis_shock_z(s):
+    """z of the largest density jump along the axis row (m = 0), z > 0."""
+    rho = s[:N_Z, 0]
+    jump = np.abs(np.diff(rho))
+    h = N_Z // 2
+    i = h + int(np.argmax(jump[h:]))
+    dx = 2.0 / (N_Z - 1)
+    return -1.0 + (i + 0.5) * dx
+
+
+def accuracy(nsteps, params):
+    """Error of the FP32 forms against the FP64 path after nsteps from t = 0:
+    the precision form (HLL + minmod) and the learned form (exact Godunov)."""
+    from asteriy_2d_gb300 import abi as A
+    from asteriy_2d_gb300 import problems, solver
+    out = {}
+    for name, flux, guess in (("precision_hll", A.FLUX_HLL, None), ("learned_godunov", A.FLUX_GODUNOV, params)):
+        res = {}
+        for prec in (A.PREC_FP64, A.PREC_FP32):
+            cfg = problems.blast_config(N_Z, M_R, flux=flux, precision=prec)
+            if prec == A.PREC_FP32 and flux == A.FLUX_GODUNOV:
+                cfg.riemann_tol = 1e-8
+                cfg.guess = A.GUESS_MLP
+            s0, u0 = solver.fill_blast(cfg)
+            with solver.Solver(cfg) as S:
+                if prec == A.PREC_FP32 and guess is not None:
+                    S.set_mlp(guess)
+                S.set_state(s0, u0)
+                S.step(nsteps)
+                res[prec] = S.get_state()[0]
+        r64, r32 = res[A.PREC_FP64], res[A.PREC_FP32]
+        d = np.abs(r32 - r64)
+        out[name] = {"steps": nsteps,
+                     "l1_rho": float(d[:, 0].sum() / np.abs(r64[:, 0]).sum()),
+                     "l1_p": float(d[:, 1].sum() / np.abs(r64[:, 1]).sum()),
+                     "linf_rho": float(d[:, 0].max() / np.abs(r64[:, 0]).max()),
+                     "linf_p": float(d[:, 1].max() / np.abs(r64[:, 1]).max()),
+                     "axis_shock_z_fp64": axis_shock_z(r64), "axis_shock_z_fp32": axis_shock_z(r32)}
+    return out
+
+
+def time_e2e(form, start, steps, torch, params=None):
     """Through the public API with host buffers: every step copies the state
     in from pinned host memory, steps once and reads the result back."""
     from asteriy_2d_gb300 import solver
+    s0, u0, clock = start
     cfg = make_config(form)
     K = cfg.N * cfg.M
     hs = torch.empty((K, 2), dtype=torch.float64, pin_memory=True)
@@ -178,6 +237,7 @@ def time_e2e(form, s0, u0, steps, torch, params=None):
     with solver.Solver(cfg) as S:
         if params is not None:
             S.set_mlp(params)
+        S.set_clock(*clock)
 
         def one():
             solver.check(lib.ast_set_state(S.h, hs.data_ptr(), hu.data_ptr(), 0), "set_state")
@@ -195,7 +255,7 @@ def time_e2e(form, s0, u0, steps, torch, params=None):
     return dt, 2 * K * 16, 2 * K * 16
 
 
-def cpu_baseline(cfg, s0, u0, nsteps):
+def cpu_baseline(cfg, s0, u0, nsteps, where="the initial state"):
     """The reference's face functions compiled for the host (oracle/_ref) in
     the oracle's step loop, on all host threads; the oracle port if the
     reference build is absent."""
@@ -213,7 +273,7 @@ def cpu_baseline(cfg, s0, u0, nsteps):
     dt = time.perf_counter() - t0
     cells = cfg.N * cfg.M * nsteps
     return {"value": cells / dt, "unit": "cell-updates/s", "cores": nt, "kind": kind,
-            "sample": f"{nsteps} step(s) of the full {cfg.N}x{cfg.M} grid from the initial state, FP64"}
+            "sample": f"{nsteps} step(s) of the full {cfg.N}x{cfg.M} grid from {where}, FP64"}
 
 
 def dist_setup():
@@ -234,6 +294,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-forms", action="store_true", help="time only --form")
     ap.add_argument("--grid", default=None, help="NxM instead of 4096x2048 (profiling runs)")
+    ap.add_argument("--start-step", type=int, default=1000, help="timed window starts at this step of the run")
+    ap.add_argument("--accuracy-steps", type=int, default=2000, help="FP32 vs FP64 error after these steps (0: skip)")
     args = ap.parse_args()
     global N_Z, M_R
     if args.grid:
@@ -246,6 +308,18 @@ def main():
             return 0
         cfg = make_config("fp64_godunov")
         s0, u0 = solver.fill_blast(cfg)
+        where = "the initial state"
+        if args.start_step:
+            # the same mid-run start state as the GPU arm: prepared once (on
+            # the GPU when there is one), outside the timed region; only the
+            # reference's own code is timed
+            try:
+                import torch
+                if torch.cuda.is_available():
+                    s0, u0, _ = advance("fp32_pvrs", s0, u0, args.start_step)
+                    where = f"the state at step {args.start_step}"
+            except Exception as e:  # noqa: BLE001
+                where = f"the initial state ({type(e).__name__} preparing step {args.start_step})"
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle as O
         nt = os.cpu_count() or 1
@@ -258,14 +332,15 @@ def main():
         run(args.steps)
         dt = time.perf_counter() - t0
         v = cfg.N * cfg.M * args.steps / dt
-        line = {"impl": "reference", "metric": "cell-updates/s", "value": v, "unit": "cell-updates/s",
+        line = {"impl": "reference", "metric": "cell-updates/s at 4096x2048 (exact Godunov + minmod)", "value": v,
+                "unit": "cell-updates/s",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": 1 if args.warmup else 0,
                 "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "dtype": "f64",
                 "data": "synthetic", "scaling": "weak", "vs_baseline": None,
                 "config": {"workload": f"blast {N_Z}x{M_R}, exact Godunov + minmod, axisymmetric",
                            "form": "fp64_godunov", "parallelism": "host threads"},
                 "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nt, "kind": kind,
-                                 "sample": f"{args.steps} full steps of the {N_Z}x{M_R} grid"},
+                                 "sample": f"{args.steps} full steps of the {N_Z}x{M_R} grid from {where}"},
                 "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return 0
@@ -279,16 +354,20 @@ def main():
     s0, u0 = solver.fill_blast(cfg)
     cells = cfg.N * cfg.M
     params, params_src = (None, None)
-    if "fp32_learned" in ((args.form,) if args.no_forms else FORMS):
+    if "fp32_learned" in ((args.form,) if args.no_forms else FORMS) or args.accuracy_steps:
         params, params_src = learned_params(s0, u0)
+    # the timing window starts mid-run: the blast advanced start_step steps
+    # from t = 0 (with the FP32 form, which is fast), the same start for all
+    # forms
+    start = advance("fp32_pvrs", s0, u0, args.start_step) if args.start_step else (s0, u0, (cfg.dt_first, 0.0, 0))
 
-    # side-by-side forms (same initial state, same step count); the headline
+    # side-by-side forms (same start state, same step count); the headline
     # form is timed last, under the clock sampler and the rank barrier
     forms, finals = {}, {}
     for form in FORMS:
         if form == args.form or args.no_forms:
             continue
-        sec, s, u, st = time_form(form, s0, u0, args.steps, args.warmup, torch,
+        sec, s, u, st = time_form(form, start, args.steps, args.warmup, torch,
                                   params if form == "fp32_learned" else None, stats_steps=0 if args.no_stats else 5)
         forms[form] = {"value": cells * args.steps / sec, "ms_per_step": sec * 1e3 / args.steps}
         finals[form] = s
@@ -300,7 +379,7 @@ def main():
         torch.distributed.barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    sec, s, u, st = time_form(args.form, s0, u0, args.steps, args.warmup, torch,
+    sec, s, u, st = time_form(args.form, start, args.steps, args.warmup, torch,
                               params if args.form == "fp32_learned" else None,
                               stats_steps=0 if args.no_stats else 5)
     clocks = sampler.stop()
@@ -315,8 +394,8 @@ def main():
         forms[args.form]["newton"] = {"mean_iters": st["newton_iters"] / st["newton_calls"],
                                       "max_iters": st["newton_max_iters"],
                                       "fallback_rate": st["mlp_fallback"] / st["newton_calls"]}
-    # density / pressure L1 error of the FP32 forms against the FP64 run after
-    # the same warmup + steps
+    # density / pressure L1 error of the FP32 forms against the FP64 run over
+    # the timed window (same start, same steps)
     if "fp64_godunov" in finals:
         ref = finals["fp64_godunov"]
         for form, sf in finals.items():
@@ -328,7 +407,7 @@ def main():
         forms[args.form]["speedup_vs_fp64"] = forms[args.form]["value"] / forms["fp64_godunov"]["value"]
 
     e2e_steps = max(3, args.steps // 4)
-    esec, bi, bo = time_e2e(args.form, s0, u0, e2e_steps, torch, params if args.form == "fp32_learned" else None)
+    esec, bi, bo = time_e2e(args.form, start, e2e_steps, torch, params if args.form == "fp32_learned" else None)
     hbm, src = peaks()
     prec = "fp64" if args.form.startswith("fp64") else "fp32"
     achieved = BYTES_PER_CELL[prec] * cells / (sec / args.steps) / 1e9
@@ -351,8 +430,12 @@ def main():
         "gpu_launches": args.steps,
         "clocks": clocks,
     }
+    line["config"]["start_step"] = args.start_step
+    if rank == 0 and args.accuracy_steps:
+        line["accuracy_vs_fp64"] = accuracy(args.accuracy_steps, params)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(make_config("fp64_godunov"), s0, u0, 1)
+        line["cpu_baseline"] = cpu_baseline(make_config("fp64_godunov"), start[0], start[1], 1,
+                                            where=f"the state at step {args.start_step}")
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
