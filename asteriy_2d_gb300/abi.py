@@ -58,7 +58,7 @@ class ast_config(C.Structure):
         ("dt_first", C.c_double), ("dt_cap", C.c_double), ("p_floor", C.c_double),
         ("riemann_tol", C.c_double),
         ("collect_stats", C.c_int32), ("riemann_newton", C.c_int32), ("reserved_i", C.c_int32 * 6),
-        ("reserved_d", C.c_double * 8),
+        ("mlp_gate", C.c_double), ("reserved_d", C.c_double * 7),
     ]
 
     def copy(self):
@@ -82,7 +82,8 @@ class ast_stats(C.Structure):
         ("rho_floor", C.c_uint64), ("p_floor", C.c_uint64),
         ("newton_calls", C.c_uint64), ("newton_iters", C.c_uint64),
         ("bisect_calls", C.c_uint64), ("bisect_iters", C.c_uint64),
-        ("mlp_fallback", C.c_uint64), ("reserved", C.c_uint64 * 4),
+        ("mlp_fallback", C.c_uint64), ("strong_calls", C.c_uint64), ("strong_iters", C.c_uint64),
+        ("reserved", C.c_uint64 * 2),
     ]
 
 
@@ -105,6 +106,7 @@ def default_config():
     c.riemann_max_iter = 200
     c.dt_first, c.dt_cap, c.p_floor, c.riemann_tol = 1e-9, 1000.0, 1e-6, 10e-10
     c.collect_stats = 0
+    c.mlp_gate = 0.2
     return c
 
 

@@ -372,6 +372,8 @@ int ast_get_stats(ast_solver* S, ast_stats* out, int reset)
     out->bisect_iters = c.cnt[5];
     out->mlp_fallback = c.cnt[6];
     out->newton_max_iters = (uint32_t)c.cnt[7];
+    out->strong_calls = c.cnt[8];
+    out->strong_iters = c.cnt[9];
     if (reset) {
         c.status = 0;
         std::memset(c.cnt, 0, sizeof c.cnt);

@@ -55,6 +55,7 @@ void ast_config_default(ast_config* c)
     c->dt_cap = 1000;                   // kernel.cu:2530
     c->p_floor = 0.000001;              // kernel.cu:3072
     c->riemann_tol = 10e-10;            // Header.h:62
+    c->mlp_gate = 0.2;
 }
 
 int ast_config_check(const ast_config* c)

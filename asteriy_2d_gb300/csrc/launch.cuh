@@ -83,6 +83,7 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
     // reference's absolute bisection tolerance is below FP32 resolution
     P.riemann_newton = (c.riemann_newton || c.precision == AST_PREC_FP32) ? 1 : 0;
     P.guess = c.guess;
+    P.mlp_gate = (float)c.mlp_gate;
     P.rec_every = 1;
     for (int sd = 0; sd < 4; sd++) {
         P.bc_kind[sd] = c.bc[sd].kind;

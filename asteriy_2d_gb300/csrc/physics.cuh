@@ -58,8 +58,14 @@ __host__ __device__ inline Gas<R> make_gas(double gamma, double tol, int max_ite
 struct RiemannCount {
     int newton_calls, newton_iters, bisect_calls, bisect_iters;
     int newton_max;
+    int strong_calls, strong_iters;   // faces above the learned-start gate
     unsigned status;
-    __device__ void clear() { newton_calls = newton_iters = bisect_calls = bisect_iters = newton_max = 0; status = 0; }
+    __device__ void clear()
+    {
+        newton_calls = newton_iters = bisect_calls = bisect_iters = newton_max = 0;
+        strong_calls = strong_iters = 0;
+        status = 0;
+    }
 };
 
 // ------------------------------------------------------------------ minmod

@@ -39,8 +39,9 @@ struct DevClock {
     unsigned long long smax_r;     // same for r faces
     unsigned int done;             // CTAs of the current step that finished
     unsigned int status;           // OR of AST_ST_* bits
-    unsigned long long cnt[8];     // rho_floor, p_floor, newton_calls, newton_iters,
-                                   // bisect_calls, bisect_iters, mlp_fallback, newton_max
+    unsigned long long cnt[10];    // rho_floor, p_floor, newton_calls, newton_iters,
+                                   // bisect_calls, bisect_iters, mlp_fallback, newton_max,
+                                   // strong_calls, strong_iters
 };
 
 enum Layout { kSoA = 0, kAoS = 1 };
@@ -56,6 +57,7 @@ struct StepParams {
     int max_iter;
     int geom, grad_p, collect_stats;
     int riemann_newton, guess;     // exact solver: p* iteration and its start value
+    float mlp_gate;                // wave strength above which the learned start is used
     int bc_kind[4];
     double bc_val[4][4];           // rho, p, vz, vr of FIXED sides; vz/vr limit of SUCTION
     int fixed_region;
@@ -237,17 +239,29 @@ __device__ __forceinline__ void face_sides(const RPre<R>& q, R& rL, R& pL, R& uL
     uR = q.swap ? -q.enI : q.enII;
 }
 
+// wave strength of a face: max(|ln(p_R/p_L)|, |u_R - u_L| / min(c_L, c_R))
+template <typename R>
+__device__ __forceinline__ float wave_strength(const RPre<R>& q)
+{
+    const float lp = __logf((float)(q.pII / q.pI));
+    const float du = fabsf((float)(q.enI - q.enII)) / (float)fmin(q.cI, q.cII);
+    return fmaxf(lp, du);
+}
+
 // p* of a queued (pattern 2 or 3) face: the reference's iteration, or the
-// safeguarded Newton from the learned start value p0_mlp (when it lies in
-// the basin; otherwise the acoustic one, counted as a fallback) or from the
-// acoustic start value.
+// safeguarded Newton.  Faces above the gate start from the learned value
+// p0_mlp when the learned form is on (when it leaves the basin: from the
+// acoustic value, counted as a fallback); all other faces start from the
+// acoustic value.  Faces above the gate are counted in both forms, so the
+// two start values can be compared on the same faces.
 template <typename R>
 __device__ __forceinline__ R solve_queued(const StepParams& P, const Gas<R>& g, const RPre<R>& q, R p0_mlp,
                                           RiemannCount& rc, int& fallback)
 {
     if (!P.riemann_newton) return solve_p_reference(g, q, rc);
+    const bool strong = wave_strength(q) > P.mlp_gate;
     R p0;
-    if (P.guess == 1) {
+    if (P.guess == 1 && strong) {
         p0 = p0_mlp;
         if (!in_basin(q, p0)) {
             fallback++;
@@ -256,7 +270,13 @@ __device__ __forceinline__ R solve_queued(const StepParams& P, const Gas<R>& g, 
     } else {
         p0 = pvrs_guess(q);
     }
-    return solve_p_newton(g, q, p0, g.tol, rc);
+    const int k0 = rc.newton_iters;
+    const R p = solve_p_newton(g, q, p0, g.tol, rc);
+    if (strong) {
+        rc.strong_calls++;
+        rc.strong_iters += rc.newton_iters - k0;
+    }
+    return p;
 }
 
 // one training record of a solved face (recorder enabled)
@@ -418,7 +438,9 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
                                  (float)uR, (float)cR, x);
                 }
 #pragma unroll
-                for (int k = 0; k < kMlpIn; k++) sm.mX[w][lane][k] = (x[k] - sm.mlp[kOffShift + k]) * sm.mlp[kOffScale + k];
+                // standardised, and clamped to a range f16 holds exactly enough
+                for (int k = 0; k < kMlpIn; k++)
+                    sm.mX[w][lane][k] = fminf(fmaxf((x[k] - sm.mlp[kOffShift + k]) * sm.mlp[kOffScale + k], -30.0f), 30.0f);
                 sm.mX[w][lane][6] = 0.0f;
                 sm.mX[w][lane][7] = 0.0f;
             }
@@ -609,7 +631,11 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
             const int b1 = __reduce_add_sync(0xffffffffu, rc.bisect_calls);
             const int b2 = __reduce_add_sync(0xffffffffu, rc.bisect_iters);
             const unsigned nm = __reduce_max_sync(0xffffffffu, (unsigned)rc.newton_max);
+            const int s1 = __reduce_add_sync(0xffffffffu, rc.strong_calls);
+            const int s2 = __reduce_add_sync(0xffffffffu, rc.strong_iters);
             if (lane == 0) {
+                if (s1) atomicAdd(&P.clock->cnt[8], (unsigned long long)s1);
+                if (s2) atomicAdd(&P.clock->cnt[9], (unsigned long long)s2);
                 if (n1) atomicAdd(&P.clock->cnt[2], (unsigned long long)n1);
                 if (n2) atomicAdd(&P.clock->cnt[3], (unsigned long long)n2);
                 if (b1) atomicAdd(&P.clock->cnt[4], (unsigned long long)b1);

@@ -48,3 +48,16 @@ def train_guess(samples, epochs=20, batch=8192, lr=3e-3, seed=7):
     params = mlp_init(samples, seed)
     params, losses = mlp_train(samples, params, epochs=epochs, batch=batch, lr=lr, seed=seed)
     return params, losses
+
+
+def strength(rec):
+    """Wave strength of recorded faces, max(|ln(p_R/p_L)|, |u_R-u_L|/min(c_L,c_R)),
+    from the record's features (the gate the solver applies before using the
+    learned start value)."""
+    x1, x2, x3 = rec[:, 1].astype(np.float64), rec[:, 2].astype(np.float64), rec[:, 3].astype(np.float64)
+    return np.maximum(np.abs(np.log(x1)), np.abs(x2) / np.minimum(1.0, x3))
+
+
+def strong_records(rec, gate=0.2):
+    """The recorded faces above the gate: the ones the learned start value serves."""
+    return rec[strength(rec) > gate]

@@ -211,6 +211,21 @@ def accuracy(nsteps, params):
                 S.set_state(s0, u0)
                 S.step(nsteps)
                 res[prec] = S.get_state()[0]
+        if name == "precision_hll":
+            # the flow's own sensitivity: FP64 from an initial density
+            # perturbed by 1e-12 relative, against the unperturbed FP64 run
+            cfg = problems.blast_config(N_Z, M_R, flux=flux, precision=A.PREC_FP64)
+            s0, u0 = solver.fill_blast(cfg)
+            s0 = s0.copy()
+            s0[:, 0] *= 1.0 + 1e-12 * np.random.default_rng(1).uniform(-1.0, 1.0, len(s0))
+            with solver.Solver(cfg) as S:
+                S.set_state(s0, u0)
+                S.step(nsteps)
+                rp = S.get_state()[0]
+            d = np.abs(rp - res[A.PREC_FP64])
+            out["fp64_sensitivity_1e-12"] = {"steps": nsteps,
+                                             "l1_rho": float(d[:, 0].sum() / np.abs(res[A.PREC_FP64][:, 0]).sum()),
+                                             "linf_rho": float(d[:, 0].max() / np.abs(res[A.PREC_FP64][:, 0]).max())}
         r64, r32 = res[A.PREC_FP64], res[A.PREC_FP32]
         d = np.abs(r32 - r64)
         out[name] = {"steps": nsteps,
@@ -374,7 +389,9 @@ def main():
         if st and st["newton_calls"]:
             forms[form]["newton"] = {"mean_iters": st["newton_iters"] / st["newton_calls"],
                                      "max_iters": st["newton_max_iters"],
-                                     "fallback_rate": st["mlp_fallback"] / st["newton_calls"]}
+                                     "fallback_rate": st["mlp_fallback"] / max(1, st["strong_calls"]),
+                                     "gated_faces": st["strong_calls"],
+                                     "gated_mean_iters": st["strong_iters"] / max(1, st["strong_calls"])}
     if ws > 1:
         torch.distributed.barrier()
     sampler = ClockSampler(local)
@@ -393,7 +410,9 @@ def main():
     if st and st["newton_calls"]:
         forms[args.form]["newton"] = {"mean_iters": st["newton_iters"] / st["newton_calls"],
                                       "max_iters": st["newton_max_iters"],
-                                      "fallback_rate": st["mlp_fallback"] / st["newton_calls"]}
+                                      "fallback_rate": st["mlp_fallback"] / max(1, st["strong_calls"]),
+                                     "gated_faces": st["strong_calls"],
+                                     "gated_mean_iters": st["strong_iters"] / max(1, st["strong_calls"])}
     # density / pressure L1 error of the FP32 forms against the FP64 run over
     # the timed window (same start, same steps)
     if "fp64_godunov" in finals:

@@ -126,7 +126,11 @@ typedef struct ast_config {
        resolution).                                                          */
     int32_t riemann_newton;
     int32_t reserved_i[6];
-    double  reserved_d[8];
+    /* wave strength above which the learned start value is used:
+       max(|ln(p_R/p_L)|, |u_R - u_L| / min(c_L, c_R)); weaker faces start
+       from the acoustic value, which is already close for them (0.2)        */
+    double  mlp_gate;
+    double  reserved_d[7];
 } ast_config;
 
 typedef struct ast_stats {
@@ -137,7 +141,9 @@ typedef struct ast_stats {
     uint64_t newton_calls, newton_iters;
     uint64_t bisect_calls, bisect_iters;
     uint64_t mlp_fallback;        /* learned guesses replaced by the PVRS guess       */
-    uint64_t reserved[4];
+    uint64_t strong_calls;        /* iterative faces above mlp_gate (both start values) */
+    uint64_t strong_iters;        /* their Newton iterations                          */
+    uint64_t reserved[2];
 } ast_stats;
 
 typedef struct ast_solver ast_solver;

@@ -38,19 +38,25 @@ def test_recorder_trainer_and_learned_guess():
     assert np.all(np.isfinite(rec[:, :7]))
     pat = rec[:, 9].view(np.int32)
     assert set(np.unique(pat)) <= {2, 3}
-    samples = learned.sample_records(rec, min(len(rec), 1 << 16), seed=7)
-    params, losses = learned.train_guess(samples, epochs=60, batch=2048, lr=3e-3, seed=7)
+    strong = learned.strong_records(rec, 0.2)
+    assert len(strong) > 500
+    samples = learned.sample_records(strong, min(len(strong), 1 << 16), seed=7)
+    params, losses = learned.train_guess(samples, epochs=60, batch=1024, lr=3e-3, seed=7)
     assert losses[-1] < 0.7 * losses[0], losses
 
-    # same problem, FP32 solver: learned vs acoustic start value
+    # same problem, FP32 solver: learned vs acoustic start value; the faces
+    # above the gate are the ones the network serves, counted in both runs
     sp, up, st_p = fp32_run(cfg, s0, u0, 150)
     sm, um, st_m = fp32_run(cfg, s0, u0, 150, params)
-    it_p = st_p["newton_iters"] / st_p["newton_calls"]
-    it_m = st_m["newton_iters"] / st_m["newton_calls"]
-    fb = st_m["mlp_fallback"] / st_m["newton_calls"]
-    print(f"mean Newton iterations: PVRS {it_p:.3f}, learned {it_m:.3f}; fallback rate {fb:.4f}")
+    it_p = st_p["strong_iters"] / st_p["strong_calls"]
+    it_m = st_m["strong_iters"] / st_m["strong_calls"]
+    fb = st_m["mlp_fallback"] / st_m["strong_calls"]
+    print(f"mean Newton iterations on faces above the gate: PVRS {it_p:.3f}, learned {it_m:.3f}; "
+          f"fallback rate {fb:.4f}; all faces PVRS {st_p['newton_iters'] / st_p['newton_calls']:.3f} "
+          f"learned {st_m['newton_iters'] / st_m['newton_calls']:.3f}")
+    assert st_p["strong_calls"] > 0 and abs(st_p["strong_calls"] - st_m["strong_calls"]) < 0.2 * st_p["strong_calls"]
     assert it_m < it_p
-    assert fb < 0.2
+    assert fb < 0.1
     # both stay within the FP32 form's error bound against the FP64 oracle
     os_, ou, *_ = O.run(cfg, s0, u0, 150, nthreads=os.cpu_count() or 1)
     for s in (sp, sm):
