@@ -341,3 +341,53 @@ int ast_mlp_train(const float* samples, int64_t n, int epochs, int batch, float 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ tensor-core inference on given inputs
+namespace {
+
+// the step kernel's inference path (tc::forward16, 16 faces per warp tile)
+// applied to n given feature rows; one warp per tile
+__global__ void mlp_forward_tc_kernel(const float* __restrict__ W_g, const float* __restrict__ x, long long n,
+                                      int stride, float* __restrict__ y)
+{
+    __shared__ float W[kMlpParams];
+    __shared__ unsigned B1[tc::kL1], B2[tc::kL2];
+    __shared__ float X[4][16][8];
+    __shared__ float Y[4][16];
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) W[i] = W_g[i];
+    __syncthreads();
+    tc::pack_weights(W, B1, B2);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long t0 = ((long long)blockIdx.x * 4 + w) * 16;
+    if (lane < 16) {
+        const long long k = t0 + lane;
+        for (int i = 0; i < kMlpIn; i++) {
+            const float v = (k < n) ? x[k * stride + i] : 0.0f;
+            X[w][lane][i] = fminf(fmaxf((v - W[kOffShift + i]) * W[kOffScale + i], -30.0f), 30.0f);
+        }
+        X[w][lane][6] = 0.0f;
+        X[w][lane][7] = 0.0f;
+    }
+    __syncwarp();
+    tc::forward16(W, B1, B2, X[w], Y[w]);
+    __syncwarp();
+    if (lane < 16 && t0 + lane < n) y[t0 + lane] = Y[w][lane];
+}
+
+}  // namespace
+
+extern "C" int ast_mlp_forward_tc(const float* params, const float* x, int64_t n, int stride, float* y)
+{
+    if (!params || !x || !y || n < 1 || stride < kI) return AST_ERR_INVALID;
+    DevBuf dW, dX, dY;
+    TRY(dW.alloc(sizeof(float) * kMlpParams));
+    TRY(dX.alloc(sizeof(float) * stride * n));
+    TRY(dY.alloc(sizeof(float) * n));
+    TRY(cudaMemcpy(dW.p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice));
+    TRY(cudaMemcpy(dX.p, x, sizeof(float) * stride * n, cudaMemcpyHostToDevice));
+    mlp_forward_tc_kernel<<<(int)((n + 63) / 64), 128>>>(dW.as<float>(), dX.as<float>(), n, stride, dY.as<float>());
+    TRY(cudaGetLastError());
+    TRY(cudaMemcpy(y, dY.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    return AST_OK;
+}

@@ -52,6 +52,7 @@ SIGNATURES = {
     "ast_mlp_init": (C.c_int, [_fp, C.c_int64, C.c_uint64, _fp]),
     "ast_mlp_grad": (C.c_int, [_fp, _fp, C.c_int64, _fp, _fp]),
     "ast_mlp_forward": (C.c_int, [_fp, _fp, C.c_int64, C.c_int, _fp]),
+    "ast_mlp_forward_tc": (C.c_int, [_fp, _fp, C.c_int64, C.c_int, _fp]),
     "ast_mlp_train": (C.c_int, [_fp, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, _fp, _fp]),
 }
 
@@ -123,6 +124,15 @@ def mlp_forward(params, x):
     x = _f32(x)
     y = np.zeros(len(x), dtype=np.float32)
     check(load().ast_mlp_forward(_fptr(params), _fptr(x), len(x), x.shape[1], _fptr(y)), "ast_mlp_forward")
+    return y
+
+
+def mlp_forward_tc(params, x):
+    """The step kernel's tensor-core inference on given feature rows."""
+    params = _f32(params)
+    x = _f32(x)
+    y = np.zeros(len(x), dtype=np.float32)
+    check(load().ast_mlp_forward_tc(_fptr(params), _fptr(x), len(x), x.shape[1], _fptr(y)), "ast_mlp_forward_tc")
     return y
 
 

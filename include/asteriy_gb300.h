@@ -213,6 +213,9 @@ int ast_record_read(ast_solver* solver, float* out, int64_t n);
 int ast_mlp_init(const float* samples, int64_t n, uint64_t seed, float* params);
 int ast_mlp_grad(const float* params, const float* samples, int64_t n, float* grad, float* loss);
 int ast_mlp_forward(const float* params, const float* x, int64_t n, int stride, float* y);
+/* The step kernel's inference path (f16 tensor-core tiles of 16 faces) on
+   given feature rows, to compare it with the FP32 network above. */
+int ast_mlp_forward_tc(const float* params, const float* x, int64_t n, int stride, float* y);
 int ast_mlp_train(const float* samples, int64_t n, int epochs, int batch, float lr, uint64_t seed,
                   float* params, float* loss_per_epoch);
 

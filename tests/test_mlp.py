@@ -77,3 +77,21 @@ def test_cuda_training_lowers_the_loss():
     p, losses = solver.mlp_train(rec, p0, epochs=12, batch=4096, lr=3e-3, seed=7)
     assert losses[-1] < 0.35 * losses[0], losses
     assert MO.loss(p, rec[:, :6], rec[:, 6]) < 0.35 * MO.loss(p0, rec[:, :6], rec[:, 6])
+
+
+@pytest.mark.gpu
+def test_tensor_core_inference_matches_fp32_network():
+    """The step kernel evaluates the network on the tensor cores (f16
+    operands, f32 accumulation, tanh-form SiLU in f16x2); on the trained
+    network and recorded-like inputs it agrees with the FP32 network to the
+    precision of f16 (absolute 0.02 in log p*)."""
+    import os
+    from conftest import ROOT
+    path = os.path.join(ROOT, "asteriy_2d_gb300", "data", "guess_blast.npy")
+    params = np.load(path) if os.path.exists(path) else init_params(synthetic_records(4000)).astype(np.float32)
+    rec = synthetic_records(4000, seed=4)
+    y32 = solver.mlp_forward(params, rec[:, :6])
+    ytc = solver.mlp_forward_tc(params, rec[:, :6])
+    err = np.abs(ytc - y32)
+    print("tensor-core vs FP32 network: max", err.max(), "median", np.median(err))
+    assert np.median(err) < 5e-3 and np.percentile(err, 99) < 0.02
