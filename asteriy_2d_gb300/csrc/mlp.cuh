@@ -3,9 +3,11 @@
 // A 6-32-32-1 multilayer perceptron with SiLU activations predicts
 // y = log(p*/p_L) for one face from
 //   x = (rho_R/rho_L, p_R/p_L, (u_R - u_L)/c_L, c_R/c_L, gamma, log p_L)
-// in the face frame (L = lower cell side, u = normal velocity).  The inputs
-// are standardised with a per-feature shift and scale stored with the
-// weights.  Parameter block (AST_MLP_NPARAM floats):
+// in the face frame (L = lower cell side, u = normal velocity).  The network
+// first maps the three positive ratios to their logarithms and the velocity
+// jump to its asinh (the raw ratios are heavy-tailed: thousands across
+// strong shocks), then standardises each input with a shift and scale
+// stored with the weights.  Parameter block (AST_MLP_NPARAM floats):
 //   [0,6) shift  [6,12) scale  W1[32][6] at 12  b1[32] at 204
 //   W2[32][32] at 236  b2[32] at 1260  w3[32] at 1292  b3 at 1324
 #pragma once
@@ -42,12 +44,20 @@ __device__ __forceinline__ void mlp_features(float gamma, float rL, float pL, fl
     x[5] = __logf(pL);
 }
 
+// the fixed input map: log of the positive ratios, asinh of the velocity jump
+__device__ __forceinline__ float mlp_map(int i, float v)
+{
+    if (i == 0 || i == 1 || i == 3) return __logf(v);
+    if (i == 2) return copysignf(__logf(fabsf(v) + sqrtf(v * v + 1.0f)), v);
+    return v;
+}
+
 // forward pass; W may live in shared or global memory
 __device__ __forceinline__ float mlp_forward(const float* __restrict__ W, const float xin[kMlpIn])
 {
     float x[kMlpIn];
 #pragma unroll
-    for (int i = 0; i < kMlpIn; i++) x[i] = (xin[i] - W[kOffShift + i]) * W[kOffScale + i];
+    for (int i = 0; i < kMlpIn; i++) x[i] = (mlp_map(i, xin[i]) - W[kOffShift + i]) * W[kOffScale + i];
     float h1[kMlpH];
 #pragma unroll
     for (int j = 0; j < kMlpH; j++) {

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(kB) mlp_grad_kernel(const float* __restrict__ 
         const long long k = idx ? (long long)idx[first + gi] : first + gi;
         const float* r = samples + k * AST_RECORD_FLOATS;
 #pragma unroll
-        for (int i = 0; i < kI; i++) x[i] = (r[i] - s.W[kOffShift + i]) * s.W[kOffScale + i];
+        for (int i = 0; i < kI; i++) x[i] = (mlp_map(i, r[i]) - s.W[kOffShift + i]) * s.W[kOffScale + i];
         target = r[6];
     } else {
 #pragma unroll
@@ -209,8 +209,9 @@ int set_grad_smem()
 
 extern "C" {
 
-// Initial parameters: feature shift/scale = mean and 1/std of the samples'
-// features, weights ~ U(-sqrt(6/(fan_in+fan_out)), +...) from mt19937_64(seed),
+// Initial parameters: input shift/scale = mean and 1/std of the samples'
+// mapped features (log of the positive ratios, asinh of the velocity jump),
+// weights ~ U(-sqrt(6/(fan_in+fan_out)), +...) from mt19937_64(seed),
 // biases 0, output bias = mean target.  Host function.
 int ast_mlp_init(const float* samples, int64_t n, uint64_t seed, float* params)
 {
@@ -220,8 +221,11 @@ int ast_mlp_init(const float* samples, int64_t n, uint64_t seed, float* params)
     for (int64_t k = 0; k < n; k++) {
         const float* r = samples + k * AST_RECORD_FLOATS;
         for (int i = 0; i < kI; i++) {
-            mean[i] += r[i];
-            sq[i] += (double)r[i] * r[i];
+            double v = r[i];
+            if (i == 0 || i == 1 || i == 3) v = std::log(v);
+            else if (i == 2) v = std::asinh(v);
+            mean[i] += v;
+            sq[i] += v * v;
         }
         ty += r[6];
     }
@@ -363,7 +367,7 @@ __global__ void mlp_forward_tc_kernel(const float* __restrict__ W_g, const float
     if (lane < 16) {
         const long long k = t0 + lane;
         for (int i = 0; i < kMlpIn; i++) {
-            const float v = (k < n) ? x[k * stride + i] : 0.0f;
+            const float v = (k < n) ? mlp_map(i, x[k * stride + i]) : 0.0f;
             X[w][lane][i] = fminf(fmaxf((v - W[kOffShift + i]) * W[kOffScale + i], -30.0f), 30.0f);
         }
         X[w][lane][6] = 0.0f;

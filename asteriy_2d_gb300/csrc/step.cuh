@@ -170,7 +170,8 @@ struct TileSmem {
     R Fz[4][TR][TZ + 1];         // z-face flux: mass, mom_z, mom_r, energy
     R Fr[4][TR + 1][TZ];         // r-face flux
     R qv[10][kQueueCap];         // queued exact-solver faces: enI teI pI rI cI enII teII pII rII cII
-    int qcode[kQueueCap];        // face code | active << 12 | swap << 13 | pattern << 14
+    int qcode[kQueueCap];        // face code | active << 12 | swap << 13 | pattern << 14 | strong << 16
+    short sq[kQueueCap];         // queue slots of the faces above the learned-start gate
     float mlp[kMlpParams];       // learned start value (guess == MLP)
     unsigned mB1[tc::kL1];       // its W1, W2 as per-lane f16 mma fragments
     unsigned mB2[tc::kL2];
@@ -179,6 +180,7 @@ struct TileSmem {
     R qp0[kQueueCap];            // start value of each queued face
     unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
     int nq;                      // queued faces (beyond kQueueCap they are solved in place)
+    int nsq;                     // entries of sq
 };
 
 template <typename R, int TZ, int TR>
@@ -255,11 +257,10 @@ __device__ __forceinline__ float wave_strength(const RPre<R>& q)
 // acoustic value.  Faces above the gate are counted in both forms, so the
 // two start values can be compared on the same faces.
 template <typename R>
-__device__ __forceinline__ R solve_queued(const StepParams& P, const Gas<R>& g, const RPre<R>& q, R p0_mlp,
-                                          RiemannCount& rc, int& fallback)
+__device__ __forceinline__ R solve_queued(const StepParams& P, const Gas<R>& g, const RPre<R>& q, bool strong,
+                                          R p0_mlp, RiemannCount& rc, int& fallback)
 {
     if (!P.riemann_newton) return solve_p_reference(g, q, rc);
-    const bool strong = wave_strength(q) > P.mlp_gate;
     R p0;
     if (P.guess == 1 && strong) {
         p0 = p0_mlp;
@@ -378,6 +379,7 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
             const RPre<R> q = godunov_pre(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT]);
             R p = R(0);
             if (q.pattern == 2 || q.pattern == 3) {
+                const bool strong = P.riemann_newton && wave_strength(q) > P.mlp_gate;
                 const int slot = atomicAdd(&sm.nq, 1);
                 if (slot < TileSmem<R, TZ, TR>::kQueueCap) {
                     sm.qv[0][slot] = q.enI; sm.qv[1][slot] = q.teI; sm.qv[2][slot] = q.pI;
@@ -385,12 +387,13 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
                     sm.qv[6][slot] = q.teII; sm.qv[7][slot] = q.pII; sm.qv[8][slot] = q.rII;
                     sm.qv[9][slot] = q.cII;
                     sm.qcode[slot] = (ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.swap ? 1 << 13 : 0) |
-                                     (q.pattern << 14);
+                                     (q.pattern << 14) | (strong ? 1 << 16 : 0);
+                    if (strong && P.guess == 1) sm.sq[atomicAdd(&sm.nsq, 1)] = (short)slot;
                     continue;
                 }
                 // queue full (more than kQueueCap iterative faces in the tile):
                 // solve in place, from the acoustic start value
-                p = solve_queued(P, g, q, R(-1), rc, fallback);
+                p = solve_queued(P, g, q, strong, R(-1), rc, fallback);
                 if (P.rec && step % P.rec_every == 0)
                     record_face(P, g, q, p, step, 2 * (mu * P.N + nu) + (ZF ? 0 : 1));
             }
@@ -418,16 +421,18 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
 {
     constexpr int NFZ = TR * (TZ + 1);
     const int nq = min(sm.nq, TileSmem<R, TZ, TR>::kQueueCap);
+    const int nsq = sm.nsq;
     if (P.riemann_newton && P.guess == 1) {
-        // phase 1: learned start values of the queued faces, 16 per warp
-        // tile on the tensor cores
+        // phase 1: learned start values of the queued faces above the gate,
+        // 16 per warp tile on the tensor cores
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        for (int t0 = 16 * w; t0 < nq; t0 += 16 * (kThreads / 32)) {
-            const int i = t0 + (lane & 15);
+        for (int t0 = 16 * w; t0 < nsq; t0 += 16 * (kThreads / 32)) {
+            const int jj = t0 + (lane & 15);
+            const int i = (jj < nsq) ? sm.sq[jj] : 0;
             R pL = R(1);
             if (lane < 16) {
                 float x[kMlpIn] = {0, 0, 0, 0, 0, 0};
-                if (i < nq) {
+                if (jj < nsq) {
                     RPre<R> q;
                     q.enI = sm.qv[0][i]; q.pI = sm.qv[2][i]; q.rI = sm.qv[3][i]; q.cI = sm.qv[4][i];
                     q.enII = sm.qv[5][i]; q.pII = sm.qv[7][i]; q.rII = sm.qv[8][i]; q.cII = sm.qv[9][i];
@@ -440,14 +445,15 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
 #pragma unroll
                 // standardised, and clamped to a range f16 holds exactly enough
                 for (int k = 0; k < kMlpIn; k++)
-                    sm.mX[w][lane][k] = fminf(fmaxf((x[k] - sm.mlp[kOffShift + k]) * sm.mlp[kOffScale + k], -30.0f), 30.0f);
+                    sm.mX[w][lane][k] =
+                        fminf(fmaxf((mlp_map(k, x[k]) - sm.mlp[kOffShift + k]) * sm.mlp[kOffScale + k], -30.0f), 30.0f);
                 sm.mX[w][lane][6] = 0.0f;
                 sm.mX[w][lane][7] = 0.0f;
             }
             __syncwarp();
             tc::forward16(sm.mlp, sm.mB1, sm.mB2, sm.mX[w], sm.mY[w]);
             __syncwarp();
-            if (lane < 16 && i < nq) sm.qp0[i] = pL * (R)__expf(sm.mY[w][lane]);
+            if (lane < 16 && jj < nsq) sm.qp0[i] = pL * (R)__expf(sm.mY[w][lane]);
             __syncwarp();
         }
         __syncthreads();
@@ -460,12 +466,13 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
         q.cII = sm.qv[9][i];
         const int code = sm.qcode[i];
         q.swap = (code >> 13) & 1;
-        q.pattern = code >> 14;
+        q.pattern = (code >> 14) & 3;
+        const bool strong = (code >> 16) & 1;
         q.Udf = q.enI - q.enII;
         q.Urz = q.Uvk = R(0);   // only the closed-form patterns read these
         const bool active = (code >> 12) & 1;
         const int fc = code & 0xfff;
-        const R p = solve_queued(P, g, q, (P.riemann_newton && P.guess == 1) ? sm.qp0[i] : R(0), rc, fallback);
+        const R p = solve_queued(P, g, q, strong, (strong && P.guess == 1) ? sm.qp0[i] : R(0), rc, fallback);
         R F[4];
         R Sp = godunov_sample(g, q, p, F, rc);
         if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
@@ -506,6 +513,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
     const int step = (P.clock != nullptr) ? (int)P.clock->step : 0;
     if (tid == 0) {
         sm.nq = 0;
+        sm.nsq = 0;
         s_tdv = T_do / (P.dx * P.dy);
         s_tdv_f = (float)s_tdv;
         s_T_f = (float)T_do;

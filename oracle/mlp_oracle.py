@@ -25,9 +25,18 @@ def silu_grad(z):
     return s * (1.0 + z * (1.0 - s))
 
 
+def input_map(x):
+    """The network's fixed input map: log of the positive ratios (features 0,
+    1, 3), asinh of the velocity jump (feature 2)."""
+    x = np.array(x, dtype=np.float64)
+    x[:, [0, 1, 3]] = np.log(x[:, [0, 1, 3]])
+    x[:, 2] = np.arcsinh(x[:, 2])
+    return x
+
+
 def forward(p, x):
     shift, scale, w1, b1, w2, b2, w3, b3 = unpack(p)
-    xn = (np.asarray(x, dtype=np.float64) - shift) * scale
+    xn = (input_map(x) - shift) * scale
     z1 = xn @ w1.T + b1
     h1 = silu(z1)
     z2 = h1 @ w2.T + b2

@@ -28,7 +28,7 @@ def synthetic_records(n, seed=0):
 def init_params(rec, seed=3):
     rng = np.random.default_rng(seed)
     p = np.zeros(MO.NPARAM)
-    x = rec[:, :6].astype(np.float64)
+    x = MO.input_map(rec[:, :6])
     p[0:6] = x.mean(0)
     sd = x.std(0)
     p[6:12] = np.where(sd > 1e-6, 1.0 / np.maximum(sd, 1e-12), 1.0)
@@ -48,7 +48,7 @@ def test_oracle_gradient_matches_finite_differences():
 def test_mlp_init_statistics():
     rec = synthetic_records(5000)
     p = solver.mlp_init(rec, seed=7)
-    x = rec[:, :6].astype(np.float64)
+    x = MO.input_map(rec[:, :6])
     np.testing.assert_allclose(p[0:6], x.mean(0), rtol=1e-4, atol=1e-5)
     assert np.all(p[6:12] > 0)
     assert np.all(p[204:236] == 0) and abs(p[1324] - rec[:, 6].mean()) < 1e-4
@@ -94,4 +94,4 @@ def test_tensor_core_inference_matches_fp32_network():
     ytc = solver.mlp_forward_tc(params, rec[:, :6])
     err = np.abs(ytc - y32)
     print("tensor-core vs FP32 network: max", err.max(), "median", np.median(err))
-    assert np.median(err) < 5e-3 and np.percentile(err, 99) < 0.02
+    assert np.median(err) < 5e-3 and np.percentile(err, 99.9) < 0.02 and err.max() < 0.05
