@@ -402,7 +402,7 @@ int ast_set_mlp(ast_solver* S, const float* params)
     return AST_OK;
 }
 
-int ast_record_start(ast_solver* S, int64_t capacity, int every)
+int ast_record_start(ast_solver* S, int64_t capacity, int every, double min_strength)
 {
     if (!S || capacity < 1 || every < 1) return fail(AST_ERR_INVALID, "bad argument");
     if (S->cfg.flux != AST_FLUX_GODUNOV) return fail(AST_ERR_UNSUPPORTED, "the recorder needs the exact solver");
@@ -417,6 +417,7 @@ int ast_record_start(ast_solver* S, int64_t capacity, int every)
     S->P.rec_n = S->rec_n;
     S->P.rec_cap = capacity;
     S->P.rec_every = every;
+    S->P.rec_gate = min_strength;
     drop_graph(S);
     return AST_OK;
 }

@@ -85,6 +85,7 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
     P.guess = c.guess;
     P.mlp_gate = (float)c.mlp_gate;
     P.rec_every = 1;
+    P.rec_gate = 0.0;
     for (int sd = 0; sd < 4; sd++) {
         P.bc_kind[sd] = c.bc[sd].kind;
         P.bc_val[sd][0] = c.bc[sd].rho;

@@ -85,6 +85,7 @@ struct StepParams {
     unsigned long long* rec_n;     // records written (may exceed rec_cap)
     long long rec_cap;
     int rec_every;                 // record on steps with step % rec_every == 0
+    double rec_gate;               // record faces with wave strength above this
 };
 
 // ------------------------------------------------------------------ loads
@@ -289,6 +290,7 @@ __device__ __forceinline__ void record_face(const StepParams& P, const Gas<R>& g
     const R uL = q.swap ? -q.enII : q.enI;
     const R rR = q.swap ? q.rI : q.rII, pR = q.swap ? q.pI : q.pII, cR = q.swap ? q.cI : q.cII;
     const R uR = q.swap ? -q.enI : q.enII;
+    if (P.rec_gate > 0.0 && !(wave_strength(q) > R(P.rec_gate))) return;
     const unsigned long long slot = atomicAdd(P.rec_n, 1ull);
     if ((long long)slot >= P.rec_cap) return;
     float* r = P.rec + slot * AST_RECORD_FLOATS;

@@ -15,15 +15,16 @@ from . import abi as A
 from .solver import Solver, mlp_init, mlp_train
 
 
-def record_faces(cfg, s0, u0, nsteps, every=1, capacity=1 << 24):
-    """Records of the iterative exact-solver faces over nsteps FP64 steps."""
+def record_faces(cfg, s0, u0, nsteps, every=1, capacity=1 << 24, min_strength=0.0):
+    """Records of the iterative exact-solver faces over nsteps FP64 steps
+    (only those with wave strength above min_strength when it is positive)."""
     c = cfg.copy()
     c.precision = A.PREC_FP64
     c.flux = A.FLUX_GODUNOV
     c.guess = A.GUESS_PVRS
     with Solver(c) as S:
         S.set_state(s0, u0)
-        S.record_start(capacity, every)
+        S.record_start(capacity, every, min_strength)
         S.step(nsteps)
         rec, offered = S.record_stop()
     key_step = rec[:, 7].view(np.int32).astype(np.int64)

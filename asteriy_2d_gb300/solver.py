@@ -46,7 +46,7 @@ SIGNATURES = {
     "ast_read_bin": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
     "ast_write_tecplot": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_int, C.c_double, C.c_char_p]),
     "ast_set_mlp": (C.c_int, [C.c_void_p, _fp]),
-    "ast_record_start": (C.c_int, [C.c_void_p, C.c_int64, C.c_int]),
+    "ast_record_start": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_double]),
     "ast_record_stop": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "ast_record_read": (C.c_int, [C.c_void_p, _fp, C.c_int64]),
     "ast_mlp_init": (C.c_int, [_fp, C.c_int64, C.c_uint64, _fp]),
@@ -260,8 +260,8 @@ class Solver:
         assert params.shape == (A.AST_MLP_NPARAM,)
         check(self.lib.ast_set_mlp(self.h, _fptr(params)), "ast_set_mlp")
 
-    def record_start(self, capacity, every=1):
-        check(self.lib.ast_record_start(self.h, capacity, every), "ast_record_start")
+    def record_start(self, capacity, every=1, min_strength=0.0):
+        check(self.lib.ast_record_start(self.h, capacity, every, min_strength), "ast_record_start")
         self._rec_cap = capacity
 
     def record_stop(self):

@@ -40,7 +40,8 @@ def main(argv=None):
     cfg = problems.blast_config(N, M, flux=A.FLUX_GODUNOV)
     s0, u0 = solver.fill_blast(cfg)
     t0 = time.time()
-    rec, offered = learned.record_faces(cfg, s0, u0, args.steps, every=args.every, capacity=args.capacity)
+    rec, offered = learned.record_faces(cfg, s0, u0, args.steps, every=args.every, capacity=args.capacity,
+                                        min_strength=args.gate)
     recorded = len(rec)
     rec = learned.strong_records(rec, args.gate)
     t1 = time.time()

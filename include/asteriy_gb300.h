@@ -201,11 +201,13 @@ int ast_device_state(ast_solver* solver, void** planes, int64_t* ld, int* elem_b
    prediction lies outside the pattern's bracket (counted in mlp_fallback). */
 int ast_set_mlp(ast_solver* solver, const float* params);  /* AST_MLP_NPARAM host floats */
 /* Face recorder: on the following steps with step % every == 0, every exact-
-   solver face that needs the iterative p* solve is written as one record of
-   AST_RECORD_FLOATS floats, up to `capacity` records (device buffer owned by
-   the solver).  ast_record_stop returns the number of faces offered, which
-   may exceed the capacity; ast_record_read copies min(n, stored) records. */
-int ast_record_start(ast_solver* solver, int64_t capacity, int every);
+   solver face that needs the iterative p* solve and whose wave strength
+   max(|ln(p_R/p_L)|, |u_R-u_L|/min(c_L,c_R)) exceeds min_strength (0 keeps
+   all) is written as one record of AST_RECORD_FLOATS floats, up to
+   `capacity` records (device buffer owned by the solver).  ast_record_stop
+   returns the number of faces offered, which may exceed the capacity;
+   ast_record_read copies min(n, stored) records. */
+int ast_record_start(ast_solver* solver, int64_t capacity, int every, double min_strength);
 int ast_record_stop(ast_solver* solver, int64_t* offered);
 int ast_record_read(ast_solver* solver, float* out, int64_t n);
 /* Training kernels (host arrays in and out, work on the current device).

@@ -40,6 +40,14 @@ def test_recorder_trainer_and_learned_guess():
     assert set(np.unique(pat)) <= {2, 3}
     strong = learned.strong_records(rec, 0.2)
     assert len(strong) > 500
+    # the recorder's own gate keeps the same faces (up to rounding of the
+    # strength right at the gate: the kernel tests it in FP64 state, the
+    # filter here from the float records)
+    gated, offered_g = learned.record_faces(cfg, s0, u0, 150, every=1, capacity=1 << 20, min_strength=0.2)
+    assert offered_g == len(gated)
+    assert abs(len(gated) - len(strong)) <= max(2, len(strong) // 1000), (len(gated), len(strong))
+    key = lambda r: set(zip(r[:, 7].view(np.int32).tolist(), r[:, 8].view(np.int32).tolist()))
+    assert len(key(gated) ^ key(strong)) <= max(4, len(strong) // 500)
     samples = learned.sample_records(strong, min(len(strong), 1 << 16), seed=7)
     params, losses = learned.train_guess(samples, epochs=60, batch=1024, lr=3e-3, seed=7)
     assert losses[-1] < 0.7 * losses[0], losses
