@@ -248,9 +248,12 @@ struct RPre {
     int pattern;
 };
 
+// the side swap (pI <= pII, normal velocities negated when swapped) and the
+// sound speeds of the two sides: the part of godunov_pre an iterative face
+// needs again once its pattern is known
 template <typename R>
-__device__ __forceinline__ RPre<R> godunov_pre(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR, R unR,
-                                               R utR)
+__device__ __forceinline__ RPre<R> godunov_sides(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR, R unR,
+                                                 R utR)
 {
     RPre<R> q;
     q.swap = pL > pR;
@@ -263,6 +266,17 @@ __device__ __forceinline__ RPre<R> godunov_pre(const Gas<R>& g, R rL, R pL, R un
     }
     q.cI = (q.rI != R(0)) ? sqrt(g.ga * q.pI / q.rI) : R(0);
     q.cII = (q.rII != R(0)) ? sqrt(g.ga * q.pII / q.rII) : R(0);
+    q.Udf = q.enI - q.enII;
+    q.Urz = q.Uvk = R(0);
+    q.pattern = 4;
+    return q;
+}
+
+template <typename R>
+__device__ __forceinline__ RPre<R> godunov_pre(const Gas<R>& g, R rL, R pL, R unL, R utL, R rR, R pR, R unR,
+                                               R utR)
+{
+    RPre<R> q = godunov_sides(g, rL, pL, unL, utL, rR, pR, unR, utR);
     const R a = sqrt(q.rI * (g.g2 * q.pII + g.g1 * q.pI) / R(2));
     const R Uud = (q.pII - q.pI) / a;
     q.Urz = R(-2) * q.cII / g.g1 * (R(1) - pow(q.pI / q.pII, g.gm));

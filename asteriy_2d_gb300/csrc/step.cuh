@@ -24,11 +24,6 @@
 namespace ast {
 
 constexpr int kThreads = 256;
-// queued exact-solver faces per tile (shared memory): 512 of the tile's 1072
-// faces in FP32, 256 in FP64; more iterative faces than that in one tile are
-// solved in place, from the acoustic start value
-template <typename R, int TZ, int TR>
-constexpr int queue_cap() { return sizeof(R) == 4 ? 512 : 256; }
 
 // device-resident clock and counters of a solver (one per solver)
 struct DevClock {
@@ -166,13 +161,15 @@ __device__ __forceinline__ T warp_max(T v)
 template <typename R, int TZ, int TR>
 struct TileSmem {
     static constexpr int HZ = TZ + 4, HR = TR + 4;
-    static constexpr int kQueueCap = queue_cap<R, TZ, TR>();
+    static constexpr int kNFZ = TR * (TZ + 1);                 // z faces of the tile
+    static constexpr int kQueueCap = kNFZ + (TR + 1) * TZ;    // all faces of the tile
     R q[4][HR][HZ];              // staged state with a two-cell halo
     R Fz[4][TR][TZ + 1];         // z-face flux: mass, mom_z, mom_r, energy
     R Fr[4][TR + 1][TZ];         // r-face flux
-    R qv[10][kQueueCap];         // queued exact-solver faces: enI teI pI rI cI enII teII pII rII cII
-    int qcode[kQueueCap];        // face code | active << 12 | swap << 13 | pattern << 14 | strong << 16
-    short sq[kQueueCap];         // queue slots of the faces above the learned-start gate
+    // queued exact-solver faces: face code | active << 12 | pattern << 14.
+    // Faces above the learned-start gate fill the queue from the front, the
+    // others from the back, so the two kinds sit in separate warps.
+    int qcode[kQueueCap];
     float mlp[kMlpParams];       // learned start value (guess == MLP)
     unsigned mB1[tc::kL1];       // its W1, W2 as per-lane f16 mma fragments
     unsigned mB2[tc::kL2];
@@ -180,8 +177,7 @@ struct TileSmem {
     float mY[kThreads / 32][16];     // per warp: network outputs
     R qp0[kQueueCap];            // start value of each queued face
     unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
-    int nq;                      // queued faces (beyond kQueueCap they are solved in place)
-    int nsq;                     // entries of sq
+    unsigned qn;                 // queued faces: above the gate (low 16 bits), others (high 16 bits)
 };
 
 template <typename R, int TZ, int TR>
@@ -313,6 +309,38 @@ __device__ __forceinline__ void record_face(const StepParams& P, const Gas<R>& g
 // mom_r, energy) order, to sm.Fz / sm.Fr and raises smax to the largest wave
 // speed of the faces that belong to at least one updated cell.  Exact-solver
 // faces of patterns 2 and 3 go to the queue instead.
+template <typename R, bool RECON, int TZ, int TR, bool ZF>
+__device__ __forceinline__ void face_states(const StepParams& P, const TileSmem<R, TZ, TR>& sm, int a, int c, bool hi,
+                                            R L[4], R U[4])
+{
+    constexpr int DJ = ZF ? 0 : 1, DI = ZF ? 1 : 0;
+    // smem indices of the lower (l) and upper (u) cell of the face
+    const int jl = ZF ? a + 2 : a + 1, il = ZF ? c + 1 : c + 2;
+    const int ju = a + 2, iu = c + 2;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const R tl = sm.q[k][jl][il], tu = sm.q[k][ju][iu];
+        L[k] = tl;
+        U[k] = tu;
+        if (RECON && hi) {
+            const R tll = sm.q[k][jl - DJ][il - DI], tuu = sm.q[k][ju + DJ][iu + DI];
+            R x0, x1;
+            recon_pair(tll, tl, tu, x0, x1);
+            L[k] = x1;                  // right/top value of the lower cell
+            recon_pair(tl, tu, tuu, x0, x1);
+            U[k] = x0;                  // left/bottom value of the upper cell
+            // positivity of the reconstructed rho and p (kernel.cu:2706-2743)
+            if (k == 0) {
+                if (L[0] <= R(0)) L[0] = tl;
+                if (U[0] <= R(0)) U[0] = tu;
+            } else if (k == 1) {
+                if (L[1] <= R(0) || !P.grad_p) L[1] = tl;
+                if (U[1] <= R(0) || !P.grad_p) U[1] = tu;
+            }
+        }
+    }
+}
+
 template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF>
 __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
                                           int m0, int step, RiemannCount& rc, int& fallback, R& smax)
@@ -322,7 +350,6 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
     constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
     constexpr int NN = ZF ? 2 : 3;           // normal velocity component
     constexpr int TT = ZF ? 3 : 2;           // tangential velocity component
-    constexpr int DJ = ZF ? 0 : 1, DI = ZF ? 1 : 0;
     for (int f = threadIdx.x; f < NF; f += kThreads) {
         const int a = f / W, c = f - a * W;
         // smem indices of the lower (l) and upper (u) cell of the face
@@ -341,28 +368,7 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
             hi = (xf > P.region_lo && xf < P.region_hi);
         }
         R L[4], U[4], F[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const R tl = sm.q[k][jl][il], tu = sm.q[k][ju][iu];
-            L[k] = tl;
-            U[k] = tu;
-            if (RECON && hi) {
-                const R tll = sm.q[k][jl - DJ][il - DI], tuu = sm.q[k][ju + DJ][iu + DI];
-                R x0, x1;
-                recon_pair(tll, tl, tu, x0, x1);
-                L[k] = x1;                  // right/top value of the lower cell
-                recon_pair(tl, tu, tuu, x0, x1);
-                U[k] = x0;                  // left/bottom value of the upper cell
-                // positivity of the reconstructed rho and p (kernel.cu:2706-2743)
-                if (k == 0) {
-                    if (L[0] <= R(0)) L[0] = tl;
-                    if (U[0] <= R(0)) U[0] = tu;
-                } else if (k == 1) {
-                    if (L[1] <= R(0) || !P.grad_p) L[1] = tl;
-                    if (U[1] <= R(0) || !P.grad_p) U[1] = tu;
-                }
-            }
-        }
+        face_states<R, RECON, TZ, TR, ZF>(P, sm, a, c, hi, L, U);
         R Sp;
         if (FLUX == 2 && hi && L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]) {
             // identical states: the exact solution is that state (the
@@ -379,27 +385,16 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
             Sp = fmax(fabs(un) + c, g.eps8);
         } else if (FLUX == 2 && hi) {
             const RPre<R> q = godunov_pre(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT]);
-            R p = R(0);
             if (q.pattern == 2 || q.pattern == 3) {
+                // the iterative faces go to the queue (room for every face
+                // of the tile); their flux is written by queue_pass
                 const bool strong = P.riemann_newton && wave_strength(q) > P.mlp_gate;
-                const int slot = atomicAdd(&sm.nq, 1);
-                if (slot < TileSmem<R, TZ, TR>::kQueueCap) {
-                    sm.qv[0][slot] = q.enI; sm.qv[1][slot] = q.teI; sm.qv[2][slot] = q.pI;
-                    sm.qv[3][slot] = q.rI; sm.qv[4][slot] = q.cI; sm.qv[5][slot] = q.enII;
-                    sm.qv[6][slot] = q.teII; sm.qv[7][slot] = q.pII; sm.qv[8][slot] = q.rII;
-                    sm.qv[9][slot] = q.cII;
-                    sm.qcode[slot] = (ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.swap ? 1 << 13 : 0) |
-                                     (q.pattern << 14) | (strong ? 1 << 16 : 0);
-                    if (strong && P.guess == 1) sm.sq[atomicAdd(&sm.nsq, 1)] = (short)slot;
-                    continue;
-                }
-                // queue full (more than kQueueCap iterative faces in the tile):
-                // solve in place, from the acoustic start value
-                p = solve_queued(P, g, q, strong, R(-1), rc, fallback);
-                if (P.rec && step % P.rec_every == 0)
-                    record_face(P, g, q, p, step, 2 * (mu * P.N + nu) + (ZF ? 0 : 1));
+                const unsigned old = atomicAdd(&sm.qn, strong ? 1u : 0x10000u);
+                const int slot = strong ? (int)(old & 0xffffu) : TileSmem<R, TZ, TR>::kQueueCap - 1 - (int)(old >> 16);
+                sm.qcode[slot] = (ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.pattern << 14);
+                continue;
             }
-            Sp = godunov_sample(g, q, p, F, rc);
+            Sp = godunov_sample(g, q, R(0), F, rc);
         } else if (FLUX == 1 && hi) {
             Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         } else {
@@ -416,36 +411,61 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
     }
 }
 
+// the exact-solver states of queued face fc (z faces first, then r faces):
+// its reconstructed sides, swapped as godunov_pre swaps them, with the
+// pattern found in face_pass; lower/upper states in the face frame too
+template <typename R, bool RECON, int TZ, int TR>
+__device__ __forceinline__ RPre<R> queued_face(const StepParams& P, const TileSmem<R, TZ, TR>& sm, const Gas<R>& g,
+                                               int fc, int pattern, int& a, int& c, bool& zf)
+{
+    constexpr int NFZ = TileSmem<R, TZ, TR>::kNFZ;
+    R L[4], U[4];
+    zf = fc < NFZ;
+    if (zf) {
+        a = fc / (TZ + 1);
+        c = fc - a * (TZ + 1);
+        face_states<R, RECON, TZ, TR, true>(P, sm, a, c, true, L, U);
+    } else {
+        a = (fc - NFZ) / TZ;
+        c = (fc - NFZ) - a * TZ;
+        face_states<R, RECON, TZ, TR, false>(P, sm, a, c, true, L, U);
+    }
+    // normal and tangential velocity: (v_z, v_r) on z faces, (v_r, v_z) on r faces
+    const R unL = zf ? L[2] : L[3], utL = zf ? L[3] : L[2];
+    const R unU = zf ? U[2] : U[3], utU = zf ? U[3] : U[2];
+    RPre<R> q = godunov_sides(g, L[0], L[1], unL, utL, U[0], U[1], unU, utU);
+    q.pattern = pattern;
+    return q;
+}
+
 // the queued exact-solver faces, solved by all threads of the CTA
-template <typename R, int TZ, int TR>
+template <typename R, bool RECON, int TZ, int TR>
 __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
                                            int m0, int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
 {
-    constexpr int NFZ = TR * (TZ + 1);
-    const int nq = min(sm.nq, TileSmem<R, TZ, TR>::kQueueCap);
-    const int nsq = sm.nsq;
+    constexpr int CAP = TileSmem<R, TZ, TR>::kQueueCap;
+    const int ns = (int)(sm.qn & 0xffffu), nw = (int)(sm.qn >> 16);
     if (P.riemann_newton && P.guess == 1) {
-        // phase 1: learned start values of the queued faces above the gate,
-        // 16 per warp tile on the tensor cores
+        // phase 1: learned start values of the faces above the gate (queue
+        // slots 0..ns-1), 16 per warp tile on the tensor cores
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        for (int t0 = 16 * w; t0 < nsq; t0 += 16 * (kThreads / 32)) {
-            const int jj = t0 + (lane & 15);
-            const int i = (jj < nsq) ? sm.sq[jj] : 0;
+        for (int t0 = 16 * w; t0 < ns; t0 += 16 * (kThreads / 32)) {
+            const int i = t0 + (lane & 15);
             R pL = R(1);
             if (lane < 16) {
                 float x[kMlpIn] = {0, 0, 0, 0, 0, 0};
-                if (jj < nsq) {
-                    RPre<R> q;
-                    q.enI = sm.qv[0][i]; q.pI = sm.qv[2][i]; q.rI = sm.qv[3][i]; q.cI = sm.qv[4][i];
-                    q.enII = sm.qv[5][i]; q.pII = sm.qv[7][i]; q.rII = sm.qv[8][i]; q.cII = sm.qv[9][i];
-                    q.swap = (sm.qcode[i] >> 13) & 1;
+                if (i < ns) {
+                    const int code = sm.qcode[i];
+                    int a, c;
+                    bool zf;
+                    const RPre<R> q = queued_face<R, RECON, TZ, TR>(P, sm, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
                     R rL, uL, cL, rR, pR, uR, cR;
                     face_sides(q, rL, pL, uL, cL, rR, pR, uR, cR);
                     mlp_features((float)g.ga, (float)rL, (float)pL, (float)uL, (float)cL, (float)rR, (float)pR,
                                  (float)uR, (float)cR, x);
                 }
-#pragma unroll
                 // standardised, and clamped to a range f16 holds exactly enough
+#pragma unroll
                 for (int k = 0; k < kMlpIn; k++)
                     sm.mX[w][lane][k] =
                         fminf(fmaxf((mlp_map(k, x[k]) - sm.mlp[kOffShift + k]) * sm.mlp[kOffScale + k], -30.0f), 30.0f);
@@ -455,42 +475,34 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
             __syncwarp();
             tc::forward16(sm.mlp, sm.mB1, sm.mB2, sm.mX[w], sm.mY[w]);
             __syncwarp();
-            if (lane < 16 && jj < nsq) sm.qp0[i] = pL * (R)__expf(sm.mY[w][lane]);
+            if (lane < 16 && i < ns) sm.qp0[i] = pL * (R)__expf(sm.mY[w][lane]);
             __syncwarp();
         }
         __syncthreads();
     }
-    // phase 2: p* (iteration), sampling and the flux of each queued face
-    for (int i = threadIdx.x; i < nq; i += kThreads) {
-        RPre<R> q;
-        q.enI = sm.qv[0][i]; q.teI = sm.qv[1][i]; q.pI = sm.qv[2][i]; q.rI = sm.qv[3][i]; q.cI = sm.qv[4][i];
-        q.enII = sm.qv[5][i]; q.teII = sm.qv[6][i]; q.pII = sm.qv[7][i]; q.rII = sm.qv[8][i];
-        q.cII = sm.qv[9][i];
+    // phase 2: p* (iteration), sampling and the flux of each queued face;
+    // threads 0..ns-1 take the faces above the gate
+    for (int t = threadIdx.x; t < ns + nw; t += kThreads) {
+        const bool strong = t < ns;
+        const int i = strong ? t : CAP - 1 - (t - ns);
         const int code = sm.qcode[i];
-        q.swap = (code >> 13) & 1;
-        q.pattern = (code >> 14) & 3;
-        const bool strong = (code >> 16) & 1;
-        q.Udf = q.enI - q.enII;
-        q.Urz = q.Uvk = R(0);   // only the closed-form patterns read these
         const bool active = (code >> 12) & 1;
-        const int fc = code & 0xfff;
+        int a, c;
+        bool zf;
+        const RPre<R> q = queued_face<R, RECON, TZ, TR>(P, sm, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
         const R p = solve_queued(P, g, q, strong, (strong && P.guess == 1) ? sm.qp0[i] : R(0), rc, fallback);
         R F[4];
         R Sp = godunov_sample(g, q, p, F, rc);
         if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
-        if (fc < NFZ) {
-            const int a = fc / (TZ + 1), c = fc - a * (TZ + 1);
+        if (zf) {
             sm.Fz[0][a][c] = F[0]; sm.Fz[1][a][c] = F[1]; sm.Fz[2][a][c] = F[2]; sm.Fz[3][a][c] = F[3];
             if (active) smz = fmax(smz, Sp);
-            if (P.rec && step % P.rec_every == 0)
-                record_face(P, g, q, p, step, 2 * ((m0 + a) * P.N + (n0 + c)) + 0);
         } else {
-            const int f2 = fc - NFZ, a = f2 / TZ, c = f2 - a * TZ;
             sm.Fr[0][a][c] = F[0]; sm.Fr[1][a][c] = F[2]; sm.Fr[2][a][c] = F[1]; sm.Fr[3][a][c] = F[3];
             if (active) smr = fmax(smr, Sp);
-            if (P.rec && step % P.rec_every == 0)
-                record_face(P, g, q, p, step, 2 * ((m0 + a) * P.N + (n0 + c)) + 1);
         }
+        if (P.rec && step % P.rec_every == 0)
+            record_face(P, g, q, p, step, 2 * ((m0 + a) * P.N + (n0 + c)) + (zf ? 0 : 1));
     }
 }
 
@@ -514,8 +526,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
     const double T_do = (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr;
     const int step = (P.clock != nullptr) ? (int)P.clock->step : 0;
     if (tid == 0) {
-        sm.nq = 0;
-        sm.nsq = 0;
+        sm.qn = 0u;
         s_tdv = T_do / (P.dx * P.dy);
         s_tdv_f = (float)s_tdv;
         s_T_f = (float)T_do;
@@ -551,7 +562,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
     face_pass<R, FLUX, RECON, TZ, TR, false>(P, sm, g, n0, m0, step, rc, fallback, smr);
     __syncthreads();
     if (FLUX == 2) {
-        queue_pass<R, TZ, TR>(P, sm, g, n0, m0, step, rc, fallback, smz, smr);
+        queue_pass<R, RECON, TZ, TR>(P, sm, g, n0, m0, step, rc, fallback, smz, smr);
         __syncthreads();
     }
 
