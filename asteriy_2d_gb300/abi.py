@@ -34,6 +34,8 @@ PREC_FP64, PREC_FP32 = 0, 1
 GUESS_PVRS, GUESS_MLP = 0, 1
 Z_LO, Z_HI, R_LO, R_HI = 0, 1, 2, 3
 BC_REFLECT, BC_OUTFLOW, BC_FIXED, BC_SUCTION = 0, 1, 2, 3
+SETUP_BLAST, SETUP_WIND = 0, 1
+AST_BATCH_MAX = 4096
 
 
 class ast_bc(C.Structure):
@@ -84,6 +86,13 @@ class ast_stats(C.Structure):
         ("bisect_calls", C.c_uint64), ("bisect_iters", C.c_uint64),
         ("mlp_fallback", C.c_uint64), ("strong_calls", C.c_uint64), ("strong_iters", C.c_uint64),
         ("reserved", C.c_uint64 * 2),
+    ]
+
+
+class ast_problem(C.Structure):
+    _fields_ = [
+        ("cfg", ast_config), ("setup", C.c_int32), ("reserved_i", C.c_int32),
+        ("mach", C.c_double), ("seed", C.c_uint64), ("reserved_d", C.c_double * 5),
     ]
 
 

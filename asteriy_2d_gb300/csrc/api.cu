@@ -17,6 +17,7 @@
 #include <string>
 
 #include "../../include/asteriy_gb300.h"
+#include "convert.cuh"
 #include "launch.cuh"
 
 using namespace ast;
@@ -37,31 +38,6 @@ int fail(int code, const char* msg)
     return code;
 }
 
-// ---------------------------------------------------------------- layout conversion
-template <typename R>
-__global__ void aos_to_soa(const double2* __restrict__ s, const double2* __restrict__ u, R* __restrict__ q,
-                           int N, int M, long long ld, long long plane)
-{
-    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (long long)N * M) return;
-    int m = (int)(k / N), n = (int)(k - (long long)m * N);
-    long long o = (long long)m * ld + n;
-    double2 a = s[k], b = u[k];
-    q[o] = (R)a.x; q[o + plane] = (R)a.y; q[o + 2 * plane] = (R)b.x; q[o + 3 * plane] = (R)b.y;
-}
-
-template <typename R>
-__global__ void soa_to_aos(const R* __restrict__ q, double2* __restrict__ s, double2* __restrict__ u, int N,
-                           int M, long long ld, long long plane)
-{
-    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (long long)N * M) return;
-    int m = (int)(k / N), n = (int)(k - (long long)m * N);
-    long long o = (long long)m * ld + n;
-    s[k] = make_double2((double)q[o], (double)q[o + plane]);
-    u[k] = make_double2((double)q[o + 2 * plane], (double)q[o + 3 * plane]);
-}
-
 __global__ void funk_time_kernel(double* T, double* T_do, double* TT, int* i)
 {
     *T_do = *T;
@@ -77,6 +53,8 @@ int ast::cuda_fail(cudaError_t e, const char* what)
     g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
     return AST_ERR_CUDA;
 }
+
+int ast::set_error(int code, const char* msg) { return fail(code, msg); }
 
 // ==================================================================== solver
 struct ast_solver {

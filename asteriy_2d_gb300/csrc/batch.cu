@@ -1,0 +1,493 @@
+// batch.cu - many independent problems advanced together (the ast_batch_*
+// entry points of include/asteriy_gb300.h).
+//
+// The problems are grouped into classes by (flux, recon), the two template
+// parameters of the step code that differ between them; inside a class
+// they are ordered by decreasing tile count.  A class owns one contiguous
+// range of the device parameter arrays (one StepParams per problem, one
+// array per ping-pong parity) and one tile prefix sum, and steps with one
+// launch of batch_kernel over all of its problems' tiles.  Each problem has
+// its own DevClock, so its dt reduction and funk_time shift stay its own
+// (the last of its tiles to finish performs them).
+//
+// Blocks of 16 steps are captured into one CUDA graph in which every class
+// is an independent chain of launches: classes are forked from the caller's
+// stream at the start of the block and joined at its end, so cheap (HLLC)
+// and expensive (exact Godunov) classes overlap on the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "../../include/asteriy_gb300.h"
+#include "convert.cuh"
+#include "launch.cuh"
+
+using namespace ast;
+
+namespace {
+
+struct BatchClass {
+    int flux, recon;
+    int first, count;    // slots [first, first + count) of the parameter arrays
+    int tiles;           // work-list length
+    int ts_off;          // offset of its count+1 prefix sums in the tile_start array
+};
+
+#define BATCH_CUDA(call)                                    \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+int tiles_of(const ast_config& c) { return ((c.N + kTZ - 1) / kTZ) * ((c.M + kTR - 1) / kTR); }
+
+}  // namespace
+
+struct ast_batch {
+    int nprob = 0;
+    size_t elem = 8;
+    std::vector<ast_config> cfg;        // user order
+    std::vector<int> slot;              // user index -> parameter slot
+    std::vector<long long> ld, plane;   // user order
+    std::vector<size_t> off;            // user order: byte offset of time level 0 in the arena
+    std::vector<size_t> level_bytes;    // user order: bytes of one time level
+    std::vector<StepParams> hP;         // slot order, without state pointers
+    std::vector<BatchClass> cls;
+    void* arena = nullptr;
+    DevClock* clocks = nullptr;         // user order
+    StepParams* dP[2] = {nullptr, nullptr};
+    int* tile_start = nullptr;
+    double* stage_s = nullptr;
+    double* stage_u = nullptr;
+    float* mlp = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaStream_t> aux;      // one per class beyond the first
+    std::vector<cudaEvent_t> ev;        // fork event + one join event per aux stream
+    int cur = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0, graph_cur = -1;
+    long long cells = 0, tiles = 0;
+};
+
+namespace {
+
+void drop_graph(ast_batch* B)
+{
+    if (B->graph) {
+        cudaGraphExecDestroy(B->graph);
+        B->graph = nullptr;
+    }
+}
+
+// parameter arrays of both parities (state pointers of each problem's two
+// time levels) from the host copies
+int upload_params(ast_batch* B)
+{
+    std::vector<StepParams> P(B->hP);
+    for (int par = 0; par < 2; par++) {
+        for (int i = 0; i < B->nprob; i++) {
+            StepParams& p = P[B->slot[i]];
+            char* base = (char*)B->arena + B->off[i];
+            p.in = base + (par ? B->level_bytes[i] : 0);
+            p.out = base + (par ? 0 : B->level_bytes[i]);
+        }
+        BATCH_CUDA(cudaMemcpy(B->dP[par], P.data(), sizeof(StepParams) * P.size(), cudaMemcpyHostToDevice));
+    }
+    return AST_OK;
+}
+
+int launch_class(ast_batch* B, const BatchClass& c, cudaStream_t st, bool launch)
+{
+    const StepParams* Ps = B->dP[B->cur] + c.first;
+    const int* ts = B->tile_start + c.ts_off;
+    return (B->elem == 8) ? launch_batch_r<double>(Ps, ts, c.count, c.tiles, c.flux, c.recon, st, launch)
+                          : launch_batch_r<float>(Ps, ts, c.count, c.tiles, c.flux, c.recon, st, launch);
+}
+
+// `count` steps of every class; classes beyond the first run on their own
+// streams, forked from and joined back into `st`
+int enqueue_steps(ast_batch* B, cudaStream_t st, int count)
+{
+    const int nc = (int)B->cls.size();
+    if (nc > 1) {
+        BATCH_CUDA(cudaEventRecord(B->ev[0], st));
+        for (int c = 1; c < nc; c++) BATCH_CUDA(cudaStreamWaitEvent(B->aux[c - 1], B->ev[0], 0));
+    }
+    const int cur0 = B->cur;
+    for (int c = 0; c < nc; c++) {
+        cudaStream_t sc = (c == 0) ? st : B->aux[c - 1];
+        B->cur = cur0;
+        for (int i = 0; i < count; i++) {
+            int rc = launch_class(B, B->cls[c], sc, true);
+            if (rc != AST_OK) {
+                B->cur = cur0;
+                return rc;
+            }
+            B->cur ^= 1;
+        }
+    }
+    if (nc > 1) {
+        for (int c = 1; c < nc; c++) {
+            BATCH_CUDA(cudaEventRecord(B->ev[c], B->aux[c - 1]));
+            BATCH_CUDA(cudaStreamWaitEvent(st, B->ev[c], 0));
+        }
+    }
+    return AST_OK;
+}
+
+int capture_block(ast_batch* B, int count)
+{
+    drop_graph(B);
+    cudaStream_t cs;
+    BATCH_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    const int cur0 = B->cur;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    int rc = AST_OK;
+    if (e == cudaSuccess) {
+        rc = enqueue_steps(B, cs, count);
+        e = cudaStreamEndCapture(cs, &graph);
+    }
+    B->cur = cur0;
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
+    if (rc != AST_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    e = cudaGraphInstantiate(&B->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    B->graph_steps = count;
+    B->graph_cur = cur0;
+    return AST_OK;
+}
+
+bool bad_prob(const ast_batch* B, int prob) { return !B || prob < 0 || prob >= B->nprob; }
+
+}  // namespace
+
+extern "C" {
+
+int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
+{
+    if (!cfgs || !out || nprob < 1 || nprob > AST_BATCH_MAX) return set_error(AST_ERR_INVALID, "bad argument");
+    *out = nullptr;
+    for (int i = 0; i < nprob; i++) {
+        const int rc = ast_config_check(&cfgs[i]);
+        if (rc != AST_OK) return set_error(rc, "invalid problem configuration");
+        if (cfgs[i].precision != cfgs[0].precision)
+            return set_error(AST_ERR_INVALID, "all problems of a batch share one precision");
+    }
+    ast_batch* B = new (std::nothrow) ast_batch();
+    if (!B) return set_error(AST_ERR_NOMEM, "host allocation");
+    B->nprob = nprob;
+    B->elem = (cfgs[0].precision == AST_PREC_FP32) ? 4 : 8;
+    B->cfg.assign(cfgs, cfgs + nprob);
+    B->ld.resize(nprob);
+    B->plane.resize(nprob);
+    B->off.resize(nprob);
+    B->level_bytes.resize(nprob);
+    B->slot.resize(nprob);
+
+    // arena layout: per problem two time levels of four planes, each level
+    // 256-byte aligned, rows padded to 128 bytes
+    size_t total = 0, maxK = 0;
+    const long long align = 128 / (long long)B->elem;
+    for (int i = 0; i < nprob; i++) {
+        const ast_config& c = B->cfg[i];
+        B->ld[i] = ((long long)c.N + align - 1) / align * align;
+        B->plane[i] = B->ld[i] * c.M;
+        B->level_bytes[i] = ((size_t)B->plane[i] * 4 * B->elem + 255) / 256 * 256;
+        B->off[i] = total;
+        total += 2 * B->level_bytes[i];
+        maxK = std::max(maxK, (size_t)c.N * c.M);
+        B->cells += (long long)c.N * c.M;
+        B->tiles += tiles_of(c);
+    }
+
+    // classes by (flux, recon); inside a class, larger problems first
+    std::vector<int> order(nprob);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const ast_config &x = B->cfg[a], &y = B->cfg[b];
+        if (x.flux != y.flux) return x.flux > y.flux;   // exact Godunov first
+        if (x.recon != y.recon) return x.recon > y.recon;
+        return tiles_of(x) > tiles_of(y);
+    });
+    std::vector<int> ts_host;
+    for (int s = 0; s < nprob; s++) {
+        const ast_config& c = B->cfg[order[s]];
+        if (B->cls.empty() || B->cls.back().flux != c.flux || B->cls.back().recon != c.recon) {
+            BatchClass k;
+            k.flux = c.flux;
+            k.recon = c.recon;
+            k.first = s;
+            k.count = 0;
+            k.tiles = 0;
+            k.ts_off = (int)ts_host.size();
+            ts_host.push_back(0);
+            B->cls.push_back(k);
+        }
+        BatchClass& k = B->cls.back();
+        k.count++;
+        k.tiles += tiles_of(c);
+        ts_host.push_back(k.tiles);
+        B->slot[order[s]] = s;
+    }
+
+    cudaError_t e;
+    const size_t nts = ts_host.size();
+    if ((e = cudaMalloc(&B->arena, total)) != cudaSuccess ||
+        (e = cudaMalloc(&B->clocks, sizeof(DevClock) * nprob)) != cudaSuccess ||
+        (e = cudaMalloc(&B->dP[0], sizeof(StepParams) * nprob)) != cudaSuccess ||
+        (e = cudaMalloc(&B->dP[1], sizeof(StepParams) * nprob)) != cudaSuccess ||
+        (e = cudaMalloc(&B->tile_start, sizeof(int) * nts)) != cudaSuccess ||
+        (e = cudaMalloc(&B->stage_s, maxK * 2 * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&B->stage_u, maxK * 2 * sizeof(double))) != cudaSuccess) {
+        ast_batch_destroy(B);
+        set_error(AST_ERR_NOMEM, "batch device allocation");
+        return AST_ERR_NOMEM;
+    }
+    int rc = AST_OK;
+    if ((e = cudaMemset(B->arena, 0, total)) != cudaSuccess ||
+        (e = cudaMemcpy(B->tile_start, ts_host.data(), sizeof(int) * nts, cudaMemcpyHostToDevice)) != cudaSuccess)
+        rc = cuda_fail(e, "batch initialisation");
+    std::vector<DevClock> clk(nprob);
+    B->hP.resize(nprob);
+    for (int i = 0; i < nprob && rc == AST_OK; i++) {
+        std::memset(&clk[i], 0, sizeof(DevClock));
+        clk[i].T_do = B->cfg[i].dt_first;
+        StepParams& p = B->hP[B->slot[i]];
+        fill_step_params(p, B->cfg[i]);
+        p.ld = B->ld[i];
+        p.plane = B->plane[i];
+        p.clock = B->clocks + i;
+    }
+    if (rc == AST_OK &&
+        (e = cudaMemcpy(B->clocks, clk.data(), sizeof(DevClock) * nprob, cudaMemcpyHostToDevice)) != cudaSuccess)
+        rc = cuda_fail(e, "batch clocks");
+    if (rc == AST_OK) rc = upload_params(B);
+    for (size_t c = 0; c < B->cls.size() && rc == AST_OK; c++) rc = launch_class(B, B->cls[c], nullptr, false);
+    for (size_t c = 1; c < B->cls.size() && rc == AST_OK; c++) {
+        cudaStream_t s;
+        if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) {
+            rc = cuda_fail(e, "batch stream");
+            break;
+        }
+        B->aux.push_back(s);
+    }
+    for (size_t c = 0; c < B->cls.size() && rc == AST_OK; c++) {
+        cudaEvent_t ev;
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+            rc = cuda_fail(e, "batch event");
+            break;
+        }
+        B->ev.push_back(ev);
+    }
+    if (rc != AST_OK) {
+        ast_batch_destroy(B);
+        return rc;
+    }
+    *out = B;
+    return AST_OK;
+}
+
+int ast_batch_destroy(ast_batch* B)
+{
+    if (!B) return AST_OK;
+    drop_graph(B);
+    for (cudaStream_t s : B->aux) cudaStreamDestroy(s);
+    for (cudaEvent_t e : B->ev) cudaEventDestroy(e);
+    cudaFree(B->arena);
+    cudaFree(B->clocks);
+    cudaFree(B->dP[0]);
+    cudaFree(B->dP[1]);
+    cudaFree(B->tile_start);
+    cudaFree(B->stage_s);
+    cudaFree(B->stage_u);
+    cudaFree(B->mlp);
+    delete B;
+    return AST_OK;
+}
+
+int ast_batch_set_stream(ast_batch* B, void* stream)
+{
+    if (!B) return set_error(AST_ERR_INVALID, "null batch");
+    B->stream = (cudaStream_t)stream;
+    drop_graph(B);
+    return AST_OK;
+}
+
+int ast_batch_set_state(ast_batch* B, int prob, const double* s, const double* u, int on_device)
+{
+    if (bad_prob(B, prob) || !s || !u) return set_error(AST_ERR_INVALID, "bad argument");
+    const ast_config& c = B->cfg[prob];
+    const long long K = (long long)c.N * c.M;
+    const size_t bytes = (size_t)K * 2 * sizeof(double);
+    const double* ds = s;
+    const double* du = u;
+    if (!on_device) {
+        BATCH_CUDA(cudaMemcpyAsync(B->stage_s, s, bytes, cudaMemcpyHostToDevice, B->stream));
+        BATCH_CUDA(cudaMemcpyAsync(B->stage_u, u, bytes, cudaMemcpyHostToDevice, B->stream));
+        ds = B->stage_s;
+        du = B->stage_u;
+    }
+    void* dst = (char*)B->arena + B->off[prob] + (B->cur ? B->level_bytes[prob] : 0);
+    const int nb = (int)((K + 255) / 256);
+    if (B->elem == 8)
+        aos_to_soa<double><<<nb, 256, 0, B->stream>>>((const double2*)ds, (const double2*)du, (double*)dst, c.N, c.M,
+                                                      B->ld[prob], B->plane[prob]);
+    else
+        aos_to_soa<float><<<nb, 256, 0, B->stream>>>((const double2*)ds, (const double2*)du, (float*)dst, c.N, c.M,
+                                                     B->ld[prob], B->plane[prob]);
+    BATCH_CUDA(cudaGetLastError());
+    if (!on_device) BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    return AST_OK;
+}
+
+int ast_batch_get_state(ast_batch* B, int prob, double* s, double* u, int on_device)
+{
+    if (bad_prob(B, prob) || !s || !u) return set_error(AST_ERR_INVALID, "bad argument");
+    const ast_config& c = B->cfg[prob];
+    const long long K = (long long)c.N * c.M;
+    double* ds = on_device ? s : B->stage_s;
+    double* du = on_device ? u : B->stage_u;
+    const void* src = (const char*)B->arena + B->off[prob] + (B->cur ? B->level_bytes[prob] : 0);
+    const int nb = (int)((K + 255) / 256);
+    if (B->elem == 8)
+        soa_to_aos<double><<<nb, 256, 0, B->stream>>>((const double*)src, (double2*)ds, (double2*)du, c.N, c.M,
+                                                      B->ld[prob], B->plane[prob]);
+    else
+        soa_to_aos<float><<<nb, 256, 0, B->stream>>>((const float*)src, (double2*)ds, (double2*)du, c.N, c.M,
+                                                     B->ld[prob], B->plane[prob]);
+    BATCH_CUDA(cudaGetLastError());
+    if (!on_device) {
+        const size_t bytes = (size_t)K * 2 * sizeof(double);
+        BATCH_CUDA(cudaMemcpyAsync(s, ds, bytes, cudaMemcpyDeviceToHost, B->stream));
+        BATCH_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, B->stream));
+        BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    }
+    return AST_OK;
+}
+
+int ast_batch_set_clock(ast_batch* B, int prob, double T_do, double TT, int64_t step)
+{
+    if (bad_prob(B, prob)) return set_error(AST_ERR_INVALID, "bad argument");
+    DevClock c;
+    BATCH_CUDA(cudaMemcpyAsync(&c, B->clocks + prob, sizeof c, cudaMemcpyDeviceToHost, B->stream));
+    BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    c.T_do = T_do;
+    c.TT = TT;
+    c.step = step;
+    c.smax_z = c.smax_r = 0;
+    c.done = 0;
+    BATCH_CUDA(cudaMemcpyAsync(B->clocks + prob, &c, sizeof c, cudaMemcpyHostToDevice, B->stream));
+    BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    return AST_OK;
+}
+
+int ast_batch_get_clock(ast_batch* B, int prob, double* T_do, double* TT, int64_t* step)
+{
+    if (bad_prob(B, prob)) return set_error(AST_ERR_INVALID, "bad argument");
+    DevClock c;
+    BATCH_CUDA(cudaMemcpyAsync(&c, B->clocks + prob, sizeof c, cudaMemcpyDeviceToHost, B->stream));
+    BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    if (T_do) *T_do = c.T_do;
+    if (TT) *TT = c.TT;
+    if (step) *step = c.step;
+    return AST_OK;
+}
+
+int ast_batch_step(ast_batch* B, int nsteps)
+{
+    if (!B || nsteps < 0) return set_error(AST_ERR_INVALID, "bad argument");
+    for (int i = 0; i < B->nprob; i++) {
+        const ast_config& c = B->cfg[i];
+        if (c.flux == AST_FLUX_GODUNOV && c.guess == AST_GUESS_MLP && B->hP[B->slot[i]].riemann_newton && !B->mlp)
+            return set_error(AST_ERR_INVALID, "guess == MLP needs ast_batch_set_mlp first");
+    }
+    // a block of an even number of steps returns to the same buffers, so
+    // one captured block is replayed back to back
+    const int block = 16;
+    while (nsteps >= block) {
+        if (!B->graph || B->graph_steps != block || B->graph_cur != B->cur) {
+            const int rc = capture_block(B, block);
+            if (rc != AST_OK) return rc;
+        }
+        BATCH_CUDA(cudaGraphLaunch(B->graph, B->stream));
+        nsteps -= block;
+    }
+    if (nsteps > 0) {
+        const int cur0 = B->cur;
+        const int rc = enqueue_steps(B, B->stream, nsteps);
+        if (rc != AST_OK) return rc;
+        B->cur = cur0 ^ (nsteps & 1);
+    }
+    return AST_OK;
+}
+
+int ast_batch_synchronize(ast_batch* B)
+{
+    if (!B) return set_error(AST_ERR_INVALID, "null batch");
+    BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    std::vector<DevClock> c(B->nprob);
+    BATCH_CUDA(cudaMemcpy(c.data(), B->clocks, sizeof(DevClock) * B->nprob, cudaMemcpyDeviceToHost));
+    for (const DevClock& k : c)
+        if (k.status & AST_ST_NONFINITE) return set_error(AST_ERR_NUMERIC, "non-finite wave speed");
+    return AST_OK;
+}
+
+int ast_batch_get_stats(ast_batch* B, int prob, ast_stats* out, int reset)
+{
+    if (bad_prob(B, prob) || !out) return set_error(AST_ERR_INVALID, "bad argument");
+    DevClock c;
+    BATCH_CUDA(cudaMemcpyAsync(&c, B->clocks + prob, sizeof c, cudaMemcpyDeviceToHost, B->stream));
+    BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    std::memset(out, 0, sizeof *out);
+    out->status = c.status;
+    out->rho_floor = c.cnt[0];
+    out->p_floor = c.cnt[1];
+    out->newton_calls = c.cnt[2];
+    out->newton_iters = c.cnt[3];
+    out->bisect_calls = c.cnt[4];
+    out->bisect_iters = c.cnt[5];
+    out->mlp_fallback = c.cnt[6];
+    out->newton_max_iters = (uint32_t)c.cnt[7];
+    out->strong_calls = c.cnt[8];
+    out->strong_iters = c.cnt[9];
+    if (reset) {
+        c.status = 0;
+        std::memset(c.cnt, 0, sizeof c.cnt);
+        BATCH_CUDA(cudaMemcpyAsync(B->clocks + prob, &c, sizeof c, cudaMemcpyHostToDevice, B->stream));
+        BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    }
+    return AST_OK;
+}
+
+int ast_batch_set_mlp(ast_batch* B, const float* params)
+{
+    if (!B || !params) return set_error(AST_ERR_INVALID, "null argument");
+    // the parameter arrays may be in use by queued steps
+    BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    if (!B->mlp) BATCH_CUDA(cudaMalloc(&B->mlp, sizeof(float) * AST_MLP_NPARAM));
+    BATCH_CUDA(cudaMemcpy(B->mlp, params, sizeof(float) * AST_MLP_NPARAM, cudaMemcpyHostToDevice));
+    for (StepParams& p : B->hP) p.mlp = B->mlp;
+    drop_graph(B);
+    return upload_params(B);
+}
+
+int ast_batch_info(ast_batch* B, int64_t* cells, int64_t* tiles, int* launches_per_step)
+{
+    if (!B) return set_error(AST_ERR_INVALID, "null batch");
+    if (cells) *cells = B->cells;
+    if (tiles) *tiles = B->tiles;
+    if (launches_per_step) *launches_per_step = (int)B->cls.size();
+    return AST_OK;
+}
+
+}  // extern "C"

@@ -126,6 +126,84 @@ int ast_fill_wind(const ast_config* c, double r_w, double rho_w, double v_w, dou
     return AST_OK;
 }
 
+// ---------------------------------------------------------------- problem sets
+namespace {
+
+inline double unit_draw(std::mt19937_64& gen) { return (double)(gen() >> 11) * 0x1.0p-53; }
+
+void set_side(ast_config* c, int side, int kind, double rho = 0, double p = 0, double vz = 0, double vr = 0)
+{
+    c->bc[side].kind = kind;
+    c->bc[side].rho = rho;
+    c->bc[side].p = p;
+    c->bc[side].vz = vz;
+    c->bc[side].vr = vr;
+}
+
+// the blast / wind configurations of the single-problem benchmarks: z in
+// [-1, 1], r in [0, 1], minmod, axisymmetric, CFL 0.4, reflecting axis
+void base_config(ast_config* c, int N, int M, double gamma, int flux, int precision)
+{
+    ast_config_default(c);
+    c->N = N;
+    c->M = M;
+    c->x_min = -1.0;
+    c->x_max = 1.0;
+    c->y_max = 1.0;
+    c->gamma = gamma;
+    c->cfl = 0.4;
+    c->flux = flux;
+    c->recon = AST_RECON_MINMOD;
+    c->geom = AST_GEOM_AXISYM;
+    c->precision = precision;
+    set_side(c, AST_Z_LO, AST_BC_OUTFLOW);
+    set_side(c, AST_Z_HI, AST_BC_OUTFLOW);
+    set_side(c, AST_R_LO, AST_BC_REFLECT);
+    set_side(c, AST_R_HI, AST_BC_OUTFLOW);
+}
+
+}  // namespace
+
+int ast_problem_set(uint64_t seed, int nprob, int precision, ast_problem* out)
+{
+    if (!out || nprob < 1 || precision < AST_PREC_FP64 || precision > AST_PREC_FP32) return AST_ERR_INVALID;
+    std::mt19937_64 gen(seed);
+    for (int i = 0; i < nprob; i++) {
+        ast_problem* P = &out[i];
+        std::memset(P, 0, sizeof *P);
+        const int M = (int)std::lround(64.0 * std::pow(8.0, unit_draw(gen)));
+        P->mach = 1.5 + 4.5 * unit_draw(gen);
+        const double gamma = (gen() >> 63) ? 1.4 : 5.0 / 3.0;
+        P->setup = (gen() >> 63) ? AST_SETUP_WIND : AST_SETUP_BLAST;
+        const int flux = (gen() >> 63) ? AST_FLUX_GODUNOV : AST_FLUX_HLLC;
+        P->seed = gen();
+        base_config(&P->cfg, 2 * M, M, gamma, flux, precision);
+        if (P->setup == AST_SETUP_WIND) {
+            // counterflow (rho 1, p 1/gamma: sound speed 1) entering at z = 1;
+            // the wind sphere R < 0.05 at the origin is held fixed
+            set_side(&P->cfg, AST_Z_HI, AST_BC_FIXED, 1.0, 1.0 / gamma, -P->mach, 0.0);
+            P->cfg.fixed_region = 1;
+            P->cfg.fixed_zc = 0.0;
+            P->cfg.fixed_az = P->cfg.fixed_ar = 0.05;
+        }
+    }
+    return AST_OK;
+}
+
+int ast_problem_fill(const ast_problem* P, double* s, double* u)
+{
+    if (!P || !s || !u) return AST_ERR_INVALID;
+    const ast_config* c = &P->cfg;
+    if (P->setup == AST_SETUP_BLAST) {
+        const double g = c->gamma, m2 = P->mach * P->mach;
+        const double p_out = 0.1, p_in = p_out * (2.0 * g * m2 - (g - 1.0)) / (g + 1.0);
+        return ast_fill_blast(c, p_in, p_out, 0.2, s, u);
+    }
+    if (P->setup == AST_SETUP_WIND)
+        return ast_fill_wind(c, 0.05, 1.0, 10.0, 10.0, 1.0, 1.0 / c->gamma, -P->mach, 0.01, P->seed, s, u);
+    return AST_ERR_INVALID;
+}
+
 int ast_write_bin(const ast_config* c, const double* s, const double* u, const char* path)
 {
     if (!c || !s || !u || !path || ast_config_check(c) != AST_OK) return AST_ERR_INVALID;

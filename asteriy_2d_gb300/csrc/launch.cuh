@@ -1,6 +1,6 @@
-// launch.cuh - launch helpers of the step kernel.  The instantiations are
+// launch.cuh - launch helpers of the step kernels.  The instantiations are
 // spread over several translation units (step_f64.cu, step_f32.cu,
-// step_raw.cu) so that they compile in parallel.
+// step_raw.cu, batch_f64.cu, batch_f32.cu) so that they compile in parallel.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -16,6 +16,8 @@ constexpr int kTZ = 32, kTR = 16;
 
 // records the failure text for ast_last_error() and returns AST_ERR_CUDA
 int cuda_fail(cudaError_t e, const char* what);
+// records msg for ast_last_error() and returns code
+int set_error(int code, const char* msg);
 
 // launch=false only raises the kernel's dynamic shared-memory limit, which
 // must happen outside stream capture (ast_create, ast_step_raw)
@@ -46,6 +48,36 @@ int launch_step_r(const StepParams& P, int flux, int recon, cudaStream_t st, boo
     if (flux == AST_FLUX_HLL) return launch_step_t<R, 0, false, LAYOUT>(P, st, launch);
     if (flux == AST_FLUX_HLLC) return launch_step_t<R, 1, false, LAYOUT>(P, st, launch);
     return launch_step_t<R, 2, false, LAYOUT>(P, st, launch);
+}
+
+// the batch kernel of one (flux, recon) class over `tiles` work-list entries
+template <typename R, int FLUX, bool RECON>
+int launch_batch_t(const StepParams* Ps, const int* tile_start, int nprob, int tiles, cudaStream_t st, bool launch)
+{
+    auto k = batch_kernel<R, FLUX, RECON, kTZ, kTR>;
+    constexpr size_t smem = tile_smem_bytes<R, kTZ, kTR>();
+    cudaError_t e;
+    if (!launch) {
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaFuncSetAttribute");
+    }
+    k<<<tiles, kThreads, smem, st>>>(Ps, tile_start, nprob);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? AST_OK : cuda_fail(e, "batch kernel launch");
+}
+
+template <typename R>
+int launch_batch_r(const StepParams* Ps, const int* tile_start, int nprob, int tiles, int flux, int recon,
+                   cudaStream_t st, bool launch)
+{
+    if (recon) {
+        if (flux == AST_FLUX_HLL) return launch_batch_t<R, 0, true>(Ps, tile_start, nprob, tiles, st, launch);
+        if (flux == AST_FLUX_HLLC) return launch_batch_t<R, 1, true>(Ps, tile_start, nprob, tiles, st, launch);
+        return launch_batch_t<R, 2, true>(Ps, tile_start, nprob, tiles, st, launch);
+    }
+    if (flux == AST_FLUX_HLL) return launch_batch_t<R, 0, false>(Ps, tile_start, nprob, tiles, st, launch);
+    if (flux == AST_FLUX_HLLC) return launch_batch_t<R, 1, false>(Ps, tile_start, nprob, tiles, st, launch);
+    return launch_batch_t<R, 2, false>(Ps, tile_start, nprob, tiles, st, launch);
 }
 
 // kernel parameters of a configuration (grid spacing, constants, boundaries)
@@ -110,5 +142,7 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
 extern template int launch_step_r<double, kSoA>(const StepParams&, int, int, cudaStream_t, bool);
 extern template int launch_step_r<float, kSoA>(const StepParams&, int, int, cudaStream_t, bool);
 extern template int launch_step_r<double, kAoS>(const StepParams&, int, int, cudaStream_t, bool);
+extern template int launch_batch_r<double>(const StepParams*, const int*, int, int, int, int, cudaStream_t, bool);
+extern template int launch_batch_r<float>(const StepParams*, const int*, int, int, int, int, cudaStream_t, bool);
 
 }  // namespace ast

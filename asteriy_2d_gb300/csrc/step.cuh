@@ -41,7 +41,7 @@ struct DevClock {
 
 enum Layout { kSoA = 0, kAoS = 1 };
 
-struct StepParams {
+struct __align__(16) StepParams {
     int N, M;
     long long ld;                  // SoA row pitch in elements
     long long plane;               // SoA plane size in elements
@@ -445,9 +445,14 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
 {
     constexpr int CAP = TileSmem<R, TZ, TR>::kQueueCap;
     const int ns = (int)(sm.qn & 0xffffu), nw = (int)(sm.qn >> 16);
-    if (P.riemann_newton && P.guess == 1) {
+    if (P.riemann_newton && P.guess == 1 && P.mlp != nullptr && ns > 0) {
         // phase 1: learned start values of the faces above the gate (queue
-        // slots 0..ns-1), 16 per warp tile on the tensor cores
+        // slots 0..ns-1), 16 per warp tile on the tensor cores.  Only tiles
+        // with such faces stage the network.
+        for (int i = threadIdx.x; i < kMlpParams; i += kThreads) sm.mlp[i] = P.mlp[i];
+        __syncthreads();
+        tc::pack_weights(sm.mlp, sm.mB1, sm.mB2);
+        __syncthreads();
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         for (int t0 = 16 * w; t0 < ns; t0 += 16 * (kThreads / 32)) {
             const int i = t0 + (lane & 15);
@@ -490,7 +495,7 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
         int a, c;
         bool zf;
         const RPre<R> q = queued_face<R, RECON, TZ, TR>(P, sm, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
-        const R p = solve_queued(P, g, q, strong, (strong && P.guess == 1) ? sm.qp0[i] : R(0), rc, fallback);
+        const R p = solve_queued(P, g, q, strong, (strong && P.guess == 1 && P.mlp) ? sm.qp0[i] : R(0), rc, fallback);
         R F[4];
         R Sp = godunov_sample(g, q, p, F, rc);
         if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
@@ -506,9 +511,11 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
     }
 }
 
-// ------------------------------------------------------------------ the kernel
+// ------------------------------------------------------------------ one tile of one step
+// Tile (bx, by) of the problem P; `tiles` is the number of tiles of that
+// problem (the last of them to finish performs the dt epilogue).
 template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
-__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(StepParams P)
+__device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, unsigned int tiles)
 {
     using S = TileSmem<R, TZ, TR>;
     constexpr int HZ = S::HZ, HR = S::HR;
@@ -521,7 +528,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
     __shared__ float s_tdv_f, s_T_f;
 
     const int tid = threadIdx.x;
-    const int n0 = blockIdx.x * TZ, m0 = blockIdx.y * TR;
+    const int n0 = bx * TZ, m0 = by * TR;
     const Gas<R>& g = *reinterpret_cast<const Gas<R>*>(sizeof(R) == 8 ? (const void*)&P.gd : (const void*)&P.gf);
     const double T_do = (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr;
     const int step = (P.clock != nullptr) ? (int)P.clock->step : 0;
@@ -531,8 +538,6 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
         s_tdv_f = (float)s_tdv;
         s_T_f = (float)T_do;
     }
-    if (FLUX == 2 && P.guess == 1 && P.mlp != nullptr)
-        for (int i = tid; i < kMlpParams; i += kThreads) sm.mlp[i] = P.mlp[i];
 
     // ---- stage tile + halo; the corners are never read by the cross stencil
     for (int idx = tid; idx < HR * HZ; idx += kThreads) {
@@ -549,8 +554,6 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
         }
     }
     __syncthreads();
-
-    if (FLUX == 2 && P.guess == 1 && P.mlp != nullptr) tc::pack_weights(sm.mlp, sm.mB1, sm.mB2);
 
     RiemannCount rc;
     rc.clear();
@@ -687,9 +690,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
             if (c2) atomicAdd(&C->cnt[6], (unsigned long long)c2);
             if (st) atomicOr(&C->status, st);
             __threadfence();
-            const unsigned int total = gridDim.x * gridDim.y;
             const unsigned int ticket = atomicAdd(&C->done, 1u);
-            s_last = (ticket == total - 1) ? 1 : 0;
+            s_last = (ticket == tiles - 1) ? 1 : 0;
         } else {
             // raw mode: this CTA's dt candidate, min-reduced into *T_min
             double dt = P.dt_cap;
@@ -716,6 +718,44 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
         C->done = 0u;
         __threadfence();
     }
+}
+
+// ------------------------------------------------------------------ the kernels
+// one problem: a CTA per tile, grid (tiles along z, tiles along r)
+template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
+__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(StepParams P)
+{
+    step_tile<R, FLUX, RECON, LAYOUT, TZ, TR>(P, blockIdx.x, blockIdx.y, gridDim.x * gridDim.y);
+}
+
+// many problems of one (flux, recon) class: a CTA per (problem, tile) of the
+// work list.  Problem j of the class owns CTAs tile_start[j] ..
+// tile_start[j+1]-1, its tiles in row-major order; its parameters are
+// Ps[j] (copied into shared memory once per CTA).
+template <typename R, int FLUX, bool RECON, int TZ, int TR>
+__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2)
+    batch_kernel(const StepParams* __restrict__ Ps, const int* __restrict__ tile_start, int nprob)
+{
+    __shared__ __align__(16) StepParams sP;
+    __shared__ int s_j;
+    if (threadIdx.x == 0) {
+        // the last problem whose first tile is at or before this CTA
+        int lo = 0, hi = nprob - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tile_start[mid] <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+        }
+        s_j = lo;
+    }
+    __syncthreads();
+    const int j = s_j;
+    static_assert(sizeof(StepParams) % 16 == 0, "StepParams is copied as 16-byte words");
+    for (int w = threadIdx.x; w < (int)(sizeof(StepParams) / 16); w += kThreads)
+        reinterpret_cast<int4*>(&sP)[w] = reinterpret_cast<const int4*>(Ps + j)[w];
+    __syncthreads();
+    const int t = (int)blockIdx.x - tile_start[j];
+    const int tz = (sP.N + TZ - 1) / TZ;
+    step_tile<R, FLUX, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, (unsigned)(tile_start[j + 1] - tile_start[j]));
 }
 
 }  // namespace ast

@@ -46,6 +46,20 @@ SIGNATURES = {
     "ast_read_bin": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
     "ast_write_tecplot": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_int, C.c_double, C.c_char_p]),
     "ast_set_mlp": (C.c_int, [C.c_void_p, _fp]),
+    "ast_batch_create": (C.c_int, [C.POINTER(A.ast_config), C.c_int, C.POINTER(C.c_void_p)]),
+    "ast_batch_destroy": (C.c_int, [C.c_void_p]),
+    "ast_batch_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ast_batch_set_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "ast_batch_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "ast_batch_set_clock": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int64]),
+    "ast_batch_get_clock": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, C.POINTER(C.c_int64)]),
+    "ast_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "ast_batch_synchronize": (C.c_int, [C.c_void_p]),
+    "ast_batch_get_stats": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(A.ast_stats), C.c_int]),
+    "ast_batch_set_mlp": (C.c_int, [C.c_void_p, _fp]),
+    "ast_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+    "ast_problem_set": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.POINTER(A.ast_problem)]),
+    "ast_problem_fill": (C.c_int, [C.POINTER(A.ast_problem), _dp, _dp]),
     "ast_record_start": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_double]),
     "ast_record_stop": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "ast_record_read": (C.c_int, [C.c_void_p, _fp, C.c_int64]),
@@ -297,3 +311,108 @@ def step_noalloc(s, u, s2, u2, T_do, TT, step, cfg, status=None, stream=None):
     check(load().ast_step_noalloc(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), C.c_void_p(T_do),
                                   C.c_void_p(TT), C.c_void_p(step), C.c_void_p(status) if status else None,
                                   C.byref(cfg), C.c_void_p(stream) if stream else None), "ast_step_noalloc")
+
+
+def problem_set(seed=64, n=64, precision=A.PREC_FP32):
+    """The seeded benchmark problem set (ast_problem_set): a list of
+    ast_problem structures (config, setup, Mach number, noise seed)."""
+    arr = (A.ast_problem * n)()
+    check(load().ast_problem_set(seed, n, precision, arr), "ast_problem_set")
+    return [arr[i] for i in range(n)]
+
+
+def problem_fill(prob):
+    """Initial state (s, u) of one drawn problem."""
+    K = prob.cfg.N * prob.cfg.M
+    s = np.empty((K, 2))
+    u = np.empty((K, 2))
+    check(load().ast_problem_fill(C.byref(prob), _dptr(s), _dptr(u)), "ast_problem_fill")
+    return s, u
+
+
+class Batch:
+    """Many independent r-z problems advanced together (the ast_batch object)."""
+
+    def __init__(self, cfgs, stream=None):
+        self.lib = load()
+        n = len(cfgs)
+        self.cfgs = [c.copy() for c in cfgs]
+        arr = (A.ast_config * n)(*self.cfgs)
+        h = C.c_void_p()
+        check(self.lib.ast_batch_create(arr, n, C.byref(h)), "ast_batch_create")
+        self.h = h
+        if stream is not None:
+            check(self.lib.ast_batch_set_stream(self.h, C.c_void_p(stream)), "ast_batch_set_stream")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ast_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.cfgs)
+
+    def set_state(self, i, s, u):
+        K = self.cfgs[i].N * self.cfgs[i].M
+        s = np.ascontiguousarray(s, dtype=np.float64)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        assert s.shape == (K, 2) and u.shape == (K, 2)
+        check(self.lib.ast_batch_set_state(self.h, i, s.ctypes.data, u.ctypes.data, 0), "ast_batch_set_state")
+
+    def set_state_device(self, i, s_ptr, u_ptr):
+        check(self.lib.ast_batch_set_state(self.h, i, C.c_void_p(s_ptr), C.c_void_p(u_ptr), 1),
+              "ast_batch_set_state")
+
+    def get_state(self, i):
+        K = self.cfgs[i].N * self.cfgs[i].M
+        s = np.empty((K, 2))
+        u = np.empty((K, 2))
+        check(self.lib.ast_batch_get_state(self.h, i, s.ctypes.data, u.ctypes.data, 0), "ast_batch_get_state")
+        return s, u
+
+    def get_state_device(self, i, s_ptr, u_ptr):
+        check(self.lib.ast_batch_get_state(self.h, i, C.c_void_p(s_ptr), C.c_void_p(u_ptr), 1),
+              "ast_batch_get_state")
+
+    def set_clock(self, i, T_do, TT=0.0, step=0):
+        check(self.lib.ast_batch_set_clock(self.h, i, T_do, TT, step), "ast_batch_set_clock")
+
+    def clock(self, i):
+        a, b, c = C.c_double(), C.c_double(), C.c_int64()
+        check(self.lib.ast_batch_get_clock(self.h, i, C.byref(a), C.byref(b), C.byref(c)), "ast_batch_get_clock")
+        return a.value, b.value, c.value
+
+    def step(self, n=1, sync=True):
+        check(self.lib.ast_batch_step(self.h, n), "ast_batch_step")
+        if sync:
+            self.synchronize()
+
+    def synchronize(self):
+        check(self.lib.ast_batch_synchronize(self.h), "ast_batch_synchronize")
+
+    def stats(self, i, reset=False):
+        st = A.ast_stats()
+        check(self.lib.ast_batch_get_stats(self.h, i, C.byref(st), int(reset)), "ast_batch_get_stats")
+        return {name: getattr(st, name) for name, _ in st._fields_ if name != "reserved"}
+
+    def set_mlp(self, params):
+        params = _f32(params)
+        assert params.shape == (A.AST_MLP_NPARAM,)
+        check(self.lib.ast_batch_set_mlp(self.h, _fptr(params)), "ast_batch_set_mlp")
+
+    def info(self):
+        cells, tiles, launches = C.c_int64(), C.c_int64(), C.c_int()
+        check(self.lib.ast_batch_info(self.h, C.byref(cells), C.byref(tiles), C.byref(launches)), "ast_batch_info")
+        return {"cells": cells.value, "tiles": tiles.value, "launches_per_step": launches.value}

@@ -257,6 +257,63 @@ int ast_funk_time(double* T, double* T_do, double* TT, int* i, void* cuda_stream
 int ast_step_noalloc(const double* s, const double* u, double* s2, double* u2, double* T_do, double* TT,
                      int64_t* step, unsigned int* status, const ast_config* cfg, void* cuda_stream);
 
+/* ---- batched problems (no counterpart in the reference, which runs one
+        problem per process) ---------------------------------------------
+ * A batch holds nprob independent problems of one precision, each with its
+ * own grid, gas, flux, reconstruction, geometry, boundaries, clock and
+ * lagged dt.  ast_batch_step advances every problem by nsteps steps of its
+ * own dt.  A step is one kernel launch per (flux, recon) class present,
+ * each over a work list of (problem, tile) pairs, the problems' tiles
+ * concatenated; the launches of one step are independent branches of the
+ * captured step graph.  Problem states live in one device arena.  guess ==
+ * MLP problems share the network given to ast_batch_set_mlp. */
+typedef struct ast_batch ast_batch;
+#define AST_BATCH_MAX 4096
+int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out);
+int ast_batch_destroy(ast_batch* batch);
+int ast_batch_set_stream(ast_batch* batch, void* cuda_stream);
+/* state of problem `prob` in the layout of ast_set_state / ast_get_state */
+int ast_batch_set_state(ast_batch* batch, int prob, const double* s, const double* u, int on_device);
+int ast_batch_get_state(ast_batch* batch, int prob, double* s, double* u, int on_device);
+int ast_batch_set_clock(ast_batch* batch, int prob, double T_do, double TT, int64_t step);
+int ast_batch_get_clock(ast_batch* batch, int prob, double* T_do, double* TT, int64_t* step);
+int ast_batch_step(ast_batch* batch, int nsteps);
+/* waits for the batch's stream; AST_ERR_NUMERIC if any problem's state
+   became non-finite */
+int ast_batch_synchronize(ast_batch* batch);
+int ast_batch_get_stats(ast_batch* batch, int prob, ast_stats* out, int reset);
+int ast_batch_set_mlp(ast_batch* batch, const float* params);
+/* cells of all problems, tiles of all problems, and kernel launches per
+   step (the number of (flux, recon) classes) */
+int ast_batch_info(ast_batch* batch, int64_t* cells, int64_t* tiles, int* launches_per_step);
+
+/* A seeded set of benchmark problems: problem i draws, in this order from
+ * one std::mt19937_64(seed) stream (u = (draw >> 11) * 2^-53, b = draw >> 63):
+ *   size   M = round(64 * 8^u), N = 2M           (128x64 .. 1024x512)
+ *   mach   1.5 + 4.5 u
+ *   gamma  5/3 if b == 0, else 1.4
+ *   setup  blast if b == 0, else wind
+ *   flux   HLLC if b == 0, else exact Godunov
+ *   seed   one draw (the wind setup's density-noise seed)
+ * Blast: the blast problem of the single-problem benchmarks with the
+ * driver pressure of a normal shock of that Mach number into the ambient
+ * gas, p_in = p_out (2 gamma mach^2 - (gamma-1))/(gamma+1), p_out = 0.1.
+ * Wind: the wind-counterflow problem with counterflow Mach `mach`
+ * (rho = 1, p = 1/gamma, v_z = -mach).  Both: minmod, axisymmetric,
+ * CFL 0.4, the given precision. */
+enum ast_setup { AST_SETUP_BLAST = 0, AST_SETUP_WIND = 1 };
+typedef struct {
+    ast_config cfg;
+    int setup;              /* enum ast_setup */
+    int reserved_i;
+    double mach;
+    uint64_t seed;
+    double reserved_d[5];
+} ast_problem;
+int ast_problem_set(uint64_t seed, int nprob, int precision, ast_problem* out);
+/* initial state of a drawn problem (K = N*M pairs each) */
+int ast_problem_fill(const ast_problem* prob, double* s, double* u);
+
 /* ---- problem set-up and files (host) ------------------------------------ */
 /* Axisymmetric blast: rho=1, v=0, p=p_in for z^2+r^2 < radius^2, else p_out. */
 int ast_fill_blast(const ast_config* cfg, double p_in, double p_out, double radius,
