@@ -270,6 +270,81 @@ def time_e2e(form, start, steps, torch, params=None):
     return dt, 2 * K * 16, 2 * K * 16
 
 
+def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
+    """The batched form: the seeded set of nprob problems (ast_problem_set:
+    128x64 .. 1024x512, blast or wind, HLLC or exact Godunov, gamma 5/3 or
+    1.4, Mach 1.5-6), FP32, all advanced together by ast_batch_step.  Timed
+    with CUDA events over `steps` steps after `warmup`; the same problems
+    stepped one solver after another (each its own graph) for solo_steps
+    steps give the unbatched rate; every problem's density L1 error against
+    the FP64 run of the same steps (an FP64 batch: bitwise the FP64 solo
+    runs) is reported."""
+    from asteriy_2d_gb300 import abi as A
+    from asteriy_2d_gb300 import solver
+    probs = solver.problem_set(seed, nprob, A.PREC_FP32)
+    init = [solver.problem_fill(p) for p in probs]
+    cells = sum(p.cfg.N * p.cfg.M for p in probs)
+    stream = torch.cuda.Stream()
+    with solver.Batch([p.cfg for p in probs], stream=stream.cuda_stream) as B:
+        info = B.info()
+        for i, (s0, u0) in enumerate(init):
+            B.set_state(i, s0, u0)
+        B.step(warmup)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        B.step(steps, sync=False)
+        e1.record(stream)
+        B.synchronize()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        fp32 = [B.get_state(i)[0] for i in range(nprob)]
+    # unbatched: one solver per problem, stepped in turn on one stream
+    solos = []
+    for p, (s0, u0) in zip(probs, init):
+        S = solver.Solver(p.cfg, stream=stream.cuda_stream)
+        S.set_state(s0, u0)
+        S.step(16)   # captures its graph
+        solos.append(S)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for S in solos:
+        S.step(solo_steps, sync=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    solo_sec = e0.elapsed_time(e1) / 1e3
+    for S in solos:
+        S.close()
+    # FP64 runs of the same problems and steps
+    cfg64 = []
+    for p in probs:
+        c = p.cfg.copy()
+        c.precision = A.PREC_FP64
+        cfg64.append(c)
+    l1 = []
+    with solver.Batch(cfg64) as B:
+        for i, (s0, u0) in enumerate(init):
+            B.set_state(i, s0, u0)
+        B.step(warmup + steps)
+        for i in range(nprob):
+            r64 = B.get_state(i)[0][:, 0]
+            l1.append(float(np.sum(np.abs(fp32[i][:, 0] - r64)) / np.sum(np.abs(r64))))
+    l1 = np.array(l1)
+    kinds = [("godunov" if p.cfg.flux == A.FLUX_GODUNOV else "hllc") + "/" +
+             ("wind" if p.setup == A.SETUP_WIND else "blast") for p in probs]
+    return {
+        "value": cells * steps / sec, "unit": "cell-updates/s", "ms_per_step": sec * 1e3 / steps,
+        "steps": steps, "warmup": warmup, "problems": nprob, "seed": seed, "cells": cells,
+        "tiles": info["tiles"], "launches_per_step": info["launches_per_step"],
+        "mix": {k: kinds.count(k) for k in sorted(set(kinds))},
+        "solo_value": cells * solo_steps / solo_sec, "solo_steps": solo_steps,
+        "l1_rho_vs_fp64": {"median": float(np.median(l1)), "max": float(l1.max()),
+                           "per_problem": [float("%.3g" % v) for v in l1]},
+        "dtype": "f32",
+    }
+
+
 def cpu_baseline(cfg, s0, u0, nsteps, where="the initial state"):
     """The reference's face functions compiled for the host (oracle/_ref) in
     the oracle's step loop, on all host threads; the oracle port if the
@@ -311,6 +386,7 @@ def main():
     ap.add_argument("--grid", default=None, help="NxM instead of 4096x2048 (profiling runs)")
     ap.add_argument("--start-step", type=int, default=1000, help="timed window starts at this step of the run")
     ap.add_argument("--accuracy-steps", type=int, default=2000, help="FP32 vs FP64 error after these steps (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=1000, help="steps of the 64-problem batch (0: skip)")
     args = ap.parse_args()
     global N_Z, M_R
     if args.grid:
@@ -450,6 +526,9 @@ def main():
         "clocks": clocks,
     }
     line["config"]["start_step"] = args.start_step
+    if rank == 0 and args.batch_steps:
+        line["batch"] = time_batch(args.batch_steps, args.warmup, torch)
+        line["gpu_launches_batch_step"] = line["batch"]["launches_per_step"]
     if rank == 0 and args.accuracy_steps:
         line["accuracy_vs_fp64"] = accuracy(args.accuracy_steps, params)
     if rank == 0 and not args.no_cpu:

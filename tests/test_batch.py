@@ -1,7 +1,8 @@
 """Batched problems: the seeded problem set (host, no GPU) and the batch
-solver, whose every problem must evolve exactly as the same problem does in
-its own single-problem solver (same kernels, same per-problem clock), and
-whose FP64 problems match the oracle."""
+solver, whose every problem must evolve as the same problem does in its own
+single-problem solver (the same device code compiled into another kernel:
+the compiler may fuse a multiply and an add differently, so agreement is to
+rounding, not bitwise), and whose FP64 problems match the oracle."""
 import os
 
 import numpy as np
@@ -92,6 +93,21 @@ def small_set(precision, n=8, max_m=96, seed=64):
     return out
 
 
+# batch vs single-problem solver after a few dozen steps: relative
+# L-infinity per variable, and the clock (T_do, TT) relative
+AGREE = {A.PREC_FP64: (1e-11, 1e-13), A.PREC_FP32: (1e-5, 1e-6)}
+
+
+def assert_agree(prec, got, ref, clock, rclock, what):
+    tol, ctol = AGREE[prec]
+    for g, r in zip(got, ref):
+        err = np.max(np.abs(g - r), axis=0) / np.maximum(np.max(np.abs(r), axis=0), 1e-300)
+        assert np.all(err <= tol), (what, err)
+    assert clock[2] == rclock[2], what
+    assert abs(clock[0] - rclock[0]) <= ctol * rclock[0] and abs(clock[1] - rclock[1]) <= ctol * rclock[1], \
+        (what, clock, rclock)
+
+
 def single_run(cfg, s0, u0, steps, params=None):
     with solver.Solver(cfg) as S:
         if params is not None:
@@ -123,8 +139,7 @@ def test_batch_matches_single_solvers(precision):
         for i, c in enumerate(cfgs):
             s, u = B.get_state(i)
             rs, ru, rclock = single_run(c, *init[i], steps)
-            assert B.clock(i) == rclock, i
-            assert np.array_equal(s, rs) and np.array_equal(u, ru), (i, np.max(np.abs(s - rs)))
+            assert_agree(precision, (s, u), (rs, ru), B.clock(i), rclock, i)
 
 
 @pytest.mark.gpu
@@ -189,5 +204,5 @@ def test_batch_stats_and_learned_guess():
             assert st["newton_calls"] > 0
             assert st["mlp_fallback"] <= st["strong_calls"]
             s, u = B.get_state(i)
-            rs, ru, _ = single_run(c, *init[i], 40, params)
-            assert np.array_equal(s, rs) and np.array_equal(u, ru), i
+            rs, ru, rclock = single_run(c, *init[i], 40, params)
+            assert_agree(A.PREC_FP32, (s, u), (rs, ru), B.clock(i), rclock, i)
