@@ -32,9 +32,11 @@ namespace {
 
 struct BatchClass {
     int flux, recon;
-    int first, count;    // slots [first, first + count) of the parameter arrays
-    int tiles;           // work-list length
-    int ts_off;          // offset of its count+1 prefix sums in the tile_start array
+    int first, count;             // slots [first, first + count) of the parameter arrays
+    int shape;                    // tile shape in use (index into kShapeTZ / kShapeTR)
+    int tiles[kNumShapes];        // work-list length per tile shape
+    int ts_off[kNumShapes];       // offset of its count+1 prefix sums in the tile_start array
+    float ms[kNumShapes];         // autotuner: ms per step per shape (0: not timed)
 };
 
 #define BATCH_CUDA(call)                                    \
@@ -43,7 +45,10 @@ struct BatchClass {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
-int tiles_of(const ast_config& c) { return ((c.N + kTZ - 1) / kTZ) * ((c.M + kTR - 1) / kTR); }
+int tiles_of(const ast_config& c, int shape)
+{
+    return ((c.N + kShapeTZ[shape] - 1) / kShapeTZ[shape]) * ((c.M + kShapeTR[shape] - 1) / kShapeTR[shape]);
+}
 
 }  // namespace
 
@@ -70,7 +75,8 @@ struct ast_batch {
     int cur = 0;
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0, graph_cur = -1;
-    long long cells = 0, tiles = 0;
+    long long cells = 0;
+    DevClock* clock_save = nullptr;     // autotuner: clocks saved around the trials
 };
 
 namespace {
@@ -100,12 +106,11 @@ int upload_params(ast_batch* B)
     return AST_OK;
 }
 
-int launch_class(ast_batch* B, const BatchClass& c, cudaStream_t st, bool launch)
+int launch_class(ast_batch* B, const BatchClass& c, int shape, cudaStream_t st, bool launch)
 {
     const StepParams* Ps = B->dP[B->cur] + c.first;
-    const int* ts = B->tile_start + c.ts_off;
-    return (B->elem == 8) ? launch_batch_r<double>(Ps, ts, c.count, c.tiles, c.flux, c.recon, st, launch)
-                          : launch_batch_r<float>(Ps, ts, c.count, c.tiles, c.flux, c.recon, st, launch);
+    const int* ts = B->tile_start + c.ts_off[shape];
+    return launch_batch(B->elem, shape, Ps, ts, c.count, c.tiles[shape], c.flux, c.recon, st, launch);
 }
 
 // `count` steps of every class; classes beyond the first run on their own
@@ -122,7 +127,7 @@ int enqueue_steps(ast_batch* B, cudaStream_t st, int count)
         cudaStream_t sc = (c == 0) ? st : B->aux[c - 1];
         B->cur = cur0;
         for (int i = 0; i < count; i++) {
-            int rc = launch_class(B, B->cls[c], sc, true);
+            int rc = launch_class(B, B->cls[c], B->cls[c].shape, sc, true);
             if (rc != AST_OK) {
                 B->cur = cur0;
                 return rc;
@@ -207,7 +212,6 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
         total += 2 * B->level_bytes[i];
         maxK = std::max(maxK, (size_t)c.N * c.M);
         B->cells += (long long)c.N * c.M;
-        B->tiles += tiles_of(c);
     }
 
     // classes by (flux, recon); inside a class, larger problems first
@@ -217,33 +221,40 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
         const ast_config &x = B->cfg[a], &y = B->cfg[b];
         if (x.flux != y.flux) return x.flux > y.flux;   // exact Godunov first
         if (x.recon != y.recon) return x.recon > y.recon;
-        return tiles_of(x) > tiles_of(y);
+        return (long long)x.N * x.M > (long long)y.N * y.M;
     });
-    std::vector<int> ts_host;
     for (int s = 0; s < nprob; s++) {
         const ast_config& c = B->cfg[order[s]];
         if (B->cls.empty() || B->cls.back().flux != c.flux || B->cls.back().recon != c.recon) {
             BatchClass k;
+            std::memset(&k, 0, sizeof k);
             k.flux = c.flux;
             k.recon = c.recon;
             k.first = s;
-            k.count = 0;
-            k.tiles = 0;
-            k.ts_off = (int)ts_host.size();
-            ts_host.push_back(0);
             B->cls.push_back(k);
         }
-        BatchClass& k = B->cls.back();
-        k.count++;
-        k.tiles += tiles_of(c);
-        ts_host.push_back(k.tiles);
+        B->cls.back().count++;
         B->slot[order[s]] = s;
+    }
+    // work lists: per class and tile shape, the prefix sums of its problems'
+    // tile counts (count + 1 entries)
+    std::vector<int> ts_host;
+    for (BatchClass& k : B->cls) {
+        for (int sh = 0; sh < kNumShapes; sh++) {
+            k.ts_off[sh] = (int)ts_host.size();
+            ts_host.push_back(0);
+            for (int s = k.first; s < k.first + k.count; s++) {
+                k.tiles[sh] += tiles_of(B->cfg[order[s]], sh);
+                ts_host.push_back(k.tiles[sh]);
+            }
+        }
     }
 
     cudaError_t e;
     const size_t nts = ts_host.size();
     if ((e = cudaMalloc(&B->arena, total)) != cudaSuccess ||
         (e = cudaMalloc(&B->clocks, sizeof(DevClock) * nprob)) != cudaSuccess ||
+        (e = cudaMalloc(&B->clock_save, sizeof(DevClock) * nprob)) != cudaSuccess ||
         (e = cudaMalloc(&B->dP[0], sizeof(StepParams) * nprob)) != cudaSuccess ||
         (e = cudaMalloc(&B->dP[1], sizeof(StepParams) * nprob)) != cudaSuccess ||
         (e = cudaMalloc(&B->tile_start, sizeof(int) * nts)) != cudaSuccess ||
@@ -272,7 +283,8 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
         (e = cudaMemcpy(B->clocks, clk.data(), sizeof(DevClock) * nprob, cudaMemcpyHostToDevice)) != cudaSuccess)
         rc = cuda_fail(e, "batch clocks");
     if (rc == AST_OK) rc = upload_params(B);
-    for (size_t c = 0; c < B->cls.size() && rc == AST_OK; c++) rc = launch_class(B, B->cls[c], nullptr, false);
+    for (size_t c = 0; c < B->cls.size() && rc == AST_OK; c++)
+        for (int sh = 0; sh < kNumShapes && rc == AST_OK; sh++) rc = launch_class(B, B->cls[c], sh, nullptr, false);
     for (size_t c = 1; c < B->cls.size() && rc == AST_OK; c++) {
         cudaStream_t s;
         if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) {
@@ -305,6 +317,7 @@ int ast_batch_destroy(ast_batch* B)
     for (cudaEvent_t e : B->ev) cudaEventDestroy(e);
     cudaFree(B->arena);
     cudaFree(B->clocks);
+    cudaFree(B->clock_save);
     cudaFree(B->dP[0]);
     cudaFree(B->dP[1]);
     cudaFree(B->tile_start);
@@ -485,9 +498,82 @@ int ast_batch_info(ast_batch* B, int64_t* cells, int64_t* tiles, int* launches_p
 {
     if (!B) return set_error(AST_ERR_INVALID, "null batch");
     if (cells) *cells = B->cells;
-    if (tiles) *tiles = B->tiles;
+    if (tiles) {
+        *tiles = 0;
+        for (const BatchClass& k : B->cls) *tiles += k.tiles[k.shape];
+    }
     if (launches_per_step) *launches_per_step = (int)B->cls.size();
     return AST_OK;
+}
+
+int ast_batch_class(ast_batch* B, int cls, int* flux, int* recon, int* nprob, int* tile_z, int* tile_r,
+                    float* ms_per_shape)
+{
+    if (!B || cls < 0 || cls >= (int)B->cls.size()) return set_error(AST_ERR_INVALID, "bad argument");
+    const BatchClass& k = B->cls[cls];
+    if (flux) *flux = k.flux;
+    if (recon) *recon = k.recon;
+    if (nprob) *nprob = k.count;
+    if (tile_z) *tile_z = kShapeTZ[k.shape];
+    if (tile_r) *tile_r = kShapeTR[k.shape];
+    if (ms_per_shape)
+        for (int sh = 0; sh < kNumShapes; sh++) ms_per_shape[sh] = k.ms[sh];
+    return AST_OK;
+}
+
+int ast_batch_set_tiles(ast_batch* B, int cls, int tile_z, int tile_r)
+{
+    if (!B || cls < 0 || cls >= (int)B->cls.size()) return set_error(AST_ERR_INVALID, "bad argument");
+    for (int sh = 0; sh < kNumShapes; sh++) {
+        if (kShapeTZ[sh] == tile_z && kShapeTR[sh] == tile_r) {
+            B->cls[cls].shape = sh;
+            drop_graph(B);
+            return AST_OK;
+        }
+    }
+    return set_error(AST_ERR_UNSUPPORTED, "tile shape not built");
+}
+
+int ast_batch_autotune(ast_batch* B, int trials)
+{
+    if (!B || trials < 1) return set_error(AST_ERR_INVALID, "bad argument");
+    // every trial step reads the current time level and writes the other
+    // one, so the state is left as it was; the clocks (dt, time, counters)
+    // are saved first and put back afterwards
+    cudaEvent_t e0, e1;
+    BATCH_CUDA(cudaEventCreate(&e0));
+    BATCH_CUDA(cudaEventCreate(&e1));
+    int rc = AST_OK;
+    cudaError_t e = cudaMemcpyAsync(B->clock_save, B->clocks, sizeof(DevClock) * B->nprob,
+                                    cudaMemcpyDeviceToDevice, B->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "autotune clock save");
+    for (BatchClass& k : B->cls) {
+        float best = 0.0f;
+        for (int sh = 0; sh < kNumShapes && rc == AST_OK; sh++) {
+            rc = launch_class(B, k, sh, B->stream, true);   // warm-up
+            if (rc == AST_OK && (e = cudaEventRecord(e0, B->stream)) != cudaSuccess) rc = cuda_fail(e, "event");
+            for (int t = 0; t < trials && rc == AST_OK; t++) rc = launch_class(B, k, sh, B->stream, true);
+            if (rc == AST_OK && (e = cudaEventRecord(e1, B->stream)) != cudaSuccess) rc = cuda_fail(e, "event");
+            if (rc == AST_OK && (e = cudaEventSynchronize(e1)) != cudaSuccess) rc = cuda_fail(e, "event");
+            float ms = 0.0f;
+            if (rc == AST_OK && (e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) rc = cuda_fail(e, "event");
+            if (rc != AST_OK) break;
+            k.ms[sh] = ms / trials;
+            if (sh == 0 || k.ms[sh] < best) {
+                best = k.ms[sh];
+                k.shape = sh;
+            }
+        }
+    }
+    e = cudaMemcpyAsync(B->clocks, B->clock_save, sizeof(DevClock) * B->nprob, cudaMemcpyDeviceToDevice,
+                        B->stream);
+    if (e != cudaSuccess && rc == AST_OK) rc = cuda_fail(e, "autotune clock restore");
+    e = cudaStreamSynchronize(B->stream);
+    if (e != cudaSuccess && rc == AST_OK) rc = cuda_fail(e, "autotune");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    drop_graph(B);
+    return rc;
 }
 
 }  // extern "C"

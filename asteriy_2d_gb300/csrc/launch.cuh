@@ -1,6 +1,7 @@
 // launch.cuh - launch helpers of the step kernels.  The instantiations are
 // spread over several translation units (step_f64.cu, step_f32.cu,
-// step_raw.cu, batch_f64.cu, batch_f32.cu) so that they compile in parallel.
+// step_raw.cu, batch_f64_s*.cu, batch_f32_s*.cu) so that they compile in
+// parallel.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -50,12 +51,17 @@ int launch_step_r(const StepParams& P, int flux, int recon, cudaStream_t st, boo
     return launch_step_t<R, 2, false, LAYOUT>(P, st, launch);
 }
 
+// tile shapes of the batch kernels (the autotuner's choices): z x r cells
+constexpr int kNumShapes = 3;
+constexpr int kShapeTZ[kNumShapes] = {32, 16, 64};
+constexpr int kShapeTR[kNumShapes] = {16, 16, 8};
+
 // the batch kernel of one (flux, recon) class over `tiles` work-list entries
-template <typename R, int FLUX, bool RECON>
+template <typename R, int FLUX, bool RECON, int TZ, int TR>
 int launch_batch_t(const StepParams* Ps, const int* tile_start, int nprob, int tiles, cudaStream_t st, bool launch)
 {
-    auto k = batch_kernel<R, FLUX, RECON, kTZ, kTR>;
-    constexpr size_t smem = tile_smem_bytes<R, kTZ, kTR>();
+    auto k = batch_kernel<R, FLUX, RECON, TZ, TR>;
+    constexpr size_t smem = tile_smem_bytes<R, TZ, TR>();
     cudaError_t e;
     if (!launch) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -66,18 +72,46 @@ int launch_batch_t(const StepParams* Ps, const int* tile_start, int nprob, int t
     return e == cudaSuccess ? AST_OK : cuda_fail(e, "batch kernel launch");
 }
 
-template <typename R>
+template <typename R, int TZ, int TR>
 int launch_batch_r(const StepParams* Ps, const int* tile_start, int nprob, int tiles, int flux, int recon,
                    cudaStream_t st, bool launch)
 {
     if (recon) {
-        if (flux == AST_FLUX_HLL) return launch_batch_t<R, 0, true>(Ps, tile_start, nprob, tiles, st, launch);
-        if (flux == AST_FLUX_HLLC) return launch_batch_t<R, 1, true>(Ps, tile_start, nprob, tiles, st, launch);
-        return launch_batch_t<R, 2, true>(Ps, tile_start, nprob, tiles, st, launch);
+        if (flux == AST_FLUX_HLL) return launch_batch_t<R, 0, true, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
+        if (flux == AST_FLUX_HLLC) return launch_batch_t<R, 1, true, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
+        return launch_batch_t<R, 2, true, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
     }
-    if (flux == AST_FLUX_HLL) return launch_batch_t<R, 0, false>(Ps, tile_start, nprob, tiles, st, launch);
-    if (flux == AST_FLUX_HLLC) return launch_batch_t<R, 1, false>(Ps, tile_start, nprob, tiles, st, launch);
-    return launch_batch_t<R, 2, false>(Ps, tile_start, nprob, tiles, st, launch);
+    if (flux == AST_FLUX_HLL) return launch_batch_t<R, 0, false, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
+    if (flux == AST_FLUX_HLLC) return launch_batch_t<R, 1, false, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
+    return launch_batch_t<R, 2, false, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
+}
+
+#define AST_BATCH_EXTERN(R, S)                                                                          \
+    extern template int launch_batch_r<R, kShapeTZ[S], kShapeTR[S]>(const StepParams*, const int*, int, int, \
+                                                                    int, int, cudaStream_t, bool);
+AST_BATCH_EXTERN(double, 0)
+AST_BATCH_EXTERN(double, 1)
+AST_BATCH_EXTERN(double, 2)
+AST_BATCH_EXTERN(float, 0)
+AST_BATCH_EXTERN(float, 1)
+AST_BATCH_EXTERN(float, 2)
+#undef AST_BATCH_EXTERN
+
+// a batch class launch in precision `elem` (bytes) with tile shape `shape`
+inline int launch_batch(size_t elem, int shape, const StepParams* Ps, const int* tile_start, int nprob, int tiles,
+                        int flux, int recon, cudaStream_t st, bool launch)
+{
+#define AST_BATCH_CASE(R, S)                                                                             \
+    return launch_batch_r<R, kShapeTZ[S], kShapeTR[S]>(Ps, tile_start, nprob, tiles, flux, recon, st, launch)
+    if (elem == 8) {
+        if (shape == 1) AST_BATCH_CASE(double, 1);
+        if (shape == 2) AST_BATCH_CASE(double, 2);
+        AST_BATCH_CASE(double, 0);
+    }
+    if (shape == 1) AST_BATCH_CASE(float, 1);
+    if (shape == 2) AST_BATCH_CASE(float, 2);
+    AST_BATCH_CASE(float, 0);
+#undef AST_BATCH_CASE
 }
 
 // kernel parameters of a configuration (grid spacing, constants, boundaries)
@@ -142,7 +176,6 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
 extern template int launch_step_r<double, kSoA>(const StepParams&, int, int, cudaStream_t, bool);
 extern template int launch_step_r<float, kSoA>(const StepParams&, int, int, cudaStream_t, bool);
 extern template int launch_step_r<double, kAoS>(const StepParams&, int, int, cudaStream_t, bool);
-extern template int launch_batch_r<double>(const StepParams*, const int*, int, int, int, int, cudaStream_t, bool);
-extern template int launch_batch_r<float>(const StepParams*, const int*, int, int, int, int, cudaStream_t, bool);
+
 
 }  // namespace ast

@@ -58,6 +58,10 @@ SIGNATURES = {
     "ast_batch_get_stats": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(A.ast_stats), C.c_int]),
     "ast_batch_set_mlp": (C.c_int, [C.c_void_p, _fp]),
     "ast_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+    "ast_batch_autotune": (C.c_int, [C.c_void_p, C.c_int]),
+    "ast_batch_class": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int), C.POINTER(C.c_int), _fp]),
+    "ast_batch_set_tiles": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "ast_problem_set": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.POINTER(A.ast_problem)]),
     "ast_problem_fill": (C.c_int, [C.POINTER(A.ast_problem), _dp, _dp]),
     "ast_record_start": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_double]),
@@ -330,6 +334,9 @@ def problem_fill(prob):
     return s, u
 
 
+TILE_SHAPES = ((32, 16), (16, 16), (64, 8))
+
+
 class Batch:
     """Many independent r-z problems advanced together (the ast_batch object)."""
 
@@ -416,3 +423,22 @@ class Batch:
         cells, tiles, launches = C.c_int64(), C.c_int64(), C.c_int()
         check(self.lib.ast_batch_info(self.h, C.byref(cells), C.byref(tiles), C.byref(launches)), "ast_batch_info")
         return {"cells": cells.value, "tiles": tiles.value, "launches_per_step": launches.value}
+
+    def classes(self):
+        """Per (flux, recon) class: problems, tile shape in use, and the
+        autotuner's ms per step of each built shape."""
+        out = []
+        for k in range(self.info()["launches_per_step"]):
+            v = [C.c_int() for _ in range(5)]
+            ms = np.zeros(3, dtype=np.float32)
+            check(self.lib.ast_batch_class(self.h, k, *[C.byref(x) for x in v], _fptr(ms)), "ast_batch_class")
+            out.append({"flux": v[0].value, "recon": v[1].value, "problems": v[2].value,
+                        "tile": (v[3].value, v[4].value), "ms_per_shape": [float(x) for x in ms]})
+        return out
+
+    def autotune(self, trials=3):
+        check(self.lib.ast_batch_autotune(self.h, trials), "ast_batch_autotune")
+        return self.classes()
+
+    def set_tiles(self, cls, tile_z, tile_r):
+        check(self.lib.ast_batch_set_tiles(self.h, cls, tile_z, tile_r), "ast_batch_set_tiles")

@@ -101,14 +101,17 @@ class ClockSampler:
 # the measured forms: FP64 plain (the reference's solver), and the FP32 form
 # started from the acoustic value or from the learned network, both at the
 # Newton tolerance 1e-8 (clamped to 4 ulps of FP32)
-FORMS = ("fp64_godunov", "fp32_pvrs", "fp32_learned")
+# (the HLL pair is the precision form of the small config's flux at full
+# size, timed for its own rate and %HBM)
+FORMS = ("fp64_godunov", "fp32_pvrs", "fp32_learned", "fp64_hll", "fp32_hll")
 
 
 def make_config(form):
     from asteriy_2d_gb300 import abi as A
     from asteriy_2d_gb300 import problems
     prec = A.PREC_FP64 if form.startswith("fp64") else A.PREC_FP32
-    cfg = problems.blast_config(N_Z, M_R, flux=A.FLUX_GODUNOV, precision=prec)
+    flux = A.FLUX_HLL if form.endswith("_hll") else A.FLUX_GODUNOV
+    cfg = problems.blast_config(N_Z, M_R, flux=flux, precision=prec)
     if prec == A.PREC_FP32:
         cfg.riemann_tol = 1e-8
         cfg.guess = A.GUESS_MLP if form == "fp32_learned" else A.GUESS_PVRS
@@ -286,9 +289,12 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
     cells = sum(p.cfg.N * p.cfg.M for p in probs)
     stream = torch.cuda.Stream()
     with solver.Batch([p.cfg for p in probs], stream=stream.cuda_stream) as B:
-        info = B.info()
         for i, (s0, u0) in enumerate(init):
             B.set_state(i, s0, u0)
+        # tile shape per class, timed on the initial states (the tuner
+        # leaves the state and clocks as they were)
+        classes = B.autotune(3)
+        info = B.info()
         B.step(warmup)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -337,6 +343,10 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
         "value": cells * steps / sec, "unit": "cell-updates/s", "ms_per_step": sec * 1e3 / steps,
         "steps": steps, "warmup": warmup, "problems": nprob, "seed": seed, "cells": cells,
         "tiles": info["tiles"], "launches_per_step": info["launches_per_step"],
+        "classes": [{"flux": ["hll", "hllc", "godunov"][c["flux"]], "problems": c["problems"],
+                     "tile": "%dx%d" % c["tile"],
+                     "tuner_ms": {"%dx%d" % t: round(m, 4) for t, m in zip(solver.TILE_SHAPES, c["ms_per_shape"])}}
+                    for c in classes],
         "mix": {k: kinds.count(k) for k in sorted(set(kinds))},
         "solo_value": cells * solo_steps / solo_sec, "solo_steps": solo_steps,
         "l1_rho_vs_fp64": {"median": float(np.median(l1)), "max": float(l1.max()),
@@ -461,6 +471,8 @@ def main():
         sec, s, u, st = time_form(form, start, args.steps, args.warmup, torch,
                                   params if form == "fp32_learned" else None, stats_steps=0 if args.no_stats else 5)
         forms[form] = {"value": cells * args.steps / sec, "ms_per_step": sec * 1e3 / args.steps}
+        pf = "fp64" if form.startswith("fp64") else "fp32"
+        forms[form]["hbm_frac"] = BYTES_PER_CELL[pf] * cells / (sec / args.steps) / 1e9 / peaks()[0]
         finals[form] = s
         if st and st["newton_calls"]:
             forms[form]["newton"] = {"mean_iters": st["newton_iters"] / st["newton_calls"],
@@ -491,10 +503,12 @@ def main():
                                      "gated_mean_iters": st["strong_iters"] / max(1, st["strong_calls"])}
     # density / pressure L1 error of the FP32 forms against the FP64 run over
     # the timed window (same start, same steps)
-    if "fp64_godunov" in finals:
-        ref = finals["fp64_godunov"]
+    for ref_form, pair in (("fp64_godunov", ("fp32_pvrs", "fp32_learned")), ("fp64_hll", ("fp32_hll",))):
+        if ref_form not in finals:
+            continue
+        ref = finals[ref_form]
         for form, sf in finals.items():
-            if form == "fp64_godunov":
+            if form not in pair:
                 continue
             forms[form]["l1_rho_vs_fp64"] = float(np.sum(np.abs(sf[:, 0] - ref[:, 0])) / np.sum(np.abs(ref[:, 0])))
             forms[form]["l1_p_vs_fp64"] = float(np.sum(np.abs(sf[:, 1] - ref[:, 1])) / np.sum(np.abs(ref[:, 1])))

@@ -264,9 +264,11 @@ int ast_step_noalloc(const double* s, const double* u, double* s2, double* u2, d
  * lagged dt.  ast_batch_step advances every problem by nsteps steps of its
  * own dt.  A step is one kernel launch per (flux, recon) class present,
  * each over a work list of (problem, tile) pairs, the problems' tiles
- * concatenated; the launches of one step are independent branches of the
- * captured step graph.  Problem states live in one device arena.  guess ==
- * MLP problems share the network given to ast_batch_set_mlp. */
+ * concatenated.  Steps are captured in blocks of 16 into a CUDA graph in
+ * which every class is its own chain of launches (the classes' problems are
+ * independent), forked from the batch's stream and joined back at the end
+ * of the block.  Problem states live in one device arena.  guess == MLP
+ * problems share the network given to ast_batch_set_mlp. */
 typedef struct ast_batch ast_batch;
 #define AST_BATCH_MAX 4096
 int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out);
@@ -283,9 +285,23 @@ int ast_batch_step(ast_batch* batch, int nsteps);
 int ast_batch_synchronize(ast_batch* batch);
 int ast_batch_get_stats(ast_batch* batch, int prob, ast_stats* out, int reset);
 int ast_batch_set_mlp(ast_batch* batch, const float* params);
-/* cells of all problems, tiles of all problems, and kernel launches per
-   step (the number of (flux, recon) classes) */
+/* cells of all problems, tiles of all problems (at the tile shapes in use),
+   and kernel launches per step (the number of (flux, recon) classes) */
 int ast_batch_info(ast_batch* batch, int64_t* cells, int64_t* tiles, int* launches_per_step);
+/* Tile shapes.  Each class steps with one of the built tile shapes
+ * (z x r cells: 32x16, the default; 16x16; 64x8).  ast_batch_autotune
+ * times every shape on every class, `trials` steps each on the current
+ * state (each trial reads the current time level and writes the other;
+ * the clocks and counters are restored afterwards, so the run continues
+ * exactly as without the call) and keeps the fastest shape per class.
+ * ast_batch_class reports class `cls` (0 <= cls < launches_per_step): its
+ * flux, reconstruction, problem count, tile shape in use and the tuner's ms
+ * per step of each shape (three floats, 0 when not timed);
+ * ast_batch_set_tiles sets a class's shape by hand. */
+int ast_batch_autotune(ast_batch* batch, int trials);
+int ast_batch_class(ast_batch* batch, int cls, int* flux, int* recon, int* nprob, int* tile_z, int* tile_r,
+                    float* ms_per_shape);
+int ast_batch_set_tiles(ast_batch* batch, int cls, int tile_z, int tile_r);
 
 /* A seeded set of benchmark problems: problem i draws, in this order from
  * one std::mt19937_64(seed) stream (u = (draw >> 11) * 2^-53, b = draw >> 63):

@@ -206,3 +206,51 @@ def test_batch_stats_and_learned_guess():
             s, u = B.get_state(i)
             rs, ru, rclock = single_run(c, *init[i], 40, params)
             assert_agree(A.PREC_FP32, (s, u), (rs, ru), B.clock(i), rclock, i)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", solver.TILE_SHAPES)
+def test_batch_tile_shapes_agree(shape):
+    probs = small_set(A.PREC_FP32, n=6)
+    probs[0].cfg.N, probs[0].cfg.M = 150, 70
+    cfgs = [p.cfg for p in probs]
+    init = [solver.problem_fill(p) for p in probs]
+    with solver.Batch(cfgs) as B:
+        for k in range(B.info()["launches_per_step"]):
+            B.set_tiles(k, *shape)
+        assert all(c["tile"] == shape for c in B.classes())
+        for i, (s0, u0) in enumerate(init):
+            B.set_state(i, s0, u0)
+        B.step(21)
+        for i, c in enumerate(cfgs):
+            rs, ru, rclock = single_run(c, *init[i], 21)
+            assert_agree(A.PREC_FP32, B.get_state(i), (rs, ru), B.clock(i), rclock, (shape, i))
+    with solver.Batch(cfgs[:1]) as B:
+        with pytest.raises(solver.AstError):
+            B.set_tiles(0, 8, 8)
+
+
+@pytest.mark.gpu
+def test_autotune_leaves_the_run_unchanged():
+    probs = small_set(A.PREC_FP32, n=6)
+    cfgs = [p.cfg for p in probs]
+    init = [solver.problem_fill(p) for p in probs]
+    with solver.Batch(cfgs) as T, solver.Batch(cfgs) as U:
+        for Bt in (T, U):
+            for i, (s0, u0) in enumerate(init):
+                Bt.set_state(i, s0, u0)
+            Bt.step(10)
+        before = [(T.get_state(i), T.clock(i), T.stats(i)) for i in range(len(cfgs))]
+        classes = T.autotune(2)
+        for c in classes:
+            assert c["tile"] in solver.TILE_SHAPES
+            assert all(ms > 0 for ms in c["ms_per_shape"])
+            assert min(c["ms_per_shape"]) == c["ms_per_shape"][solver.TILE_SHAPES.index(c["tile"])]
+        for i in range(len(cfgs)):
+            s, u = T.get_state(i)
+            assert np.array_equal(s, before[i][0][0]) and np.array_equal(u, before[i][0][1])
+            assert T.clock(i) == before[i][1] and T.stats(i) == before[i][2]
+        T.step(20)
+        U.step(20)
+        for i in range(len(cfgs)):
+            assert_agree(A.PREC_FP32, T.get_state(i), U.get_state(i), T.clock(i), U.clock(i), i)
