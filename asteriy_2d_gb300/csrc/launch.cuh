@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 
 #include "../../include/asteriy_gb300.h"
@@ -163,6 +164,13 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
     P.fixed_zc = c.fixed_zc;
     P.fixed_az2 = c.fixed_az * c.fixed_az;
     P.fixed_ar2 = c.fixed_ar * c.fixed_ar;
+    {
+        // index box of |z - zc| <= az, 0 <= r <= ar, widened by one cell
+        auto clampi = [](double v) { return (int)std::fmax(-1e9, std::fmin(1e9, v)); };
+        P.fixed_nlo = clampi(std::floor((c.fixed_zc - c.fixed_az - c.x_min) / P.dx) - 1.0);
+        P.fixed_nhi = clampi(std::ceil((c.fixed_zc + c.fixed_az - c.x_min) / P.dx) + 1.0);
+        P.fixed_mhi = clampi(std::ceil((c.fixed_ar - P.y_min) / P.dy) + 1.0);
+    }
     P.region_select = c.region_select;
     P.region_lo = c.region_lo;
     P.region_hi = c.region_hi;

@@ -57,6 +57,7 @@ struct __align__(16) StepParams {
     double bc_val[4][4];           // rho, p, vz, vr of FIXED sides; vz/vr limit of SUCTION
     int fixed_region;
     double fixed_zc, fixed_az2, fixed_ar2;
+    int fixed_nlo, fixed_nhi, fixed_mhi;   // cells that can lie in the region (one cell of margin)
     int region_select;
     double region_lo, region_hi;
     int body_force;
@@ -303,12 +304,9 @@ __device__ __forceinline__ void record_face(const StepParams& P, const Gas<R>& g
 }
 
 // ------------------------------------------------------------------ face passes
-// All faces of one orientation in the tile, one thread per face.  ZF: z
-// faces (between tile columns c-1 and c of a row), else r faces (between
-// tile rows a-1 and a of a column).  Writes the flux, in (mass, mom_z,
-// mom_r, energy) order, to sm.Fz / sm.Fr and raises smax to the largest wave
-// speed of the faces that belong to at least one updated cell.  Exact-solver
-// faces of patterns 2 and 3 go to the queue instead.
+// the reconstructed states on both sides of face (a, c) of orientation ZF
+// (minmod on the staged cells when RECON and the face is in the
+// high-order region `hi`; the cell values otherwise)
 template <typename R, bool RECON, int TZ, int TR, bool ZF>
 __device__ __forceinline__ void face_states(const StepParams& P, const TileSmem<R, TZ, TR>& sm, int a, int c, bool hi,
                                             R L[4], R U[4])
@@ -341,16 +339,21 @@ __device__ __forceinline__ void face_states(const StepParams& P, const TileSmem<
     }
 }
 
+// Face f of one orientation in the tile.  ZF: z faces (between tile
+// columns c-1 and c of a row), else r faces (between tile rows a-1 and a of
+// a column).  Writes the flux, in (mass, mom_z, mom_r, energy) order, to
+// sm.Fz / sm.Fr and raises smax to the largest wave speed of the faces that
+// belong to at least one updated cell.  Exact-solver faces of patterns 2
+// and 3 go to the queue instead.
 template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF>
-__device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
-                                          int m0, int step, RiemannCount& rc, int& fallback, R& smax)
+__device__ __forceinline__ void face_one(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
+                                         int m0, int step, RiemannCount& rc, int& fallback, R& smax, int f)
 {
-    constexpr int NF = ZF ? TR * (TZ + 1) : (TR + 1) * TZ;
     constexpr int NFZ = TR * (TZ + 1);
     constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
     constexpr int NN = ZF ? 2 : 3;           // normal velocity component
     constexpr int TT = ZF ? 3 : 2;           // tangential velocity component
-    for (int f = threadIdx.x; f < NF; f += kThreads) {
+    {
         const int a = f / W, c = f - a * W;
         // smem indices of the lower (l) and upper (u) cell of the face
         const int jl = ZF ? a + 2 : a + 1, il = ZF ? c + 1 : c + 2;
@@ -392,7 +395,7 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
                 const unsigned old = atomicAdd(&sm.qn, strong ? 1u : 0x10000u);
                 const int slot = strong ? (int)(old & 0xffffu) : TileSmem<R, TZ, TR>::kQueueCap - 1 - (int)(old >> 16);
                 sm.qcode[slot] = (ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.pattern << 14);
-                continue;
+                return;
             }
             Sp = godunov_sample(g, q, R(0), F, rc);
         } else if (FLUX == 1 && hi) {
@@ -408,6 +411,23 @@ __device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, T
             sm.Fr[0][a][c] = F[0]; sm.Fr[1][a][c] = F[2]; sm.Fr[2][a][c] = F[1]; sm.Fr[3][a][c] = F[3];
         }
         if (active) smax = fmax(smax, Sp);
+    }
+}
+
+// every face of the tile once, z faces then r faces, in one loop over the
+// CTA's threads; the z faces are padded to whole warps so that no warp
+// mixes the two orientations
+template <typename R, int FLUX, bool RECON, int TZ, int TR>
+__device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
+                                          int m0, int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
+{
+    constexpr int NFZ = TR * (TZ + 1), NFR = (TR + 1) * TZ;
+    constexpr int NFZP = (NFZ + 31) / 32 * 32;
+    for (int t = threadIdx.x; t < NFZP + NFR; t += kThreads) {
+        if (t < NFZ)
+            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, g, n0, m0, step, rc, fallback, smz, t);
+        else if (t >= NFZP)
+            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, g, n0, m0, step, rc, fallback, smr, t - NFZP);
     }
 }
 
@@ -539,6 +559,12 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
         s_T_f = (float)T_do;
     }
 
+    // the fixed region's exact test (FP64 divisions, as the reference
+    // evaluates it) only in tiles whose cells, halo included, meet the
+    // region's cell bounding box
+    const bool near_fixed = P.fixed_region && n0 - 2 <= P.fixed_nhi && n0 + TZ + 1 >= P.fixed_nlo &&
+                            m0 - 2 <= P.fixed_mhi;
+
     // ---- stage tile + halo; the corners are never read by the cross stencil
     for (int idx = tid; idx < HR * HZ; idx += kThreads) {
         const int j = idx / HZ, i = idx - j * HZ;
@@ -550,7 +576,8 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
         sm.q[0][j][i] = v[0]; sm.q[1][j][i] = v[1]; sm.q[2][j][i] = v[2]; sm.q[3][j][i] = v[3];
         if (P.fixed_region) {
             const bool inside = (n >= 0 && n < P.N && m >= 0 && m < P.M);
-            sm.fx[j][i] = inside ? (unsigned char)cell_fixed(P, P.x_min + n * P.dx, P.y_min + m * P.dy) : 0;
+            sm.fx[j][i] = (inside && near_fixed) ? (unsigned char)cell_fixed(P, P.x_min + n * P.dx, P.y_min + m * P.dy)
+                                                 : 0;
         }
     }
     __syncthreads();
@@ -561,8 +588,7 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
     R smz = R(0), smr = R(0);
 
     // ---- every face of the tile once: z faces, then r faces, then the queue
-    face_pass<R, FLUX, RECON, TZ, TR, true>(P, sm, g, n0, m0, step, rc, fallback, smz);
-    face_pass<R, FLUX, RECON, TZ, TR, false>(P, sm, g, n0, m0, step, rc, fallback, smr);
+    face_pass<R, FLUX, RECON, TZ, TR>(P, sm, g, n0, m0, step, rc, fallback, smz, smr);
     __syncthreads();
     if (FLUX == 2) {
         queue_pass<R, RECON, TZ, TR>(P, sm, g, n0, m0, step, rc, fallback, smz, smr);
@@ -721,9 +747,15 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
 }
 
 // ------------------------------------------------------------------ the kernels
+// CTAs per SM the register allocation is sized for: FP64 2 (shared memory
+// allows no more); FP32 4 for HLL / HLLC (64 registers), 3 for the exact
+// solver (its Newton and sampling code needs more registers than 64)
+template <typename R, int FLUX>
+constexpr int min_ctas() { return sizeof(R) == 8 ? 2 : (FLUX == 2 ? 3 : 4); }
+
 // one problem: a CTA per tile, grid (tiles along z, tiles along r)
 template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
-__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(StepParams P)
+__global__ void __launch_bounds__(kThreads, min_ctas<R, FLUX>()) step_kernel(StepParams P)
 {
     step_tile<R, FLUX, RECON, LAYOUT, TZ, TR>(P, blockIdx.x, blockIdx.y, gridDim.x * gridDim.y);
 }
@@ -733,7 +765,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2) step_kernel(
 // tile_start[j+1]-1, its tiles in row-major order; its parameters are
 // Ps[j] (copied into shared memory once per CTA).
 template <typename R, int FLUX, bool RECON, int TZ, int TR>
-__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(kThreads, min_ctas<R, FLUX>())
     batch_kernel(const StepParams* __restrict__ Ps, const int* __restrict__ tile_start, int nprob)
 {
     __shared__ __align__(16) StepParams sP;

@@ -52,24 +52,38 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, interval_ms=50):
         self.index = index
+        self.interval_ms = interval_ms
         self.proc = None
-        self.lines = []
+        self.lines = []          # (host time, line)
+        self.window = None       # (begin, end) host times of the timed region
 
-    def start(self):
+    def start(self, ready_timeout=10.0):
+        """Starts nvidia-smi and waits for its first sample, so that the
+        timed region that follows is sampled from its beginning."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (FileNotFoundError, OSError):
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.lines and time.perf_counter() - t0 < ready_timeout:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def begin(self):
+        self.window = (time.perf_counter(), None)
+
+    def end(self):
+        self.window = (self.window[0], time.perf_counter())
 
     def stop(self):
         if self.proc is None:
@@ -82,7 +96,14 @@ class ClockSampler:
         self.thread.join(timeout=2)
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.window and self.window[1] is not None:
+            # the samples taken while the timed region ran (each sample
+            # reports the state over the interval before it is printed)
+            b, e = self.window
+            inside = [x for x in lines if b <= x[0] <= e + self.interval_ms / 1e3]
+            lines = inside if inside else lines
+        for _, ln in lines:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 8:
                 continue
@@ -95,7 +116,7 @@ class ClockSampler:
                 if val.lower() == "active":
                     reasons.add(name)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "interval_ms": self.interval_ms}
 
 
 # the measured forms: FP64 plain (the reference's solver), and the FP32 form
@@ -131,7 +152,7 @@ def learned_params(s0, u0):
     return params, "trained in this run on faces of 200 FP64 steps"
 
 
-def time_form(form, start, steps, warmup, torch, params=None, stats_steps=0):
+def time_form(form, start, steps, warmup, torch, params=None, stats_steps=0, sampler=None):
     """Device-timed steps of one form from the start state `start` = (s, u,
     (T_do, TT, step)): inputs resident in HBM, CUDA events on the solver's
     stream.  Returns (seconds, final s, final u, stats)."""
@@ -149,11 +170,15 @@ def time_form(form, start, steps, warmup, torch, params=None, stats_steps=0):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
+        if sampler:
+            sampler.begin()
         e0.record(stream)
         S.step(steps, sync=False)
         e1.record(stream)
         S.synchronize()
         torch.cuda.synchronize()
+        if sampler:
+            sampler.end()
         ms = e0.elapsed_time(e1)
         s, u = S.get_state()
     st = None
@@ -196,47 +221,72 @@ def axis_shock_z(s):
 
 def accuracy(nsteps, params):
     """Error of the FP32 forms against the FP64 path after nsteps from t = 0:
-    the precision form (HLL + minmod) and the learned form (exact Godunov)."""
+    the precision form (HLL + minmod) and the learned form (exact Godunov).
+    Two comparisons: at the same step count, and at the same simulated time
+    (the FP64 solution linearly interpolated in time to the FP32 run's final
+    time: the two runs' lagged time steps differ by ~1e-3 after 2000 steps,
+    which moves every shock by a fraction of a cell)."""
     from asteriy_2d_gb300 import abi as A
     from asteriy_2d_gb300 import problems, solver
+
+    def errs(r32, r64):
+        d = np.abs(r32 - r64)
+        return {"l1_rho": float(d[:, 0].sum() / np.abs(r64[:, 0]).sum()),
+                "l1_p": float(d[:, 1].sum() / np.abs(r64[:, 1]).sum()),
+                "linf_rho": float(d[:, 0].max() / np.abs(r64[:, 0]).max()),
+                "linf_p": float(d[:, 1].max() / np.abs(r64[:, 1]).max())}
+
     out = {}
     for name, flux, guess in (("precision_hll", A.FLUX_HLL, None), ("learned_godunov", A.FLUX_GODUNOV, params)):
-        res = {}
-        for prec in (A.PREC_FP64, A.PREC_FP32):
-            cfg = problems.blast_config(N_Z, M_R, flux=flux, precision=prec)
-            if prec == A.PREC_FP32 and flux == A.FLUX_GODUNOV:
-                cfg.riemann_tol = 1e-8
-                cfg.guess = A.GUESS_MLP
-            s0, u0 = solver.fill_blast(cfg)
-            with solver.Solver(cfg) as S:
-                if prec == A.PREC_FP32 and guess is not None:
-                    S.set_mlp(guess)
-                S.set_state(s0, u0)
-                S.step(nsteps)
-                res[prec] = S.get_state()[0]
+        cfg32 = problems.blast_config(N_Z, M_R, flux=flux, precision=A.PREC_FP32)
+        if flux == A.FLUX_GODUNOV:
+            cfg32.riemann_tol = 1e-8
+            cfg32.guess = A.GUESS_MLP
+        cfg64 = problems.blast_config(N_Z, M_R, flux=flux, precision=A.PREC_FP64)
+        s0, u0 = solver.fill_blast(cfg64)
+        with solver.Solver(cfg32) as S:
+            if guess is not None:
+                S.set_mlp(guess)
+            S.set_state(s0, u0)
+            S.step(nsteps)
+            r32 = S.get_state()[0]
+            tt32 = S.clock()[1]
+        # FP64: to nsteps - 8, then single steps, keeping the two states that
+        # bracket tt32 in time (at most 16 more steps)
+        with solver.Solver(cfg64) as S:
+            S.set_state(s0, u0)
+            S.step(nsteps - 8)
+            prev = (S.clock()[1], S.get_state()[0])
+            r64, bracket = None, None
+            for k in range(nsteps - 8, nsteps + 8):
+                S.step(1)
+                cur = (S.clock()[1], S.get_state()[0])
+                if k + 1 == nsteps:
+                    r64, tt64 = cur[1], cur[0]
+                if bracket is None and prev[0] <= tt32 <= cur[0]:
+                    bracket = (prev, cur)
+                if r64 is not None and bracket is not None:
+                    break
+                prev = cur
+        res = {"steps": nsteps, "same_step": errs(r32, r64), "tt_fp32": tt32, "tt_fp64": tt64,
+               "axis_shock_z_fp64": axis_shock_z(r64), "axis_shock_z_fp32": axis_shock_z(r32)}
+        if bracket is not None:
+            (ta, sa), (tb, sb) = bracket
+            w = (tt32 - ta) / (tb - ta) if tb > ta else 0.0
+            res["same_time"] = errs(r32, (1.0 - w) * sa + w * sb)
+        out[name] = res
         if name == "precision_hll":
             # the flow's own sensitivity: FP64 from an initial density
             # perturbed by 1e-12 relative, against the unperturbed FP64 run
-            cfg = problems.blast_config(N_Z, M_R, flux=flux, precision=A.PREC_FP64)
-            s0, u0 = solver.fill_blast(cfg)
-            s0 = s0.copy()
-            s0[:, 0] *= 1.0 + 1e-12 * np.random.default_rng(1).uniform(-1.0, 1.0, len(s0))
-            with solver.Solver(cfg) as S:
-                S.set_state(s0, u0)
+            sp = s0.copy()
+            sp[:, 0] *= 1.0 + 1e-12 * np.random.default_rng(1).uniform(-1.0, 1.0, len(sp))
+            with solver.Solver(cfg64) as S:
+                S.set_state(sp, u0)
                 S.step(nsteps)
                 rp = S.get_state()[0]
-            d = np.abs(rp - res[A.PREC_FP64])
-            out["fp64_sensitivity_1e-12"] = {"steps": nsteps,
-                                             "l1_rho": float(d[:, 0].sum() / np.abs(res[A.PREC_FP64][:, 0]).sum()),
-                                             "linf_rho": float(d[:, 0].max() / np.abs(res[A.PREC_FP64][:, 0]).max())}
-        r64, r32 = res[A.PREC_FP64], res[A.PREC_FP32]
-        d = np.abs(r32 - r64)
-        out[name] = {"steps": nsteps,
-                     "l1_rho": float(d[:, 0].sum() / np.abs(r64[:, 0]).sum()),
-                     "l1_p": float(d[:, 1].sum() / np.abs(r64[:, 1]).sum()),
-                     "linf_rho": float(d[:, 0].max() / np.abs(r64[:, 0]).max()),
-                     "linf_p": float(d[:, 1].max() / np.abs(r64[:, 1]).max()),
-                     "axis_shock_z_fp64": axis_shock_z(r64), "axis_shock_z_fp32": axis_shock_z(r32)}
+            d = np.abs(rp - r64)
+            out["fp64_sensitivity_1e-12"] = {"steps": nsteps, "l1_rho": float(d[:, 0].sum() / np.abs(r64[:, 0]).sum()),
+                                             "linf_rho": float(d[:, 0].max() / np.abs(r64[:, 0]).max())}
     return out
 
 
@@ -386,7 +436,7 @@ def dist_setup():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="fp32_learned", choices=list(FORMS))
@@ -486,7 +536,7 @@ def main():
     sampler.start()
     sec, s, u, st = time_form(args.form, start, args.steps, args.warmup, torch,
                               params if args.form == "fp32_learned" else None,
-                              stats_steps=0 if args.no_stats else 5)
+                              stats_steps=0 if args.no_stats else 5, sampler=sampler)
     clocks = sampler.stop()
     if ws > 1:
         t = torch.tensor([sec], dtype=torch.float64, device="cuda")
@@ -515,7 +565,7 @@ def main():
     if "fp64_godunov" in forms and args.form != "fp64_godunov":
         forms[args.form]["speedup_vs_fp64"] = forms[args.form]["value"] / forms["fp64_godunov"]["value"]
 
-    e2e_steps = max(3, args.steps // 4)
+    e2e_steps = max(3, min(args.steps // 4, 50))
     esec, bi, bo = time_e2e(args.form, start, e2e_steps, torch, params if args.form == "fp32_learned" else None)
     hbm, src = peaks()
     prec = "fp64" if args.form.startswith("fp64") else "fp32"
