@@ -279,9 +279,17 @@ __device__ __forceinline__ RPre<R> godunov_pre(const Gas<R>& g, R rL, R pL, R un
     RPre<R> q = godunov_sides(g, rL, pL, unL, utL, rR, pR, unR, utR);
     const R a = sqrt(q.rI * (g.g2 * q.pII + g.g1 * q.pI) / R(2));
     const R Uud = (q.pII - q.pI) / a;
+    if (q.Udf > R(0)) {
+        // Uvk <= 0 and Urz <= 0 (pI <= pII, so (pI/pII)^gm <= 1): neither
+        // vacuum nor two rarefactions, and only pattern 1 reads Urz and Uvk,
+        // so the pow of Urz is not needed (same patterns as the full test)
+        if (q.Udf <= Uud) q.pattern = 2;
+        else if (q.Udf > Uud) q.pattern = 3;
+        else q.pattern = 4;
+        return q;
+    }
     q.Urz = R(-2) * q.cII / g.g1 * (R(1) - pow(q.pI / q.pII, g.gm));
     q.Uvk = R(-2) * (q.cII + q.cI) / g.g1;
-    q.Udf = q.enI - q.enII;
     if (q.Udf < q.Uvk) q.pattern = 0;
     else if (q.Udf <= q.Urz) q.pattern = 1;
     else if (q.Udf <= Uud) q.pattern = 2;

@@ -748,10 +748,11 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
 
 // ------------------------------------------------------------------ the kernels
 // CTAs per SM the register allocation is sized for: FP64 2 (shared memory
-// allows no more); FP32 4 for HLL / HLLC (64 registers), 3 for the exact
-// solver (its Newton and sampling code needs more registers than 64)
+// allows no more); FP32 4 (64 registers; the exact solver spills a few
+// dozen bytes there and still runs 13% faster than at 3 CTAs and 85
+// registers, measured at 4096x2048)
 template <typename R, int FLUX>
-constexpr int min_ctas() { return sizeof(R) == 8 ? 2 : (FLUX == 2 ? 3 : 4); }
+constexpr int min_ctas() { return sizeof(R) == 8 ? 2 : 4; }
 
 // one problem: a CTA per tile, grid (tiles along z, tiles along r)
 template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
