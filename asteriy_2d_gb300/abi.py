@@ -24,6 +24,7 @@ AST_ST_BISECT_CAP = 0x08
 AST_ST_NONFINITE = 0x10
 AST_ST_VACUUM = 0x20
 AST_ST_MLP_FALLBACK = 0x40
+AST_ST_TIMEOUT = 0x80
 AST_MLP_NPARAM = 1325
 AST_RECORD_FLOATS = 10
 
@@ -59,7 +60,8 @@ class ast_config(C.Structure):
         ("body_rsplit", C.c_double), ("body_amp", C.c_double),
         ("dt_first", C.c_double), ("dt_cap", C.c_double), ("p_floor", C.c_double),
         ("riemann_tol", C.c_double),
-        ("collect_stats", C.c_int32), ("riemann_newton", C.c_int32), ("reserved_i", C.c_int32 * 6),
+        ("collect_stats", C.c_int32), ("riemann_newton", C.c_int32), ("persistent", C.c_int32),
+        ("reserved_i", C.c_int32 * 5),
         ("mlp_gate", C.c_double), ("reserved_d", C.c_double * 7),
     ]
 
@@ -115,6 +117,7 @@ def default_config():
     c.riemann_max_iter = 200
     c.dt_first, c.dt_cap, c.p_floor, c.riemann_tol = 1e-9, 1000.0, 1e-6, 10e-10
     c.collect_stats = 0
+    c.persistent = 1
     c.mlp_gate = 0.2
     return c
 

@@ -8,8 +8,11 @@
 // on the device inside the step kernel, so nsteps steps cost nsteps launches
 // and no host synchronisation.  Repeated step counts are replayed from a
 // captured CUDA graph.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -56,6 +59,34 @@ int ast::cuda_fail(cudaError_t e, const char* what)
 
 int ast::set_error(int code, const char* msg) { return fail(code, msg); }
 
+namespace {
+
+// the four FP32 state planes of one time level as a 3-D tensor (x = z
+// cells, y = rows, z = planes) with a TMA box of `bx` x `by` x 4
+int encode_planes(CUtensorMap* map, void* base, const ast_config& c, long long ld, long long plane, unsigned bx,
+                  unsigned by)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+            return fail(AST_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled not available");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dim[3] = {(cuuint64_t)c.N, (cuuint64_t)c.M, 4};
+    const cuuint64_t stride[2] = {(cuuint64_t)ld * sizeof(float), (cuuint64_t)plane * sizeof(float)};
+    const cuuint32_t box[3] = {bx, by, 4};
+    const cuuint32_t estride[3] = {1, 1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dim, stride, box, estride,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? AST_OK : fail(AST_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+}
+
+}  // namespace
+
 // ==================================================================== solver
 struct ast_solver {
     ast_config cfg;
@@ -75,6 +106,9 @@ struct ast_solver {
     float* rec = nullptr;            // face recorder buffer (device)
     unsigned long long* rec_n = nullptr;
     long long rec_cap = 0;
+    bool tma = false;                // FP32 persistent kernel
+    int tma_grid = 0;                // its CTAs
+    CUtensorMap tin[2], tout[2];     // tile-box load and store maps of buf[0], buf[1]
 };
 
 extern "C" {
@@ -140,6 +174,24 @@ int ast_create(const ast_config* cfg, ast_solver** out)
     }
     rc = (S->elem == 8) ? launch_step_r<double, kSoA>(S->P, cfg->flux, cfg->recon, nullptr, false)
                         : launch_step_r<float, kSoA>(S->P, cfg->flux, cfg->recon, nullptr, false);
+    if (rc == AST_OK && S->elem == 4 && cfg->persistent) {
+        // box loads of tile + halo (TZ+8 x TR+4), stores of the tile (TZ x TR)
+        for (int b = 0; b < 2 && rc == AST_OK; b++) {
+            rc = encode_planes(&S->tin[b], S->buf[b], *cfg, S->ld, S->plane, kTZ + 8, kTR + 4);
+            if (rc == AST_OK) rc = encode_planes(&S->tout[b], S->buf[b], *cfg, S->ld, S->plane, kTZ, kTR);
+        }
+        int per_sm = 0, dev = 0, sms = 0;
+        if (rc == AST_OK) rc = launch_step_tma(S->P, S->tin[0], S->tout[1], cfg->flux, cfg->recon, 0, nullptr, false,
+                                               &per_sm);
+        if (rc == AST_OK && (e = cudaGetDevice(&dev)) != cudaSuccess) rc = cuda_fail(e, "cudaGetDevice");
+        if (rc == AST_OK && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            rc = cuda_fail(e, "cudaDeviceGetAttribute");
+        if (rc == AST_OK) {
+            const long long tiles = (long long)((cfg->N + kTZ - 1) / kTZ) * ((cfg->M + kTR - 1) / kTR);
+            S->tma_grid = (int)std::min<long long>(tiles, (long long)std::max(per_sm, 1) * sms);
+            S->tma = true;
+        }
+    }
     if (rc != AST_OK) {
         ast_destroy(S);
         return rc;
@@ -260,7 +312,12 @@ static int enqueue_one(ast_solver* S)
     StepParams P = S->P;
     P.in = S->buf[S->cur];
     P.out = S->buf[S->cur ^ 1];
-    int rc = (S->elem == 8) ? launch_step_r<double, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true)
+    int rc;
+    if (S->tma)
+        rc = launch_step_tma(P, S->tin[S->cur], S->tout[S->cur ^ 1], S->cfg.flux, S->cfg.recon, S->tma_grid,
+                             S->stream, true, nullptr);
+    else
+        rc = (S->elem == 8) ? launch_step_r<double, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true)
                             : launch_step_r<float, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true);
     if (rc == AST_OK) S->cur ^= 1;
     return rc;
@@ -331,6 +388,7 @@ int ast_synchronize(ast_solver* S)
     unsigned int status = 0;
     AST_CUDA(cudaMemcpy(&status, &S->clock->status, sizeof status, cudaMemcpyDeviceToHost));
     if (status & AST_ST_NONFINITE) return fail(AST_ERR_NUMERIC, "non-finite wave speed");
+    if (status & AST_ST_TIMEOUT) return fail(AST_ERR_CUDA, "a bulk tile copy did not arrive in time");
     return AST_OK;
 }
 

@@ -4,6 +4,7 @@
 // parallel.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -27,7 +28,7 @@ template <typename R, int FLUX, bool RECON, int LAYOUT>
 int launch_step_t(const StepParams& P, cudaStream_t st, bool launch)
 {
     auto k = step_kernel<R, FLUX, RECON, LAYOUT, kTZ, kTR>;
-    constexpr size_t smem = tile_smem_bytes<R, kTZ, kTR>();
+    constexpr size_t smem = tile_smem_bytes<R, FLUX, kTZ, kTR>();
     cudaError_t e;
     if (!launch) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -38,6 +39,29 @@ int launch_step_t(const StepParams& P, cudaStream_t st, bool launch)
     e = cudaGetLastError();
     return e == cudaSuccess ? AST_OK : cuda_fail(e, "step kernel launch");
 }
+
+// the persistent FP32 kernel over `grid` CTAs; launch=false raises its
+// shared-memory limit and returns the CTAs per SM it reaches in *per_sm
+template <int FLUX, bool RECON>
+int launch_tma_t(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int grid, cudaStream_t st,
+                 bool launch, int* per_sm)
+{
+    auto k = step_kernel_tma<FLUX, RECON>;
+    constexpr size_t smem = tile_smem_bytes<float, FLUX, 32, 16, 2>();
+    cudaError_t e;
+    if (!launch) {
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, kThreads, smem);
+        return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    }
+    k<<<grid, kThreads, smem, st>>>(P, tin, tout);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? AST_OK : cuda_fail(e, "persistent step kernel launch");
+}
+
+int launch_step_tma(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int flux, int recon,
+                    int grid, cudaStream_t st, bool launch, int* per_sm);
 
 template <typename R, int LAYOUT>
 int launch_step_r(const StepParams& P, int flux, int recon, cudaStream_t st, bool launch)
@@ -62,7 +86,7 @@ template <typename R, int FLUX, bool RECON, int TZ, int TR>
 int launch_batch_t(const StepParams* Ps, const int* tile_start, int nprob, int tiles, cudaStream_t st, bool launch)
 {
     auto k = batch_kernel<R, FLUX, RECON, TZ, TR>;
-    constexpr size_t smem = tile_smem_bytes<R, TZ, TR>();
+    constexpr size_t smem = tile_smem_bytes<R, FLUX, TZ, TR>();
     cudaError_t e;
     if (!launch) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -18,8 +18,11 @@
 // run in full warps instead of in one or two lanes of many warps.
 #pragma once
 
+#include <type_traits>
+
 #include "mlp.cuh"
 #include "physics.cuh"
+#include "tma.cuh"
 
 namespace ast {
 
@@ -37,6 +40,8 @@ struct DevClock {
     unsigned long long cnt[10];    // rho_floor, p_floor, newton_calls, newton_iters,
                                    // bisect_calls, bisect_iters, mlp_fallback, newton_max,
                                    // strong_calls, strong_iters
+    unsigned int next_tile;        // persistent kernel: next tile to hand out
+    unsigned int pad_;
 };
 
 enum Layout { kSoA = 0, kAoS = 1 };
@@ -159,30 +164,65 @@ __device__ __forceinline__ T warp_max(T v)
 }
 
 // ------------------------------------------------------------------ shared memory of a tile
-template <typename R, int TZ, int TR>
-struct TileSmem {
-    static constexpr int HZ = TZ + 4, HR = TR + 4;
+// The staged tile: NB buffers of the four planes, each TR+4 rows of TZ+8
+// cells.  Cell (n, m) of the tile at (n0, m0) sits at row m - m0 + 2 and
+// column n - n0 + 4 = i + QX, where i = n - n0 + 2 is the cell's index in
+// the two-cell halo; the two extra columns on either side make the row
+// start 16-byte aligned in global memory (n0 - 4 is a multiple of 4), so a
+// TMA box can fill the buffer.
+template <typename R, int TZ, int TR, int NB>
+struct TileCore {
+    static constexpr int HZ = TZ + 4, HR = TR + 4, HZP = TZ + 8, QX = 2;
     static constexpr int kNFZ = TR * (TZ + 1);                 // z faces of the tile
     static constexpr int kQueueCap = kNFZ + (TR + 1) * TZ;    // all faces of the tile
-    R q[4][HR][HZ];              // staged state with a two-cell halo
+    alignas(128) R qb[NB][4][HR][HZP];   // staged state with a two-cell halo
     R Fz[4][TR][TZ + 1];         // z-face flux: mass, mom_z, mom_r, energy
     R Fr[4][TR + 1][TZ];         // r-face flux
-    // queued exact-solver faces: face code | active << 12 | pattern << 14.
-    // Faces above the learned-start gate fill the queue from the front, the
-    // others from the back, so the two kinds sit in separate warps.
-    int qcode[kQueueCap];
+    unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
+    unsigned qn;                 // queued faces: above the gate (low 16 bits), others (high 16 bits)
+};
+
+// the exact solver's part: queued faces as codes (face index | active << 12
+// | pattern << 14; faces above the learned-start gate fill the queue from
+// the front, the others from the back, so the two kinds sit in separate
+// warps), the start-value network and its tensor-core operands
+template <typename R, int TZ, int TR>
+struct QueueSmem {
+    static constexpr int kCap = TR * (TZ + 1) + (TR + 1) * TZ;
+    int qcode[kCap];
     float mlp[kMlpParams];       // learned start value (guess == MLP)
     unsigned mB1[tc::kL1];       // its W1, W2 as per-lane f16 mma fragments
     unsigned mB2[tc::kL2];
     float mX[kThreads / 32][16][8];  // per warp: standardised features of 16 faces
     float mY[kThreads / 32][16];     // per warp: network outputs
-    R qp0[kQueueCap];            // start value of each queued face
-    unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
-    unsigned qn;                 // queued faces: above the gate (low 16 bits), others (high 16 bits)
+    R qp0[kCap];                 // start value of each queued face
+};
+template <int K>
+struct Empty {};
+
+// the output tile of the TMA kernel: the updated cells, four dense planes
+template <typename R, int TZ, int TR>
+struct OutSmem {
+    alignas(128) R out[4][TR][TZ];
 };
 
-template <typename R, int TZ, int TR>
-constexpr size_t tile_smem_bytes() { return sizeof(TileSmem<R, TZ, TR>); }
+template <typename R, int FLUX, int TZ, int TR, int NB = 1>
+struct TileSmem : TileCore<R, TZ, TR, NB>,
+                  std::conditional_t<FLUX == 2, QueueSmem<R, TZ, TR>, Empty<0>>,
+                  std::conditional_t<(NB > 1), OutSmem<R, TZ, TR>, Empty<1>> {
+};
+
+// dynamic shared memory of a kernel: the tile plus 128 bytes to align it
+template <typename R, int FLUX, int TZ, int TR, int NB = 1>
+constexpr size_t tile_smem_bytes() { return sizeof(TileSmem<R, FLUX, TZ, TR, NB>) + 128; }
+
+template <typename S>
+__device__ __forceinline__ S& tile_smem()
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const size_t a = reinterpret_cast<size_t>(smem_raw);
+    return *reinterpret_cast<S*>(smem_raw + ((128 - (a & 127)) & 127));
+}
 
 // ------------------------------------------------------------------ cell update
 // Conservative update of one cell in arithmetic C from its state `in`
@@ -307,21 +347,22 @@ __device__ __forceinline__ void record_face(const StepParams& P, const Gas<R>& g
 // the reconstructed states on both sides of face (a, c) of orientation ZF
 // (minmod on the staged cells when RECON and the face is in the
 // high-order region `hi`; the cell values otherwise)
-template <typename R, bool RECON, int TZ, int TR, bool ZF>
-__device__ __forceinline__ void face_states(const StepParams& P, const TileSmem<R, TZ, TR>& sm, int a, int c, bool hi,
-                                            R L[4], R U[4])
+template <typename R, bool RECON, bool ZF, typename S>
+__device__ __forceinline__ void face_states(const StepParams& P, const S& sm, int b, int a, int c, bool hi, R L[4],
+                                            R U[4])
 {
-    constexpr int DJ = ZF ? 0 : 1, DI = ZF ? 1 : 0;
-    // smem indices of the lower (l) and upper (u) cell of the face
-    const int jl = ZF ? a + 2 : a + 1, il = ZF ? c + 1 : c + 2;
-    const int ju = a + 2, iu = c + 2;
+    constexpr int DJ = ZF ? 0 : 1, DI = ZF ? 1 : 0, QX = S::QX;
+    // buffer indices of the lower (l) and upper (u) cell of the face
+    const int jl = ZF ? a + 2 : a + 1, il = (ZF ? c + 1 : c + 2) + QX;
+    const int ju = a + 2, iu = c + 2 + QX;
+    const auto& q = sm.qb[b];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const R tl = sm.q[k][jl][il], tu = sm.q[k][ju][iu];
+        const R tl = q[k][jl][il], tu = q[k][ju][iu];
         L[k] = tl;
         U[k] = tu;
         if (RECON && hi) {
-            const R tll = sm.q[k][jl - DJ][il - DI], tuu = sm.q[k][ju + DJ][iu + DI];
+            const R tll = q[k][jl - DJ][il - DI], tuu = q[k][ju + DJ][iu + DI];
             R x0, x1;
             recon_pair(tll, tl, tu, x0, x1);
             L[k] = x1;                  // right/top value of the lower cell
@@ -345,9 +386,9 @@ __device__ __forceinline__ void face_states(const StepParams& P, const TileSmem<
 // sm.Fz / sm.Fr and raises smax to the largest wave speed of the faces that
 // belong to at least one updated cell.  Exact-solver faces of patterns 2
 // and 3 go to the queue instead.
-template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF>
-__device__ __forceinline__ void face_one(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
-                                         int m0, int step, RiemannCount& rc, int& fallback, R& smax, int f)
+template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF, typename S>
+__device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0, int step,
+                                         RiemannCount& rc, int& fallback, R& smax, int f)
 {
     constexpr int NFZ = TR * (TZ + 1);
     constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
@@ -371,9 +412,10 @@ __device__ __forceinline__ void face_one(const StepParams& P, TileSmem<R, TZ, TR
             hi = (xf > P.region_lo && xf < P.region_hi);
         }
         R L[4], U[4], F[4];
-        face_states<R, RECON, TZ, TR, ZF>(P, sm, a, c, hi, L, U);
+        face_states<R, RECON, ZF>(P, sm, b, a, c, hi, L, U);
         R Sp;
-        if (FLUX == 2 && hi && L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]) {
+        if constexpr (FLUX == 2) {
+        if (hi && L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]) {
             // identical states: the exact solution is that state (the
             // reference reaches it through the two-rarefaction branch with
             // p* = p, u* = u_n, up to rounding), its flux the physical flux
@@ -386,20 +428,24 @@ __device__ __forceinline__ void face_one(const StepParams& P, TileSmem<R, TZ, TR
             F[2] = m * ut;
             F[3] = un * (p * g.inv_g1 + R(0.5) * r * (un * un + ut * ut) + p);
             Sp = fmax(fabs(un) + c, g.eps8);
-        } else if (FLUX == 2 && hi) {
+        } else if (hi) {
             const RPre<R> q = godunov_pre(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT]);
             if (q.pattern == 2 || q.pattern == 3) {
                 // the iterative faces go to the queue (room for every face
                 // of the tile); their flux is written by queue_pass
                 const bool strong = P.riemann_newton && wave_strength(q) > P.mlp_gate;
                 const unsigned old = atomicAdd(&sm.qn, strong ? 1u : 0x10000u);
-                const int slot = strong ? (int)(old & 0xffffu) : TileSmem<R, TZ, TR>::kQueueCap - 1 - (int)(old >> 16);
+                const int slot = strong ? (int)(old & 0xffffu) : S::kQueueCap - 1 - (int)(old >> 16);
                 sm.qcode[slot] = (ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.pattern << 14);
                 return;
             }
             Sp = godunov_sample(g, q, R(0), F, rc);
-        } else if (FLUX == 1 && hi) {
-            Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+        } else {
+            Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+        }
+        } else if constexpr (FLUX == 1) {
+            if (hi) Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+            else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         } else {
             Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         }
@@ -417,38 +463,38 @@ __device__ __forceinline__ void face_one(const StepParams& P, TileSmem<R, TZ, TR
 // every face of the tile once, z faces then r faces, in one loop over the
 // CTA's threads; the z faces are padded to whole warps so that no warp
 // mixes the two orientations
-template <typename R, int FLUX, bool RECON, int TZ, int TR>
-__device__ __forceinline__ void face_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
-                                          int m0, int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
+template <typename R, int FLUX, bool RECON, int TZ, int TR, typename S>
+__device__ __forceinline__ void face_pass(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
+                                          int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
 {
     constexpr int NFZ = TR * (TZ + 1), NFR = (TR + 1) * TZ;
     constexpr int NFZP = (NFZ + 31) / 32 * 32;
     for (int t = threadIdx.x; t < NFZP + NFR; t += kThreads) {
         if (t < NFZ)
-            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, g, n0, m0, step, rc, fallback, smz, t);
+            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, rc, fallback, smz, t);
         else if (t >= NFZP)
-            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, g, n0, m0, step, rc, fallback, smr, t - NFZP);
+            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, rc, fallback, smr, t - NFZP);
     }
 }
 
 // the exact-solver states of queued face fc (z faces first, then r faces):
 // its reconstructed sides, swapped as godunov_pre swaps them, with the
 // pattern found in face_pass; lower/upper states in the face frame too
-template <typename R, bool RECON, int TZ, int TR>
-__device__ __forceinline__ RPre<R> queued_face(const StepParams& P, const TileSmem<R, TZ, TR>& sm, const Gas<R>& g,
-                                               int fc, int pattern, int& a, int& c, bool& zf)
+template <typename R, bool RECON, int TZ, int TR, typename S>
+__device__ __forceinline__ RPre<R> queued_face(const StepParams& P, const S& sm, int b, const Gas<R>& g, int fc,
+                                               int pattern, int& a, int& c, bool& zf)
 {
-    constexpr int NFZ = TileSmem<R, TZ, TR>::kNFZ;
+    constexpr int NFZ = S::kNFZ;
     R L[4], U[4];
     zf = fc < NFZ;
     if (zf) {
         a = fc / (TZ + 1);
         c = fc - a * (TZ + 1);
-        face_states<R, RECON, TZ, TR, true>(P, sm, a, c, true, L, U);
+        face_states<R, RECON, true>(P, sm, b, a, c, true, L, U);
     } else {
         a = (fc - NFZ) / TZ;
         c = (fc - NFZ) - a * TZ;
-        face_states<R, RECON, TZ, TR, false>(P, sm, a, c, true, L, U);
+        face_states<R, RECON, false>(P, sm, b, a, c, true, L, U);
     }
     // normal and tangential velocity: (v_z, v_r) on z faces, (v_r, v_z) on r faces
     const R unL = zf ? L[2] : L[3], utL = zf ? L[3] : L[2];
@@ -459,11 +505,11 @@ __device__ __forceinline__ RPre<R> queued_face(const StepParams& P, const TileSm
 }
 
 // the queued exact-solver faces, solved by all threads of the CTA
-template <typename R, bool RECON, int TZ, int TR>
-__device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, TR>& sm, const Gas<R>& g, int n0,
-                                           int m0, int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
+template <typename R, bool RECON, int TZ, int TR, typename S>
+__device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
+                                           int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
 {
-    constexpr int CAP = TileSmem<R, TZ, TR>::kQueueCap;
+    constexpr int CAP = S::kQueueCap;
     const int ns = (int)(sm.qn & 0xffffu), nw = (int)(sm.qn >> 16);
     if (P.riemann_newton && P.guess == 1 && P.mlp != nullptr && ns > 0) {
         // phase 1: learned start values of the faces above the gate (queue
@@ -483,7 +529,8 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
                     const int code = sm.qcode[i];
                     int a, c;
                     bool zf;
-                    const RPre<R> q = queued_face<R, RECON, TZ, TR>(P, sm, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
+                    const RPre<R> q =
+                        queued_face<R, RECON, TZ, TR>(P, sm, b, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
                     R rL, uL, cL, rR, pR, uR, cR;
                     face_sides(q, rL, pL, uL, cL, rR, pR, uR, cR);
                     mlp_features((float)g.ga, (float)rL, (float)pL, (float)uL, (float)cL, (float)rR, (float)pR,
@@ -514,7 +561,7 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
         const bool active = (code >> 12) & 1;
         int a, c;
         bool zf;
-        const RPre<R> q = queued_face<R, RECON, TZ, TR>(P, sm, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
+        const RPre<R> q = queued_face<R, RECON, TZ, TR>(P, sm, b, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
         const R p = solve_queued(P, g, q, strong, (strong && P.guess == 1 && P.mlp) ? sm.qp0[i] : R(0), rc, fallback);
         R F[4];
         R Sp = godunov_sample(g, q, p, F, rc);
@@ -532,81 +579,158 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, TileSmem<R, TZ, 
 }
 
 // ------------------------------------------------------------------ one tile of one step
-// Tile (bx, by) of the problem P; `tiles` is the number of tiles of that
-// problem (the last of them to finish performs the dt epilogue).
-template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
-__device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, unsigned int tiles)
-{
-    using S = TileSmem<R, TZ, TR>;
-    constexpr int HZ = S::HZ, HR = S::HR;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    S& sm = *reinterpret_cast<S*>(smem_raw);
-    __shared__ R red_r[2][kThreads / 32];
-    __shared__ int red_i[4][kThreads / 32];
-    __shared__ int s_last;
-    __shared__ double s_tdv;
-    __shared__ float s_tdv_f, s_T_f;
-
-    const int tid = threadIdx.x;
-    const int n0 = bx * TZ, m0 = by * TR;
-    const Gas<R>& g = *reinterpret_cast<const Gas<R>*>(sizeof(R) == 8 ? (const void*)&P.gd : (const void*)&P.gf);
-    const double T_do = (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr;
-    const int step = (P.clock != nullptr) ? (int)P.clock->step : 0;
-    if (tid == 0) {
-        sm.qn = 0u;
-        s_tdv = T_do / (P.dx * P.dy);
-        s_tdv_f = (float)s_tdv;
-        s_T_f = (float)T_do;
+// per-thread running values over the tiles a CTA processes in one step
+template <typename R>
+struct TileAcc {
+    RiemannCount rc;
+    int fallback, nrho, np;
+    R smz, smr;
+    __device__ __forceinline__ void clear()
+    {
+        rc.clear();
+        fallback = nrho = np = 0;
+        smz = smr = R(0);
     }
+};
 
-    // the fixed region's exact test (FP64 divisions, as the reference
-    // evaluates it) only in tiles whose cells, halo included, meet the
-    // region's cell bounding box
-    const bool near_fixed = P.fixed_region && n0 - 2 <= P.fixed_nhi && n0 + TZ + 1 >= P.fixed_nlo &&
-                            m0 - 2 <= P.fixed_mhi;
+// constants of the step every tile shares (set by thread 0, read after a barrier)
+struct StepConsts {
+    double T_do;           // the step's dt
+    double tdv;            // T_do / (dx dy)
+    float tdv_f, T_f;
+    int step;
+};
 
-    // ---- stage tile + halo; the corners are never read by the cross stencil
-    for (int idx = tid; idx < HR * HZ; idx += kThreads) {
+__device__ __forceinline__ void step_consts(const StepParams& P, StepConsts& K)
+{
+    K.T_do = (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr;
+    K.step = (P.clock != nullptr) ? (int)P.clock->step : 0;
+    K.tdv = K.T_do / (P.dx * P.dy);
+    K.tdv_f = (float)K.tdv;
+    K.T_f = (float)K.T_do;
+}
+
+// the fixed region's exact test (FP64 divisions, as the reference evaluates
+// it) only in tiles whose cells, halo included, meet the region's cell
+// bounding box
+template <int TZ, int TR>
+__device__ __forceinline__ bool tile_near_fixed(const StepParams& P, int n0, int m0)
+{
+    return P.fixed_region && n0 - 2 <= P.fixed_nhi && n0 + TZ + 1 >= P.fixed_nlo && m0 - 2 <= P.fixed_mhi;
+}
+
+// stage tile + halo from global memory into buffer b, ghost rules applied;
+// the corners are never read by the cross stencil
+template <typename R, int LAYOUT, int TZ, int TR, typename S>
+__device__ __forceinline__ void stage_tile(const StepParams& P, S& sm, int b, int n0, int m0)
+{
+    constexpr int HZ = S::HZ, HR = S::HR, QX = S::QX;
+    const bool near_fixed = tile_near_fixed<TZ, TR>(P, n0, m0);
+    for (int idx = threadIdx.x; idx < HR * HZ; idx += kThreads) {
         const int j = idx / HZ, i = idx - j * HZ;
         const bool rin = (j >= 2 && j < TR + 2), cin = (i >= 2 && i < TZ + 2);
         if (!rin && !cin) continue;
         const int n = n0 - 2 + i, m = m0 - 2 + j;
         R v[4];
         fetch_cell<R, LAYOUT>(P, n, m, v);
-        sm.q[0][j][i] = v[0]; sm.q[1][j][i] = v[1]; sm.q[2][j][i] = v[2]; sm.q[3][j][i] = v[3];
+        sm.qb[b][0][j][i + QX] = v[0]; sm.qb[b][1][j][i + QX] = v[1];
+        sm.qb[b][2][j][i + QX] = v[2]; sm.qb[b][3][j][i + QX] = v[3];
         if (P.fixed_region) {
             const bool inside = (n >= 0 && n < P.N && m >= 0 && m < P.M);
             sm.fx[j][i] = (inside && near_fixed) ? (unsigned char)cell_fixed(P, P.x_min + n * P.dx, P.y_min + m * P.dy)
                                                  : 0;
         }
     }
-    __syncthreads();
+}
 
-    RiemannCount rc;
-    rc.clear();
-    int fallback = 0;
-    R smz = R(0), smr = R(0);
+// After a bulk copy of the tile box into buffer b (zeros outside the
+// grid): the cross-stencil cells outside the grid get their ghost values
+// from the staged cells, as fetch_cell gives them from global memory, for
+// the two ghost layers next to the boundary; deeper ghost cells (those of a
+// partial tile beyond its last row or column, which feed only faces that
+// no updated cell uses) become copies of the boundary cell.  Also sets the
+// fixed-region flags.
+template <typename R, int TZ, int TR, typename S>
+__device__ __forceinline__ void patch_tile(const StepParams& P, S& sm, int b, int n0, int m0)
+{
+    constexpr int HZ = S::HZ, HR = S::HR, QX = S::QX;
+    const int N = P.N, M = P.M;
+    const bool edge = n0 - 2 < 0 || n0 + TZ + 2 > N || m0 - 2 < 0 || m0 + TR + 2 > M;
+    const bool near_fixed = tile_near_fixed<TZ, TR>(P, n0, m0);
+    if (!edge && !P.fixed_region) return;
+    auto& q = sm.qb[b];
+    for (int idx = threadIdx.x; idx < HR * HZ; idx += kThreads) {
+        const int j = idx / HZ, i = idx - j * HZ;
+        const bool rin = (j >= 2 && j < TR + 2), cin = (i >= 2 && i < TZ + 2);
+        if (!rin && !cin) continue;
+        const int n = n0 - 2 + i, m = m0 - 2 + j;
+        const bool inside = (n >= 0 && n < N && m >= 0 && m < M);
+        if (P.fixed_region)
+            sm.fx[j][i] = (inside && near_fixed) ? (unsigned char)cell_fixed(P, P.x_min + n * P.dx, P.y_min + m * P.dy)
+                                                 : 0;
+        if (inside) continue;
+        int side, g, bn, bm, mn, mm;
+        bool low;
+        if (n < 0)       { side = 0; g = -1 - n; low = true;  bn = 0;     bm = m; mn = g;         mm = m; }
+        else if (n >= N) { side = 1; g = n - N;  low = false; bn = N - 1; bm = m; mn = N - 1 - g; mm = m; }
+        else if (m < 0)  { side = 2; g = -1 - m; low = true;  bn = n; bm = 0;     mn = n; mm = g; }
+        else             { side = 3; g = m - M;  low = false; bn = n; bm = M - 1; mn = n; mm = M - 1 - g; }
+        mn = min(max(mn, 0), N - 1);
+        mm = min(max(mm, 0), M - 1);
+        bm = min(max(bm, 0), M - 1);
+        bn = min(max(bn, 0), N - 1);
+        const int kind = (g >= 2) ? 1 : P.bc_kind[side];
+        const bool zside = side < 2;
+        R v[4];
+        if (kind == 0) {            // REFLECT
+            const int si = mn - n0 + 2 + QX, sj = mm - m0 + 2;
+            v[0] = q[0][sj][si]; v[1] = q[1][sj][si]; v[2] = q[2][sj][si]; v[3] = q[3][sj][si];
+            if (zside) v[2] = -v[2]; else v[3] = -v[3];
+        } else if (kind == 2) {     // FIXED
+            v[0] = (R)P.bc_val[side][0]; v[1] = (R)P.bc_val[side][1];
+            v[2] = (R)P.bc_val[side][2]; v[3] = (R)P.bc_val[side][3];
+        } else {                    // OUTFLOW, SUCTION, deeper ghost layers
+            const int si = bn - n0 + 2 + QX, sj = bm - m0 + 2;
+            v[0] = q[0][sj][si]; v[1] = q[1][sj][si]; v[2] = q[2][sj][si]; v[3] = q[3][sj][si];
+            if (kind == 3) {
+                R lim = (R)(zside ? P.bc_val[side][2] : P.bc_val[side][3]);
+                R& vn = zside ? v[2] : v[3];
+                if (low) { if (vn > lim) vn = lim; }
+                else     { if (vn < lim) vn = lim; }
+            }
+        }
+        q[0][j][i + QX] = v[0]; q[1][j][i + QX] = v[1]; q[2][j][i + QX] = v[2]; q[3][j][i + QX] = v[3];
+    }
+}
 
-    // ---- every face of the tile once: z faces, then r faces, then the queue
-    face_pass<R, FLUX, RECON, TZ, TR>(P, sm, g, n0, m0, step, rc, fallback, smz, smr);
+// faces, exact-solver queue and conservative update of the tile staged in
+// buffer b.  TO_SMEM: the updated cells go to sm.out (for a bulk store)
+// instead of global memory.  Ends without a barrier.
+template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR, bool TO_SMEM, typename S>
+__device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
+                                          const StepConsts& K, TileAcc<R>& acc)
+{
+    constexpr int QX = S::QX;
+    // ---- every face of the tile once, then the queue
+    face_pass<R, FLUX, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
     __syncthreads();
-    if (FLUX == 2) {
-        queue_pass<R, RECON, TZ, TR>(P, sm, g, n0, m0, step, rc, fallback, smz, smr);
+    if constexpr (FLUX == 2) {
+        queue_pass<R, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
         __syncthreads();
     }
 
     // ---- conservative update of the tile's cells
-    int nrho = 0, np = 0;
-    const double tdv_d = s_tdv;
-    const float tdv_f = s_tdv_f, Tf = s_T_f, dxf = P.dxf, dyf = P.dyf;
+    const double T_do = K.T_do, tdv_d = K.tdv;
+    const float tdv_f = K.tdv_f, Tf = K.T_f, dxf = P.dxf, dyf = P.dyf;
     const float yminf = P.y_minf;
     const float gaf = P.gf.ga, g1f = P.gf.g1, ig1f = P.gf.inv_g1;
-    for (int cidx = tid; cidx < TZ * TR; cidx += kThreads) {
+    const auto& qv = sm.qb[b];
+    for (int cidx = threadIdx.x; cidx < TZ * TR; cidx += kThreads) {
         const int row = cidx / TZ, col = cidx - row * TZ;
         const int n = n0 + col, m = m0 + row;
         if (n >= P.N || m >= P.M) continue;
         const int j = row + 2, i = col + 2;
-        R o[4] = {sm.q[0][j][i], sm.q[1][j][i], sm.q[2][j][i], sm.q[3][j][i]};
+        R o[4] = {qv[0][j][i + QX], qv[1][j][i + QX], qv[2][j][i + QX], qv[3][j][i + QX]};
         if (!(P.fixed_region && sm.fx[j][i])) {
             R in[4] = {o[0], o[1], o[2], o[3]};
             R f[4][4];
@@ -629,7 +753,7 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
                 }
                 const double ty = (P.geom == 1) ? T_do / y : 0.0;
                 update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty, P.dx,
-                                    P.dy, Q2, nrho, np, o);
+                                    P.dy, Q2, acc.nrho, acc.np, o);
             } else {
                 // FP32 form: float arithmetic only
                 const float y = yminf + (float)m * dyf;
@@ -641,7 +765,8 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
                 }
                 const float ty = (P.geom == 1) ? Tf / y : 0.0f;
                 float E2, KE2;
-                update_cell<float>(P, gaf, g1f, ig1f, in, f, Tf, tdv_f, ty, dxf, dyf, Q2, nrho, np, o, &E2, &KE2);
+                update_cell<float>(P, gaf, g1f, ig1f, in, f, Tf, tdv_f, ty, dxf, dyf, Q2, acc.nrho, acc.np, o, &E2,
+                                   &KE2);
                 // pressure recovery p = (g-1)(E - rho v^2/2) in FP64 where the
                 // kinetic energy is more than 99% of the total
                 if (KE2 > 0.99f * E2) {
@@ -653,7 +778,10 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
                 }
             }
         }
-        if (LAYOUT == kSoA) {
+        if constexpr (TO_SMEM) {
+            sm.out[0][row][col] = o[0]; sm.out[1][row][col] = o[1];
+            sm.out[2][row][col] = o[2]; sm.out[3][row][col] = o[3];
+        } else if (LAYOUT == kSoA) {
             R* out = (R*)P.out;
             const long long k = (long long)m * P.ld + n;
             out[k] = o[0]; out[k + P.plane] = o[1]; out[k + 2 * P.plane] = o[2]; out[k + 3 * P.plane] = o[3];
@@ -663,13 +791,27 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
             ((double2*)P.out_u)[k] = make_double2((double)o[2], (double)o[3]);
         }
     }
+}
 
-    // ---- block reductions and the step epilogue
+// Block reduction of the CTA's accumulators and the step epilogue.  `units`
+// = the number of CTAs that report for this problem and step (one ticket
+// each); the last of them turns the wave-speed maxima into the next dt and
+// performs the reference's funk_time shift (kernel.cu:1525-1536), and with
+// reset_tiles also rewinds the tile counter of the persistent kernel.
+template <typename R>
+__device__ __forceinline__ void cta_epilogue(const StepParams& P, TileAcc<R>& acc, unsigned int units,
+                                             bool reset_tiles)
+{
+    __shared__ R red_r[2][kThreads / 32];
+    __shared__ int red_i[4][kThreads / 32];
+    __shared__ int s_last;
+    const int tid = threadIdx.x;
     const int lane = tid & 31, wid = tid >> 5;
+    RiemannCount& rc = acc.rc;
     {
-        const R a = warp_max(smz), b = warp_max(smr);
-        const int c0 = __reduce_add_sync(0xffffffffu, nrho), c1 = __reduce_add_sync(0xffffffffu, np);
-        const int c2 = __reduce_add_sync(0xffffffffu, fallback);
+        const R a = warp_max(acc.smz), b = warp_max(acc.smr);
+        const int c0 = __reduce_add_sync(0xffffffffu, acc.nrho), c1 = __reduce_add_sync(0xffffffffu, acc.np);
+        const int c2 = __reduce_add_sync(0xffffffffu, acc.fallback);
         const unsigned st = __reduce_or_sync(0xffffffffu, rc.status);
         if (lane == 0) {
             red_r[0][wid] = a; red_r[1][wid] = b;
@@ -717,7 +859,7 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
             if (st) atomicOr(&C->status, st);
             __threadfence();
             const unsigned int ticket = atomicAdd(&C->done, 1u);
-            s_last = (ticket == tiles - 1) ? 1 : 0;
+            s_last = (ticket == units - 1) ? 1 : 0;
         } else {
             // raw mode: this CTA's dt candidate, min-reduced into *T_min
             double dt = P.dt_cap;
@@ -742,8 +884,31 @@ __device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, u
         C->TT = C->TT + dt;
         C->step = C->step + 1;
         C->done = 0u;
+        if (reset_tiles) C->next_tile = 0u;
         __threadfence();
     }
+}
+
+// Tile (bx, by) of the problem P; `tiles` is the number of tiles of that
+// problem (the last of them to finish performs the dt epilogue).
+template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
+__device__ __forceinline__ void step_tile(const StepParams& P, int bx, int by, unsigned int tiles)
+{
+    using S = TileSmem<R, FLUX, TZ, TR>;
+    S& sm = tile_smem<S>();
+    __shared__ StepConsts sK;
+    const int n0 = bx * TZ, m0 = by * TR;
+    const Gas<R>& g = *reinterpret_cast<const Gas<R>*>(sizeof(R) == 8 ? (const void*)&P.gd : (const void*)&P.gf);
+    if (threadIdx.x == 0) {
+        sm.qn = 0u;
+        step_consts(P, sK);
+    }
+    stage_tile<R, LAYOUT, TZ, TR>(P, sm, 0, n0, m0);
+    __syncthreads();
+    TileAcc<R> acc;
+    acc.clear();
+    tile_body<R, FLUX, RECON, LAYOUT, TZ, TR, false>(P, sm, 0, g, n0, m0, sK, acc);
+    cta_epilogue<R>(P, acc, tiles, false);
 }
 
 // ------------------------------------------------------------------ the kernels
@@ -789,6 +954,97 @@ __global__ void __launch_bounds__(kThreads, min_ctas<R, FLUX>())
     const int t = (int)blockIdx.x - tile_start[j];
     const int tz = (sP.N + TZ - 1) / TZ;
     step_tile<R, FLUX, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, (unsigned)(tile_start[j + 1] - tile_start[j]));
+}
+
+// The FP32 solver's persistent kernel: as many CTAs as fit on the GPU at
+// once, each taking tiles from a counter in the clock until none are left.
+// A tile and its halo arrive by one bulk-tensor copy of the box (x = z
+// cells n0-4 .. n0+TZ+3, y = rows m0-2 .. m0+TR+1, all four planes) into
+// one of two buffers; the copy of the CTA's next tile runs while the current
+// one is computed.  The updated cells leave by a bulk-tensor store from a
+// shared-memory tile.  The CTA's wave-speed maxima and counters accumulate
+// over its tiles and are reported once (one ticket per CTA).  A bulk copy
+// that does not arrive within the wait limit sets AST_ST_TIMEOUT and ends
+// the CTA's loop.
+template <int FLUX, bool RECON>
+__global__ void __launch_bounds__(kThreads, 4)
+    step_kernel_tma(StepParams P, const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout)
+{
+    using R = float;
+    constexpr int TZ = 32, TR = 16;
+    using S = TileSmem<R, FLUX, TZ, TR, 2>;
+    constexpr uint32_t kBoxBytes = 4u * S::HR * S::HZP * sizeof(R);
+    static_assert(sizeof(((S*)nullptr)->qb[0]) == kBoxBytes, "tile buffer is the TMA box");
+    S& sm = tile_smem<S>();
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int s_tile[2];
+    __shared__ StepConsts sK;
+    const int tid = threadIdx.x;
+    const int tiles_z = (P.N + TZ - 1) / TZ;
+    const int tiles = tiles_z * ((P.M + TR - 1) / TR);
+    if (tid == 0) {
+        tma::prefetch_map(&tin);
+        tma::prefetch_map(&tout);
+        tma::mbar_init(&bar[0], 1);
+        tma::mbar_init(&bar[1], 1);
+        tma::fence_async_shared();
+        step_consts(P, sK);
+        const int t0 = (int)atomicAdd(&P.clock->next_tile, 1u);
+        s_tile[0] = t0;
+        if (t0 < tiles) {
+            tma::mbar_expect(&bar[0], kBoxBytes);
+            tma::load_3d(&tin, &sm.qb[0][0][0][0], &bar[0], (t0 % tiles_z) * TZ - 4, (t0 / tiles_z) * TR - 2, 0);
+        }
+    }
+    __syncthreads();
+    TileAcc<R> acc;
+    acc.clear();
+    const Gas<R>& g = P.gf;
+    for (int k = 0;; k++) {
+        const int b = k & 1;
+        const int t = s_tile[b];
+        if (t >= tiles) break;
+        if (tid == 0) {
+            // prefetch: the other buffer was last read by the previous tile,
+            // which every thread finished before the barrier that ended it
+            const int tn = (int)atomicAdd(&P.clock->next_tile, 1u);
+            s_tile[b ^ 1] = tn;
+            if (tn < tiles) {
+                tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
+                tma::load_3d(&tin, &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], (tn % tiles_z) * TZ - 4,
+                             (tn / tiles_z) * TR - 2, 0);
+            }
+        }
+        const bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+        if (__syncthreads_or(!arrived)) {
+            // give up this step's remaining tiles; wait (bounded) for the
+            // prefetch in flight and for the stores before leaving
+            if (tid == 0) {
+                acc.rc.status |= AST_ST_TIMEOUT;
+                tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+                if (s_tile[b ^ 1] < tiles) tma::mbar_wait(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
+            }
+            break;
+        }
+        const int n0 = (t % tiles_z) * TZ, m0 = (t / tiles_z) * TR;
+        patch_tile<R, TZ, TR>(P, sm, b, n0, m0);
+        if (tid == 0) {
+            sm.qn = 0u;
+            tma::store_wait_read();   // the previous tile's store has read sm.out
+        }
+        __syncthreads();
+        tile_body<R, FLUX, RECON, kSoA, TZ, TR, true>(P, sm, b, g, n0, m0, sK, acc);
+        // this thread's shared-memory writes (sm.out, ghost cells) before
+        // the bulk copies that read or overwrite them
+        tma::fence_async_shared();
+        __syncthreads();
+        if (tid == 0) {
+            tma::store_3d(&tout, &sm.out[0][0][0], n0, m0, 0);
+            tma::store_commit();
+        }
+    }
+    if (tid == 0) tma::store_wait_all();
+    cta_epilogue<R>(P, acc, gridDim.x, true);
 }
 
 }  // namespace ast

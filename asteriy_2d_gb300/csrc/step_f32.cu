@@ -3,4 +3,17 @@
 
 namespace ast {
 template int launch_step_r<float, kSoA>(const StepParams&, int, int, cudaStream_t, bool);
+
+int launch_step_tma(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int flux, int recon,
+                    int grid, cudaStream_t st, bool launch, int* per_sm)
+{
+    if (recon) {
+        if (flux == AST_FLUX_HLL) return launch_tma_t<0, true>(P, tin, tout, grid, st, launch, per_sm);
+        if (flux == AST_FLUX_HLLC) return launch_tma_t<1, true>(P, tin, tout, grid, st, launch, per_sm);
+        return launch_tma_t<2, true>(P, tin, tout, grid, st, launch, per_sm);
+    }
+    if (flux == AST_FLUX_HLL) return launch_tma_t<0, false>(P, tin, tout, grid, st, launch, per_sm);
+    if (flux == AST_FLUX_HLLC) return launch_tma_t<1, false>(P, tin, tout, grid, st, launch, per_sm);
+    return launch_tma_t<2, false>(P, tin, tout, grid, st, launch, per_sm);
+}
 }  // namespace ast

@@ -1,0 +1,99 @@
+// tma.cuh - the bulk-tensor (TMA) copies and mbarrier waits of the
+// persistent FP32 step kernel, as inline PTX for sm_103a.
+//
+// Loads: cp.async.bulk.tensor.3d (x = cells along z, y = rows along r,
+// z = the four state planes) into shared memory, completion signalled on an
+// mbarrier with an expected byte count.  Stores: the updated tile from
+// shared memory back to the state planes through a bulk group.  Every wait
+// is bounded: after kWaitLimit failed polls the caller gets `false` and
+// must report the failure instead of waiting on.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ast {
+namespace tma {
+
+constexpr int kWaitLimit = 1 << 21;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// orders this thread's shared-memory writes (generic proxy) before later
+// accesses by the bulk-copy engine (async proxy), and makes an mbarrier's
+// initialisation visible to it
+__device__ __forceinline__ void fence_async_shared()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// arms the barrier for `bytes` of incoming data (one arrival)
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// waits for the completion of phase `parity` of the barrier; false after
+// kWaitLimit polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+    const uint32_t a = smem_addr(bar);
+    for (int i = 0; i < kWaitLimit; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n"
+            ".reg .pred p;\n"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n"
+            "}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// box of the 3-D tensor map at (x, y, z) into shared memory, completing on bar
+__device__ __forceinline__ void load_3d(const CUtensorMap* map, void* dst, uint64_t* bar, int x, int y, int z)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// shared-memory box to the tensor at (x, y, z); parts outside the tensor
+// are not written
+__device__ __forceinline__ void store_3d(const CUtensorMap* map, const void* src, int x, int y, int z)
+{
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];"
+                 ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(src))
+                 : "memory");
+}
+
+__device__ __forceinline__ void store_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// the committed stores have read their shared-memory source
+__device__ __forceinline__ void store_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// the committed stores are complete
+__device__ __forceinline__ void store_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+__device__ __forceinline__ void prefetch_map(const CUtensorMap* map)
+{
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+}  // namespace tma
+}  // namespace ast

@@ -55,6 +55,7 @@ extern "C" {
 #define AST_ST_NONFINITE    0x10u /* a wave speed or state became NaN/Inf              */
 #define AST_ST_VACUUM       0x20u /* exact solver met the vacuum pattern               */
 #define AST_ST_MLP_FALLBACK 0x40u /* learned guess rejected, PVRS guess used           */
+#define AST_ST_TIMEOUT      0x80u /* a bulk copy did not arrive within the wait limit  */
 
 /* ---- enumerations ------------------------------------------------------ */
 enum ast_flux   { AST_FLUX_HLL = 0, AST_FLUX_HLLC = 1, AST_FLUX_GODUNOV = 2 };
@@ -125,7 +126,12 @@ typedef struct ast_config {
        always uses 1 (the reference's absolute tolerance is below FP32
        resolution).                                                          */
     int32_t riemann_newton;
-    int32_t reserved_i[6];
+    /* 1: the FP32 solver steps with the persistent kernel (tiles staged and
+       stored by bulk-tensor copies, double-buffered); 0: one CTA per tile.
+       Same results; the FP64 solver and the raw entry points always use one
+       CTA per tile (default 1)                                              */
+    int32_t persistent;
+    int32_t reserved_i[5];
     /* wave strength above which the learned start value is used:
        max(|ln(p_R/p_L)|, |u_R - u_L| / min(c_L, c_R)); weaker faces start
        from the acoustic value, which is already close for them (0.2)        */
