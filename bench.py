@@ -34,6 +34,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_Z, M_R = 4096, 2048   # overridable with --grid for profiling runs
+PERSISTENT = 1          # FP32 kernel: persistent (bulk-tensor staging) or one CTA per tile
 BYTES_PER_CELL = {"fp64": 64, "fp32": 32}   # one read + one write of 4 state values
 
 
@@ -133,6 +134,7 @@ def make_config(form):
     prec = A.PREC_FP64 if form.startswith("fp64") else A.PREC_FP32
     flux = A.FLUX_HLL if form.endswith("_hll") else A.FLUX_GODUNOV
     cfg = problems.blast_config(N_Z, M_R, flux=flux, precision=prec)
+    cfg.persistent = PERSISTENT
     if prec == A.PREC_FP32:
         cfg.riemann_tol = 1e-8
         cfg.guess = A.GUESS_MLP if form == "fp32_learned" else A.GUESS_PVRS
@@ -447,8 +449,10 @@ def main():
     ap.add_argument("--start-step", type=int, default=1000, help="timed window starts at this step of the run")
     ap.add_argument("--accuracy-steps", type=int, default=2000, help="FP32 vs FP64 error after these steps (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=1000, help="steps of the 64-problem batch (0: skip)")
+    ap.add_argument("--per-tile", action="store_true", help="FP32 forms with one CTA per tile, not the persistent kernel")
     args = ap.parse_args()
-    global N_Z, M_R
+    global N_Z, M_R, PERSISTENT
+    PERSISTENT = 0 if args.per_tile else 1
     if args.grid:
         N_Z, M_R = (int(v) for v in args.grid.lower().split("x"))
     ws, rank, local = dist_setup()
@@ -577,6 +581,7 @@ def main():
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
         "config": {"workload": f"blast {N_Z}x{M_R}, exact Godunov + minmod, axisymmetric, CFL 0.4",
                    "form": args.form, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "fp32_kernel": "persistent, bulk-tensor staged" if PERSISTENT else "one CTA per tile",
                    "mlp_params": params_src,
                    "l2": "inputs larger than L2 (state ping-pong 2x%d MB)" % (cells * BYTES_PER_CELL[prec] // 2 // 2**20)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
