@@ -41,6 +41,18 @@ int fail(int code, const char* msg)
     return code;
 }
 
+// density of the state planes q at cells k = m*N + n
+template <typename R>
+__global__ void probe_kernel(const R* __restrict__ q, long long ld, int N, const int64_t* __restrict__ cells, int n,
+                             double* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long k = cells[i];
+    const long long m = k / N, c = k - m * N;
+    out[i] = (double)q[m * ld + c];
+}
+
 __global__ void funk_time_kernel(double* T, double* T_do, double* TT, int* i)
 {
     *T_do = *T;
@@ -106,6 +118,8 @@ struct ast_solver {
     float* rec = nullptr;            // face recorder buffer (device)
     unsigned long long* rec_n = nullptr;
     long long rec_cap = 0;
+    int64_t* probe_buf = nullptr;    // watch cells (device): n indices, then n doubles
+    int probe_cap = 0;
     bool tma = false;                // FP32 persistent kernel
     int tma_grid = 0;                // its CTAs
     CUtensorMap tin[2], tout[2];     // tile-box load and store maps of buf[0], buf[1]
@@ -212,6 +226,7 @@ int ast_destroy(ast_solver* S)
     cudaFree(S->mlp);
     cudaFree(S->rec);
     cudaFree(S->rec_n);
+    cudaFree(S->probe_buf);
     delete S;
     return AST_OK;
 }
@@ -435,6 +450,37 @@ int ast_set_mlp(ast_solver* S, const float* params)
     AST_CUDA(cudaStreamSynchronize(S->stream));
     S->P.mlp = S->mlp;
     drop_graph(S);
+    return AST_OK;
+}
+
+int ast_probe(ast_solver* S, const int64_t* cells, int n, double* rho, double* TT)
+{
+    if (!S || n < 0 || (n > 0 && (!cells || !rho))) return fail(AST_ERR_INVALID, "bad argument");
+    const long long K = (long long)S->cfg.N * S->cfg.M;
+    for (int i = 0; i < n; i++)
+        if (cells[i] < 0 || cells[i] >= K) return fail(AST_ERR_INVALID, "probe cell outside the grid");
+    if (n > S->probe_cap) {
+        cudaFree(S->probe_buf);
+        S->probe_buf = nullptr;
+        S->probe_cap = 0;
+        AST_CUDA(cudaMalloc(&S->probe_buf, (size_t)n * 16));
+        S->probe_cap = n;
+    }
+    if (n > 0) {
+        double* dout = reinterpret_cast<double*>(S->probe_buf + n);
+        AST_CUDA(cudaMemcpyAsync(S->probe_buf, cells, (size_t)n * 8, cudaMemcpyHostToDevice, S->stream));
+        const void* q = S->buf[S->cur];
+        if (S->elem == 8)
+            probe_kernel<double><<<(n + 127) / 128, 128, 0, S->stream>>>((const double*)q, S->ld, S->cfg.N, S->probe_buf,
+                                                                        n, dout);
+        else
+            probe_kernel<float><<<(n + 127) / 128, 128, 0, S->stream>>>((const float*)q, S->ld, S->cfg.N, S->probe_buf,
+                                                                       n, dout);
+        AST_CUDA(cudaGetLastError());
+        AST_CUDA(cudaMemcpyAsync(rho, dout, (size_t)n * 8, cudaMemcpyDeviceToHost, S->stream));
+    }
+    if (TT) AST_CUDA(cudaMemcpyAsync(TT, &S->clock->TT, sizeof(double), cudaMemcpyDeviceToHost, S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
     return AST_OK;
 }
 

@@ -276,4 +276,68 @@ int ast_write_tecplot(const ast_config* c, const double* s, const double* u, int
     return f.good() ? AST_OK : AST_ERR_IO;
 }
 
+int ast_write_tecplot_final(const ast_config* c, const double* s, const double* u, int stride, const char* path)
+{
+    if (!c || !s || !u || !path || stride < 1 || ast_config_check(c) != AST_OK) return AST_ERR_INVALID;
+    std::ofstream f(path);
+    if (!f) return AST_ERR_IO;
+    const int N = c->N, M = c->M;
+    const long long K = (long long)N * M;
+    const double dx = (c->x_max - c->x_min) / (N - 1), dy = c->y_max / M;
+    const int nn = (N + stride - 1) / stride, mm = (M + stride - 1) / stride;
+    f << "TITLE = \"HP\"  VARIABLES = \"X\", \"Y\", \"Ro\", \"P\", \"Vx\", \"Vy\", \"Mach\", \"T\", \"Zav\", ZONE T = "
+         "\"HP\", N = "
+      << nn * mm << " , E = " << (long long)(nn - 1) * (mm - 1) << ", F = FEPOINT, ET = quadrilateral" << std::endl;
+    for (long long k = 0; k < K; k++) {
+        const int n = (int)(k % N), m = (int)(k / N);
+        if ((n % stride != 0) || (m % stride != 0)) continue;
+        double zav = 0.0;
+        if (n > 0 && m > 0 && n < N - 1 && m < M - 1)
+            zav = (u[2 * ((long long)m * N + n + 1) + 1] - u[2 * ((long long)m * N + n - 1) + 1]) / (2 * dx) -
+                  (u[2 * ((long long)(m + 1) * N + n)] - u[2 * ((long long)(m - 1) * N + n)]) / (2 * dy);
+        double mach = 0.0, temp = 0.0;
+        if (s[2 * k] > 0.0) {
+            mach = std::sqrt((u[2 * k] * u[2 * k] + u[2 * k + 1] * u[2 * k + 1]) / (c->gamma * s[2 * k + 1] / s[2 * k]));
+            temp = s[2 * k + 1] / s[2 * k];
+        }
+        f << out_x(c, n) << " " << out_y(c, m) << " " << s[2 * k] << " " << s[2 * k + 1] << " " << u[2 * k] << " "
+          << u[2 * k + 1] << " " << mach << " " << temp << " " << zav << std::endl;
+    }
+    for (long long k = 0; k < (long long)nn * mm; k++) {
+        const long long n = k % nn, m = k / nn;
+        if ((m < mm - 1) && (n < nn - 1))
+            f << m * nn + n + 1 << " " << m * nn + n + 2 << " " << (m + 1) * nn + n + 2 << " " << (m + 1) * nn + n + 1
+              << std::endl;
+    }
+    return f.good() ? AST_OK : AST_ERR_IO;
+}
+
+int ast_write_axis(const ast_config* c, const double* s, const double* u, const char* path)
+{
+    if (!c || !s || !u || !path || ast_config_check(c) != AST_OK) return AST_ERR_INVALID;
+    std::ofstream f(path);
+    if (!f) return AST_ERR_IO;
+    for (int n = 0; n < c->N; n++) {
+        const long long k = n;   // row m = 0
+        double ss = 0.0;
+        if (s[2 * k] > 0) ss = 1.0 / std::sqrt(c->gamma * s[2 * k + 1] / s[2 * k]);
+        f << out_x(c, n) << " " << out_y(c, 0) << " " << s[2 * k] << " " << s[2 * k + 1] << " " << u[2 * k] << " "
+          << u[2 * k + 1] << " " << ss << std::endl;
+    }
+    return f.good() ? AST_OK : AST_ERR_IO;
+}
+
+int ast_write_inform(const ast_config* c, double TT, double mach_inf, double chi, const char* path)
+{
+    if (!c || !path || ast_config_check(c) != AST_OK) return AST_ERR_INVALID;
+    std::ofstream f(path);
+    if (!f) return AST_ERR_IO;
+    const long long K = (long long)c->N * c->M;
+    f << "TT = " << TT << "    N = " << c->N << "   M = " << c->M << "   K = " << K << std::endl;
+    f << "x_min = " << c->x_min << " " << "x_max = " << c->x_max << " " << "y_min = " << c->y_max / (2.0 * c->M) << " "
+      << "y_max = " << c->y_max << std::endl;
+    f << "M_inf = " << mach_inf << " " << "chi_ = " << chi << std::endl;
+    return f.good() ? AST_OK : AST_ERR_IO;
+}
+
 }  // extern "C"

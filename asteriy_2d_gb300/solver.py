@@ -45,6 +45,10 @@ SIGNATURES = {
     "ast_write_bin": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
     "ast_read_bin": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
     "ast_write_tecplot": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_int, C.c_double, C.c_char_p]),
+    "ast_write_tecplot_final": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_int, C.c_char_p]),
+    "ast_write_axis": (C.c_int, [C.POINTER(A.ast_config), _dp, _dp, C.c_char_p]),
+    "ast_write_inform": (C.c_int, [C.POINTER(A.ast_config), C.c_double, C.c_double, C.c_double, C.c_char_p]),
+    "ast_probe": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_int, _dp, _dp]),
     "ast_set_mlp": (C.c_int, [C.c_void_p, _fp]),
     "ast_batch_create": (C.c_int, [C.POINTER(A.ast_config), C.c_int, C.POINTER(C.c_void_p)]),
     "ast_batch_destroy": (C.c_int, [C.c_void_p]),
@@ -201,6 +205,28 @@ def write_tecplot(cfg, s, u, path, stride=2, soltime=0.0):
                                    stride, soltime, os.fsencode(path)), "ast_write_tecplot")
 
 
+def write_tecplot_final(cfg, s, u, path, stride=2):
+    check(load().ast_write_tecplot_final(C.byref(cfg), _dptr(np.ascontiguousarray(s)),
+                                         _dptr(np.ascontiguousarray(u)), stride, os.fsencode(path)),
+          "ast_write_tecplot_final")
+
+
+def write_axis(cfg, s, u, path):
+    check(load().ast_write_axis(C.byref(cfg), _dptr(np.ascontiguousarray(s)), _dptr(np.ascontiguousarray(u)),
+                                os.fsencode(path)), "ast_write_axis")
+
+
+def write_inform(cfg, TT, path, mach_inf=0.0, chi=0.0):
+    check(load().ast_write_inform(C.byref(cfg), TT, mach_inf, chi, os.fsencode(path)), "ast_write_inform")
+
+
+def write_probe_series(path, series):
+    """One watch cell's samples as the reference's "TT rho" lines."""
+    with open(path, "w") as f:
+        for tt, rho in series:
+            f.write("%g %g\n" % (tt, rho))
+
+
 class Solver:
     """One r-z problem resident on the GPU (the ast_solver object)."""
 
@@ -277,6 +303,15 @@ class Solver:
         params = _f32(params)
         assert params.shape == (A.AST_MLP_NPARAM,)
         check(self.lib.ast_set_mlp(self.h, _fptr(params)), "ast_set_mlp")
+
+    def probe(self, cells):
+        """Density at the watch cells (k = m*N + n) and the time TT."""
+        cells = np.ascontiguousarray(cells, dtype=np.int64)
+        rho = np.zeros(len(cells))
+        tt = C.c_double()
+        check(self.lib.ast_probe(self.h, cells.ctypes.data_as(C.POINTER(C.c_int64)), len(cells), _dptr(rho),
+                                 C.byref(tt)), "ast_probe")
+        return rho, tt.value
 
     def record_start(self, capacity, every=1, min_strength=0.0):
         check(self.lib.ast_record_start(self.h, capacity, every, min_strength), "ast_record_start")

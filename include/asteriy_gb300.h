@@ -206,6 +206,12 @@ int ast_device_state(ast_solver* solver, void** planes, int64_t* ld, int* elem_b
    prediction p_L exp(y) and falls back to the acoustic start value when the
    prediction lies outside the pattern's bracket (counted in mlp_fallback). */
 int ast_set_mlp(ast_solver* solver, const float* params);  /* AST_MLP_NPARAM host floats */
+/* Watch cells: the density of the current state at n cells (indices
+   k = m*N + n into the state) and the solver's time TT, the reference's
+   probe kernel funk_my (kernel.cu:1538-1545) that its loop samples every
+   200 steps into "TT rho" series (kernel.cu:3547-3555, 3950-3960).
+   Waits for the solver's stream. */
+int ast_probe(ast_solver* solver, const int64_t* cells, int n, double* rho, double* TT);
 /* Face recorder: on the following steps with step % every == 0, every exact-
    solver face that needs the iterative p* solve and whose wave strength
    max(|ln(p_R/p_L)|, |u_R-u_L|/min(c_L,c_R)) exceeds min_strength (0 keeps
@@ -356,6 +362,18 @@ int ast_read_bin(const ast_config* cfg, double* s, double* u, const char* path);
    X Y Ro P Vx Vy Mach omega (print_file_mini, kernel.cu:3109-3173). */
 int ast_write_tecplot(const ast_config* cfg, const double* s, const double* u,
                       int stride, double soltime, const char* path);
+/* The end-of-run Tecplot file ("_param_for_texplot_mini.txt",
+   kernel.cu:4125-4129, 4156-4215): every stride-th cell, variables
+   X Y Ro P Vx Vy Mach T Zav with T = p/rho and the vorticity
+   Zav = dvr/dz - dvz/dr by central differences (0 on the outer cells). */
+int ast_write_tecplot_final(const ast_config* cfg, const double* s, const double* u, int stride,
+                            const char* path);
+/* The axis line ("_param_y=0.txt", kernel.cu:4151-4164): the cells of the
+   first row, one line each: x y rho p vx vy 1/c (0 where rho <= 0). */
+int ast_write_axis(const ast_config* cfg, const double* s, const double* u, const char* path);
+/* The run summary ("_inform.txt", kernel.cu:4166-4169): time, grid, domain
+   and the problem's Mach number and chi. */
+int ast_write_inform(const ast_config* cfg, double TT, double mach_inf, double chi, const char* path);
 
 #ifdef __cplusplus
 }

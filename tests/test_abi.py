@@ -123,3 +123,51 @@ def test_tecplot_writer(tmp_path):
     assert "SOLUTIONTIME = 0.5, N = 32 , E = 21, F = FEPOINT, ET = quadrilateral" in lines[0]
     assert len(lines) == 1 + 32 + 21
     assert lines[-1] == "23 24 32 31"
+
+
+def test_tecplot_final_writer(tmp_path):
+    c = problems.blast_config(16, 8)
+    rng = np.random.default_rng(3)
+    s = 0.5 + rng.random((128, 2))
+    u = rng.random((128, 2)) - 0.5
+    p = str(tmp_path / "final.dat")
+    solver.write_tecplot_final(c, s, u, p, stride=2)
+    lines = open(p).read().splitlines()
+    assert lines[0] == ('TITLE = "HP"  VARIABLES = "X", "Y", "Ro", "P", "Vx", "Vy", "Mach", "T", "Zav", '
+                        'ZONE T = "HP", N = 32 , E = 21, F = FEPOINT, ET = quadrilateral')
+    assert len(lines) == 1 + 32 + 21
+    rows = np.array([[float(v) for v in ln.split()] for ln in lines[1:33]])
+    # cell (n, m) = (2, 2): the sixth sampled cell of the second sampled row
+    n, m, N = 2, 2, 16
+    k = m * N + n
+    dx, dy = 2.0 / 15, 1.0 / 8
+    zav = (u[k + 1, 1] - u[k - 1, 1]) / (2 * dx) - (u[k + N, 0] - u[k - N, 0]) / (2 * dy)
+    mach = np.sqrt((u[k, 0] ** 2 + u[k, 1] ** 2) / (c.gamma * s[k, 1] / s[k, 0]))
+    r = rows[1 * 8 + 1]
+    expect = [-1.0 + n * dx, 1.0 / 16 + m * dy, s[k, 0], s[k, 1], u[k, 0], u[k, 1], mach, s[k, 1] / s[k, 0], zav]
+    assert np.allclose(r, expect, rtol=1e-5, atol=1e-6), (r, expect)
+    assert rows[0, 8] == 0.0      # outer cell: no vorticity
+
+
+def test_axis_and_inform_writers(tmp_path):
+    c = problems.blast_config(16, 8)
+    s, u = solver.fill_blast(c)
+    p = str(tmp_path / "axis.txt")
+    solver.write_axis(c, s, u, p)
+    rows = np.loadtxt(p)
+    assert rows.shape == (16, 7)
+    assert np.allclose(rows[:, 0], -1.0 + np.arange(16) * 2.0 / 15, atol=1e-6)
+    assert np.allclose(rows[:, 1], 1.0 / 16)
+    assert np.allclose(rows[:, 6], 1.0 / np.sqrt(c.gamma * s[:16, 1] / s[:16, 0]), rtol=1e-5)
+    q = str(tmp_path / "inform.txt")
+    solver.write_inform(c, 0.25, q, mach_inf=2.0, chi=0.5)
+    lines = open(q).read().splitlines()
+    assert lines == ["TT = 0.25    N = 16   M = 8   K = 128",
+                     "x_min = -1 x_max = 1 y_min = 0.0625 y_max = 1",
+                     "M_inf = 2 chi_ = 0.5"]
+
+
+def test_probe_series_file(tmp_path):
+    p = str(tmp_path / "1_inStable.txt")
+    solver.write_probe_series(p, [(0.125, 1.5), (0.25, 2.0)])
+    assert open(p).read() == "0.125 1.5\n0.25 2\n"

@@ -242,3 +242,19 @@ def test_fp32_form_error_against_fp64_oracle(flux):
     l1_p = np.sum(np.abs(s[:, 1] - os_[:, 1])) / np.sum(np.abs(os_[:, 1]))
     assert l1_rho < 1e-4 and l1_p < 1e-4, (l1_rho, l1_p)
     assert step == ost and abs(tt - ott) < 1e-4 * ott
+
+
+@pytest.mark.parametrize("precision", [A.PREC_FP64, A.PREC_FP32])
+def test_probe_matches_state(precision):
+    cfg = problems.blast_config(64, 32, precision=precision)
+    s0, u0 = solver.fill_blast(cfg)
+    with solver.Solver(cfg) as S:
+        S.set_state(s0, u0)
+        S.step(30)
+        cells = [0, 5, 64 * 10 + 7, 64 * 32 - 1]
+        rho, tt = S.probe(cells)
+        s, _ = S.get_state()
+        assert np.array_equal(rho, s[cells, 0])
+        assert tt == S.clock()[1]
+        with pytest.raises(solver.AstError):
+            S.probe([64 * 32])
