@@ -34,7 +34,7 @@ GEOM_PLANAR, GEOM_AXISYM = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 GUESS_PVRS, GUESS_MLP = 0, 1
 Z_LO, Z_HI, R_LO, R_HI = 0, 1, 2, 3
-BC_REFLECT, BC_OUTFLOW, BC_FIXED, BC_SUCTION = 0, 1, 2, 3
+BC_REFLECT, BC_OUTFLOW, BC_FIXED, BC_SUCTION, BC_NONREFLECT = 0, 1, 2, 3, 4
 SETUP_BLAST, SETUP_WIND = 0, 1
 AST_BATCH_MAX = 4096
 
@@ -62,7 +62,8 @@ class ast_config(C.Structure):
         ("riemann_tol", C.c_double),
         ("collect_stats", C.c_int32), ("riemann_newton", C.c_int32), ("persistent", C.c_int32),
         ("reserved_i", C.c_int32 * 5),
-        ("mlp_gate", C.c_double), ("reserved_d", C.c_double * 7),
+        ("mlp_gate", C.c_double), ("inflow_p", C.c_double), ("inflow_v", C.c_double),
+        ("reserved_d", C.c_double * 5),
     ]
 
     def copy(self):
@@ -119,6 +120,7 @@ def default_config():
     c.collect_stats = 0
     c.persistent = 1
     c.mlp_gate = 0.2
+    c.inflow_p, c.inflow_v = 0.0, 1.0
     return c
 
 

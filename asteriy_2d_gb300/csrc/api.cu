@@ -334,6 +334,15 @@ static int enqueue_one(ast_solver* S)
     else
         rc = (S->elem == 8) ? launch_step_r<double, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true)
                             : launch_step_r<float, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true);
+    if (rc == AST_OK && S->cfg.inflow_p > 0.0) {
+        const int nb = (S->cfg.M + 127) / 128;
+        if (S->elem == 8)
+            inflow_kernel<double, kSoA><<<nb, 128, 0, S->stream>>>(P, S->cfg.inflow_p, S->cfg.inflow_v);
+        else
+            inflow_kernel<float, kSoA><<<nb, 128, 0, S->stream>>>(P, S->cfg.inflow_p, S->cfg.inflow_v);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_fail(e, "inflow kernel launch");
+    }
     if (rc == AST_OK) S->cur ^= 1;
     return rc;
 }
@@ -562,6 +571,24 @@ int ast_step_raw(const double* s, const double* u, double* s2, double* u2, doubl
     rc = launch_step_r<double, kAoS>(P, cfg->flux, cfg->recon, (cudaStream_t)stream, false);
     if (rc != AST_OK) return rc;
     return launch_step_r<double, kAoS>(P, cfg->flux, cfg->recon, (cudaStream_t)stream, true);
+}
+
+int ast_inflow_raw(const double* s, const double* u, double* s2, double* u2, const ast_config* cfg, void* stream)
+{
+    if (!s || !u || !s2 || !u2 || !cfg) return fail(AST_ERR_INVALID, "null argument");
+    int rc = ast_config_check(cfg);
+    if (rc != AST_OK) return rc;
+    if (!(cfg->inflow_p > 0.0)) return fail(AST_ERR_INVALID, "inflow_p must be positive");
+    StepParams P;
+    fill_step_params(P, *cfg);
+    P.in = s;
+    P.in_u = u;
+    P.out = s2;
+    P.out_u = u2;
+    inflow_kernel<double, kAoS><<<(cfg->M + 127) / 128, 128, 0, (cudaStream_t)stream>>>(P, cfg->inflow_p,
+                                                                                       cfg->inflow_v);
+    AST_CUDA(cudaGetLastError());
+    return AST_OK;
 }
 
 int ast_funk_time(double* T, double* T_do, double* TT, int* i, void* stream)

@@ -56,6 +56,7 @@ void ast_config_default(ast_config* c)
     c->p_floor = 0.000001;              // kernel.cu:3072
     c->riemann_tol = 10e-10;            // Header.h:62
     c->mlp_gate = 0.2;
+    c->inflow_v = 1.0;
     c->persistent = 1;
 }
 
@@ -72,8 +73,9 @@ int ast_config_check(const ast_config* c)
     if (c->precision < AST_PREC_FP64 || c->precision > AST_PREC_FP32) return AST_ERR_INVALID;
     if (c->guess < AST_GUESS_PVRS || c->guess > AST_GUESS_MLP) return AST_ERR_INVALID;
     if (c->persistent < 0 || c->persistent > 1) return AST_ERR_INVALID;
+    if (!(c->inflow_p >= 0.0)) return AST_ERR_INVALID;
     for (int s = 0; s < 4; s++) {
-        if (c->bc[s].kind < AST_BC_REFLECT || c->bc[s].kind > AST_BC_SUCTION) return AST_ERR_INVALID;
+        if (c->bc[s].kind < AST_BC_REFLECT || c->bc[s].kind > AST_BC_NONREFLECT) return AST_ERR_INVALID;
         if (c->bc[s].kind == AST_BC_FIXED && !(c->bc[s].rho > 0.0 && c->bc[s].p > 0.0)) return AST_ERR_INVALID;
     }
     if (c->fixed_region && !(c->fixed_az > 0.0 && c->fixed_ar > 0.0)) return AST_ERR_INVALID;

@@ -89,6 +89,29 @@ struct __align__(16) StepParams {
     double rec_gate;               // record faces with wave strength above this
 };
 
+// the gas constants of the arithmetic R
+template <typename R>
+__device__ __forceinline__ const Gas<R>& gas_of(const StepParams& P)
+{
+    return *reinterpret_cast<const Gas<R>*>(sizeof(R) == 8 ? (const void*)&P.gd : (const void*)&P.gf);
+}
+
+// the NONREFLECT ghost state from the boundary cell's state v (rho, p, vz,
+// vr): carried along the outgoing characteristic (the rule the reference
+// leaves commented in add2, kernel.cu:1979-1985, written there for the z_hi
+// side; w is the velocity along the side's outward normal)
+template <typename R>
+__device__ __forceinline__ void ghost_nonreflect(const Gas<R>& g, bool zside, bool low, R v[4])
+{
+    R& vn = zside ? v[2] : v[3];
+    const R w = low ? -vn : vn;
+    const R cc = sqrt(g.ga * v[1] / v[0]);
+    const R cg = g.g1 / g.g2 * (w + R(2) / g.g1 * cc);
+    v[0] = v[0] * pow(cg / cc, R(2) / g.g1);
+    v[1] = v[0] * cg * cg / g.ga;
+    vn = low ? -cg : cg;
+}
+
 // ------------------------------------------------------------------ loads
 template <typename R, int LAYOUT>
 __device__ __forceinline__ void read_cell(const StepParams& P, int n, int m, R v[4])
@@ -138,13 +161,15 @@ __device__ __forceinline__ void fetch_cell(const StepParams& P, int n, int m, R 
     } else if (kind == 2) {     // FIXED
         v[0] = (R)P.bc_val[side][0]; v[1] = (R)P.bc_val[side][1];
         v[2] = (R)P.bc_val[side][2]; v[3] = (R)P.bc_val[side][3];
-    } else {                    // OUTFLOW, SUCTION
+    } else {                    // OUTFLOW, SUCTION, NONREFLECT
         read_cell<R, LAYOUT>(P, bn, bm, v);
         if (kind == 3) {
             R lim = (R)(zside ? P.bc_val[side][2] : P.bc_val[side][3]);
             R& vn = zside ? v[2] : v[3];
             if (low) { if (vn > lim) vn = lim; }
             else     { if (vn < lim) vn = lim; }
+        } else if (kind == 4) {
+            ghost_nonreflect(gas_of<R>(P), zside, low, v);
         }
     }
 }
@@ -689,7 +714,7 @@ __device__ __forceinline__ void patch_tile(const StepParams& P, S& sm, int b, in
         } else if (kind == 2) {     // FIXED
             v[0] = (R)P.bc_val[side][0]; v[1] = (R)P.bc_val[side][1];
             v[2] = (R)P.bc_val[side][2]; v[3] = (R)P.bc_val[side][3];
-        } else {                    // OUTFLOW, SUCTION, deeper ghost layers
+        } else {                    // OUTFLOW, SUCTION, NONREFLECT, deeper ghost layers
             const int si = bn - n0 + 2 + QX, sj = bm - m0 + 2;
             v[0] = q[0][sj][si]; v[1] = q[1][sj][si]; v[2] = q[2][sj][si]; v[3] = q[3][sj][si];
             if (kind == 3) {
@@ -697,6 +722,8 @@ __device__ __forceinline__ void patch_tile(const StepParams& P, S& sm, int b, in
                 R& vn = zside ? v[2] : v[3];
                 if (low) { if (vn > lim) vn = lim; }
                 else     { if (vn < lim) vn = lim; }
+            } else if (kind == 4) {
+                ghost_nonreflect(gas_of<R>(P), zside, low, v);
             }
         }
         q[0][j][i + QX] = v[0]; q[1][j][i + QX] = v[1]; q[2][j][i + QX] = v[2]; q[3][j][i + QX] = v[3];
@@ -1045,6 +1072,46 @@ __global__ void __launch_bounds__(kThreads, 4)
     }
     if (tid == 0) tma::store_wait_all();
     cta_epilogue<R>(P, acc, gridDim.x, true);
+}
+
+// Characteristic inflow at z_lo after a step (add2_bound, kernel.cu:1895-
+// 1925): one thread per row m; from the old state of cell (0, m) (P.in)
+// and the new state of cell (1, m) (P.out), cell (0, m) of P.out becomes
+// rho = pp/(gamma-1)/T0, p = p_in, (v_z, v_r) = (v_in, 0), with
+// T0 = p_in/(gamma-1) and pp = p'(1) - rho(0) c(0) (v_z'(1) - v_in).
+template <typename R, int LAYOUT>
+__global__ void inflow_kernel(StepParams P, double p_in, double v_in)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= P.M) return;
+    const Gas<R>& g = gas_of<R>(P);
+    R r0, p0, p1, u1;
+    if (LAYOUT == kSoA) {
+        const R* q = (const R*)P.in;
+        const R* o = (const R*)P.out;
+        const long long k = (long long)m * P.ld;
+        r0 = q[k]; p0 = q[k + P.plane];
+        p1 = o[k + 1 + P.plane]; u1 = o[k + 1 + 2 * P.plane];
+    } else {
+        const long long k = (long long)m * P.N;
+        const double2 s0 = ((const double2*)P.in)[k];
+        r0 = (R)s0.x; p0 = (R)s0.y;
+        p1 = (R)((const double2*)P.out)[k + 1].y;
+        u1 = (R)((const double2*)P.out_u)[k + 1].x;
+    }
+    const R cc = sqrt(g.ga * p0 / r0);
+    const R T0 = (R)p_in / g.g1 / R(1);
+    const R pp = p1 - r0 * cc * (u1 - (R)v_in);
+    const R rho = pp / g.g1 / T0;
+    if (LAYOUT == kSoA) {
+        R* o = (R*)P.out;
+        const long long k = (long long)m * P.ld;
+        o[k] = rho; o[k + P.plane] = (R)p_in; o[k + 2 * P.plane] = (R)v_in; o[k + 3 * P.plane] = R(0);
+    } else {
+        const long long k = (long long)m * P.N;
+        ((double2*)P.out)[k] = make_double2((double)rho, p_in);
+        ((double2*)P.out_u)[k] = make_double2(v_in, 0.0);
+    }
 }
 
 }  // namespace ast

@@ -37,6 +37,8 @@ SIGNATURES = {
     "ast_step_raw": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_int, C.POINTER(A.ast_config), C.c_void_p]),
     "ast_funk_time": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ast_inflow_raw": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(A.ast_config),
+                                 C.c_void_p]),
     "ast_step_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.POINTER(A.ast_config), C.c_void_p]),
     "ast_fill_blast": (C.c_int, [C.POINTER(A.ast_config), C.c_double, C.c_double, C.c_double, _dp, _dp]),
@@ -337,6 +339,12 @@ def step_raw(s, u, s2, u2, T, T_do, TT, cfg, method=1, stream=None):
     check(load().ast_step_raw(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), C.c_void_p(T),
                               C.c_void_p(T_do), C.c_void_p(TT), method, C.byref(cfg),
                               C.c_void_p(stream) if stream else None), "ast_step_raw")
+
+
+def inflow_raw(s, u, s2, u2, cfg, stream=None):
+    """ast_inflow_raw on device pointers (ints), the add2_bound drop-in."""
+    check(load().ast_inflow_raw(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), C.byref(cfg),
+                                C.c_void_p(stream) if stream else None), "ast_inflow_raw")
 
 
 def funk_time(T, T_do, TT, i, stream=None):

@@ -75,9 +75,16 @@ enum ast_side   { AST_Z_LO = 0, AST_Z_HI = 1, AST_R_LO = 2, AST_R_HI = 3 };
  *   SUCTION  ghost j = b0 with the normal velocity limited: on a low side
  *            v_n = min(v_n, limit), on a high side v_n = max(v_n, limit),
  *            limit = the side's vz (z sides) or vr (r sides)
- *            (add_MK, kernel.cu:2340-2354).
+ *            (add_MK, kernel.cu:2340-2354);
+ *   NONREFLECT ghost j = b0 carried along the outgoing characteristic, the
+ *            rule the reference leaves commented in add2 for its z_hi side
+ *            (kernel.cu:1979-1985): with c = sqrt(gamma p/rho) and w the
+ *            velocity along the outward normal, c_g = (gamma-1)/(gamma+1)
+ *            (w + 2c/(gamma-1)), ghost w = c_g, rho = rho (c_g/c)^(2/(gamma-1)),
+ *            p = rho_g c_g^2/gamma, tangential velocity kept.
  */
-enum ast_bc_kind { AST_BC_REFLECT = 0, AST_BC_OUTFLOW = 1, AST_BC_FIXED = 2, AST_BC_SUCTION = 3 };
+enum ast_bc_kind { AST_BC_REFLECT = 0, AST_BC_OUTFLOW = 1, AST_BC_FIXED = 2, AST_BC_SUCTION = 3,
+                   AST_BC_NONREFLECT = 4 };
 
 typedef struct ast_bc {
     int32_t kind;
@@ -136,7 +143,15 @@ typedef struct ast_config {
        max(|ln(p_R/p_L)|, |u_R - u_L| / min(c_L, c_R)); weaker faces start
        from the acoustic value, which is already close for them (0.2)        */
     double  mlp_gate;
-    double  reserved_d[7];
+    /* characteristic inflow at z_lo after every step (add2_bound,
+       kernel.cu:1895-1925; p_H = inflow_p, inflow speed inflow_v): cell
+       column n = 0 becomes rho = pp/(gamma-1)/T0, p = inflow_p,
+       (v_z, v_r) = (inflow_v, 0), with T0 = inflow_p/(gamma-1) and
+       pp = p'(1) - rho(0) c(0) (v_z'(1) - inflow_v), primes the new state of
+       column 1, unprimed the old state of column 0.  0 disables (default);
+       the reference's values are 7 and 1.                                  */
+    double  inflow_p, inflow_v;
+    double  reserved_d[5];
 } ast_config;
 
 typedef struct ast_stats {
@@ -245,6 +260,13 @@ int ast_mlp_train(const float* samples, int64_t n, int epochs, int batch, float 
 int ast_step_raw(const double* s, const double* u, double* s2, double* u2,
                  double* T, const double* T_do, const double* TT, int method,
                  const ast_config* cfg, void* cuda_stream);
+/* Replacement for add2_bound<<<K/256,256>>>(s, u, s2, u2, ...)
+   (kernel.cu:1895-1925, launched after the step at kernel.cu:3565, 3590):
+   column n = 0 of (s2, u2) from the old state (s, u) and the new column 1,
+   as described at ast_config.inflow_p (which must be positive; the
+   reference's p_H is 7, its inflow speed 1).  Device pointers. */
+int ast_inflow_raw(const double* s, const double* u, double* s2, double* u2, const ast_config* cfg,
+                   void* cuda_stream);
 /* Replacement for funk_time<<<1,1>>>(T, T_do, TT, i) (kernel.cu:1525-1536):
    T_do = T; TT += T_do; T = 1e7; i += 1.  Device pointers. */
 int ast_funk_time(double* T, double* T_do, double* TT, int* i, void* cuda_stream);

@@ -24,6 +24,10 @@
  *   planar update .................. kernel.cu:3027-3073
  *   axisymmetric update ............ kernel.cu:2480-2509
  *   dt (exact min, lagged) ......... kernel.cu:3013-3017, funk_time :1525-1536
+ *   characteristic inflow .......... add2_bound kernel.cu:1895-1925
+ *   non-reflecting ghost ........... the commented rule of add2, kernel.cu:1979-1985
+ *                                    (restated from the comment: the reference
+ *                                    compiles no code for it, so it is not pinned)
  *
  * Differences from the reference, all deliberate:
  *   - gamma, CFL, grid, boundaries, flux and tolerances are runtime values;
@@ -554,6 +558,19 @@ static void ora_get(const ora_grid* g, const ast_config* c, const d2* s, const d
         else     { if (*vn < lim) *vn = lim; }
         break;
     }
+    case AST_BC_NONREFLECT: {
+        /* kernel.cu:1979-1985 (commented there), along the outward normal */
+        *so = s[b0]; *uo = u[b0];
+        double* vn = zside ? &uo->x : &uo->y;
+        double w = low ? -*vn : *vn;
+        double ggg = c->gamma;
+        double cc = sqrt(ggg * so->y / so->x);
+        double cg = (ggg - 1.0) / (ggg + 1.0) * (w + 2.0 / (ggg - 1.0) * cc);
+        so->x = so->x * pow(cg / cc, 2.0 / (ggg - 1.0));
+        so->y = so->x * cg * cg / ggg;
+        *vn = low ? -cg : cg;
+        break;
+    }
     default: /* OUTFLOW */
         *so = s[b0]; *uo = u[b0];
         break;
@@ -830,6 +847,35 @@ double ora_step(const ast_config* c, const double* s, const double* u, double* s
 }
 
 /*
+ * Characteristic inflow at z_lo after a step (add2_bound, kernel.cu:1895-
+ * 1925) with p_H = c->inflow_p and inflow speed c->inflow_v: column 0 of
+ * (s2, u2) from the old column 0 of (s, u) and the new column 1 of (s2, u2).
+ */
+void ora_inflow(const ast_config* c, const double* s, const double* u, double* s2, double* u2)
+{
+    const int N = c->N, M = c->M;
+    const double ggg = c->gamma, p_H = c->inflow_p, v_in = c->inflow_v;
+    const d2* S = (const d2*)s;
+    d2* S2 = (d2*)s2;
+    d2* U2 = (d2*)u2;
+    (void)u;
+    for (int m = 0; m < M; m++) {
+        const int index = m * N + 0;
+        double pp2 = S2[(m)*N + 0 + 1].y;
+        double uu2 = U2[(m)*N + 0 + 1].x;
+        d2 s_do = S[index];
+        double cc = sqrt(ggg * s_do.y / s_do.x);
+        double T0 = p_H / (ggg - 1.0) / 1.0;
+        double pp = pp2 - s_do.x * cc * (uu2 - v_in);
+        double rho = pp / (ggg - 1.0) / T0;
+        S2[index].x = rho;
+        S2[index].y = p_H;
+        U2[index].x = v_in;
+        U2[index].y = 0.0;
+    }
+}
+
+/*
  * nsteps steps in place on (s, u) with the reference's host protocol
  * (kernel.cu:3868-3947 + funk_time): each step uses *T_do, then
  * T_do <- new dt, TT += T_do, step += 1.
@@ -843,6 +889,7 @@ int ora_run(const ast_config* c, double* s, double* u, int nsteps, double* T_do,
     if (!s2 || !u2) { free(s2); free(u2); return -3; }
     for (int i = 0; i < nsteps; i++) {
         double T = ora_step(c, s, u, s2, u2, *T_do, nthreads, counters);
+        if (c->inflow_p > 0.0) ora_inflow(c, s, u, s2, u2);
         *T_do = T;
         *TT = *TT + *T_do;
         *step = *step + 1;

@@ -39,6 +39,7 @@ RANGES = [
     ("kernel.cu", 1399, 1523, "double HLL("),
     ("Gas_Dinamic.cu", 1604, 1826, "double HLLC_2d_Korolkov_b_s("),
     ("kernel.cu", 1525, 1536, "void funk_time("),
+    ("kernel.cu", 1895, 1925, "void add2_bound("),
     ("kernel.cu", 1928, 2291, "void add2("),
     ("kernel.cu", 2293, 2511, "void add_MK("),
     ("kernel.cu", 2513, 3093, "void Kernel_TVD("),

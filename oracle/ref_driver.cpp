@@ -127,6 +127,20 @@ double ref_kernel_step(int kernel, const double* s, const double* u, double* s2,
     return T;
 }
 
+/* One launch of the reference's add2_bound (kernel.cu:1895-1925) over all K
+   cells on (s, u) -> (s2, u2); p_H is the shim's 7. */
+void ref_bound(const double* s, const double* u, double* s2, double* u2)
+{
+    const int Kc = ref_N * ref_M;
+    double T = 10000000, Tdo = 0.0, TTl = 0.0;
+    blockIdx.x = 0;
+    blockDim.x = 1;
+    for (int k = 0; k < Kc; k++) {
+        threadIdx.x = (unsigned int)k;
+        add2_bound((double2*)s, (double2*)u, (double2*)s2, (double2*)u2, &T, &Tdo, &TTl, 1, 0);
+    }
+}
+
 /* nsteps launches with the host protocol of kernel.cu:3868-3947 and
    funk_time (kernel.cu:1525-1536), in place on s, u. */
 int ref_kernel_run(int kernel, double* s, double* u, int nsteps, int method, double* T_do,
