@@ -54,6 +54,8 @@ def lib():
         L.ora_run.restype = C.c_int
         L.ora_run.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _i64p, C.c_int, _i64p]
         L.ora_max_threads.restype = C.c_int
+        L.ora_inflow.restype = None
+        L.ora_inflow.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -83,6 +85,8 @@ def ref():
                                      C.POINTER(C.c_longlong), C.c_int]
         R.ora_run.restype = C.c_int
         R.ora_run.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _i64p, C.c_int, _i64p]
+        R.ref_bound.restype = None
+        R.ref_bound.argtypes = [_dp, _dp, _dp, _dp]
         R.ref_diag_count.restype = C.c_longlong
         R.ref_max_threads.restype = C.c_int
         _ref = R
@@ -161,6 +165,27 @@ def ref_run(kernel, cfg, s, u, nsteps, method=0, nthreads=1):
     ref().ref_kernel_run(kernel, _ptr(s), _ptr(u), nsteps, method, C.byref(tdo), C.byref(tt),
                          C.byref(st), nthreads)
     return s, u, tdo.value, tt.value, st.value
+
+
+def inflow(cfg, s, u, s2, u2):
+    """The oracle's characteristic inflow (add2_bound restated): column 0 of
+    copies of (s2, u2) from the old (s, u) and the new column 1."""
+    s2 = np.array(s2, dtype=np.float64, order="C")
+    u2 = np.array(u2, dtype=np.float64, order="C")
+    lib().ora_inflow(C.byref(cfg), _ptr(np.ascontiguousarray(s, dtype=np.float64)),
+                     _ptr(np.ascontiguousarray(u, dtype=np.float64)), _ptr(s2), _ptr(u2))
+    return s2, u2
+
+
+def ref_bound(cfg, s, u, s2, u2):
+    """The reference's own add2_bound (p_H = 7, inflow speed 1) on copies of
+    (s2, u2)."""
+    ref_set(cfg)
+    s2 = np.array(s2, dtype=np.float64, order="C")
+    u2 = np.array(u2, dtype=np.float64, order="C")
+    ref().ref_bound(_ptr(np.ascontiguousarray(s, dtype=np.float64)), _ptr(np.ascontiguousarray(u, dtype=np.float64)),
+                    _ptr(s2), _ptr(u2))
+    return s2, u2
 
 
 def ref_run_composed(cfg, s, u, nsteps, nthreads=1):

@@ -55,3 +55,11 @@ def random_state(K, rng):
     s = np.stack([rng.uniform(0.5, 2.0, K), rng.uniform(2.0, 10.0, K)], 1)
     u = np.stack([rng.uniform(-1.0, 2.0, K), rng.uniform(-0.5, 0.5, K)], 1)
     return s, u
+
+
+def inflow_config(N=24, M=8):
+    """add2_bound (kernel.cu:1895-1925): p_H = 7 (Header.h:6), inflow speed 1."""
+    c = A.default_config()
+    c.N, c.M = N, M
+    c.inflow_p, c.inflow_v = 7.0, 1.0
+    return c

@@ -13,7 +13,9 @@ records their outputs on seeded inputs:
                  96x12 grid with a random state;
   step_mk_hll.npz, step_mk_god.npz
                  20 launches of add_MK (kernel.cu:2293), method 0 (HLL) and
-                 method 2 (exact Godunov), on a 48x24 axisymmetric grid.
+                 method 2 (exact Godunov), on a 48x24 axisymmetric grid;
+  inflow.npz     one launch of add2_bound (kernel.cu:1895-1925, p_H = 7,
+                 inflow speed 1) on a random old and new state, 24x8.
 
 The configurations that reproduce those kernels live in golden_configs.py so
 the tests use exactly the same ones.  Usage:  python tests/golden/make_golden.py
@@ -84,6 +86,15 @@ def make_step(fname, cfg, kernel, method, nsteps, rng):
                         steps=st, nsteps=nsteps)
 
 
+def make_inflow(rng):
+    cfg = G.inflow_config()
+    K = cfg.N * cfg.M
+    s, u = G.random_state(K, rng)
+    s2, u2 = G.random_state(K, rng)
+    b2, c2 = O.ref_bound(cfg, s, u, s2, u2)
+    np.savez_compressed(os.path.join(HERE, "inflow.npz"), s=s, u=u, s2=s2, u2=u2, s2_out=b2, u2_out=c2)
+
+
 def main():
     make_ref.main([])
     rng = np.random.default_rng(20261203)
@@ -91,6 +102,7 @@ def main():
     make_step("step_tvd.npz", G.tvd_config(), O.REF_KERNEL_TVD, 1, 20, rng)
     make_step("step_mk_hll.npz", G.add_mk_config(0), O.REF_ADD_MK, 0, 20, rng)
     make_step("step_mk_god.npz", G.add_mk_config(2), O.REF_ADD_MK, 2, 20, rng)
+    make_inflow(np.random.default_rng(1895))
     print("golden vectors written to", HERE)
 
 

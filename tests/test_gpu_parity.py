@@ -258,3 +258,46 @@ def test_probe_matches_state(precision):
         assert tt == S.clock()[1]
         with pytest.raises(solver.AstError):
             S.probe([64 * 32])
+
+
+def test_characteristic_inflow_matches_oracle():
+    """Kernel_TVD's problem with add2_bound after every step (p_H = 7,
+    inflow speed 1): the solver against the oracle's step + inflow."""
+    d = golden("step_tvd.npz")
+    cfg = G.tvd_config()
+    cfg.inflow_p, cfg.inflow_v = 7.0, 1.0
+    s, u, os_, ou = assert_parity(cfg, d["s0"], d["u0"], 40)
+    assert np.all(os_[0::cfg.N, 1] == 7.0) and np.all(s[0::cfg.N, 1] == 7.0)
+    c32 = cfg.copy()
+    c32.precision = A.PREC_FP32
+    s32, *_ = run_gpu(c32, d["s0"], d["u0"], 40)
+    assert np.max(np.abs(s32 - os_)) / np.max(np.abs(os_)) < 1e-4
+
+
+def test_inflow_raw_drop_in_matches_oracle():
+    import torch
+    z = golden("inflow.npz")
+    cfg = G.inflow_config()
+    dev = torch.device("cuda:0")
+    t = {k: torch.tensor(z[k], device=dev) for k in ("s", "u", "s2", "u2")}
+    solver.inflow_raw(t["s"].data_ptr(), t["u"].data_ptr(), t["s2"].data_ptr(), t["u2"].data_ptr(), cfg)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(t["s2"].cpu().numpy(), z["s2_out"])
+    np.testing.assert_array_equal(t["u2"].cpu().numpy(), z["u2_out"])
+
+
+@pytest.mark.parametrize("flux", [A.FLUX_HLL, A.FLUX_GODUNOV])
+def test_nonreflecting_sides_match_oracle(flux):
+    cfg = problems.blast_config(128, 64, flux=flux)
+    A.set_bc(cfg, A.Z_LO, A.BC_NONREFLECT)
+    A.set_bc(cfg, A.Z_HI, A.BC_NONREFLECT)
+    A.set_bc(cfg, A.R_HI, A.BC_NONREFLECT)
+    s0, u0 = solver.fill_blast(cfg, radius=0.7)
+    tol = TOL_GODUNOV if flux == A.FLUX_GODUNOV else TOL
+    assert_parity(cfg, s0, u0, 100, tol=tol)
+    c32 = cfg.copy()
+    c32.precision = A.PREC_FP32
+    for persistent in (0, 1):
+        c32.persistent = persistent
+        s32, *_ = run_gpu(c32, s0, u0, 100)
+        assert np.all(np.isfinite(s32))

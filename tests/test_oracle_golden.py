@@ -97,3 +97,18 @@ def test_composed_step_with_reference_faces_is_bitwise(flux):
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
     assert a[2] == b[2]
+
+
+def test_inflow_bitwise_against_reference_add2_bound():
+    """The oracle's characteristic inflow equals the reference's add2_bound
+    (kernel.cu:1895-1925) on the recorded random old/new states."""
+    z = golden("inflow.npz")
+    cfg = G.inflow_config()
+    s2, u2 = O.inflow(cfg, z["s"], z["u"], z["s2"], z["u2"])
+    assert np.array_equal(s2, z["s2_out"]) and np.array_equal(u2, z["u2_out"])
+    # only column 0 changes
+    changed = np.any(z["s2_out"] != z["s2"], axis=1).reshape(cfg.M, cfg.N)
+    assert changed[:, 0].all() and not changed[:, 1:].any()
+    if O.have_ref():
+        b2, c2 = O.ref_bound(cfg, z["s"], z["u"], z["s2"], z["u2"])
+        assert np.array_equal(b2, s2) and np.array_equal(c2, u2)
