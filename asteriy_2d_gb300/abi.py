@@ -28,7 +28,7 @@ AST_ST_TIMEOUT = 0x80
 AST_MLP_NPARAM = 1325
 AST_RECORD_FLOATS = 10
 
-FLUX_HLL, FLUX_HLLC, FLUX_GODUNOV = 0, 1, 2
+FLUX_HLL, FLUX_HLLC, FLUX_GODUNOV, FLUX_HLLC_A = 0, 1, 2, 3
 RECON_NONE, RECON_MINMOD = 0, 1
 GEOM_PLANAR, GEOM_AXISYM = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1

@@ -69,10 +69,12 @@ int launch_step_r(const StepParams& P, int flux, int recon, cudaStream_t st, boo
     if (recon) {
         if (flux == AST_FLUX_HLL) return launch_step_t<R, 0, true, LAYOUT>(P, st, launch);
         if (flux == AST_FLUX_HLLC) return launch_step_t<R, 1, true, LAYOUT>(P, st, launch);
+        if (flux == AST_FLUX_HLLC_A) return launch_step_t<R, 3, true, LAYOUT>(P, st, launch);
         return launch_step_t<R, 2, true, LAYOUT>(P, st, launch);
     }
     if (flux == AST_FLUX_HLL) return launch_step_t<R, 0, false, LAYOUT>(P, st, launch);
     if (flux == AST_FLUX_HLLC) return launch_step_t<R, 1, false, LAYOUT>(P, st, launch);
+    if (flux == AST_FLUX_HLLC_A) return launch_step_t<R, 3, false, LAYOUT>(P, st, launch);
     return launch_step_t<R, 2, false, LAYOUT>(P, st, launch);
 }
 
@@ -104,10 +106,13 @@ int launch_batch_r(const StepParams* Ps, const int* tile_start, int nprob, int t
     if (recon) {
         if (flux == AST_FLUX_HLL) return launch_batch_t<R, 0, true, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
         if (flux == AST_FLUX_HLLC) return launch_batch_t<R, 1, true, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
+        if (flux == AST_FLUX_HLLC_A)
+            return launch_batch_t<R, 3, true, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
         return launch_batch_t<R, 2, true, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
     }
     if (flux == AST_FLUX_HLL) return launch_batch_t<R, 0, false, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
     if (flux == AST_FLUX_HLLC) return launch_batch_t<R, 1, false, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
+    if (flux == AST_FLUX_HLLC_A) return launch_batch_t<R, 3, false, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
     return launch_batch_t<R, 2, false, TZ, TR>(Ps, tile_start, nprob, tiles, st, launch);
 }
 

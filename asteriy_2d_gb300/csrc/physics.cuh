@@ -118,6 +118,58 @@ __device__ __forceinline__ R flux_hll(const Gas<R>& g, R rL, R pL, R unL, R utL,
     return S;
 }
 
+// ------------------------------------------------------------------ HLLC (Aleksashov)
+// The reference's second HLLC (HLLC_Aleksashov, kernel.cu:767-1079), an MHD
+// HLLC solver it calls with zero magnetic field.  In the face frame (normal
+// velocity un, tangential ut): fast speed sqrt(c c) (the B = 0 value of its
+// fast-magnetosonic speed), Davis-type bounds, the contact speed SM and the
+// star states with each side's own tangential velocity; the magnetic terms
+// only add zeros.  The tangential flux is odd in ut, so one face-frame
+// evaluation serves z faces (tangent +v_r) and r faces (the reference's
+// tangent there is -v_z, its flux rotated back by the same sign).
+template <typename R>
+__device__ __forceinline__ R flux_hllc_a(const Gas<R>& g, R r1, R p1, R un1, R ut1, R r2, R p2, R un2, R ut2,
+                                         R F[4])
+{
+    const R cL = sqrt(g.ga * p1 / r1), cR = sqrt(g.ga * p2 / r2);
+    const R cfL = sqrt(cL * cL), cfR = sqrt(cR * cR);
+    const R SL = fmin(un1 - cfL, un2 - cfR);
+    const R SR = fmax(un1 + cfL, un2 + cfR);
+    const R suR = SR - un2, suL = SL - un1;
+    const R SM = (suR * r2 * un2 - p2 + p1 - suL * r1 * un1) / (suR * r2 - suL * r1);
+    const R UU = fmax(fabs(SL), fabs(SR));
+    const R e1 = p1 / g.g1 + r1 * ((un1 * un1 + ut1 * ut1) / R(2));
+    const R e2 = p2 / g.g1 + r2 * ((un2 * un2 + ut2 * ut2) / R(2));
+    // the reference's order of the four cases (SM can fall outside [SL, SR]
+    // by rounding)
+    if (SL > R(0)) {
+        F[0] = r1 * un1; F[1] = r1 * un1 * un1 + p1; F[2] = r1 * un1 * ut1; F[3] = (e1 + p1) * un1;
+    } else if (SM >= R(0)) {
+        // left star state
+        const R suLm = suL / (SL - SM), rz = r1 * suLm;
+        const R ptz = ((p2 + r2 * suR * (SM - un2)) + (p1 + r1 * suL * (SM - un1))) / R(2);
+        const R ez = e1 * suLm + (ptz * SM - p1 * un1) / (SL - SM);
+        F[0] = r1 * un1 + SL * (rz - r1);
+        F[1] = (r1 * un1 * un1 + p1) + SL * (SM * rz - r1 * un1);
+        F[2] = r1 * un1 * ut1 + SL * (ut1 * rz - r1 * ut1);
+        F[3] = (e1 + p1) * un1 + SL * (ez - e1);
+    } else if (SR >= R(0)) {
+        // right star state
+        const R suRm = suR / (SR - SM), rz = r2 * suRm;
+        const R ptz = ((p2 + r2 * suR * (SM - un2)) + (p1 + r1 * suL * (SM - un1))) / R(2);
+        const R ez = e2 * suRm + (ptz * SM - p2 * un2) / (SR - SM);
+        F[0] = r2 * un2 + SR * (rz - r2);
+        F[1] = (r2 * un2 * un2 + p2) + SR * (SM * rz - r2 * un2);
+        F[2] = r2 * un2 * ut2 + SR * (ut2 * rz - r2 * ut2);
+        F[3] = (e2 + p2) * un2 + SR * (ez - e2);
+    } else if (SR < R(0)) {
+        F[0] = r2 * un2; F[1] = r2 * un2 * un2 + p2; F[2] = r2 * un2 * ut2; F[3] = (e2 + p2) * un2;
+    } else {
+        F[0] = F[1] = F[2] = F[3] = R(NAN);
+    }
+    return UU;
+}
+
 // ------------------------------------------------------------------ HLLC
 template <typename R>
 __device__ __forceinline__ R flux_hllc(const Gas<R>& g, R rL, R pL, R u1, R v1, R rR, R pR, R u2, R v2, R F[4])

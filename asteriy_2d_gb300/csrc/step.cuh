@@ -471,6 +471,9 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
         } else if constexpr (FLUX == 1) {
             if (hi) Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
             else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+        } else if constexpr (FLUX == 3) {
+            if (hi) Sp = flux_hllc_a(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+            else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         } else {
             Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         }
@@ -1079,6 +1082,15 @@ __global__ void __launch_bounds__(kThreads, 4)
 // and the new state of cell (1, m) (P.out), cell (0, m) of P.out becomes
 // rho = pp/(gamma-1)/T0, p = p_in, (v_z, v_r) = (v_in, 0), with
 // T0 = p_in/(gamma-1) and pp = p'(1) - rho(0) c(0) (v_z'(1) - v_in).
+// separately rounded multiply / subtract / divide (no contraction into an
+// FMA), for the few operations per row of the inflow rule
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+
 template <typename R, int LAYOUT>
 __global__ void inflow_kernel(StepParams P, double p_in, double v_in)
 {
@@ -1099,10 +1111,10 @@ __global__ void inflow_kernel(StepParams P, double p_in, double v_in)
         p1 = (R)((const double2*)P.out)[k + 1].y;
         u1 = (R)((const double2*)P.out_u)[k + 1].x;
     }
-    const R cc = sqrt(g.ga * p0 / r0);
-    const R T0 = (R)p_in / g.g1 / R(1);
-    const R pp = p1 - r0 * cc * (u1 - (R)v_in);
-    const R rho = pp / g.g1 / T0;
+    const R cc = sqrt(div_rn(mul_rn(g.ga, p0), r0));
+    const R T0 = div_rn(div_rn((R)p_in, g.g1), R(1));
+    const R pp = sub_rn(p1, mul_rn(mul_rn(r0, cc), sub_rn(u1, (R)v_in)));
+    const R rho = div_rn(div_rn(pp, g.g1), T0);
     if (LAYOUT == kSoA) {
         R* o = (R*)P.out;
         const long long k = (long long)m * P.ld;

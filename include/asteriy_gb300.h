@@ -58,7 +58,10 @@ extern "C" {
 #define AST_ST_TIMEOUT      0x80u /* a bulk copy did not arrive within the wait limit  */
 
 /* ---- enumerations ------------------------------------------------------ */
-enum ast_flux   { AST_FLUX_HLL = 0, AST_FLUX_HLLC = 1, AST_FLUX_GODUNOV = 2 };
+/* HLLC is the Korolkov solver (HLLC_2d_Korolkov, Gas_Dinamic.cu:1814);
+   HLLC_A the reference's second HLLC (HLLC_Aleksashov, kernel.cu:767), an
+   MHD formulation it calls with zero magnetic field (add_MK method 1). */
+enum ast_flux   { AST_FLUX_HLL = 0, AST_FLUX_HLLC = 1, AST_FLUX_GODUNOV = 2, AST_FLUX_HLLC_A = 3 };
 enum ast_recon  { AST_RECON_NONE = 0, AST_RECON_MINMOD = 1 };
 enum ast_geom   { AST_GEOM_PLANAR = 0, AST_GEOM_AXISYM = 1 };
 enum ast_prec   { AST_PREC_FP64 = 0, AST_PREC_FP32 = 1 };

@@ -16,6 +16,7 @@
  *   minmod / linear / linear2 ...... kernel.cu:22-50, sign Gas_Dinamic.cu:858-872
  *   HLL ............................ kernel.cu:1399-1523
  *   HLLC (Korolkov, metod 2, W=0) .. Gas_Dinamic.cu:1604-1826
+ *   HLLC (Aleksashov, B = 0) ....... kernel.cu:767-1079
  *   exact Godunov .................. kernel.cu:128-570, newton :635-680,
  *                                    devtwo :682-749, lev :751-765
  *   stencil + ghost rules .......... kernel.cu:2549-2698 (Kernel_TVD),
@@ -480,6 +481,67 @@ static double godunov(const ora_phys* ph, ora_stats* st, d2 Ls, d2 Lu, d2 Rs, d2
 /* exported face functions (for the pinning tests)                           */
 /* in: sL=(rho,p) uL=(vz,vr) sR uR; out[4] = (mass, mom_z, mom_r, energy)    */
 /* ------------------------------------------------------------------------ */
+/* ------------------------------------------------------------------------ */
+/* HLLC_Aleksashov (kernel.cu:767-1079): an MHD HLLC solver that the        */
+/* reference calls with zero magnetic field.  With B = 0 its frame is the   */
+/* normal n, the third axis and t = (-n_y, n_x) (the branch d <= eps of its */
+/* frame construction; d = 1), the fast speed is sqrt(c c), the tangential  */
+/* star velocities are the side's own, and the magnetic terms add zeros,    */
+/* which are left out here (adding +0 to a nonzero sum changes nothing).    */
+/* ------------------------------------------------------------------------ */
+static double hllc_a(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double n1, double n2,
+                     d2* Ps, d2* Pu, double rad)
+{
+    const double ga = ph->ga, g1 = ph->g1, wv = 0.0;
+    const double r1 = Ls.x, p1 = Ls.y, u1 = Lu.x, v1 = Lu.y;
+    const double r2 = Rs.x, p2 = Rs.y, u2 = Ru.x, v2 = Ru.y;
+    /* frame: columns a0 = n, a1 = (0, 0, 1), a2 = (-n_y, n_x, 0) */
+    const double a02 = (0.0 * 0.0 - 1.0 * n2), a12 = (1.0 * n1 - 0.0 * 0.0);
+    const double vL0 = n1 * u1 + n2 * v1, vR0 = n1 * u2 + n2 * v2;
+    const double vL2 = a02 * u1 + a12 * v1, vR2 = a02 * u2 + a12 * v2;
+    const double cL = sqrt(ga * p1 / r1), cR = sqrt(ga * p2 / r2);
+    const double cfL = sqrt(cL * cL), cfR = sqrt(cR * cR);
+    const double SL = fmin(vL0 - cfL, vR0 - cfR);
+    const double SR = fmax(vL0 + cfL, vR0 + cfR);
+    const double suR = SR - vR0, suL = SL - vL0;
+    const double SM = (suR * r2 * vR0 - p2 + p1 - suL * r1 * vL0) / (suR * r2 - suL * r1);
+    const double UU = fmax(fabs(SL), fabs(SR));
+    const double time = ph->krit * rad / UU;
+    const double upt1 = (u1 * u1 + v1 * v1) / 2.0, upt2 = (u2 * u2 + v2 * v2) / 2.0;
+    const double e1 = p1 / g1 + r1 * upt1, e2 = p2 / g1 + r2 * upt2;
+    /* side fluxes and conserved states: mass, normal / tangential momentum, energy */
+    const double FL[4] = {r1 * vL0, r1 * vL0 * vL0 + p1, r1 * vL0 * vL2, (e1 + p1) * vL0};
+    const double FR[4] = {r2 * vR0, r2 * vR0 * vR0 + p2, r2 * vR0 * vR2, (e2 + p2) * vR0};
+    const double UL[4] = {r1, r1 * vL0, r1 * vL2, e1};
+    const double UR[4] = {r2, r2 * vR0, r2 * vR2, e2};
+    const double suRm = suR / (SR - SM), suLm = suL / (SL - SM);
+    const double rzR = r2 * suRm, rzL = r1 * suLm;
+    const double ptzR = p2 + r2 * suR * (SM - vR0);
+    const double ptzL = p1 + r1 * suL * (SM - vL0);
+    const double ptz = (ptzR + ptzL) / 2.0;
+    const double ezR = e2 * suRm + (ptz * SM - p2 * vR0) / (SR - SM);
+    const double ezL = e1 * suLm + (ptz * SM - p1 * vL0) / (SL - SM);
+    const double UZL[4] = {rzL, SM * rzL, vL2 * rzL, ezL};
+    const double UZR[4] = {rzR, SM * rzR, vR2 * rzR, ezR};
+    double q[4];
+    if (SL > wv) {
+        for (int k = 0; k < 4; k++) q[k] = FL[k] - wv * UL[k];
+    } else if ((SL <= wv) && (SM >= wv)) {
+        for (int k = 0; k < 4; k++) q[k] = FL[k] + SL * (UZL[k] - UL[k]) - wv * UZL[k];
+    } else if ((SM <= wv) && (SR >= wv)) {
+        for (int k = 0; k < 4; k++) q[k] = FR[k] + SR * (UZR[k] - UR[k]) - wv * UZR[k];
+    } else if (SR < wv) {
+        for (int k = 0; k < 4; k++) q[k] = FR[k] - wv * UR[k];
+    } else {
+        for (int k = 0; k < 4; k++) q[k] = NAN;
+    }
+    Ps->x = q[0];
+    Ps->y = q[3];
+    Pu->x = n1 * q[1] + a02 * q[2];
+    Pu->y = n2 * q[1] + a12 * q[2];
+    return time;
+}
+
 static void pack_out(d2 Ps, d2 Pu, double* out)
 {
     out[0] = Ps.x; out[1] = Pu.x; out[2] = Pu.y; out[3] = Ps.y;
@@ -498,6 +560,7 @@ double ora_face(int flux, double gamma, double krit, double tol, int max_iter,
     double t;
     if (flux == AST_FLUX_HLL) t = hll(&ph, Ls, Lu, Rs, Ru, n1, n2, &Ps, &Pu, rad);
     else if (flux == AST_FLUX_HLLC) t = hllc(&ph, Ls, Lu, Rs, Ru, n1, n2, &Ps, &Pu, rad, 0);
+    else if (flux == AST_FLUX_HLLC_A) t = hllc_a(&ph, Ls, Lu, Rs, Ru, n1, n2, &Ps, &Pu, rad);
     else t = godunov(&ph, &st, Ls, Lu, Rs, Ru, n1, n2, &Ps, &Pu, rad);
     pack_out(Ps, Pu, out);
     if (counters) {
@@ -597,6 +660,7 @@ static double ora_flux(int flux, const ora_phys* ph, ora_stats* st, d2 Ls, d2 Lu
     return t;
 #endif
     if (flux == AST_FLUX_HLLC) return hllc(ph, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad, 0);
+    if (flux == AST_FLUX_HLLC_A) return hllc_a(ph, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
     if (flux == AST_FLUX_GODUNOV) return godunov(ph, st, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
     return hll(ph, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
 }

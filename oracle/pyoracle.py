@@ -95,7 +95,7 @@ def ref():
 
 # ---------------------------------------------------------------- oracle
 
-FACE_HLL, FACE_HLLC, FACE_GODUNOV = 0, 1, 2
+FACE_HLL, FACE_HLLC, FACE_GODUNOV, FACE_HLLC_A = 0, 1, 2, 3
 
 
 def face(flux, sL, uL, sR, uR, n1, n2, rad, gamma=5.0 / 3.0, cfl=0.05, tol=10e-10, max_iter=200):

@@ -34,14 +34,15 @@ def tvd_config(N=96, M=12):
 
 def add_mk_config(method, N=48, M=24):
     """add_MK (kernel.cu:2293-2511) on z in [-1,1], r in [0,1]: first order,
-    method 0 = HLL, 2 = exact Godunov (hx, hy of Header.h:29-30 select no HLL
+    method 0 = HLL, 1 = HLLC_Aleksashov, 2 = exact Godunov (hx, hy of
+    Header.h:29-30 select no HLL
     face), axisymmetric source, free stream (1, 1) (V_inf, 0) at n=N-1,
     suction clamp v_z <= V_inf/2 at n=0, zero gradient at r=y_max, axis
     reflection, cells inside z^2/0.04 + r^2/0.04 < 1 held fixed."""
     c = A.default_config()
     c.N, c.M = N, M
     c.x_min, c.x_max, c.y_max = -1.0, 1.0, 1.0
-    c.flux = A.FLUX_HLL if method == 0 else A.FLUX_GODUNOV
+    c.flux = {0: A.FLUX_HLL, 1: A.FLUX_HLLC_A, 2: A.FLUX_GODUNOV}[method]
     c.recon, c.geom = A.RECON_NONE, A.GEOM_AXISYM
     A.set_bc(c, A.Z_HI, A.BC_FIXED, 1.0, 1.0, V_INF, 0.0)
     A.set_bc(c, A.Z_LO, A.BC_SUCTION, 0.0, 0.0, 0.5 * V_INF, 0.0)

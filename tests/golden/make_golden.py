@@ -4,16 +4,17 @@ Runs only where the reference sources exist: it builds oracle/_ref/libastref.so
 (oracle/make_ref.py, the reference's functions compiled for the host) and
 records their outputs on seeded inputs:
 
-  faces.npz      HLL, HLLC and exact-Godunov fluxes + dt on 1024 random
+  faces.npz      HLL, HLLC, HLLC_Aleksashov and exact-Godunov fluxes + dt on 1024 random
                  states and on hand-picked states that reach every wave
                  pattern of the exact solver (two shocks, shock-rarefaction,
                  two rarefactions, vacuum) and the uniform-state case of the
                  reference's `test` kernel (kernel.cu:3095-3107);
   step_tvd.npz   20 launches of Kernel_TVD (kernel.cu:2513) + funk_time on a
                  96x12 grid with a random state;
-  step_mk_hll.npz, step_mk_god.npz
-                 20 launches of add_MK (kernel.cu:2293), method 0 (HLL) and
-                 method 2 (exact Godunov), on a 48x24 axisymmetric grid;
+  step_mk_hll.npz, step_mk_hllca.npz, step_mk_god.npz
+                 20 launches of add_MK (kernel.cu:2293), method 0 (HLL),
+                 method 1 (HLLC_Aleksashov) and method 2 (exact Godunov), on
+                 a 48x24 axisymmetric grid;
   inflow.npz     one launch of add2_bound (kernel.cu:1895-1925, p_H = 7,
                  inflow speed 1) on a random old and new state, 24x8.
 
@@ -67,7 +68,7 @@ def make_faces(rng):
     n[-8:] = (1.0, 0.0)
     rad = np.where(n[:, 0] != 0, 0.01, 0.02)
     out = {}
-    for name, which in (("hll", 0), ("hllc", 1), ("godunov", 2)):
+    for name, which in (("hll", 0), ("hllc", 1), ("godunov", 2), ("hllca", 3)):
         F = np.zeros((len(X), 4))
         T = np.zeros(len(X))
         for i, row in enumerate(X):
@@ -102,6 +103,7 @@ def main():
     make_step("step_tvd.npz", G.tvd_config(), O.REF_KERNEL_TVD, 1, 20, rng)
     make_step("step_mk_hll.npz", G.add_mk_config(0), O.REF_ADD_MK, 0, 20, rng)
     make_step("step_mk_god.npz", G.add_mk_config(2), O.REF_ADD_MK, 2, 20, rng)
+    make_step("step_mk_hllca.npz", G.add_mk_config(1), O.REF_ADD_MK, 1, 20, rng)
     make_inflow(np.random.default_rng(1895))
     print("golden vectors written to", HERE)
 

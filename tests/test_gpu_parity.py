@@ -118,6 +118,7 @@ def test_wind_counterflow_hllc_fixed_sphere():
     ("step_tvd.npz", G.tvd_config()),
     ("step_mk_hll.npz", G.add_mk_config(0)),
     ("step_mk_god.npz", G.add_mk_config(2)),
+    ("step_mk_hllca.npz", G.add_mk_config(1)),
 ])
 def test_reference_kernel_fixtures(fname, cfg):
     """Kernel_TVD and add_MK outputs recorded from the reference itself."""
@@ -301,3 +302,22 @@ def test_nonreflecting_sides_match_oracle(flux):
         c32.persistent = persistent
         s32, *_ = run_gpu(c32, s0, u0, 100)
         assert np.all(np.isfinite(s32))
+
+
+@pytest.mark.parametrize("precision", [A.PREC_FP64, A.PREC_FP32])
+def test_hllc_aleksashov_blast(precision):
+    """The second HLLC with minmod on the small blast: FP64 at the parity
+    bar, FP32 (persistent and per-tile kernels) within the FP32 form's
+    error of the oracle."""
+    cfg = problems.blast_config(256, 128, flux=A.FLUX_HLLC_A, precision=precision)
+    s0, u0 = solver.fill_blast(cfg)
+    if precision == A.PREC_FP64:
+        s, u, os_, ou = assert_parity(cfg, s0, u0, 100)
+        assert_same_shock_cells(s, os_, cfg)
+        return
+    os_, *_ = O.run(cfg, s0, u0, 100, nthreads=NT)
+    for persistent in (1, 0):
+        cfg.persistent = persistent
+        s, *_ = run_gpu(cfg, s0, u0, 100)
+        l1 = np.sum(np.abs(s[:, 0] - os_[:, 0])) / np.sum(np.abs(os_[:, 0]))
+        assert l1 < 1e-5, (persistent, l1)

@@ -11,7 +11,7 @@ from conftest import golden
 
 
 @pytest.mark.parametrize("name,flux", [("hll", O.FACE_HLL), ("hllc", O.FACE_HLLC),
-                                       ("godunov", O.FACE_GODUNOV)])
+                                       ("godunov", O.FACE_GODUNOV), ("hllca", O.FACE_HLLC_A)])
 def test_face_functions_bitwise(name, flux):
     d = golden("faces.npz")
     X, n, rad = d["states"], d["normals"], d["rad"]
@@ -52,6 +52,7 @@ def test_uniform_state_flux_is_physical_flux():
     ("step_tvd.npz", G.tvd_config()),
     ("step_mk_hll.npz", G.add_mk_config(0)),
     ("step_mk_god.npz", G.add_mk_config(2)),
+    ("step_mk_hllca.npz", G.add_mk_config(1)),
 ])
 def test_steps_bitwise_against_reference_kernels(fname, cfg):
     d = golden(fname)
