@@ -24,6 +24,21 @@ constexpr int kOffShift = 0, kOffScale = 6, kOffW1 = 12, kOffB1 = 204, kOffW2 = 
               kOffB3 = 1324, kMlpParams = 1325;
 static_assert(kMlpParams == AST_MLP_NPARAM, "parameter block size");
 
+// The vectors of the block the tensor-core inference reads from shared
+// memory (its W1 and W2 become mma fragments): shift, scale, b1, b2, w3, b3
+constexpr int kVShift = 0, kVScale = 6, kVB1 = 12, kVB2 = 44, kVW3 = 76, kVB3 = 108, kVLen = 112;
+
+// entry i of that compact vector block, from the parameter block W
+__device__ __forceinline__ float mlp_vec(const float* W, int i)
+{
+    if (i < kVScale) return W[kOffShift + i];
+    if (i < kVB1) return W[kOffScale + i - kVScale];
+    if (i < kVB2) return W[kOffB1 + i - kVB1];
+    if (i < kVW3) return W[kOffB2 + i - kVB2];
+    if (i < kVB3) return W[kOffW3 + i - kVW3];
+    return (i == kVB3) ? W[kOffB3] : 0.0f;
+}
+
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
 // d silu / dz
 __device__ __forceinline__ float silu_grad(float z)
@@ -136,8 +151,9 @@ __device__ __forceinline__ void pack_weights(const float* W, unsigned* B1, unsig
 }
 
 // y for 16 faces whose standardised features sit in X[16][8] (f32, cols 6-7
-// zero); result for face r in y[r] (written by the lanes with t == 0)
-__device__ __forceinline__ void forward16(const float* W, const unsigned* B1, const unsigned* B2, const float (*X)[8],
+// zero); result for face r in y[r] (written by the lanes with t == 0).  V:
+// the compact vector block (kV* offsets)
+__device__ __forceinline__ void forward16(const float* V, const unsigned* B1, const unsigned* B2, const float (*X)[8],
                                           float* y)
 {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -147,7 +163,7 @@ __device__ __forceinline__ void forward16(const float* W, const unsigned* B1, co
     float c1[4][4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        const float b0 = W[kOffB1 + 8 * j + 2 * t], b1 = W[kOffB1 + 8 * j + 2 * t + 1];
+        const float b0 = V[kVB1 + 8 * j + 2 * t], b1 = V[kVB1 + 8 * j + 2 * t + 1];
         c1[j][0] = b0; c1[j][1] = b1; c1[j][2] = b0; c1[j][3] = b1;
         mma16816(c1[j], a0, a1, 0u, 0u, B1[(j * 32 + lane) * 2], B1[(j * 32 + lane) * 2 + 1]);
     }
@@ -161,14 +177,14 @@ __device__ __forceinline__ void forward16(const float* W, const unsigned* B1, co
     float yg = 0.0f, yg8 = 0.0f;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        const float b0 = W[kOffB2 + 8 * j + 2 * t], b1 = W[kOffB2 + 8 * j + 2 * t + 1];
+        const float b0 = V[kVB2 + 8 * j + 2 * t], b1 = V[kVB2 + 8 * j + 2 * t + 1];
         float c[4] = {b0, b1, b0, b1};
 #pragma unroll
         for (int kb = 0; kb < 2; kb++) {
             const int idx = ((kb * 4 + j) * 32 + lane) * 2;
             mma16816(c, h[2 * kb][0], h[2 * kb][1], h[2 * kb + 1][0], h[2 * kb + 1][1], B2[idx], B2[idx + 1]);
         }
-        const float w0 = W[kOffW3 + 8 * j + 2 * t], w1 = W[kOffW3 + 8 * j + 2 * t + 1];
+        const float w0 = V[kVW3 + 8 * j + 2 * t], w1 = V[kVW3 + 8 * j + 2 * t + 1];
         unsigned s0 = silu_h2(c[0], c[1]), s1 = silu_h2(c[2], c[3]);
         const float2 v0 = __half22float2(*reinterpret_cast<__half2*>(&s0));
         const float2 v1 = __half22float2(*reinterpret_cast<__half2*>(&s1));
@@ -180,8 +196,8 @@ __device__ __forceinline__ void forward16(const float* W, const unsigned* B1, co
     yg8 += __shfl_xor_sync(0xffffffffu, yg8, 1);
     yg8 += __shfl_xor_sync(0xffffffffu, yg8, 2);
     if (t == 0) {
-        y[g] = yg + W[kOffB3];
-        y[g + 8] = yg8 + W[kOffB3];
+        y[g] = yg + V[kVB3];
+        y[g + 8] = yg8 + V[kVB3];
     }
 }
 

@@ -354,13 +354,12 @@ namespace {
 __global__ void mlp_forward_tc_kernel(const float* __restrict__ W_g, const float* __restrict__ x, long long n,
                                       int stride, float* __restrict__ y)
 {
-    __shared__ float W[kMlpParams];
+    __shared__ float V[kVLen];
     __shared__ unsigned B1[tc::kL1], B2[tc::kL2];
     __shared__ float X[4][16][8];
     __shared__ float Y[4][16];
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) W[i] = W_g[i];
-    __syncthreads();
-    tc::pack_weights(W, B1, B2);
+    for (int i = threadIdx.x; i < kVLen; i += blockDim.x) V[i] = mlp_vec(W_g, i);
+    tc::pack_weights(W_g, B1, B2);
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const long long t0 = ((long long)blockIdx.x * 4 + w) * 16;
@@ -368,13 +367,13 @@ __global__ void mlp_forward_tc_kernel(const float* __restrict__ W_g, const float
         const long long k = t0 + lane;
         for (int i = 0; i < kMlpIn; i++) {
             const float v = (k < n) ? mlp_map(i, x[k * stride + i]) : 0.0f;
-            X[w][lane][i] = fminf(fmaxf((v - W[kOffShift + i]) * W[kOffScale + i], -30.0f), 30.0f);
+            X[w][lane][i] = fminf(fmaxf((v - V[kVShift + i]) * V[kVScale + i], -30.0f), 30.0f);
         }
         X[w][lane][6] = 0.0f;
         X[w][lane][7] = 0.0f;
     }
     __syncwarp();
-    tc::forward16(W, B1, B2, X[w], Y[w]);
+    tc::forward16(V, B1, B2, X[w], Y[w]);
     __syncwarp();
     if (lane < 16 && t0 + lane < n) y[t0 + lane] = Y[w][lane];
 }

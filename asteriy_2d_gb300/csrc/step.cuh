@@ -207,34 +207,58 @@ struct TileCore {
     unsigned qn;                 // queued faces: above the gate (low 16 bits), others (high 16 bits)
 };
 
-// the exact solver's part: queued faces as codes (face index | active << 12
-// | pattern << 14; faces above the learned-start gate fill the queue from
-// the front, the others from the back, so the two kinds sit in separate
-// warps), the start-value network and its tensor-core operands
+// the exact solver's queue: faces as 16-bit codes (face index | active <<
+// 12 | pattern << 14); faces above the learned-start gate fill it from the
+// front, the others from the back, so the two kinds sit in separate warps
 template <typename R, int TZ, int TR>
 struct QueueSmem {
     static constexpr int kCap = TR * (TZ + 1) + (TR + 1) * TZ;
-    int qcode[kCap];
-    float mlp[kMlpParams];       // learned start value (guess == MLP)
-    unsigned mB1[tc::kL1];       // its W1, W2 as per-lane f16 mma fragments
-    unsigned mB2[tc::kL2];
-    float mX[kThreads / 32][16][8];  // per warp: standardised features of 16 faces
-    float mY[kThreads / 32][16];     // per warp: network outputs
-    R qp0[kCap];                 // start value of each queued face
+    static_assert(kCap <= 4096, "face index fits 12 bits");
+    unsigned short qcode[kCap];
 };
 template <int K>
 struct Empty {};
 
-// the output tile of the TMA kernel: the updated cells, four dense planes
+// the start-value network in the queue phase: its vector block, W1 and W2
+// as per-lane f16 mma fragments, and per warp the standardised features
+// and outputs of 16 faces
+struct NetSmem {
+    float v[kVLen];
+    unsigned B1[tc::kL1];
+    unsigned B2[tc::kL2];
+    float X[kThreads / 32][16][8];
+    float Y[kThreads / 32][16];
+};
+
+// the output tile of the TMA kernel (the updated cells, four dense planes)
+// and the network's space: the network is used in the queue phase, before
+// the update writes the output tile, and the previous tile's store has
+// read the output tile before the next tile's faces start, so the two share
+// memory
+template <typename R, int TZ, int TR, bool OUT, bool NET>
+struct OutNet;
 template <typename R, int TZ, int TR>
-struct OutSmem {
+struct OutNet<R, TZ, TR, false, false> {};
+template <typename R, int TZ, int TR>
+struct OutNet<R, TZ, TR, true, false> {
     alignas(128) R out[4][TR][TZ];
+};
+template <typename R, int TZ, int TR>
+struct OutNet<R, TZ, TR, false, true> {
+    NetSmem net;
+};
+template <typename R, int TZ, int TR>
+struct OutNet<R, TZ, TR, true, true> {
+    union {
+        alignas(128) R out[4][TR][TZ];
+        NetSmem net;
+    };
 };
 
 template <typename R, int FLUX, int TZ, int TR, int NB = 1>
 struct TileSmem : TileCore<R, TZ, TR, NB>,
                   std::conditional_t<FLUX == 2, QueueSmem<R, TZ, TR>, Empty<0>>,
-                  std::conditional_t<(NB > 1), OutSmem<R, TZ, TR>, Empty<1>> {
+                  OutNet<R, TZ, TR, (NB > 1), FLUX == 2> {
 };
 
 // dynamic shared memory of a kernel: the tile plus 128 bytes to align it
@@ -461,7 +485,7 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
                 const bool strong = P.riemann_newton && wave_strength(q) > P.mlp_gate;
                 const unsigned old = atomicAdd(&sm.qn, strong ? 1u : 0x10000u);
                 const int slot = strong ? (int)(old & 0xffffu) : S::kQueueCap - 1 - (int)(old >> 16);
-                sm.qcode[slot] = (ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.pattern << 14);
+                sm.qcode[slot] = (unsigned short)((ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.pattern << 14));
                 return;
             }
             Sp = godunov_sample(g, q, R(0), F, rc);
@@ -542,15 +566,16 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, co
     if (P.riemann_newton && P.guess == 1 && P.mlp != nullptr && ns > 0) {
         // phase 1: learned start values of the faces above the gate (queue
         // slots 0..ns-1), 16 per warp tile on the tensor cores.  Only tiles
-        // with such faces stage the network.
-        for (int i = threadIdx.x; i < kMlpParams; i += kThreads) sm.mlp[i] = P.mlp[i];
-        __syncthreads();
-        tc::pack_weights(sm.mlp, sm.mB1, sm.mB2);
+        // with such faces stage the network.  A face's start value waits in
+        // its own flux slot (written with the flux in phase 2).
+        for (int i = threadIdx.x; i < kVLen; i += kThreads) sm.net.v[i] = mlp_vec(P.mlp, i);
+        tc::pack_weights(P.mlp, sm.net.B1, sm.net.B2);
         __syncthreads();
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         for (int t0 = 16 * w; t0 < ns; t0 += 16 * (kThreads / 32)) {
             const int i = t0 + (lane & 15);
             R pL = R(1);
+            R* p0_slot = nullptr;
             if (lane < 16) {
                 float x[kMlpIn] = {0, 0, 0, 0, 0, 0};
                 if (i < ns) {
@@ -563,19 +588,21 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, co
                     face_sides(q, rL, pL, uL, cL, rR, pR, uR, cR);
                     mlp_features((float)g.ga, (float)rL, (float)pL, (float)uL, (float)cL, (float)rR, (float)pR,
                                  (float)uR, (float)cR, x);
+                    p0_slot = zf ? &sm.Fz[0][a][c] : &sm.Fr[0][a][c];
                 }
                 // standardised, and clamped to a range f16 holds exactly enough
 #pragma unroll
                 for (int k = 0; k < kMlpIn; k++)
-                    sm.mX[w][lane][k] =
-                        fminf(fmaxf((mlp_map(k, x[k]) - sm.mlp[kOffShift + k]) * sm.mlp[kOffScale + k], -30.0f), 30.0f);
-                sm.mX[w][lane][6] = 0.0f;
-                sm.mX[w][lane][7] = 0.0f;
+                    sm.net.X[w][lane][k] =
+                        fminf(fmaxf((mlp_map(k, x[k]) - sm.net.v[kVShift + k]) * sm.net.v[kVScale + k], -30.0f),
+                              30.0f);
+                sm.net.X[w][lane][6] = 0.0f;
+                sm.net.X[w][lane][7] = 0.0f;
             }
             __syncwarp();
-            tc::forward16(sm.mlp, sm.mB1, sm.mB2, sm.mX[w], sm.mY[w]);
+            tc::forward16(sm.net.v, sm.net.B1, sm.net.B2, sm.net.X[w], sm.net.Y[w]);
             __syncwarp();
-            if (lane < 16 && i < ns) sm.qp0[i] = pL * (R)__expf(sm.mY[w][lane]);
+            if (p0_slot) *p0_slot = pL * (R)__expf(sm.net.Y[w][lane]);
             __syncwarp();
         }
         __syncthreads();
@@ -590,7 +617,9 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, co
         int a, c;
         bool zf;
         const RPre<R> q = queued_face<R, RECON, TZ, TR>(P, sm, b, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
-        const R p = solve_queued(P, g, q, strong, (strong && P.guess == 1 && P.mlp) ? sm.qp0[i] : R(0), rc, fallback);
+        // a gated face's learned start value, left in its flux slot by phase 1
+        const R p0 = (strong && P.guess == 1 && P.mlp) ? (zf ? sm.Fz[0][a][c] : sm.Fr[0][a][c]) : R(0);
+        const R p = solve_queued(P, g, q, strong, p0, rc, fallback);
         R F[4];
         R Sp = godunov_sample(g, q, p, F, rc);
         if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
