@@ -72,9 +72,11 @@ struct RiemannCount {
 template <typename R>
 __device__ __forceinline__ R minmod_d(R a, R b)
 {
-    // (sign a + sign b)/2 * min(|a|, |b|): zero unless both have one sign
-    R m = fmin(fabs(a), fabs(b));
-    return (a > R(0) && b > R(0)) ? m : ((a < R(0) && b < R(0)) ? -m : R(0));
+    // (sign a + sign b)/2 * min(|a|, |b|): zero unless both have one sign,
+    // as sign(a) max(0, min(|a|, sign(a) b)) (the same value; a zero result
+    // may differ in the sign of zero only)
+    const R s = copysign(R(1), a);
+    return s * fmax(R(0), fmin(fabs(a), s * b));
 }
 
 // left / right face values of a cell from its three-point stencil; the

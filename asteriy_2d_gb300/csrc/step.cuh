@@ -437,7 +437,7 @@ __device__ __forceinline__ void face_states(const StepParams& P, const S& sm, in
 // and 3 go to the queue instead.
 template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF, typename S>
 __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0, int step,
-                                         RiemannCount& rc, int& fallback, R& smax, int f)
+                                         bool interior, RiemannCount& rc, int& fallback, R& smax, int f)
 {
     constexpr int NFZ = TR * (TZ + 1);
     constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
@@ -448,15 +448,19 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
         // smem indices of the lower (l) and upper (u) cell of the face
         const int jl = ZF ? a + 2 : a + 1, il = ZF ? c + 1 : c + 2;
         const int ju = a + 2, iu = c + 2;
-        const int nl = n0 + il - 2, ml = m0 + jl - 2, nu = n0 + iu - 2, mu = m0 + ju - 2;
-        const bool lval = nl >= 0 && nl < P.N && ml >= 0 && ml < P.M;
-        const bool uval = nu >= 0 && nu < P.N && mu >= 0 && mu < P.M;
+        // both cells inside the grid (always so in an interior tile)
+        bool lval = true, uval = true;
+        if (!interior) {
+            const int nl = n0 + il - 2, ml = m0 + jl - 2, nu = n0 + iu - 2, mu = m0 + ju - 2;
+            lval = nl >= 0 && nl < P.N && ml >= 0 && ml < P.M;
+            uval = nu >= 0 && nu < P.N && mu >= 0 && mu < P.M;
+        }
         bool active = lval || uval;
         if (active && P.fixed_region) active = (lval && !sm.fx[jl][il]) || (uval && !sm.fx[ju][iu]);
         bool hi = true;
         if (P.region_select) {
             // the face's z position as the reference's lower cell sees it
-            const double xl = P.x_min + nl * P.dx;
+            const double xl = P.x_min + (n0 + il - 2) * P.dx;
             const double xf = ZF ? xl + P.dx / 2.0 : xl;
             hi = (xf > P.region_lo && xf < P.region_hi);
         }
@@ -521,11 +525,13 @@ __device__ __forceinline__ void face_pass(const StepParams& P, S& sm, int b, con
 {
     constexpr int NFZ = TR * (TZ + 1), NFR = (TR + 1) * TZ;
     constexpr int NFZP = (NFZ + 31) / 32 * 32;
+    // every cell the tile's faces touch lies inside the grid
+    const bool interior = n0 >= 1 && n0 + TZ < P.N && m0 >= 1 && m0 + TR < P.M;
     for (int t = threadIdx.x; t < NFZP + NFR; t += kThreads) {
         if (t < NFZ)
-            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, rc, fallback, smz, t);
+            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz, t);
         else if (t >= NFZP)
-            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, rc, fallback, smr, t - NFZP);
+            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smr, t - NFZP);
     }
 }
 
