@@ -71,12 +71,10 @@ int ast::cuda_fail(cudaError_t e, const char* what)
 
 int ast::set_error(int code, const char* msg) { return fail(code, msg); }
 
-namespace {
-
 // the four FP32 state planes of one time level as a 3-D tensor (x = z
 // cells, y = rows, z = planes) with a TMA box of `bx` x `by` x 4
-int encode_planes(CUtensorMap* map, void* base, const ast_config& c, long long ld, long long plane, unsigned bx,
-                  unsigned by)
+int ast::encode_planes(CUtensorMap* map, void* base, const ast_config& c, long long ld, long long plane, unsigned bx,
+                       unsigned by)
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
@@ -96,8 +94,6 @@ int encode_planes(CUtensorMap* map, void* base, const ast_config& c, long long l
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? AST_OK : fail(AST_ERR_CUDA, "cuTensorMapEncodeTiled failed");
 }
-
-}  // namespace
 
 // ==================================================================== solver
 struct ast_solver {

@@ -30,13 +30,19 @@ using namespace ast;
 
 namespace {
 
+// Schedules of a class: 0..kNumShapes-1 one CTA per tile with tile shape
+// kShapeTZ/kShapeTR[s]; kPersistent the persistent FP32 kernel (32x16 tiles,
+// the work list of shape 0)
+constexpr int kPersistent = kNumShapes, kNumSchedules = kNumShapes + 1;
+
 struct BatchClass {
     int flux, recon;
     int first, count;             // slots [first, first + count) of the parameter arrays
-    int shape;                    // tile shape in use (index into kShapeTZ / kShapeTR)
-    int tiles[kNumShapes];        // work-list length per tile shape
-    int ts_off[kNumShapes];       // offset of its count+1 prefix sums in the tile_start array
-    float ms[kNumShapes];         // autotuner: ms per step per shape (0: not timed)
+    int shape;                    // schedule in use
+    int tiles[kNumSchedules];     // work-list length per schedule
+    int ts_off[kNumSchedules];    // offset of its count+1 prefix sums in the tile_start array
+    float ms[kNumSchedules];      // autotuner: ms per step per schedule (0: not timed)
+    int grid;                     // persistent kernel: CTAs
 };
 
 #define BATCH_CUDA(call)                                    \
@@ -77,6 +83,9 @@ struct ast_batch {
     int graph_steps = 0, graph_cur = -1;
     long long cells = 0;
     DevClock* clock_save = nullptr;     // autotuner: clocks saved around the trials
+    int schedules = kNumShapes;         // schedules built for this precision
+    CUtensorMap* maps = nullptr;        // FP32: per parity, load maps then store maps, slot order
+    unsigned int* counters = nullptr;   // FP32: per class, the persistent kernel's tile counter
 };
 
 namespace {
@@ -106,10 +115,28 @@ int upload_params(ast_batch* B)
     return AST_OK;
 }
 
-int launch_class(ast_batch* B, const BatchClass& c, int shape, cudaStream_t st, bool launch)
+int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool launch)
 {
     const StepParams* Ps = B->dP[B->cur] + c.first;
     const int* ts = B->tile_start + c.ts_off[shape];
+    if (shape == kPersistent) {
+        const int ci = (int)(&c - B->cls.data());
+        const CUtensorMap* tin = B->maps + (size_t)(2 * B->cur) * B->nprob + c.first;
+        const CUtensorMap* tout = B->maps + (size_t)(2 * B->cur + 1) * B->nprob + c.first;
+        if (!launch) {
+            int per_sm = 0, dev = 0, sms = 0;
+            int rc = launch_batch_tma(Ps, tin, tout, ts, c.count, B->counters + ci, c.flux, c.recon, 0, st, false,
+                                      &per_sm);
+            if (rc != AST_OK) return rc;
+            BATCH_CUDA(cudaGetDevice(&dev));
+            BATCH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            c.grid = std::min(c.tiles[shape], std::max(per_sm, 1) * sms);
+            return AST_OK;
+        }
+        BATCH_CUDA(cudaMemsetAsync(B->counters + ci, 0, sizeof(unsigned int), st));
+        return launch_batch_tma(Ps, tin, tout, ts, c.count, B->counters + ci, c.flux, c.recon, c.grid, st, true,
+                                nullptr);
+    }
     return launch_batch(B->elem, shape, Ps, ts, c.count, c.tiles[shape], c.flux, c.recon, st, launch);
 }
 
@@ -239,7 +266,7 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
         B->slot[order[s]] = s;
     }
     // work lists: per class and tile shape, the prefix sums of its problems'
-    // tile counts (count + 1 entries)
+    // tile counts (count + 1 entries); the persistent kernel uses shape 0's
     std::vector<int> ts_host;
     for (BatchClass& k : B->cls) {
         for (int sh = 0; sh < kNumShapes; sh++) {
@@ -250,7 +277,10 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
                 ts_host.push_back(k.tiles[sh]);
             }
         }
+        k.ts_off[kPersistent] = k.ts_off[0];
+        k.tiles[kPersistent] = k.tiles[0];
     }
+    if (B->elem == 4) B->schedules = kNumSchedules;
 
     cudaError_t e;
     const size_t nts = ts_host.size();
@@ -285,8 +315,34 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
         (e = cudaMemcpy(B->clocks, clk.data(), sizeof(DevClock) * nprob, cudaMemcpyHostToDevice)) != cudaSuccess)
         rc = cuda_fail(e, "batch clocks");
     if (rc == AST_OK) rc = upload_params(B);
+    if (rc == AST_OK && B->schedules > kNumShapes) {
+        // FP32: tensor maps of every problem's two time levels (tile-box
+        // loads with halo, tile stores), slot order, and the tile counters
+        std::vector<CUtensorMap> maps((size_t)4 * nprob);
+        for (int i = 0; i < nprob && rc == AST_OK; i++) {
+            const int sl = B->slot[i];
+            for (int par = 0; par < 2 && rc == AST_OK; par++) {
+                char* base = (char*)B->arena + B->off[i];
+                void* lin = base + (par ? B->level_bytes[i] : 0);
+                void* lout = base + (par ? 0 : B->level_bytes[i]);
+                rc = encode_planes(&maps[(size_t)(2 * par) * nprob + sl], lin, B->cfg[i], B->ld[i], B->plane[i],
+                                   kShapeTZ[0] + 8, kShapeTR[0] + 4);
+                if (rc == AST_OK)
+                    rc = encode_planes(&maps[(size_t)(2 * par + 1) * nprob + sl], lout, B->cfg[i], B->ld[i],
+                                       B->plane[i], kShapeTZ[0], kShapeTR[0]);
+            }
+        }
+        if (rc == AST_OK && ((e = cudaMalloc(&B->maps, sizeof(CUtensorMap) * maps.size())) != cudaSuccess ||
+                             (e = cudaMalloc(&B->counters, sizeof(unsigned int) * B->cls.size())) != cudaSuccess ||
+                             (e = cudaMemcpy(B->maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
+                                             cudaMemcpyHostToDevice)) != cudaSuccess ||
+                             (e = cudaMemset(B->counters, 0, sizeof(unsigned int) * B->cls.size())) != cudaSuccess))
+            rc = cuda_fail(e, "batch tensor maps");
+        // the persistent kernel is the FP32 default
+        for (BatchClass& k : B->cls) k.shape = kPersistent;
+    }
     for (size_t c = 0; c < B->cls.size() && rc == AST_OK; c++)
-        for (int sh = 0; sh < kNumShapes && rc == AST_OK; sh++) rc = launch_class(B, B->cls[c], sh, nullptr, false);
+        for (int sh = 0; sh < B->schedules && rc == AST_OK; sh++) rc = launch_class(B, B->cls[c], sh, nullptr, false);
     for (size_t c = 1; c < B->cls.size() && rc == AST_OK; c++) {
         cudaStream_t s;
         if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) {
@@ -320,6 +376,8 @@ int ast_batch_destroy(ast_batch* B)
     cudaFree(B->arena);
     cudaFree(B->clocks);
     cudaFree(B->clock_save);
+    cudaFree(B->maps);
+    cudaFree(B->counters);
     cudaFree(B->dP[0]);
     cudaFree(B->dP[1]);
     cudaFree(B->tile_start);
@@ -508,31 +566,38 @@ int ast_batch_info(ast_batch* B, int64_t* cells, int64_t* tiles, int* launches_p
     return AST_OK;
 }
 
-int ast_batch_class(ast_batch* B, int cls, int* flux, int* recon, int* nprob, int* tile_z, int* tile_r,
-                    float* ms_per_shape)
+int ast_batch_class(ast_batch* B, int cls, int* flux, int* recon, int* nprob, int* schedule, int* tile_z,
+                    int* tile_r, float* ms_per_schedule)
 {
     if (!B || cls < 0 || cls >= (int)B->cls.size()) return set_error(AST_ERR_INVALID, "bad argument");
     const BatchClass& k = B->cls[cls];
+    const int shape = (k.shape == kPersistent) ? 0 : k.shape;
     if (flux) *flux = k.flux;
     if (recon) *recon = k.recon;
     if (nprob) *nprob = k.count;
-    if (tile_z) *tile_z = kShapeTZ[k.shape];
-    if (tile_r) *tile_r = kShapeTR[k.shape];
-    if (ms_per_shape)
-        for (int sh = 0; sh < kNumShapes; sh++) ms_per_shape[sh] = k.ms[sh];
+    if (schedule) *schedule = k.shape;
+    if (tile_z) *tile_z = kShapeTZ[shape];
+    if (tile_r) *tile_r = kShapeTR[shape];
+    if (ms_per_schedule)
+        for (int sh = 0; sh < kNumSchedules; sh++) ms_per_schedule[sh] = (sh < B->schedules) ? k.ms[sh] : 0.0f;
+    return AST_OK;
+}
+
+int ast_batch_set_schedule(ast_batch* B, int cls, int schedule)
+{
+    if (!B || cls < 0 || cls >= (int)B->cls.size() || schedule < 0 || schedule >= AST_BATCH_SCHEDULES)
+        return set_error(AST_ERR_INVALID, "bad argument");
+    if (schedule >= B->schedules) return set_error(AST_ERR_UNSUPPORTED, "schedule not built for this precision");
+    B->cls[cls].shape = schedule;
+    drop_graph(B);
     return AST_OK;
 }
 
 int ast_batch_set_tiles(ast_batch* B, int cls, int tile_z, int tile_r)
 {
     if (!B || cls < 0 || cls >= (int)B->cls.size()) return set_error(AST_ERR_INVALID, "bad argument");
-    for (int sh = 0; sh < kNumShapes; sh++) {
-        if (kShapeTZ[sh] == tile_z && kShapeTR[sh] == tile_r) {
-            B->cls[cls].shape = sh;
-            drop_graph(B);
-            return AST_OK;
-        }
-    }
+    for (int sh = 0; sh < kNumShapes; sh++)
+        if (kShapeTZ[sh] == tile_z && kShapeTR[sh] == tile_r) return ast_batch_set_schedule(B, cls, sh);
     return set_error(AST_ERR_UNSUPPORTED, "tile shape not built");
 }
 
@@ -551,7 +616,7 @@ int ast_batch_autotune(ast_batch* B, int trials)
     if (e != cudaSuccess) rc = cuda_fail(e, "autotune clock save");
     for (BatchClass& k : B->cls) {
         float best = 0.0f;
-        for (int sh = 0; sh < kNumShapes && rc == AST_OK; sh++) {
+        for (int sh = 0; sh < B->schedules && rc == AST_OK; sh++) {
             rc = launch_class(B, k, sh, B->stream, true);   // warm-up
             if (rc == AST_OK && (e = cudaEventRecord(e0, B->stream)) != cudaSuccess) rc = cuda_fail(e, "event");
             for (int t = 0; t < trials && rc == AST_OK; t++) rc = launch_class(B, k, sh, B->stream, true);

@@ -22,6 +22,11 @@ int cuda_fail(cudaError_t e, const char* what);
 // records msg for ast_last_error() and returns code
 int set_error(int code, const char* msg);
 
+// the four FP32 state planes of one time level (base, rows of ld, planes
+// of `plane` elements) as a 3-D tensor map with a box of bx x by x 4
+int encode_planes(CUtensorMap* map, void* base, const ast_config& c, long long ld, long long plane, unsigned bx,
+                  unsigned by);
+
 // launch=false only raises the kernel's dynamic shared-memory limit, which
 // must happen outside stream capture (ast_create, ast_step_raw)
 template <typename R, int FLUX, bool RECON, int LAYOUT>
@@ -62,6 +67,30 @@ int launch_tma_t(const StepParams& P, const CUtensorMap& tin, const CUtensorMap&
 
 int launch_step_tma(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int flux, int recon,
                     int grid, cudaStream_t st, bool launch, int* per_sm);
+
+// the persistent FP32 batch kernel of one class (maps and parameters in
+// device memory, indexed by the class's problem); launch=false as above
+template <int FLUX, bool RECON>
+int launch_batch_tma_t(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int* tile_start,
+                       int nprob, unsigned int* counter, int grid, cudaStream_t st, bool launch, int* per_sm)
+{
+    auto k = batch_kernel_tma<FLUX, RECON>;
+    constexpr size_t smem = tile_smem_bytes<float, FLUX, 32, 16, 2>();
+    cudaError_t e;
+    if (!launch) {
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, kThreads, smem);
+        return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    }
+    k<<<grid, kThreads, smem, st>>>(Ps, tin, tout, tile_start, nprob, counter);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? AST_OK : cuda_fail(e, "persistent batch kernel launch");
+}
+
+int launch_batch_tma(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int* tile_start,
+                     int nprob, unsigned int* counter, int flux, int recon, int grid, cudaStream_t st, bool launch,
+                     int* per_sm);
 
 template <typename R, int LAYOUT>
 int launch_step_r(const StepParams& P, int flux, int recon, cudaStream_t st, bool launch)

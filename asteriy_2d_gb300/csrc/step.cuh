@@ -1112,6 +1112,112 @@ __global__ void __launch_bounds__(kThreads, 4)
     cta_epilogue<R>(P, acc, gridDim.x, true);
 }
 
+// The persistent FP32 kernel of one batch class: tiles of all the class's
+// problems handed out by a counter (the work list of the class, problems in
+// slot order, each problem's tiles in row-major order); each tile's box
+// arrives by a bulk-tensor copy through its problem's tensor map while the
+// CTA computes the previous tile, and leaves by a bulk-tensor store.  The
+// problem's parameters are copied to shared memory per tile; each tile
+// reports to its problem's clock (one ticket per tile; the problem's last
+// tile shifts that problem's dt).  The caller zeroes *counter before each
+// launch.
+template <int FLUX, bool RECON>
+__global__ void __launch_bounds__(kThreads, 4)
+    batch_kernel_tma(const StepParams* __restrict__ Ps, const CUtensorMap* __restrict__ tin,
+                     const CUtensorMap* __restrict__ tout, const int* __restrict__ tile_start, int nprob,
+                     unsigned int* counter)
+{
+    using R = float;
+    constexpr int TZ = 32, TR = 16;
+    using S = TileSmem<R, FLUX, TZ, TR, 2>;
+    constexpr uint32_t kBoxBytes = 4u * S::HR * S::HZP * sizeof(R);
+    S& sm = tile_smem<S>();
+    __shared__ __align__(16) StepParams sP;
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int s_tile[2], s_prob[2];
+    __shared__ StepConsts sK;
+    const int tid = threadIdx.x;
+    const int total = tile_start[nprob];
+    // problem j of work-list entry t and the tile's origin (x0, y0)
+    auto locate = [&](int t, int& j, int& x0, int& y0) {
+        int lo = 0, hi = nprob - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tile_start[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        j = lo;
+        const int tl = t - tile_start[j];
+        const int tz = (Ps[j].N + TZ - 1) / TZ;
+        x0 = (tl % tz) * TZ;
+        y0 = (tl / tz) * TR;
+    };
+    if (tid == 0) {
+        tma::mbar_init(&bar[0], 1);
+        tma::mbar_init(&bar[1], 1);
+        tma::fence_async_shared();
+        const int t0 = (int)atomicAdd(counter, 1u);
+        s_tile[0] = t0;
+        if (t0 < total) {
+            int j, x0, y0;
+            locate(t0, j, x0, y0);
+            s_prob[0] = j;
+            tma::mbar_expect(&bar[0], kBoxBytes);
+            tma::load_3d(&tin[j], &sm.qb[0][0][0][0], &bar[0], x0 - 4, y0 - 2, 0);
+        }
+    }
+    TileAcc<R> acc;
+    for (int k = 0;; k++) {
+        // the previous tile is done with sP, the buffers and s_tile / s_prob
+        __syncthreads();
+        const int b = k & 1;
+        const int t = s_tile[b];
+        if (t >= total) break;
+        const int j = s_prob[b];
+        for (int w = tid; w < (int)(sizeof(StepParams) / 16); w += kThreads)
+            reinterpret_cast<int4*>(&sP)[w] = reinterpret_cast<const int4*>(Ps + j)[w];
+        if (tid == 0) {
+            const int tn = (int)atomicAdd(counter, 1u);
+            s_tile[b ^ 1] = tn;
+            if (tn < total) {
+                int jn, x0, y0;
+                locate(tn, jn, x0, y0);
+                s_prob[b ^ 1] = jn;
+                tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
+                tma::load_3d(&tin[jn], &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], x0 - 4, y0 - 2, 0);
+            }
+        }
+        const bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+        if (__syncthreads_or(!arrived)) {
+            if (tid == 0) {
+                atomicOr(&sP.clock->status, AST_ST_TIMEOUT);
+                tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+                if (s_tile[b ^ 1] < total) tma::mbar_wait(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
+            }
+            break;
+        }
+        const int tl = t - tile_start[j];
+        const int tz = (sP.N + TZ - 1) / TZ;
+        const int n0 = (tl % tz) * TZ, m0 = (tl / tz) * TR;
+        patch_tile<R, TZ, TR>(sP, sm, b, n0, m0);
+        if (tid == 0) {
+            sm.qn = 0u;
+            step_consts(sP, sK);
+            tma::store_wait_read();   // the previous tile's store has read sm.out
+        }
+        __syncthreads();
+        acc.clear();
+        tile_body<R, FLUX, RECON, kSoA, TZ, TR, true>(sP, sm, b, sP.gf, n0, m0, sK, acc);
+        tma::fence_async_shared();
+        __syncthreads();
+        if (tid == 0) {
+            tma::store_3d(&tout[j], &sm.out[0][0][0], n0, m0, 0);
+            tma::store_commit();
+        }
+        cta_epilogue<R>(sP, acc, (unsigned)(tile_start[j + 1] - tile_start[j]), false);
+    }
+    if (tid == 0) tma::store_wait_all();
+}
+
 // Characteristic inflow at z_lo after a step (add2_bound, kernel.cu:1895-
 // 1925): one thread per row m; from the old state of cell (0, m) (P.in)
 // and the new state of cell (1, m) (P.out), cell (0, m) of P.out becomes

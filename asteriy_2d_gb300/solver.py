@@ -66,7 +66,8 @@ SIGNATURES = {
     "ast_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
     "ast_batch_autotune": (C.c_int, [C.c_void_p, C.c_int]),
     "ast_batch_class": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
-                                  C.POINTER(C.c_int), C.POINTER(C.c_int), _fp]),
+                                  C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _fp]),
+    "ast_batch_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ast_batch_set_tiles": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "ast_problem_set": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.POINTER(A.ast_problem)]),
     "ast_problem_fill": (C.c_int, [C.POINTER(A.ast_problem), _dp, _dp]),
@@ -378,6 +379,10 @@ def problem_fill(prob):
 
 
 TILE_SHAPES = ((32, 16), (16, 16), (64, 8))
+# batch schedules: one CTA per tile with each tile shape, then the
+# persistent kernel (FP32)
+SCHEDULES = ("32x16", "16x16", "64x8", "persistent")
+PERSISTENT = 3
 
 
 class Batch:
@@ -472,11 +477,12 @@ class Batch:
         autotuner's ms per step of each built shape."""
         out = []
         for k in range(self.info()["launches_per_step"]):
-            v = [C.c_int() for _ in range(5)]
-            ms = np.zeros(3, dtype=np.float32)
+            v = [C.c_int() for _ in range(6)]
+            ms = np.zeros(len(SCHEDULES), dtype=np.float32)
             check(self.lib.ast_batch_class(self.h, k, *[C.byref(x) for x in v], _fptr(ms)), "ast_batch_class")
             out.append({"flux": v[0].value, "recon": v[1].value, "problems": v[2].value,
-                        "tile": (v[3].value, v[4].value), "ms_per_shape": [float(x) for x in ms]})
+                        "schedule": v[3].value, "tile": (v[4].value, v[5].value),
+                        "ms_per_schedule": [float(x) for x in ms]})
         return out
 
     def autotune(self, trials=3):
@@ -485,3 +491,6 @@ class Batch:
 
     def set_tiles(self, cls, tile_z, tile_r):
         check(self.lib.ast_batch_set_tiles(self.h, cls, tile_z, tile_r), "ast_batch_set_tiles")
+
+    def set_schedule(self, cls, schedule):
+        check(self.lib.ast_batch_set_schedule(self.h, cls, schedule), "ast_batch_set_schedule")

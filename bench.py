@@ -395,9 +395,9 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
         "value": cells * steps / sec, "unit": "cell-updates/s", "ms_per_step": sec * 1e3 / steps,
         "steps": steps, "warmup": warmup, "problems": nprob, "seed": seed, "cells": cells,
         "tiles": info["tiles"], "launches_per_step": info["launches_per_step"],
-        "classes": [{"flux": ["hll", "hllc", "godunov"][c["flux"]], "problems": c["problems"],
-                     "tile": "%dx%d" % c["tile"],
-                     "tuner_ms": {"%dx%d" % t: round(m, 4) for t, m in zip(solver.TILE_SHAPES, c["ms_per_shape"])}}
+        "classes": [{"flux": ["hll", "hllc", "godunov", "hllc_a"][c["flux"]], "problems": c["problems"],
+                     "schedule": solver.SCHEDULES[c["schedule"]], "tile": "%dx%d" % c["tile"],
+                     "tuner_ms": {name: round(m, 4) for name, m in zip(solver.SCHEDULES, c["ms_per_schedule"])}}
                     for c in classes],
         "mix": {k: kinds.count(k) for k in sorted(set(kinds))},
         "solo_value": cells * solo_steps / solo_sec, "solo_steps": solo_steps,

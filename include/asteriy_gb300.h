@@ -325,19 +325,25 @@ int ast_batch_set_mlp(ast_batch* batch, const float* params);
 /* cells of all problems, tiles of all problems (at the tile shapes in use),
    and kernel launches per step (the number of (flux, recon) classes) */
 int ast_batch_info(ast_batch* batch, int64_t* cells, int64_t* tiles, int* launches_per_step);
-/* Tile shapes.  Each class steps with one of the built tile shapes
- * (z x r cells: 32x16, the default; 16x16; 64x8).  ast_batch_autotune
- * times every shape on every class, `trials` steps each on the current
- * state (each trial reads the current time level and writes the other;
- * the clocks and counters are restored afterwards, so the run continues
- * exactly as without the call) and keeps the fastest shape per class.
- * ast_batch_class reports class `cls` (0 <= cls < launches_per_step): its
- * flux, reconstruction, problem count, tile shape in use and the tuner's ms
- * per step of each shape (three floats, 0 when not timed);
- * ast_batch_set_tiles sets a class's shape by hand. */
+/* Schedules.  Each class steps with one schedule: 0, 1, 2 = one CTA per
+ * tile with tiles of 32x16, 16x16 or 64x8 (z x r) cells; 3 = the persistent
+ * kernel (FP32 only; tiles of 32x16 staged and stored by bulk-tensor
+ * copies, the default for FP32 batches; FP64 batches default to 0).
+ * ast_batch_autotune times every schedule on every class, `trials` steps
+ * each on the current state (each trial reads the current time level and
+ * writes the other; the clocks and counters are restored afterwards, so the
+ * run continues exactly as without the call) and keeps the fastest per
+ * class.  ast_batch_class reports class `cls` (0 <= cls < launches_per_step):
+ * its flux, reconstruction, problem count, schedule and tile shape in use,
+ * and the tuner's ms per step of each schedule (AST_BATCH_SCHEDULES floats,
+ * 0 when not timed or not built); ast_batch_set_schedule and
+ * ast_batch_set_tiles (one CTA per tile, the given shape) set a class's
+ * schedule by hand. */
+#define AST_BATCH_SCHEDULES 4
 int ast_batch_autotune(ast_batch* batch, int trials);
-int ast_batch_class(ast_batch* batch, int cls, int* flux, int* recon, int* nprob, int* tile_z, int* tile_r,
-                    float* ms_per_shape);
+int ast_batch_class(ast_batch* batch, int cls, int* flux, int* recon, int* nprob, int* schedule, int* tile_z,
+                    int* tile_r, float* ms_per_schedule);
+int ast_batch_set_schedule(ast_batch* batch, int cls, int schedule);
 int ast_batch_set_tiles(ast_batch* batch, int cls, int tile_z, int tile_r);
 
 /* A seeded set of benchmark problems: problem i draws, in this order from

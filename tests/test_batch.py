@@ -209,25 +209,38 @@ def test_batch_stats_and_learned_guess():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape", solver.TILE_SHAPES)
-def test_batch_tile_shapes_agree(shape):
+@pytest.mark.parametrize("schedule", range(len(solver.SCHEDULES)))
+def test_batch_schedules_agree(schedule):
+    """Every schedule (one CTA per tile with each tile shape, the persistent
+    kernel) gives the single-problem results, on ragged and tiny grids."""
     probs = small_set(A.PREC_FP32, n=6)
     probs[0].cfg.N, probs[0].cfg.M = 150, 70
+    probs[1].cfg.N, probs[1].cfg.M = 33, 17
+    probs[2].cfg.flux = A.FLUX_HLLC_A
     cfgs = [p.cfg for p in probs]
     init = [solver.problem_fill(p) for p in probs]
     with solver.Batch(cfgs) as B:
+        assert all(c["schedule"] == solver.PERSISTENT for c in B.classes())   # the FP32 default
         for k in range(B.info()["launches_per_step"]):
-            B.set_tiles(k, *shape)
-        assert all(c["tile"] == shape for c in B.classes())
+            B.set_schedule(k, schedule)
+        assert all(c["schedule"] == schedule for c in B.classes())
+        if schedule < len(solver.TILE_SHAPES):
+            assert all(c["tile"] == solver.TILE_SHAPES[schedule] for c in B.classes())
         for i, (s0, u0) in enumerate(init):
             B.set_state(i, s0, u0)
         B.step(21)
         for i, c in enumerate(cfgs):
             rs, ru, rclock = single_run(c, *init[i], 21)
-            assert_agree(A.PREC_FP32, B.get_state(i), (rs, ru), B.clock(i), rclock, (shape, i))
+            assert_agree(A.PREC_FP32, B.get_state(i), (rs, ru), B.clock(i), rclock, (schedule, i))
     with solver.Batch(cfgs[:1]) as B:
         with pytest.raises(solver.AstError):
             B.set_tiles(0, 8, 8)
+    c64 = cfgs[0].copy()
+    c64.precision = A.PREC_FP64
+    with solver.Batch([c64]) as B:
+        assert B.classes()[0]["schedule"] == 0
+        with pytest.raises(solver.AstError):
+            B.set_schedule(0, solver.PERSISTENT)
 
 
 @pytest.mark.gpu
@@ -244,8 +257,8 @@ def test_autotune_leaves_the_run_unchanged():
         classes = T.autotune(2)
         for c in classes:
             assert c["tile"] in solver.TILE_SHAPES
-            assert all(ms > 0 for ms in c["ms_per_shape"])
-            assert min(c["ms_per_shape"]) == c["ms_per_shape"][solver.TILE_SHAPES.index(c["tile"])]
+            assert all(ms > 0 for ms in c["ms_per_schedule"])
+            assert min(c["ms_per_schedule"]) == c["ms_per_schedule"][c["schedule"]]
         for i in range(len(cfgs)):
             s, u = T.get_state(i)
             assert np.array_equal(s, before[i][0][0]) and np.array_equal(u, before[i][0][1])
