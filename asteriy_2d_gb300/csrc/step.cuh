@@ -317,6 +317,47 @@ __device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C i
     if (E2o) { *E2o = E2; *KE2o = KE2; }
 }
 
+// The pressure of an updated FP32 cell recovered in FP64, for cells whose
+// kinetic energy is almost all of the total (there p = (g-1)(E - rho v^2/2)
+// cancels, and the FP32 E and rho v^2/2 leave too few bits).  The cell's
+// increments (flux sums and sources, as update_cell forms them) are small
+// against the state, so they are taken in FP32; the state, the updated
+// conserved sums and the recovery run in FP64.  1/rho: the FP32 reciprocal
+// refined by one Newton step in FP64 (relative error ~1e-14).
+template <typename R>
+__device__ __forceinline__ double pressure_fp64(const StepParams& P, const R in[4], const R f[4][4], float tdv,
+                                                float ty, float T_do, float Q2, float dx, float dy, int& np)
+{
+    const float r1 = (float)in[0], p1 = (float)in[1], vz1 = (float)in[2], vr1 = (float)in[3];
+    float ps[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float f12 = (float)f[k][0], f14 = -(float)f[k][1], f13 = -(float)f[k][2], f15 = (float)f[k][3];
+        if (P.geom == 1) ps[k] = (f12 + f14) * dy + (f13 + f15) * dx;
+        else ps[k] = f12 * dy + f13 * dx + f14 * dy + f15 * dx;
+    }
+    const float ke1 = r1 * (vz1 * vz1 + vr1 * vr1) * 0.5f;
+    const float gaf = P.gf.ga, ig1f = P.gf.inv_g1;
+    float dr = -tdv * ps[0], dmz = -tdv * ps[1], dmr = -tdv * ps[2] + T_do * Q2, dE = -tdv * ps[3] + T_do * Q2 * vr1;
+    if (P.geom == 1) {
+        dr -= ty * r1 * vr1;
+        dmz -= ty * r1 * vr1 * vz1;
+        dmr -= ty * r1 * vr1 * vr1;
+        dE -= ty * vr1 * (gaf * p1 * ig1f + ke1);
+    }
+    const double R1 = r1, VZ = vz1, VR = vr1;
+    const double E1 = (double)p1 * P.gd.inv_g1 + 0.5 * R1 * (VZ * VZ + VR * VR);
+    double rho2 = R1 + (double)dr;
+    if (rho2 <= 0.0) rho2 = R1;
+    const double mz = R1 * VZ + (double)dmz, mr = R1 * VR + (double)dmr;
+    const double E2 = E1 + (double)dE;
+    double ir = (double)__frcp_rn((float)rho2);
+    ir = fma(ir, fma(-rho2, ir, 1.0), ir);
+    const double p2 = (E2 - 0.5 * (mz * mz + mr * mr) * ir) * P.gd.g1;
+    if (p2 <= 0.0) { np++; return P.p_floor; }
+    return p2;
+}
+
 // ------------------------------------------------------------------ exact solver helpers
 // the face's own left/right states (before the solver's side swap)
 template <typename R>
@@ -834,13 +875,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
                                    &KE2);
                 // pressure recovery p = (g-1)(E - rho v^2/2) in FP64 where the
                 // kinetic energy is more than 99% of the total
-                if (KE2 > 0.99f * E2) {
-                    int d0 = 0, d1 = 0;
-                    const double yd = P.y_min + m * P.dy;
-                    const double ty64 = (P.geom == 1) ? T_do / yd : 0.0;
-                    update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty64,
-                                        P.dx, P.dy, (double)Q2, d0, d1, o);
-                }
+                if (KE2 > 0.99f * E2) o[1] = (R)pressure_fp64(P, in, f, tdv_f, ty, Tf, Q2, dxf, dyf, acc.np);
             }
         }
         if constexpr (TO_SMEM) {
