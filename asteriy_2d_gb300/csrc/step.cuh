@@ -557,22 +557,32 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
     }
 }
 
-// every face of the tile once, z faces then r faces, in one loop over the
-// CTA's threads; the z faces are padded to whole warps so that no warp
-// mixes the two orientations
+// every face of the tile once, in one loop over the CTA's threads: first
+// the z faces c = 0 .. TZ-1 of each row (a warp per row when TZ = 32, so the
+// warp's staged-cell loads hit distinct banks), then the last z face
+// (c = TZ) of every row, then the r faces; each group padded to whole warps
+// so that no warp mixes groups
 template <typename R, int FLUX, bool RECON, int TZ, int TR, typename S>
 __device__ __forceinline__ void face_pass(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
                                           int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
 {
-    constexpr int NFZ = TR * (TZ + 1), NFR = (TR + 1) * TZ;
-    constexpr int NFZP = (NFZ + 31) / 32 * 32;
+    constexpr int NZM = TR * TZ;                               // z faces c < TZ
+    constexpr int NZMP = (NZM + 31) / 32 * 32;
+    constexpr int NZL = NZMP + TR, NZLP = NZMP + (TR + 31) / 32 * 32;   // + the last z face of each row
+    constexpr int NFR = (TR + 1) * TZ;
     // every cell the tile's faces touch lies inside the grid
     const bool interior = n0 >= 1 && n0 + TZ < P.N && m0 >= 1 && m0 + TR < P.M;
-    for (int t = threadIdx.x; t < NFZP + NFR; t += kThreads) {
-        if (t < NFZ)
-            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz, t);
-        else if (t >= NFZP)
-            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smr, t - NFZP);
+    for (int t = threadIdx.x; t < NZLP + NFR; t += kThreads) {
+        if (t < NZM) {
+            const int a = t / TZ, c = t - a * TZ;
+            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz,
+                                                   a * (TZ + 1) + c);
+        } else if (t >= NZMP && t < NZL) {
+            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz,
+                                                   (t - NZMP) * (TZ + 1) + TZ);
+        } else if (t >= NZLP) {
+            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smr, t - NZLP);
+        }
     }
 }
 
