@@ -31,9 +31,12 @@ using namespace ast;
 namespace {
 
 // Schedules of a class: 0..kNumShapes-1 one CTA per tile with tile shape
-// kShapeTZ/kShapeTR[s]; kPersistent the persistent FP32 kernel (32x16 tiles,
-// the work list of shape 0)
-constexpr int kPersistent = kNumShapes, kNumSchedules = kNumShapes + 1;
+// kShapeTZ/kShapeTR[s]; kPersistent the persistent FP32 batch kernel (32x16
+// tiles, the work list of shape 0); kPerProblem the single-problem
+// persistent FP32 kernel once per problem, each problem its own stream
+// (its own chain of launches in the step graph)
+constexpr int kPersistent = kNumShapes, kPerProblem = kNumShapes + 1, kNumSchedules = kNumShapes + 2;
+static_assert(kNumSchedules == AST_BATCH_SCHEDULES, "schedule count");
 
 struct BatchClass {
     int flux, recon;
@@ -86,6 +89,14 @@ struct ast_batch {
     int schedules = kNumShapes;         // schedules built for this precision
     CUtensorMap* maps = nullptr;        // FP32: per parity, load maps then store maps, slot order
     unsigned int* counters = nullptr;   // FP32: per class, the persistent kernel's tile counter
+    // FP32, per-problem schedule (slot order): host copies of the maps and
+    // of each parity's parameters, CTAs, streams and join events
+    std::vector<CUtensorMap> hmaps;
+    std::vector<StepParams> hPp[2];
+    std::vector<int> pgrid;
+    std::vector<cudaStream_t> pstream;
+    std::vector<cudaEvent_t> pev;
+    cudaEvent_t pfork = nullptr;
 };
 
 namespace {
@@ -111,14 +122,51 @@ int upload_params(ast_batch* B)
             p.out = base + (par ? 0 : B->level_bytes[i]);
         }
         BATCH_CUDA(cudaMemcpy(B->dP[par], P.data(), sizeof(StepParams) * P.size(), cudaMemcpyHostToDevice));
+        B->hPp[par] = P;
     }
     return AST_OK;
+}
+
+// one step of the problem in slot s with the single-problem persistent kernel
+int launch_problem(ast_batch* B, const BatchClass& c, int s, cudaStream_t st)
+{
+    const size_t n = (size_t)B->nprob;
+    return launch_step_tma(B->hPp[B->cur][s], B->hmaps[(2 * B->cur) * n + s], B->hmaps[(2 * B->cur + 1) * n + s],
+                           c.flux, c.recon, B->pgrid[s], st, true, nullptr);
 }
 
 int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool launch)
 {
     const StepParams* Ps = B->dP[B->cur] + c.first;
     const int* ts = B->tile_start + c.ts_off[shape];
+    if (shape == kPerProblem) {
+        if (!launch) {
+            // the kernel's shared-memory limit, and each problem's CTAs
+            int per_sm = 0, dev = 0, sms = 0;
+            const size_t n = (size_t)B->nprob;
+            int rc = launch_step_tma(B->hPp[0][c.first], B->hmaps[c.first], B->hmaps[n + c.first], c.flux, c.recon, 0,
+                                     st, false, &per_sm);
+            if (rc != AST_OK) return rc;
+            BATCH_CUDA(cudaGetDevice(&dev));
+            BATCH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            for (int s = c.first; s < c.first + c.count; s++) {
+                const StepParams& P = B->hPp[0][s];
+                const int tiles = ((P.N + kShapeTZ[0] - 1) / kShapeTZ[0]) * ((P.M + kShapeTR[0] - 1) / kShapeTR[0]);
+                B->pgrid[s] = std::min(tiles, std::max(per_sm, 1) * sms);
+            }
+            return AST_OK;
+        }
+        // one step of every problem of the class, each on its stream
+        BATCH_CUDA(cudaEventRecord(B->pfork, st));
+        for (int s = c.first; s < c.first + c.count; s++) {
+            BATCH_CUDA(cudaStreamWaitEvent(B->pstream[s], B->pfork, 0));
+            const int rc = launch_problem(B, c, s, B->pstream[s]);
+            if (rc != AST_OK) return rc;
+            BATCH_CUDA(cudaEventRecord(B->pev[s], B->pstream[s]));
+            BATCH_CUDA(cudaStreamWaitEvent(st, B->pev[s], 0));
+        }
+        return AST_OK;
+    }
     if (shape == kPersistent) {
         const int ci = (int)(&c - B->cls.data());
         const CUtensorMap* tin = B->maps + (size_t)(2 * B->cur) * B->nprob + c.first;
@@ -145,29 +193,46 @@ int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool l
 int enqueue_steps(ast_batch* B, cudaStream_t st, int count)
 {
     const int nc = (int)B->cls.size();
-    if (nc > 1) {
-        BATCH_CUDA(cudaEventRecord(B->ev[0], st));
-        for (int c = 1; c < nc; c++) BATCH_CUDA(cudaStreamWaitEvent(B->aux[c - 1], B->ev[0], 0));
-    }
+    BATCH_CUDA(cudaEventRecord(B->ev[0], st));   // the fork point
     const int cur0 = B->cur;
     for (int c = 0; c < nc; c++) {
+        BatchClass& k = B->cls[c];
+        if (k.shape == kPerProblem) {
+            // every problem of the class its own chain of `count` launches
+            for (int s = k.first; s < k.first + k.count; s++) {
+                cudaStream_t ps = B->pstream[s];
+                BATCH_CUDA(cudaStreamWaitEvent(ps, B->ev[0], 0));
+                B->cur = cur0;
+                for (int i = 0; i < count; i++) {
+                    const int rc = launch_problem(B, k, s, ps);
+                    if (rc != AST_OK) {
+                        B->cur = cur0;
+                        return rc;
+                    }
+                    B->cur ^= 1;
+                }
+                BATCH_CUDA(cudaEventRecord(B->pev[s], ps));
+                BATCH_CUDA(cudaStreamWaitEvent(st, B->pev[s], 0));
+            }
+            continue;
+        }
         cudaStream_t sc = (c == 0) ? st : B->aux[c - 1];
+        if (c > 0) BATCH_CUDA(cudaStreamWaitEvent(sc, B->ev[0], 0));
         B->cur = cur0;
         for (int i = 0; i < count; i++) {
-            int rc = launch_class(B, B->cls[c], B->cls[c].shape, sc, true);
+            int rc = launch_class(B, k, k.shape, sc, true);
             if (rc != AST_OK) {
                 B->cur = cur0;
                 return rc;
             }
             B->cur ^= 1;
         }
-    }
-    if (nc > 1) {
-        for (int c = 1; c < nc; c++) {
-            BATCH_CUDA(cudaEventRecord(B->ev[c], B->aux[c - 1]));
+        if (c > 0) {
+            BATCH_CUDA(cudaEventRecord(B->ev[c], sc));
             BATCH_CUDA(cudaStreamWaitEvent(st, B->ev[c], 0));
         }
     }
+    B->cur = cur0 ^ (count & 1);
     return AST_OK;
 }
 
@@ -277,8 +342,8 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
                 ts_host.push_back(k.tiles[sh]);
             }
         }
-        k.ts_off[kPersistent] = k.ts_off[0];
-        k.tiles[kPersistent] = k.tiles[0];
+        k.ts_off[kPersistent] = k.ts_off[kPerProblem] = k.ts_off[0];
+        k.tiles[kPersistent] = k.tiles[kPerProblem] = k.tiles[0];
     }
     if (B->elem == 4) B->schedules = kNumSchedules;
 
@@ -332,6 +397,24 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
                                        B->plane[i], kShapeTZ[0], kShapeTR[0]);
             }
         }
+        B->hmaps = maps;
+        B->pgrid.assign(nprob, 0);
+        for (int s = 0; s < nprob && rc == AST_OK; s++) {
+            cudaStream_t ps;
+            cudaEvent_t pe;
+            if ((e = cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking)) != cudaSuccess) {
+                rc = cuda_fail(e, "batch problem stream");
+                break;
+            }
+            B->pstream.push_back(ps);
+            if ((e = cudaEventCreateWithFlags(&pe, cudaEventDisableTiming)) != cudaSuccess) {
+                rc = cuda_fail(e, "batch problem event");
+                break;
+            }
+            B->pev.push_back(pe);
+        }
+        if (rc == AST_OK && (e = cudaEventCreateWithFlags(&B->pfork, cudaEventDisableTiming)) != cudaSuccess)
+            rc = cuda_fail(e, "batch fork event");
         if (rc == AST_OK && ((e = cudaMalloc(&B->maps, sizeof(CUtensorMap) * maps.size())) != cudaSuccess ||
                              (e = cudaMalloc(&B->counters, sizeof(unsigned int) * B->cls.size())) != cudaSuccess ||
                              (e = cudaMemcpy(B->maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
@@ -372,6 +455,9 @@ int ast_batch_destroy(ast_batch* B)
     if (!B) return AST_OK;
     drop_graph(B);
     for (cudaStream_t s : B->aux) cudaStreamDestroy(s);
+    for (cudaStream_t s : B->pstream) cudaStreamDestroy(s);
+    for (cudaEvent_t e : B->pev) cudaEventDestroy(e);
+    if (B->pfork) cudaEventDestroy(B->pfork);
     for (cudaEvent_t e : B->ev) cudaEventDestroy(e);
     cudaFree(B->arena);
     cudaFree(B->clocks);

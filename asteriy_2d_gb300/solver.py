@@ -380,9 +380,9 @@ def problem_fill(prob):
 
 TILE_SHAPES = ((32, 16), (16, 16), (64, 8))
 # batch schedules: one CTA per tile with each tile shape, then the
-# persistent kernel (FP32)
-SCHEDULES = ("32x16", "16x16", "64x8", "persistent")
-PERSISTENT = 3
+# persistent batch kernel and one persistent kernel per problem (FP32)
+SCHEDULES = ("32x16", "16x16", "64x8", "persistent", "per-problem")
+PERSISTENT, PER_PROBLEM = 3, 4
 
 
 class Batch:

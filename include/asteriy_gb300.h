@@ -327,8 +327,10 @@ int ast_batch_set_mlp(ast_batch* batch, const float* params);
 int ast_batch_info(ast_batch* batch, int64_t* cells, int64_t* tiles, int* launches_per_step);
 /* Schedules.  Each class steps with one schedule: 0, 1, 2 = one CTA per
  * tile with tiles of 32x16, 16x16 or 64x8 (z x r) cells; 3 = the persistent
- * kernel (FP32 only; tiles of 32x16 staged and stored by bulk-tensor
- * copies, the default for FP32 batches; FP64 batches default to 0).
+ * batch kernel (FP32 only; the class's tiles of 32x16 staged and stored by
+ * bulk-tensor copies, the default for FP32 batches; FP64 batches default to
+ * 0); 4 = the single-problem persistent kernel once per problem, each
+ * problem its own chain of launches in the step graph (FP32 only).
  * ast_batch_autotune times every schedule on every class, `trials` steps
  * each on the current state (each trial reads the current time level and
  * writes the other; the clocks and counters are restored afterwards, so the
@@ -339,7 +341,7 @@ int ast_batch_info(ast_batch* batch, int64_t* cells, int64_t* tiles, int* launch
  * 0 when not timed or not built); ast_batch_set_schedule and
  * ast_batch_set_tiles (one CTA per tile, the given shape) set a class's
  * schedule by hand. */
-#define AST_BATCH_SCHEDULES 4
+#define AST_BATCH_SCHEDULES 5
 int ast_batch_autotune(ast_batch* batch, int trials);
 int ast_batch_class(ast_batch* batch, int cls, int* flux, int* recon, int* nprob, int* schedule, int* tile_z,
                     int* tile_r, float* ms_per_schedule);
