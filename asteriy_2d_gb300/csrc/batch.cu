@@ -657,7 +657,7 @@ int ast_batch_class(ast_batch* B, int cls, int* flux, int* recon, int* nprob, in
 {
     if (!B || cls < 0 || cls >= (int)B->cls.size()) return set_error(AST_ERR_INVALID, "bad argument");
     const BatchClass& k = B->cls[cls];
-    const int shape = (k.shape == kPersistent) ? 0 : k.shape;
+    const int shape = (k.shape >= kNumShapes) ? 0 : k.shape;   // the persistent schedules tile 32x16
     if (flux) *flux = k.flux;
     if (recon) *recon = k.recon;
     if (nprob) *nprob = k.count;

@@ -205,6 +205,8 @@ struct TileCore {
     R Fr[4][TR + 1][TZ];         // r-face flux
     unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
     unsigned qn;                 // queued faces: above the gate (low 16 bits), others (high 16 bits)
+    double ydrow[TR];            // r of the tile's cell rows, y_min + m dy, in FP64
+    float yfrow[TR];             // and in FP32
 };
 
 // the exact solver's queue: faces as 16-bit codes (face index | active <<
@@ -828,6 +830,13 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
 {
     constexpr int QX = S::QX;
     // ---- every face of the tile once, then the queue
+    // r of the tile's rows for the update (the barrier after the faces
+    // orders these writes before their use)
+    if (threadIdx.x < TR) {
+        const int m = m0 + threadIdx.x;
+        sm.ydrow[threadIdx.x] = P.y_min + m * P.dy;
+        sm.yfrow[threadIdx.x] = P.y_minf + (float)m * P.dyf;
+    }
     face_pass<R, FLUX, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
     __syncthreads();
     if constexpr (FLUX == 2) {
@@ -838,7 +847,6 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
     // ---- conservative update of the tile's cells
     const double T_do = K.T_do, tdv_d = K.tdv;
     const float tdv_f = K.tdv_f, Tf = K.T_f, dxf = P.dxf, dyf = P.dyf;
-    const float yminf = P.y_minf;
     const float gaf = P.gf.ga, g1f = P.gf.g1, ig1f = P.gf.inv_g1;
     const auto& qv = sm.qb[b];
     for (int cidx = threadIdx.x; cidx < TZ * TR; cidx += kThreads) {
@@ -860,7 +868,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
             if (sizeof(R) == 8 || (P.geom == 1 && m < 4)) {
                 // FP64; in the FP32 form also the four cell rows next to the
                 // axis, where the 1/r source is largest
-                const double y = P.y_min + m * P.dy;
+                const double y = sm.ydrow[row];
                 double Q2 = 0.0;
                 if (P.body_force) {
                     const double x = P.x_min + n * P.dx;
@@ -872,7 +880,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
                                     P.dy, Q2, acc.nrho, acc.np, o);
             } else {
                 // FP32 form: float arithmetic only
-                const float y = yminf + (float)m * dyf;
+                const float y = sm.yfrow[row];
                 float Q2 = 0.0f;
                 if (P.body_force) {
                     const float x = P.x_minf + (float)n * dxf;
@@ -1088,6 +1096,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     S& sm = tile_smem<S>();
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int s_tile[2];
+    __shared__ int2 s_org[2];      // tile origins (n0, m0), set with s_tile by thread 0
     __shared__ StepConsts sK;
     const int tid = threadIdx.x;
     const int tiles_z = (P.N + TZ - 1) / TZ;
@@ -1102,8 +1111,9 @@ __global__ void __launch_bounds__(kThreads, 4)
         const int t0 = (int)atomicAdd(&P.clock->next_tile, 1u);
         s_tile[0] = t0;
         if (t0 < tiles) {
+            s_org[0] = make_int2((t0 % tiles_z) * TZ, (t0 / tiles_z) * TR);
             tma::mbar_expect(&bar[0], kBoxBytes);
-            tma::load_3d(&tin, &sm.qb[0][0][0][0], &bar[0], (t0 % tiles_z) * TZ - 4, (t0 / tiles_z) * TR - 2, 0);
+            tma::load_3d(&tin, &sm.qb[0][0][0][0], &bar[0], s_org[0].x - 4, s_org[0].y - 2, 0);
         }
     }
     __syncthreads();
@@ -1120,9 +1130,9 @@ __global__ void __launch_bounds__(kThreads, 4)
             const int tn = (int)atomicAdd(&P.clock->next_tile, 1u);
             s_tile[b ^ 1] = tn;
             if (tn < tiles) {
+                s_org[b ^ 1] = make_int2((tn % tiles_z) * TZ, (tn / tiles_z) * TR);
                 tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
-                tma::load_3d(&tin, &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], (tn % tiles_z) * TZ - 4,
-                             (tn / tiles_z) * TR - 2, 0);
+                tma::load_3d(&tin, &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], s_org[b ^ 1].x - 4, s_org[b ^ 1].y - 2, 0);
             }
         }
         const bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
@@ -1136,7 +1146,9 @@ __global__ void __launch_bounds__(kThreads, 4)
             }
             break;
         }
-        const int n0 = (t % tiles_z) * TZ, m0 = (t / tiles_z) * TR;
+        // the origin thread 0 found (one integer division per tile, not one
+        // per thread)
+        const int n0 = s_org[b].x, m0 = s_org[b].y;
         patch_tile<R, TZ, TR>(P, sm, b, n0, m0);
         if (tid == 0) {
             sm.qn = 0u;
@@ -1180,6 +1192,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     __shared__ __align__(16) StepParams sP;
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int s_tile[2], s_prob[2];
+    __shared__ int2 s_org[2];
     __shared__ StepConsts sK;
     const int tid = threadIdx.x;
     const int total = tile_start[nprob];
@@ -1206,6 +1219,7 @@ __global__ void __launch_bounds__(kThreads, 4)
             int j, x0, y0;
             locate(t0, j, x0, y0);
             s_prob[0] = j;
+            s_org[0] = make_int2(x0, y0);
             tma::mbar_expect(&bar[0], kBoxBytes);
             tma::load_3d(&tin[j], &sm.qb[0][0][0][0], &bar[0], x0 - 4, y0 - 2, 0);
         }
@@ -1227,6 +1241,7 @@ __global__ void __launch_bounds__(kThreads, 4)
                 int jn, x0, y0;
                 locate(tn, jn, x0, y0);
                 s_prob[b ^ 1] = jn;
+                s_org[b ^ 1] = make_int2(x0, y0);
                 tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
                 tma::load_3d(&tin[jn], &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], x0 - 4, y0 - 2, 0);
             }
@@ -1240,9 +1255,7 @@ __global__ void __launch_bounds__(kThreads, 4)
             }
             break;
         }
-        const int tl = t - tile_start[j];
-        const int tz = (sP.N + TZ - 1) / TZ;
-        const int n0 = (tl % tz) * TZ, m0 = (tl / tz) * TR;
+        const int n0 = s_org[b].x, m0 = s_org[b].y;
         patch_tile<R, TZ, TR>(sP, sm, b, n0, m0);
         if (tid == 0) {
             sm.qn = 0u;

@@ -53,7 +53,7 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index, interval_ms=50):
+    def __init__(self, index, interval_ms=20):
         self.index = index
         self.interval_ms = interval_ms
         self.proc = None
