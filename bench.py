@@ -36,6 +36,11 @@ sys.path.insert(0, ROOT)
 N_Z, M_R = 4096, 2048   # overridable with --grid for profiling runs
 PERSISTENT = 1          # FP32 kernel: persistent (bulk-tensor staging) or one CTA per tile
 BYTES_PER_CELL = {"fp64": 64, "fp32": 32}   # one read + one write of 4 state values
+# DRAM bytes (read + write) per launch of the FP32 persistent kernel at
+# 4096x2048 from the state at step 1000, from one ncu capture of
+#   bench.py --steps 2 --warmup 1 --no-forms --no-stats --no-cpu --accuracy-steps 0 --batch-steps 0 [--form F]
+# (dram__bytes_read.sum + dram__bytes_write.sum); the default grid only
+MEASURED_TRAFFIC = {"fp32_learned": 134.46e6 + 95.39e6, "fp32_hll": 134.42e6 + 91.77e6}
 
 
 def peaks():
@@ -585,7 +590,10 @@ def main():
                    "mlp_params": params_src,
                    "l2": "inputs larger than L2 (state ping-pong 2x%d MB)" % (cells * BYTES_PER_CELL[prec] // 2 // 2**20)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "traffic": None,
+                     "peak_source": src,
+                     "traffic": (MEASURED_TRAFFIC.get(args.form) if (N_Z, M_R) == (4096, 2048) and PERSISTENT
+                                 else None),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch",
                      "note": "algorithmic bytes = %d B/cell-update (one state read + one write)" % BYTES_PER_CELL[prec]},
         "forms": forms,
         "e2e": {"value": cells * e2e_steps / esec, "unit": "cell-updates/s", "h2d_bytes_per_step": bi,
