@@ -7,6 +7,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -230,8 +231,34 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
         P.fixed_mhi = clampi(std::ceil((c.fixed_ar - P.y_min) / P.dy) + 1.0);
     }
     P.region_select = c.region_select;
-    P.region_lo = c.region_lo;
-    P.region_hi = c.region_hi;
+    {
+        // columns whose face positions pass the reference's region test
+        // lo < x < hi (x = x_min + n dx, plus dx/2 for the z face above the
+        // cell; the product rounded separately, as the reference's FP64
+        // expression is); x grows with n, so each set is one interval
+        P.region_zlo = P.region_rlo = 1;
+        P.region_zhi = P.region_rhi = 0;
+        bool zin = false, rin = false;
+        for (int n = -3; n <= c.N + 2; n++) {
+            volatile double prod = (double)n * P.dx;   // no contraction into an FMA
+            const double x = P.x_min + prod, xz = x + P.dx / 2.0;
+            if (xz > c.region_lo && xz < c.region_hi) {
+                if (!zin) P.region_zlo = n;
+                P.region_zhi = n;
+                zin = true;
+            }
+            if (x > c.region_lo && x < c.region_hi) {
+                if (!rin) P.region_rlo = n;
+                P.region_rhi = n;
+                rin = true;
+            }
+        }
+        // the tile's faces reach two columns beyond the grid
+        if (P.region_zlo == -3) P.region_zlo = INT_MIN;
+        if (P.region_zhi == c.N + 2) P.region_zhi = INT_MAX;
+        if (P.region_rlo == -3) P.region_rlo = INT_MIN;
+        if (P.region_rhi == c.N + 2) P.region_rhi = INT_MAX;
+    }
     P.body_force = c.body_force;
     P.body_lo = c.body_lo;
     P.body_hi = c.body_hi;

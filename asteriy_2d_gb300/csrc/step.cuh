@@ -64,7 +64,11 @@ struct __align__(16) StepParams {
     double fixed_zc, fixed_az2, fixed_ar2;
     int fixed_nlo, fixed_nhi, fixed_mhi;   // cells that can lie in the region (one cell of margin)
     int region_select;
-    double region_lo, region_hi;
+    // the high-order region as column intervals (found on the host from
+    // the reference's FP64 face positions): z faces whose lower cell's
+    // column lies in [region_zlo, region_zhi], r faces of the columns in
+    // [region_rlo, region_rhi]
+    int region_zlo, region_zhi, region_rlo, region_rhi;
     int body_force;
     double body_lo, body_hi, body_rsplit, body_amp;
     // state: SoA planes (in/out) or reference AoS (s, u, s2, u2)
@@ -502,10 +506,11 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
         if (active && P.fixed_region) active = (lval && !sm.fx[jl][il]) || (uval && !sm.fx[ju][iu]);
         bool hi = true;
         if (P.region_select) {
-            // the face's z position as the reference's lower cell sees it
-            const double xl = P.x_min + (n0 + il - 2) * P.dx;
-            const double xf = ZF ? xl + P.dx / 2.0 : xl;
-            hi = (xf > P.region_lo && xf < P.region_hi);
+            // the face's z position as the reference's lower cell sees it,
+            // as an interval of that cell's column (integer compares: an
+            // FP64 position test here ran on every face, region or not)
+            const int nl = n0 + il - 2;
+            hi = ZF ? (nl >= P.region_zlo && nl <= P.region_zhi) : (nl >= P.region_rlo && nl <= P.region_rhi);
         }
         R L[4], U[4], F[4];
         face_states<R, RECON, ZF>(P, sm, b, a, c, hi, L, U);
