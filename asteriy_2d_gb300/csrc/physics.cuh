@@ -69,14 +69,22 @@ struct RiemannCount {
 };
 
 // ------------------------------------------------------------------ minmod
-template <typename R>
-__device__ __forceinline__ R minmod_d(R a, R b)
+// (sign a + sign b)/2 * min(|a|, |b|): zero unless both have one sign,
+// as sign(a) max(0, min(|a|, sign(a) b)) (the same value; a zero result may
+// differ in the sign of zero only), the products with sign(a) taken as
+// sign-bit operations
+__device__ __forceinline__ float minmod_d(float a, float b)
 {
-    // (sign a + sign b)/2 * min(|a|, |b|): zero unless both have one sign,
-    // as sign(a) max(0, min(|a|, sign(a) b)) (the same value; a zero result
-    // may differ in the sign of zero only)
-    const R s = copysign(R(1), a);
-    return s * fmax(R(0), fmin(fabs(a), s * b));
+    const unsigned sa = __float_as_uint(a) & 0x80000000u;
+    const float m = fmaxf(0.0f, fminf(fabsf(a), __uint_as_float(__float_as_uint(b) ^ sa)));
+    return __uint_as_float(__float_as_uint(m) | sa);
+}
+__device__ __forceinline__ double minmod_d(double a, double b)
+{
+    const unsigned long long sa = (unsigned long long)__double_as_longlong(a) & 0x8000000000000000ull;
+    const double bs = __longlong_as_double((long long)((unsigned long long)__double_as_longlong(b) ^ sa));
+    const double m = fmax(0.0, fmin(fabs(a), bs));
+    return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(m) | sa));
 }
 
 // left / right face values of a cell from its three-point stencil; the

@@ -192,6 +192,28 @@ __device__ __forceinline__ T warp_max(T v)
     return v;
 }
 
+// the four flux components of one face in shared memory: one 16-byte
+// access in FP32, two in FP64
+__device__ __forceinline__ void put4(float* d, float a, float b, float c, float e)
+{
+    *reinterpret_cast<float4*>(d) = make_float4(a, b, c, e);
+}
+__device__ __forceinline__ void put4(double* d, double a, double b, double c, double e)
+{
+    reinterpret_cast<double2*>(d)[0] = make_double2(a, b);
+    reinterpret_cast<double2*>(d)[1] = make_double2(c, e);
+}
+__device__ __forceinline__ void get4(const float* s, float& a, float& b, float& c, float& e)
+{
+    const float4 t = *reinterpret_cast<const float4*>(s);
+    a = t.x; b = t.y; c = t.z; e = t.w;
+}
+__device__ __forceinline__ void get4(const double* s, double& a, double& b, double& c, double& e)
+{
+    const double2 t0 = reinterpret_cast<const double2*>(s)[0], t1 = reinterpret_cast<const double2*>(s)[1];
+    a = t0.x; b = t0.y; c = t1.x; e = t1.y;
+}
+
 // ------------------------------------------------------------------ shared memory of a tile
 // The staged tile: NB buffers of the four planes, each TR+4 rows of TZ+8
 // cells.  Cell (n, m) of the tile at (n0, m0) sits at row m - m0 + 2 and
@@ -205,8 +227,11 @@ struct TileCore {
     static constexpr int kNFZ = TR * (TZ + 1);                 // z faces of the tile
     static constexpr int kQueueCap = kNFZ + (TR + 1) * TZ;    // all faces of the tile
     alignas(128) R qb[NB][4][HR][HZP];   // staged state with a two-cell halo
-    R Fz[4][TR][TZ + 1];         // z-face flux: mass, mom_z, mom_r, energy
-    R Fr[4][TR + 1][TZ];         // r-face flux
+    // face fluxes, the four components of a face contiguous (one 16-byte
+    // access per face in FP32): z faces mass, mom_z, mom_r, energy; r faces
+    // in the same order
+    alignas(16) R Fz[TR][TZ + 1][4];
+    alignas(16) R Fr[TR + 1][TZ][4];
     unsigned char fx[HR][HZ];    // 1 = cell held fixed (fixed_region only)
     unsigned qn;                 // queued faces: above the gate (low 16 bits), others (high 16 bits)
     double ydrow[TR];            // r of the tile's cell rows, y_min + m dy, in FP64
@@ -484,14 +509,13 @@ __device__ __forceinline__ void face_states(const StepParams& P, const S& sm, in
 // and 3 go to the queue instead.
 template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF, typename S>
 __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0, int step,
-                                         bool interior, RiemannCount& rc, int& fallback, R& smax, int f)
+                                         bool interior, RiemannCount& rc, int& fallback, R& smax, int a, int c)
 {
     constexpr int NFZ = TR * (TZ + 1);
     constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
     constexpr int NN = ZF ? 2 : 3;           // normal velocity component
     constexpr int TT = ZF ? 3 : 2;           // tangential velocity component
     {
-        const int a = f / W, c = f - a * W;
         // smem indices of the lower (l) and upper (u) cell of the face
         const int jl = ZF ? a + 2 : a + 1, il = ZF ? c + 1 : c + 2;
         const int ju = a + 2, iu = c + 2;
@@ -537,6 +561,7 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
                 const bool strong = P.riemann_newton && wave_strength(q) > P.mlp_gate;
                 const unsigned old = atomicAdd(&sm.qn, strong ? 1u : 0x10000u);
                 const int slot = strong ? (int)(old & 0xffffu) : S::kQueueCap - 1 - (int)(old >> 16);
+                const int f = a * W + c;
                 sm.qcode[slot] = (unsigned short)((ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.pattern << 14));
                 return;
             }
@@ -555,10 +580,10 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
         }
         if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
         if (ZF) {
-            sm.Fz[0][a][c] = F[0]; sm.Fz[1][a][c] = F[1]; sm.Fz[2][a][c] = F[2]; sm.Fz[3][a][c] = F[3];
+            put4(sm.Fz[a][c], F[0], F[1], F[2], F[3]);
         } else {
             // r face: the normal momentum is mom_r, the tangential one mom_z
-            sm.Fr[0][a][c] = F[0]; sm.Fr[1][a][c] = F[2]; sm.Fr[2][a][c] = F[1]; sm.Fr[3][a][c] = F[3];
+            put4(sm.Fr[a][c], F[0], F[2], F[1], F[3]);
         }
         if (active) smax = fmax(smax, Sp);
     }
@@ -581,14 +606,16 @@ __device__ __forceinline__ void face_pass(const StepParams& P, S& sm, int b, con
     const bool interior = n0 >= 1 && n0 + TZ < P.N && m0 >= 1 && m0 + TR < P.M;
     for (int t = threadIdx.x; t < NZLP + NFR; t += kThreads) {
         if (t < NZM) {
-            const int a = t / TZ, c = t - a * TZ;
-            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz,
-                                                   a * (TZ + 1) + c);
+            const int a = t / TZ;
+            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz, a,
+                                                   t - a * TZ);
         } else if (t >= NZMP && t < NZL) {
-            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz,
-                                                   (t - NZMP) * (TZ + 1) + TZ);
+            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz, t - NZMP,
+                                                   TZ);
         } else if (t >= NZLP) {
-            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smr, t - NZLP);
+            const int a = (t - NZLP) / TZ;
+            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smr, a,
+                                                    t - NZLP - a * TZ);
         }
     }
 }
@@ -652,7 +679,7 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, co
                     face_sides(q, rL, pL, uL, cL, rR, pR, uR, cR);
                     mlp_features((float)g.ga, (float)rL, (float)pL, (float)uL, (float)cL, (float)rR, (float)pR,
                                  (float)uR, (float)cR, x);
-                    p0_slot = zf ? &sm.Fz[0][a][c] : &sm.Fr[0][a][c];
+                    p0_slot = zf ? &sm.Fz[a][c][0] : &sm.Fr[a][c][0];
                 }
                 // standardised, and clamped to a range f16 holds exactly enough
 #pragma unroll
@@ -682,16 +709,16 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, co
         bool zf;
         const RPre<R> q = queued_face<R, RECON, TZ, TR>(P, sm, b, g, code & 0xfff, (code >> 14) & 3, a, c, zf);
         // a gated face's learned start value, left in its flux slot by phase 1
-        const R p0 = (strong && P.guess == 1 && P.mlp) ? (zf ? sm.Fz[0][a][c] : sm.Fr[0][a][c]) : R(0);
+        const R p0 = (strong && P.guess == 1 && P.mlp) ? (zf ? sm.Fz[a][c][0] : sm.Fr[a][c][0]) : R(0);
         const R p = solve_queued(P, g, q, strong, p0, rc, fallback);
         R F[4];
         R Sp = godunov_sample(g, q, p, F, rc);
         if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
         if (zf) {
-            sm.Fz[0][a][c] = F[0]; sm.Fz[1][a][c] = F[1]; sm.Fz[2][a][c] = F[2]; sm.Fz[3][a][c] = F[3];
+            put4(sm.Fz[a][c], F[0], F[1], F[2], F[3]);
             if (active) smz = fmax(smz, Sp);
         } else {
-            sm.Fr[0][a][c] = F[0]; sm.Fr[1][a][c] = F[2]; sm.Fr[2][a][c] = F[1]; sm.Fr[3][a][c] = F[3];
+            put4(sm.Fr[a][c], F[0], F[2], F[1], F[3]);
             if (active) smr = fmax(smr, Sp);
         }
         if (P.rec && step % P.rec_every == 0)
@@ -863,13 +890,10 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
         if (!(P.fixed_region && sm.fx[j][i])) {
             R in[4] = {o[0], o[1], o[2], o[3]};
             R f[4][4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                f[k][0] = sm.Fz[k][row][col + 1];
-                f[k][1] = sm.Fz[k][row][col];
-                f[k][2] = sm.Fr[k][row][col];
-                f[k][3] = sm.Fr[k][row + 1][col];
-            }
+            get4(sm.Fz[row][col + 1], f[0][0], f[1][0], f[2][0], f[3][0]);
+            get4(sm.Fz[row][col], f[0][1], f[1][1], f[2][1], f[3][1]);
+            get4(sm.Fr[row][col], f[0][2], f[1][2], f[2][2], f[3][2]);
+            get4(sm.Fr[row + 1][col], f[0][3], f[1][3], f[2][3], f[3][3]);
             if (sizeof(R) == 8 || (P.geom == 1 && m < 4)) {
                 // FP64; in the FP32 form also the four cell rows next to the
                 // axis, where the 1/r source is largest
