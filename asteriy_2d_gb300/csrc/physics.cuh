@@ -493,7 +493,12 @@ __device__ __forceinline__ float rare_coef<float>(const Gas<float>& g, float rK,
 // Sampling of the solution at w = 0 and the face flux (kernel.cu:233-568).
 // p: the solved p* for patterns 2 and 3 (ignored otherwise).  Returns the dt
 // wave speed max(UU, eps8), UU the largest wave speed of the pattern.
-template <typename R>
+// MODE: every pattern (kSampleAll), or only the closed-form patterns 0 and 1
+// (kSampleClosed) or the iterative ones 2 and 3 (kSampleIterative) for a
+// caller that has sorted its faces by pattern (the other patterns' code is
+// left out of that caller; a face of another pattern samples as NaN)
+enum { kSampleAll = 0, kSampleClosed = 1, kSampleIterative = 2 };
+template <typename R, int MODE = kSampleAll>
 __device__ R godunov_sample(const Gas<R>& g, const RPre<R>& q, R p, R F[4], RiemannCount& rc)
 {
     const R enI = q.enI, teI = q.teI, pI = q.pI, rI = q.rI, cI = q.cI;
@@ -504,7 +509,7 @@ __device__ R godunov_sample(const Gas<R>& g, const RPre<R>& q, R p, R F[4], Riem
     // an earlier one; the same order is kept here.
     const R w = R(0);
     en = r = te = UU = R(0);
-    if (q.pattern == 0) {
+    if (MODE != kSampleIterative && q.pattern == 0) {
         // vacuum between two rarefactions
         rc.status |= 0x20u;
         p = R(0);
@@ -522,7 +527,7 @@ __device__ R godunov_sample(const Gas<R>& g, const RPre<R>& q, R p, R F[4], Riem
             en = w - ce; p = pII * pow(ce / cII, R(1) / g.gm); r = g.ga * p / ce / ce; te = teII;
         }
         if (w >= dII) { en = enII; p = pII; r = rII; te = teII; }
-    } else if (q.pattern == 1) {
+    } else if (MODE != kSampleIterative && q.pattern == 1) {
         // two rarefactions, closed form
         p = pI * pow((q.Udf - q.Uvk) / (q.Urz - q.Uvk), R(1) / g.gm);
         R aI = rare_coef(g, rI, cI, p, pI);
@@ -551,7 +556,7 @@ __device__ R godunov_sample(const Gas<R>& g, const RPre<R>& q, R p, R F[4], Riem
             en = w - ce; p = pII * pow(ce / cII, R(1) / g.gm); r = g.ga * p / ce / ce; te = teII;
         }
         if (w >= dII) { en = enII; p = pII; r = rII; te = teII; }
-    } else if (q.pattern == 2) {
+    } else if (MODE != kSampleClosed && q.pattern == 2) {
         // shock on side I, rarefaction on side II
         R aI = sqrt(rI * (g.g2 / R(2) * p + g.g1 / R(2) * pI));
         R aII = rare_coef(g, rII, cII, p, pII);
@@ -571,7 +576,7 @@ __device__ R godunov_sample(const Gas<R>& g, const RPre<R>& q, R p, R F[4], Riem
             en = w - ce; p = pII * pow(ce / cII, R(1) / g.gm); r = g.ga * p / ce / ce; te = teII;
         }
         if (w >= dII) { en = enII; p = pII; r = rII; te = teII; }
-    } else if (q.pattern == 3) {
+    } else if (MODE != kSampleClosed && q.pattern == 3) {
         // two shocks
         R aI = sqrt(rI * (g.g2 / R(2) * p + g.g1 / R(2) * pI));
         R aII = sqrt(rII * (g.g2 / R(2) * p + g.g1 / R(2) * pII));

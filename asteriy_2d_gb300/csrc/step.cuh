@@ -565,7 +565,7 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
                 sm.qcode[slot] = (unsigned short)((ZF ? f : NFZ + f) | (active ? 1 << 12 : 0) | (q.pattern << 14));
                 return;
             }
-            Sp = godunov_sample(g, q, R(0), F, rc);
+            Sp = godunov_sample<R, kSampleClosed>(g, q, R(0), F, rc);
         } else {
             Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         }
@@ -605,14 +605,20 @@ __device__ __forceinline__ void face_pass(const StepParams& P, S& sm, int b, con
     // every cell the tile's faces touch lies inside the grid
     const bool interior = n0 >= 1 && n0 + TZ < P.N && m0 >= 1 && m0 + TR < P.M;
     for (int t = threadIdx.x; t < NZLP + NFR; t += kThreads) {
-        if (t < NZM) {
-            const int a = t / TZ;
-            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz, a,
-                                                   t - a * TZ);
-        } else if (t >= NZMP && t < NZL) {
-            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz, t - NZMP,
-                                                   TZ);
-        } else if (t >= NZLP) {
+        if (t < NZLP) {
+            // one call site for both z groups (a smaller kernel)
+            int a, c;
+            if (t < NZM) {
+                a = t / TZ;
+                c = t - a * TZ;
+            } else if (t >= NZMP && t < NZL) {
+                a = t - NZMP;
+                c = TZ;
+            } else {
+                continue;
+            }
+            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz, a, c);
+        } else {
             const int a = (t - NZLP) / TZ;
             face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smr, a,
                                                     t - NZLP - a * TZ);
@@ -712,7 +718,7 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, co
         const R p0 = (strong && P.guess == 1 && P.mlp) ? (zf ? sm.Fz[a][c][0] : sm.Fr[a][c][0]) : R(0);
         const R p = solve_queued(P, g, q, strong, p0, rc, fallback);
         R F[4];
-        R Sp = godunov_sample(g, q, p, F, rc);
+        R Sp = godunov_sample<R, kSampleIterative>(g, q, p, F, rc);
         if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
         if (zf) {
             put4(sm.Fz[a][c], F[0], F[1], F[2], F[3]);
