@@ -27,6 +27,10 @@
 namespace ast {
 
 constexpr int kThreads = 256;
+// the thread of the persistent kernels that issues the bulk copies: lane 0
+// of the last warp (in the face pass the first two warps take one face more
+// than the others)
+constexpr int kCopyThread = kThreads - 32;
 
 // device-resident clock and counters of a solver (one per solver)
 struct DevClock {
@@ -876,6 +880,12 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
         sm.yfrow[threadIdx.x] = P.y_minf + (float)m * P.dyf;
     }
     face_pass<R, FLUX, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
+    // persistent kernel: the previous tile's bulk store, issued by the copy
+    // thread at the start of this face pass, has read sm.out before anything
+    // overwrites it (the network's space in the queue phase, then the update)
+    if constexpr (TO_SMEM) {
+        if (threadIdx.x == kCopyThread) tma::store_wait_read();
+    }
     __syncthreads();
     if constexpr (FLUX == 2) {
         queue_pass<R, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
@@ -1115,10 +1125,15 @@ __global__ void __launch_bounds__(kThreads, min_ctas<R, FLUX>())
 // cells n0-4 .. n0+TZ+3, y = rows m0-2 .. m0+TR+1, all four planes) into
 // one of two buffers; the copy of the CTA's next tile runs while the current
 // one is computed.  The updated cells leave by a bulk-tensor store from a
-// shared-memory tile.  The CTA's wave-speed maxima and counters accumulate
-// over its tiles and are reported once (one ticket per CTA).  A bulk copy
-// that does not arrive within the wait limit sets AST_ST_TIMEOUT and ends
-// the CTA's loop.
+// shared-memory tile.  The bulk copies, the store and the counter's atomic
+// are issued by one thread of the last warp at the start of the face pass
+// (their issue takes hundreds of cycles; that warp has one face fewer to
+// compute than the first two, so the barrier after the faces does not wait
+// for it): the store of the previous tile's cells, the copy of the next
+// tile, and the counter's atomic for the tile after it.  The CTA's
+// wave-speed maxima and counters accumulate over its tiles and are reported
+// once (one ticket per CTA).  A bulk copy that does not arrive within the
+// wait limit sets AST_ST_TIMEOUT and ends the CTA's loop.
 template <int FLUX, bool RECON>
 __global__ void __launch_bounds__(kThreads, 4)
     step_kernel_tma(StepParams P, const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout)
@@ -1130,21 +1145,29 @@ __global__ void __launch_bounds__(kThreads, 4)
     static_assert(sizeof(((S*)nullptr)->qb[0]) == kBoxBytes, "tile buffer is the TMA box");
     S& sm = tile_smem<S>();
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ int s_tile[2];
-    __shared__ int2 s_org[2];      // tile origins (n0, m0), set with s_tile by thread 0
+    __shared__ int s_tile[2];      // tiles of the current and the next iteration (per buffer)
+    __shared__ int2 s_org[2];      // their origins (n0, m0), set with s_tile by the copy thread
     __shared__ StepConsts sK;
+    __shared__ int2 s_pend;        // copy thread: origin of the tile whose cells wait in sm.out
     const int tid = threadIdx.x;
+    const bool copier = tid == kCopyThread;
     const int tiles_z = (P.N + TZ - 1) / TZ;
     const int tiles = tiles_z * ((P.M + TR - 1) / TR);
-    if (tid == 0) {
+    if (copier) {
         tma::prefetch_map(&tin);
         tma::prefetch_map(&tout);
         tma::mbar_init(&bar[0], 1);
         tma::mbar_init(&bar[1], 1);
         tma::fence_async_shared();
         step_consts(P, sK);
+        s_pend = make_int2(-1, -1);
+        // the first two tiles: the first is copied now, the second at the
+        // start of the first tile's face pass
         const int t0 = (int)atomicAdd(&P.clock->next_tile, 1u);
+        const int t1 = (t0 < tiles) ? (int)atomicAdd(&P.clock->next_tile, 1u) : tiles;
         s_tile[0] = t0;
+        s_tile[1] = t1;
+        s_org[1] = make_int2((t1 % tiles_z) * TZ, (t1 / tiles_z) * TR);
         if (t0 < tiles) {
             s_org[0] = make_int2((t0 % tiles_z) * TZ, (t0 / tiles_z) * TR);
             tma::mbar_expect(&bar[0], kBoxBytes);
@@ -1159,48 +1182,60 @@ __global__ void __launch_bounds__(kThreads, 4)
         const int b = k & 1;
         const int t = s_tile[b];
         if (t >= tiles) break;
-        if (tid == 0) {
-            // prefetch: the other buffer was last read by the previous tile,
-            // which every thread finished before the barrier that ended it
-            const int tn = (int)atomicAdd(&P.clock->next_tile, 1u);
-            s_tile[b ^ 1] = tn;
-            if (tn < tiles) {
-                s_org[b ^ 1] = make_int2((tn % tiles_z) * TZ, (tn / tiles_z) * TR);
-                tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
-                tma::load_3d(&tin, &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], s_org[b ^ 1].x - 4, s_org[b ^ 1].y - 2, 0);
-            }
-        }
         const bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
         if (__syncthreads_or(!arrived)) {
             // give up this step's remaining tiles; wait (bounded) for the
-            // prefetch in flight and for the stores before leaving
-            if (tid == 0) {
+            // copy in flight before leaving (the next tile's copy is not
+            // issued yet)
+            if (copier) {
                 acc.rc.status |= AST_ST_TIMEOUT;
                 tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
-                if (s_tile[b ^ 1] < tiles) tma::mbar_wait(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
             }
             break;
         }
-        // the origin thread 0 found (one integer division per tile, not one
-        // per thread)
+        // the origin the copy thread found (one integer division per tile,
+        // not one per thread)
         const int n0 = s_org[b].x, m0 = s_org[b].y;
         patch_tile<R, TZ, TR>(P, sm, b, n0, m0);
-        if (tid == 0) {
-            sm.qn = 0u;
-            tma::store_wait_read();   // the previous tile's store has read sm.out
-        }
+        if (copier) sm.qn = 0u;
         __syncthreads();
+        if (copier) {
+            // the previous tile's cells (sm.out is not written again before
+            // the store has read it: see tile_body)
+            const int2 pend = s_pend;
+            if (pend.x >= 0) {
+                tma::store_3d(&tout, &sm.out[0][0][0], pend.x, pend.y, 0);
+                tma::store_commit();
+            }
+            s_pend = make_int2(n0, m0);
+            // the next tile's box into the other buffer (last read by the
+            // previous tile, which every thread finished before the barriers
+            // above), then the counter's atomic for the tile after it, into
+            // this buffer's slots (every thread has read them)
+            int tnn = tiles;
+            if (s_tile[b ^ 1] < tiles) {
+                tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
+                tma::load_3d(&tin, &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], s_org[b ^ 1].x - 4, s_org[b ^ 1].y - 2,
+                             0);
+                tnn = (int)atomicAdd(&P.clock->next_tile, 1u);
+            }
+            s_tile[b] = tnn;
+            s_org[b] = make_int2((tnn % tiles_z) * TZ, (tnn / tiles_z) * TR);
+        }
         tile_body<R, FLUX, RECON, kSoA, TZ, TR, true>(P, sm, b, g, n0, m0, sK, acc);
         // this thread's shared-memory writes (sm.out, ghost cells) before
         // the bulk copies that read or overwrite them
         tma::fence_async_shared();
         __syncthreads();
-        if (tid == 0) {
-            tma::store_3d(&tout, &sm.out[0][0][0], n0, m0, 0);
+    }
+    if (copier) {
+        const int2 pend = s_pend;
+        if (pend.x >= 0) {
+            tma::store_3d(&tout, &sm.out[0][0][0], pend.x, pend.y, 0);
             tma::store_commit();
         }
+        tma::store_wait_all();
     }
-    if (tid == 0) tma::store_wait_all();
     cta_epilogue<R>(P, acc, gridDim.x, true);
 }
 
