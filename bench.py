@@ -40,7 +40,7 @@ BYTES_PER_CELL = {"fp64": 64, "fp32": 32}   # one read + one write of 4 state va
 # 4096x2048 from the state at step 1000, from one ncu capture of
 #   bench.py --steps 2 --warmup 1 --no-forms --no-stats --no-cpu --accuracy-steps 0 --batch-steps 0 [--form F]
 # (dram__bytes_read.sum + dram__bytes_write.sum); the default grid only
-MEASURED_TRAFFIC = {"fp32_learned": 134.46e6 + 95.39e6, "fp32_hll": 134.42e6 + 91.77e6}
+MEASURED_TRAFFIC = {"fp32_learned": 134.99e6 + 96.65e6, "fp32_hll": 134.45e6 + 91.92e6}
 
 
 def peaks():
