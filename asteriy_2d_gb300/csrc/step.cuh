@@ -893,65 +893,116 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
     }
 
     // ---- conservative update of the tile's cells
-    const double T_do = K.T_do, tdv_d = K.tdv;
     const float tdv_f = K.tdv_f, Tf = K.T_f, dxf = P.dxf, dyf = P.dyf;
     const float gaf = P.gf.ga, g1f = P.gf.g1, ig1f = P.gf.inv_g1;
     const auto& qv = sm.qb[b];
-    for (int cidx = threadIdx.x; cidx < TZ * TR; cidx += kThreads) {
+    // cell cidx of the tile: its staged state and its four face fluxes
+    auto load_cell = [&](int row, int col, R in[4], R f[4][4]) {
+        const int j = row + 2, i = col + 2;
+        in[0] = qv[0][j][i + QX]; in[1] = qv[1][j][i + QX]; in[2] = qv[2][j][i + QX]; in[3] = qv[3][j][i + QX];
+        get4(sm.Fz[row][col + 1], f[0][0], f[1][0], f[2][0], f[3][0]);
+        get4(sm.Fz[row][col], f[0][1], f[1][1], f[2][1], f[3][1]);
+        get4(sm.Fr[row][col], f[0][2], f[1][2], f[2][2], f[3][2]);
+        get4(sm.Fr[row + 1][col], f[0][3], f[1][3], f[2][3], f[3][3]);
+    };
+    // the update in FP64 (the FP64 solver; in the FP32 form the four cell
+    // rows next to the axis, where the 1/r source is largest); the step's
+    // FP64 constants read where they are used (not held in registers
+    // through the FP32 form's loop)
+    auto update_fp64 = [&](int row, int n, const R in[4], const R f[4][4], R o[4]) {
+        const double T_do = K.T_do, tdv_d = K.tdv;
+        const double y = sm.ydrow[row];
+        double Q2 = 0.0;
+        if (P.body_force) {
+            const double x = P.x_min + n * P.dx;
+            if (x > P.body_lo && x < P.body_hi)
+                Q2 = (y >= P.body_rsplit) ? -P.body_amp * (double)in[0] : P.body_amp * (double)in[0];
+        }
+        const double ty = (P.geom == 1) ? T_do / y : 0.0;
+        update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty, P.dx, P.dy, Q2, acc.nrho,
+                            acc.np, o);
+    };
+    // the FP32 form's source terms of a cell: ty = T_do/r and the body force
+    auto sources_fp32 = [&](int row, int n, const R in[4], float& ty, float& Q2) {
+        const float y = sm.yfrow[row];
+        Q2 = 0.0f;
+        if (P.body_force) {
+            const float x = P.x_minf + (float)n * dxf;
+            if (x > P.body_lof && x < P.body_hif)
+                Q2 = (y >= P.body_rsplitf) ? -P.body_ampf * (float)in[0] : P.body_ampf * (float)in[0];
+        }
+        ty = (P.geom == 1) ? Tf / y : 0.0f;
+    };
+    auto store_cell = [&](int row, int col, int n, int m, const R o[4], bool p_only) {
+        if constexpr (TO_SMEM) {
+            sm.out[1][row][col] = o[1];
+            if (!p_only) { sm.out[0][row][col] = o[0]; sm.out[2][row][col] = o[2]; sm.out[3][row][col] = o[3]; }
+        } else if (LAYOUT == kSoA) {
+            R* out = (R*)P.out;
+            const long long k = (long long)m * P.ld + n;
+            out[k + P.plane] = o[1];
+            if (!p_only) { out[k] = o[0]; out[k + 2 * P.plane] = o[2]; out[k + 3 * P.plane] = o[3]; }
+        } else {
+            const long long k = (long long)m * P.N + n;
+            ((double2*)P.out)[k] = make_double2((double)o[0], (double)o[1]);
+            if (!p_only) ((double2*)P.out_u)[k] = make_double2((double)o[2], (double)o[3]);
+        }
+    };
+    // FP32 form: cells whose FP64 part is done after the loop, so that its
+    // code stays out of the loop's register allocation (bit 2 it: a
+    // near-axis cell, its whole update; bit 2 it + 1: the FP64 pressure
+    // recovery of a cell whose kinetic energy is above 99% of the total)
+    unsigned deferred = 0u;
+    int it = 0;
+    for (int cidx = threadIdx.x; cidx < TZ * TR; cidx += kThreads, it++) {
         const int row = cidx / TZ, col = cidx - row * TZ;
         const int n = n0 + col, m = m0 + row;
         if (n >= P.N || m >= P.M) continue;
         const int j = row + 2, i = col + 2;
         R o[4] = {qv[0][j][i + QX], qv[1][j][i + QX], qv[2][j][i + QX], qv[3][j][i + QX]};
         if (!(P.fixed_region && sm.fx[j][i])) {
-            R in[4] = {o[0], o[1], o[2], o[3]};
-            R f[4][4];
-            get4(sm.Fz[row][col + 1], f[0][0], f[1][0], f[2][0], f[3][0]);
-            get4(sm.Fz[row][col], f[0][1], f[1][1], f[2][1], f[3][1]);
-            get4(sm.Fr[row][col], f[0][2], f[1][2], f[2][2], f[3][2]);
-            get4(sm.Fr[row + 1][col], f[0][3], f[1][3], f[2][3], f[3][3]);
-            if (sizeof(R) == 8 || (P.geom == 1 && m < 4)) {
-                // FP64; in the FP32 form also the four cell rows next to the
-                // axis, where the 1/r source is largest
-                const double y = sm.ydrow[row];
-                double Q2 = 0.0;
-                if (P.body_force) {
-                    const double x = P.x_min + n * P.dx;
-                    if (x > P.body_lo && x < P.body_hi)
-                        Q2 = (y >= P.body_rsplit) ? -P.body_amp * (double)in[0] : P.body_amp * (double)in[0];
-                }
-                const double ty = (P.geom == 1) ? T_do / y : 0.0;
-                update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty, P.dx,
-                                    P.dy, Q2, acc.nrho, acc.np, o);
+            R in[4], f[4][4];
+            load_cell(row, col, in, f);
+            if constexpr (sizeof(R) == 8) {
+                update_fp64(row, n, in, f, o);
             } else {
-                // FP32 form: float arithmetic only
-                const float y = sm.yfrow[row];
-                float Q2 = 0.0f;
-                if (P.body_force) {
-                    const float x = P.x_minf + (float)n * dxf;
-                    if (x > P.body_lof && x < P.body_hif)
-                        Q2 = (y >= P.body_rsplitf) ? -P.body_ampf * (float)in[0] : P.body_ampf * (float)in[0];
+                if (P.geom == 1 && m < 4) {
+                    deferred |= 1u << (2 * it);
+                    continue;
                 }
-                const float ty = (P.geom == 1) ? Tf / y : 0.0f;
+                float ty, Q2;
+                sources_fp32(row, n, in, ty, Q2);
                 float E2, KE2;
                 update_cell<float>(P, gaf, g1f, ig1f, in, f, Tf, tdv_f, ty, dxf, dyf, Q2, acc.nrho, acc.np, o, &E2,
                                    &KE2);
-                // pressure recovery p = (g-1)(E - rho v^2/2) in FP64 where the
-                // kinetic energy is more than 99% of the total
-                if (KE2 > 0.99f * E2) o[1] = (R)pressure_fp64(P, in, f, tdv_f, ty, Tf, Q2, dxf, dyf, acc.np);
+                // pressure recovery p = (g-1)(E - rho v^2/2) in FP64 where
+                // the kinetic energy is more than 99% of the total
+                if (KE2 > 0.99f * E2) deferred |= 2u << (2 * it);
             }
         }
-        if constexpr (TO_SMEM) {
-            sm.out[0][row][col] = o[0]; sm.out[1][row][col] = o[1];
-            sm.out[2][row][col] = o[2]; sm.out[3][row][col] = o[3];
-        } else if (LAYOUT == kSoA) {
-            R* out = (R*)P.out;
-            const long long k = (long long)m * P.ld + n;
-            out[k] = o[0]; out[k + P.plane] = o[1]; out[k + 2 * P.plane] = o[2]; out[k + 3 * P.plane] = o[3];
-        } else {
-            const long long k = (long long)m * P.N + n;
-            ((double2*)P.out)[k] = make_double2((double)o[0], (double)o[1]);
-            ((double2*)P.out_u)[k] = make_double2((double)o[2], (double)o[3]);
+        store_cell(row, col, n, m, o, false);
+    }
+    if constexpr (sizeof(R) == 4) {
+        static_assert(TO_SMEM || LAYOUT == kSoA, "FP32 state is SoA planes");
+        if (deferred) {
+            it = 0;
+            for (int cidx = threadIdx.x; cidx < TZ * TR; cidx += kThreads, it++) {
+                const unsigned d = (deferred >> (2 * it)) & 3u;
+                if (!d) continue;
+                const int row = cidx / TZ, col = cidx - row * TZ;
+                const int n = n0 + col, m = m0 + row;
+                R in[4], f[4][4], o[4];
+                load_cell(row, col, in, f);
+                if (d & 1u) {
+                    update_fp64(row, n, in, f, o);
+                    store_cell(row, col, n, m, o, false);
+                } else {
+                    float ty, Q2;
+                    sources_fp32(row, n, in, ty, Q2);
+                    o[1] = (R)pressure_fp64(P, in, f, tdv_f, ty, Tf, Q2, dxf, dyf, acc.np);
+                    store_cell(row, col, n, m, o, true);
+                }
+            }
         }
     }
 }
