@@ -505,58 +505,64 @@ __device__ __forceinline__ void face_states(const StepParams& P, const S& sm, in
     }
 }
 
-// Face f of one orientation in the tile.  ZF: z faces (between tile
-// columns c-1 and c of a row), else r faces (between tile rows a-1 and a of
-// a column).  Writes the flux, in (mass, mom_z, mom_r, energy) order, to
-// sm.Fz / sm.Fr and raises smax to the largest wave speed of the faces that
-// belong to at least one updated cell.  Exact-solver faces of patterns 2
-// and 3 go to the queue instead.
-template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF, typename S>
-__device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0, int step,
-                                         bool interior, RiemannCount& rc, int& fallback, R& smax, int a, int c)
+// Whether face (a, c) of orientation ZF belongs to an updated cell
+// (active: its wave speed counts for dt) and lies in the high-order region
+// (hi).  ZF: z faces (between tile columns c-1 and c of row a), else r
+// faces (between tile rows a-1 and a of column c).
+template <int TZ, int TR, bool ZF, typename S>
+__device__ __forceinline__ void face_meta(const StepParams& P, const S& sm, int n0, int m0, bool interior, int a,
+                                          int c, bool& active, bool& hi)
+{
+    // smem indices of the lower (l) and upper (u) cell of the face
+    const int jl = ZF ? a + 2 : a + 1, il = ZF ? c + 1 : c + 2;
+    const int ju = a + 2, iu = c + 2;
+    // both cells inside the grid (always so in an interior tile)
+    bool lval = true, uval = true;
+    if (!interior) {
+        const int nl = n0 + il - 2, ml = m0 + jl - 2, nu = n0 + iu - 2, mu = m0 + ju - 2;
+        lval = nl >= 0 && nl < P.N && ml >= 0 && ml < P.M;
+        uval = nu >= 0 && nu < P.N && mu >= 0 && mu < P.M;
+    }
+    active = lval || uval;
+    if (active && P.fixed_region) active = (lval && !sm.fx[jl][il]) || (uval && !sm.fx[ju][iu]);
+    hi = true;
+    if (P.region_select) {
+        // the face's z position as the reference's lower cell sees it, as an
+        // interval of that cell's column (integer compares: an FP64 position
+        // test here ran on every face, region or not)
+        const int nl = n0 + il - 2;
+        hi = ZF ? (nl >= P.region_zlo && nl <= P.region_zhi) : (nl >= P.region_rlo && nl <= P.region_rhi);
+    }
+}
+
+// The flux of face (a, c) from its reconstructed states L (lower cell) and U
+// (upper cell): written, in (mass, mom_z, mom_r, energy) order, to sm.Fz /
+// sm.Fr, and smax raised to its wave speed when the face is active.
+// Exact-solver faces of patterns 2 and 3 go to the queue instead.
+template <typename R, int FLUX, int TZ, int TR, bool ZF, typename S>
+__device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<R>& g, int a, int c, bool active,
+                                          bool hi, const R L[4], const R U[4], RiemannCount& rc, R& smax)
 {
     constexpr int NFZ = TR * (TZ + 1);
     constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
     constexpr int NN = ZF ? 2 : 3;           // normal velocity component
     constexpr int TT = ZF ? 3 : 2;           // tangential velocity component
-    {
-        // smem indices of the lower (l) and upper (u) cell of the face
-        const int jl = ZF ? a + 2 : a + 1, il = ZF ? c + 1 : c + 2;
-        const int ju = a + 2, iu = c + 2;
-        // both cells inside the grid (always so in an interior tile)
-        bool lval = true, uval = true;
-        if (!interior) {
-            const int nl = n0 + il - 2, ml = m0 + jl - 2, nu = n0 + iu - 2, mu = m0 + ju - 2;
-            lval = nl >= 0 && nl < P.N && ml >= 0 && ml < P.M;
-            uval = nu >= 0 && nu < P.N && mu >= 0 && mu < P.M;
-        }
-        bool active = lval || uval;
-        if (active && P.fixed_region) active = (lval && !sm.fx[jl][il]) || (uval && !sm.fx[ju][iu]);
-        bool hi = true;
-        if (P.region_select) {
-            // the face's z position as the reference's lower cell sees it,
-            // as an interval of that cell's column (integer compares: an
-            // FP64 position test here ran on every face, region or not)
-            const int nl = n0 + il - 2;
-            hi = ZF ? (nl >= P.region_zlo && nl <= P.region_zhi) : (nl >= P.region_rlo && nl <= P.region_rhi);
-        }
-        R L[4], U[4], F[4];
-        face_states<R, RECON, ZF>(P, sm, b, a, c, hi, L, U);
-        R Sp;
-        if constexpr (FLUX == 2) {
+    R F[4];
+    R Sp;
+    if constexpr (FLUX == 2) {
         if (hi && L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]) {
             // identical states: the exact solution is that state (the
             // reference reaches it through the two-rarefaction branch with
             // p* = p, u* = u_n, up to rounding), its flux the physical flux
             // and its largest wave speed |u_n| + c
             const R r = L[0], p = L[1], un = L[NN], ut = L[TT];
-            const R c = sqrt(g.ga * p / r);
+            const R cs = sqrt(g.ga * p / r);
             const R m = r * un;
             F[0] = m;
             F[1] = m * un + p;
             F[2] = m * ut;
             F[3] = un * (p * g.inv_g1 + R(0.5) * r * (un * un + ut * ut) + p);
-            Sp = fmax(fabs(un) + c, g.eps8);
+            Sp = fmax(fabs(un) + cs, g.eps8);
         } else if (hi) {
             const RPre<R> q = godunov_pre(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT]);
             if (q.pattern == 2 || q.pattern == 3) {
@@ -573,59 +579,174 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
         } else {
             Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         }
-        } else if constexpr (FLUX == 1) {
-            if (hi) Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
-            else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
-        } else if constexpr (FLUX == 3) {
-            if (hi) Sp = flux_hllc_a(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
-            else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+    } else if constexpr (FLUX == 1) {
+        if (hi) Sp = flux_hllc(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+        else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+    } else if constexpr (FLUX == 3) {
+        if (hi) Sp = flux_hllc_a(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+        else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+    } else {
+        Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+    }
+    if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
+    if (ZF) {
+        put4(sm.Fz[a][c], F[0], F[1], F[2], F[3]);
+    } else {
+        // r face: the normal momentum is mom_r, the tangential one mom_z
+        put4(sm.Fr[a][c], F[0], F[2], F[1], F[3]);
+    }
+    if (active) smax = fmax(smax, Sp);
+}
+
+// Two adjacent faces of orientation ZF in one thread: (a, c) and the next
+// one along the normal ((a, c + 1) for z faces, (a + 1, c) for r faces), or
+// (a, c) alone when !two.  The five staged cells along the normal (the
+// first face's lower cell's lower neighbour .. the second face's upper
+// cell's upper neighbour) give the slopes of the three middle cells, each
+// once, so the cell between the two faces is reconstructed once for both
+// (minmod, linear2 and the positivity rule as face_states applies them, the
+// same values).  Z faces take c even and load the cells as aligned pairs.
+template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF, typename S>
+__device__ __forceinline__ void face_two(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
+                                         bool interior, RiemannCount& rc, R& smax, int a, int c, bool two)
+{
+    constexpr int QX = S::QX, HR = S::HR;
+    using R2 = std::conditional_t<sizeof(R) == 4, float2, double2>;
+    const int a1 = ZF ? a : a + 1, c1 = ZF ? c + 1 : c;
+    bool act0, hi0, act1 = false, hi1 = true;
+    face_meta<TZ, TR, ZF>(P, sm, n0, m0, interior, a, c, act0, hi0);
+    if (two) face_meta<TZ, TR, ZF>(P, sm, n0, m0, interior, a1, c1, act1, hi1);
+    R L0[4], U0[4], L1[4], U1[4];
+    const auto& q = sm.qb[b];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        R v[5];
+        if constexpr (ZF) {
+            // row a, columns c-2 .. c+2 (smem columns c+QX .. c+QX+4, c+QX even)
+            const R2 p0 = *reinterpret_cast<const R2*>(&q[k][a + 2][c + QX]);
+            const R2 p1 = *reinterpret_cast<const R2*>(&q[k][a + 2][c + QX + 2]);
+            const R2 p2 = *reinterpret_cast<const R2*>(&q[k][a + 2][c + QX + 4]);
+            v[0] = p0.x; v[1] = p0.y; v[2] = p1.x; v[3] = p1.y; v[4] = p2.x;
         } else {
-            Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+            // column c, rows a-2 .. a+2 (smem rows a .. a+4; the last
+            // clamped into the buffer for a single face at the tile's top)
+            v[0] = q[k][a][c + 2 + QX];
+            v[1] = q[k][a + 1][c + 2 + QX];
+            v[2] = q[k][a + 2][c + 2 + QX];
+            v[3] = q[k][a + 3][c + 2 + QX];
+            v[4] = q[k][min(a + 4, HR - 1)][c + 2 + QX];
         }
-        if (!(Sp == Sp)) { rc.status |= 0x10u; Sp = R(0); }
-        if (ZF) {
-            put4(sm.Fz[a][c], F[0], F[1], F[2], F[3]);
-        } else {
-            // r face: the normal momentum is mom_r, the tangential one mom_z
-            put4(sm.Fr[a][c], F[0], F[2], F[1], F[3]);
+        L0[k] = v[1]; U0[k] = v[2]; L1[k] = v[2]; U1[k] = v[3];
+        if (RECON) {
+            R x0, x1, y0, y1, z0, z1;
+            recon_pair(v[0], v[1], v[2], x0, x1);   // lower cell of the first face
+            recon_pair(v[1], v[2], v[3], y0, y1);   // the cell between the faces
+            recon_pair(v[2], v[3], v[4], z0, z1);   // upper cell of the second face
+            if (hi0) { L0[k] = x1; U0[k] = y0; }
+            if (hi1) { L1[k] = y1; U1[k] = z0; }
+            // positivity of the reconstructed rho and p (kernel.cu:2706-2743)
+            if (k == 0) {
+                if (L0[0] <= R(0)) L0[0] = v[1];
+                if (U0[0] <= R(0)) U0[0] = v[2];
+                if (L1[0] <= R(0)) L1[0] = v[2];
+                if (U1[0] <= R(0)) U1[0] = v[3];
+            } else if (k == 1) {
+                if (L0[1] <= R(0) || !P.grad_p) L0[1] = v[1];
+                if (U0[1] <= R(0) || !P.grad_p) U0[1] = v[2];
+                if (L1[1] <= R(0) || !P.grad_p) L1[1] = v[2];
+                if (U1[1] <= R(0) || !P.grad_p) U1[1] = v[3];
+            }
         }
-        if (active) smax = fmax(smax, Sp);
+    }
+    // one flux call site for both faces (a smaller kernel)
+#pragma unroll 1
+    for (int s = 0; s < (two ? 2 : 1); s++) {
+        face_flux<R, FLUX, TZ, TR, ZF>(P, sm, g, s ? a1 : a, s ? c1 : c, s ? act1 : act0, s ? hi1 : hi0, L0, U0, rc,
+                                       smax);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            L0[k] = L1[k];
+            U0[k] = U1[k];
+        }
     }
 }
 
-// every face of the tile once, in one loop over the CTA's threads: first
-// the z faces c = 0 .. TZ-1 of each row (a warp per row when TZ = 32, so the
-// warp's staged-cell loads hit distinct banks), then the last z face
-// (c = TZ) of every row, then the r faces; each group padded to whole warps
-// so that no warp mixes groups
+// Face (a, c) of orientation ZF alone: its states by face_states (the
+// exact solver's face pass; its kernel is large enough that the two-face
+// form's extra code costs more in instruction fetch than it saves).
+template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF, typename S>
+__device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
+                                         bool interior, RiemannCount& rc, R& smax, int a, int c)
+{
+    bool active, hi;
+    face_meta<TZ, TR, ZF>(P, sm, n0, m0, interior, a, c, active, hi);
+    R L[4], U[4];
+    face_states<R, RECON, ZF>(P, sm, b, a, c, hi, L, U);
+    face_flux<R, FLUX, TZ, TR, ZF>(P, sm, g, a, c, active, hi, L, U, rc, smax);
+}
+
+// every face of the tile once, in one loop over the CTA's threads.
+// HLL / HLLC / HLLC_A: two adjacent faces per thread, first the z face
+// pairs (c, c+1 for even c < TZ) of every row, then the r face pairs (rows
+// a, a+1 for even a < TR) of every column, then the single faces left: the
+// r faces of row TR and the z faces c = TZ (those last go to the first
+// warps; the last warp holds the copy thread of the persistent kernel).
+// Exact Godunov: one face per thread, the z faces c < TZ of each row (a warp
+// per row when TZ = 32, so the warp's staged-cell loads hit distinct
+// banks), then the last z face (c = TZ) of every row, then the r faces; each
+// group padded to whole warps so that no warp mixes groups.
 template <typename R, int FLUX, bool RECON, int TZ, int TR, typename S>
 __device__ __forceinline__ void face_pass(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
                                           int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
 {
-    constexpr int NZM = TR * TZ;                               // z faces c < TZ
-    constexpr int NZMP = (NZM + 31) / 32 * 32;
-    constexpr int NZL = NZMP + TR, NZLP = NZMP + (TR + 31) / 32 * 32;   // + the last z face of each row
-    constexpr int NFR = (TR + 1) * TZ;
     // every cell the tile's faces touch lies inside the grid
     const bool interior = n0 >= 1 && n0 + TZ < P.N && m0 >= 1 && m0 + TR < P.M;
-    for (int t = threadIdx.x; t < NZLP + NFR; t += kThreads) {
-        if (t < NZLP) {
-            // one call site for both z groups (a smaller kernel)
-            int a, c;
-            if (t < NZM) {
-                a = t / TZ;
-                c = t - a * TZ;
-            } else if (t >= NZMP && t < NZL) {
-                a = t - NZMP;
-                c = TZ;
-            } else {
-                continue;
+    if constexpr (FLUX != 2) {
+        static_assert(TZ % 2 == 0 && TR % 2 == 0, "faces in pairs");
+        constexpr int NZP = TR * (TZ / 2);          // z face pairs
+        constexpr int NP = NZP + (TR / 2) * TZ;     // + r face pairs
+        constexpr int TZP = (TZ + 31) / 32 * 32;    // r faces of row TR, padded to whole warps
+        static_assert(NZP % 32 == 0 && NP % 32 == 0, "no warp mixes groups");
+        for (int t = threadIdx.x; t < NP + TZP + TR; t += kThreads) {
+            if (t < NZP) {
+                const int a = t / (TZ / 2);
+                face_two<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, interior, rc, smz, a,
+                                                       2 * (t - a * (TZ / 2)), true);
+            } else if (t < NP) {
+                const int u = t - NZP, a = u / TZ;
+                face_two<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, interior, rc, smr, 2 * a, u - a * TZ,
+                                                        true);
+            } else if (t < NP + TZ) {
+                face_two<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, interior, rc, smr, TR, t - NP, false);
+            } else if (t >= NP + TZP) {
+                face_two<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, interior, rc, smz, t - NP - TZP, TZ,
+                                                       false);
             }
-            face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smz, a, c);
-        } else {
-            const int a = (t - NZLP) / TZ;
-            face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, step, interior, rc, fallback, smr, a,
-                                                    t - NZLP - a * TZ);
+        }
+    } else {
+        constexpr int NZM = TR * TZ;                               // z faces c < TZ
+        constexpr int NZMP = (NZM + 31) / 32 * 32;
+        constexpr int NZL = NZMP + TR, NZLP = NZMP + (TR + 31) / 32 * 32;   // + the last z face of each row
+        constexpr int NFR = (TR + 1) * TZ;
+        for (int t = threadIdx.x; t < NZLP + NFR; t += kThreads) {
+            if (t < NZLP) {
+                // one call site for both z groups (a smaller kernel)
+                int a, c;
+                if (t < NZM) {
+                    a = t / TZ;
+                    c = t - a * TZ;
+                } else if (t >= NZMP && t < NZL) {
+                    a = t - NZMP;
+                    c = TZ;
+                } else {
+                    continue;
+                }
+                face_one<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, interior, rc, smz, a, c);
+            } else {
+                const int a = (t - NZLP) / TZ;
+                face_one<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, interior, rc, smr, a,
+                                                        t - NZLP - a * TZ);
+            }
         }
     }
 }
