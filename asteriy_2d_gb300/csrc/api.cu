@@ -493,6 +493,7 @@ int ast_record_start(ast_solver* S, int64_t capacity, int every, double min_stre
 {
     if (!S || capacity < 1 || every < 1) return fail(AST_ERR_INVALID, "bad argument");
     if (S->cfg.flux != AST_FLUX_GODUNOV) return fail(AST_ERR_UNSUPPORTED, "the recorder needs the exact solver");
+    if (S->cfg.precision != AST_PREC_FP64) return fail(AST_ERR_UNSUPPORTED, "the recorder runs on the FP64 solver");
     cudaFree(S->rec);
     S->rec = nullptr;
     if (!S->rec_n) AST_CUDA(cudaMalloc(&S->rec_n, sizeof(unsigned long long)));

@@ -423,7 +423,11 @@ template <typename R>
 __device__ __forceinline__ R solve_queued(const StepParams& P, const Gas<R>& g, const RPre<R>& q, bool strong,
                                           R p0_mlp, RiemannCount& rc, int& fallback)
 {
-    if (!P.riemann_newton) return solve_p_reference(g, q, rc);
+    // the reference's own iteration (FP64 only: the FP32 form always runs
+    // the safeguarded Newton, and its kernels leave this code out)
+    if constexpr (sizeof(R) == 8) {
+        if (!P.riemann_newton) return solve_p_reference(g, q, rc);
+    }
     R p0;
     if (P.guess == 1 && strong) {
         p0 = p0_mlp;
@@ -852,8 +856,12 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, co
             put4(sm.Fr[a][c], F[0], F[2], F[1], F[3]);
             if (active) smr = fmax(smr, Sp);
         }
-        if (P.rec && step % P.rec_every == 0)
-            record_face(P, g, q, p, step, 2 * ((m0 + a) * P.N + (n0 + c)) + (zf ? 0 : 1));
+        // the recorder runs on the FP64 solver only (its records are training
+        // targets; the FP32 kernels are smaller without it)
+        if constexpr (sizeof(R) == 8) {
+            if (P.rec && step % P.rec_every == 0)
+                record_face(P, g, q, p, step, 2 * ((m0 + a) * P.N + (n0 + c)) + (zf ? 0 : 1));
+        }
     }
 }
 

@@ -236,7 +236,9 @@ int ast_probe(ast_solver* solver, const int64_t* cells, int n, double* rho, doub
    all) is written as one record of AST_RECORD_FLOATS floats, up to
    `capacity` records (device buffer owned by the solver).  ast_record_stop
    returns the number of faces offered, which may exceed the capacity;
-   ast_record_read copies min(n, stored) records. */
+   ast_record_read copies min(n, stored) records.  FP64 exact-Godunov
+   solvers only (the records are training targets of the learned start
+   value); other solvers return AST_ERR_UNSUPPORTED. */
 int ast_record_start(ast_solver* solver, int64_t capacity, int every, double min_strength);
 int ast_record_stop(ast_solver* solver, int64_t* offered);
 int ast_record_read(ast_solver* solver, float* out, int64_t n);

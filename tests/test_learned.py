@@ -70,3 +70,14 @@ def test_recorder_trainer_and_learned_guess():
     for s in (sp, sm):
         l1 = np.sum(np.abs(s[:, 0] - os_[:, 0])) / np.sum(np.abs(os_[:, 0]))
         assert l1 < 1e-4, l1
+
+
+def test_recorder_is_fp64_only():
+    # the recorder's records are training targets: FP64 exact-solver
+    # solvers only; FP32 and HLL solvers refuse it
+    for prec, flux in ((A.PREC_FP32, A.FLUX_GODUNOV), (A.PREC_FP64, A.FLUX_HLL)):
+        cfg = problems.blast_config(64, 32, flux=flux, precision=prec)
+        with solver.Solver(cfg) as S:
+            with pytest.raises(solver.AstError) as e:
+                S.record_start(1024)
+            assert e.value.code == A.AST_ERR_UNSUPPORTED
