@@ -1082,8 +1082,12 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
     // near-axis cell, its whole update; bit 2 it + 1: the FP64 pressure
     // recovery of a cell whose kinetic energy is above 99% of the total)
     unsigned deferred = 0u;
-    int it = 0;
-    for (int cidx = threadIdx.x; cidx < TZ * TR; cidx += kThreads, it++) {
+    // a fixed number of cells per thread (the loop unrolls; the uniform
+    // tests and the index arithmetic are shared by the thread's cells)
+    static_assert((TZ * TR) % kThreads == 0, "whole cells per thread");
+#pragma unroll
+    for (int it = 0; it < (TZ * TR) / kThreads; it++) {
+        const int cidx = (int)threadIdx.x + it * kThreads;
         const int row = cidx / TZ, col = cidx - row * TZ;
         const int n = n0 + col, m = m0 + row;
         if (n >= P.N || m >= P.M) continue;
@@ -1114,8 +1118,8 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
     if constexpr (sizeof(R) == 4) {
         static_assert(TO_SMEM || LAYOUT == kSoA, "FP32 state is SoA planes");
         if (deferred) {
-            it = 0;
-            for (int cidx = threadIdx.x; cidx < TZ * TR; cidx += kThreads, it++) {
+            for (int it = 0; it < (TZ * TR) / kThreads; it++) {
+                const int cidx = (int)threadIdx.x + it * kThreads;
                 const unsigned d = (deferred >> (2 * it)) & 3u;
                 if (!d) continue;
                 const int row = cidx / TZ, col = cidx - row * TZ;
