@@ -73,6 +73,7 @@ int ast_config_check(const ast_config* c)
     if (c->precision < AST_PREC_FP64 || c->precision > AST_PREC_FP32) return AST_ERR_INVALID;
     if (c->guess < AST_GUESS_PVRS || c->guess > AST_GUESS_MLP) return AST_ERR_INVALID;
     if (c->persistent < 0 || c->persistent > 1) return AST_ERR_INVALID;
+    if (c->skip_uniform < 0 || c->skip_uniform > 1) return AST_ERR_INVALID;
     if (!(c->inflow_p >= 0.0)) return AST_ERR_INVALID;
     for (int s = 0; s < 4; s++) {
         if (c->bc[s].kind < AST_BC_REFLECT || c->bc[s].kind > AST_BC_NONREFLECT) return AST_ERR_INVALID;

@@ -231,6 +231,7 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
         P.fixed_mhi = clampi(std::ceil((c.fixed_ar - P.y_min) / P.dy) + 1.0);
     }
     P.region_select = c.region_select;
+    P.skip_uniform = c.skip_uniform;
     {
         // columns whose face positions pass the reference's region test
         // lo < x < hi (x = x_min + n dx, plus dx/2 for the z face above the

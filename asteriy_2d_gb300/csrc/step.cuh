@@ -68,6 +68,7 @@ struct __align__(16) StepParams {
     double fixed_zc, fixed_az2, fixed_ar2;
     int fixed_nlo, fixed_nhi, fixed_mhi;   // cells that can lie in the region (one cell of margin)
     int region_select;
+    int skip_uniform;              // uniform tiles skip the face pass
     // the high-order region as column intervals (found on the host from
     // the reference's FP64 face positions): z faces whose lower cell's
     // column lies in [region_zlo, region_zhi], r faces of the columns in
@@ -992,6 +993,64 @@ __device__ __forceinline__ void patch_tile(const StepParams& P, S& sm, int b, in
     }
 }
 
+// The wave speed and flux of a face whose two sides hold the state
+// (r, p, un, ut) (face frame), as face_flux finds them for identical states
+// in the high-order region: the exact solver's identical-state branch, the
+// HLL-family functions themselves.
+template <typename R, int FLUX>
+__device__ __forceinline__ R uniform_face(const Gas<R>& g, R r, R p, R un, R ut, R F[4])
+{
+    if constexpr (FLUX == 2) {
+        const R cs = sqrt(g.ga * p / r);
+        const R m = r * un;
+        F[0] = m;
+        F[1] = m * un + p;
+        F[2] = m * ut;
+        F[3] = un * (p * g.inv_g1 + R(0.5) * r * (un * un + ut * ut) + p);
+        return fmax(fabs(un) + cs, g.eps8);
+    } else if constexpr (FLUX == 1) {
+        return flux_hllc(g, r, p, un, ut, r, p, un, ut, F);
+    } else if constexpr (FLUX == 3) {
+        return flux_hllc_a(g, r, p, un, ut, r, p, un, ut, F);
+    } else {
+        return flux_hll(g, r, p, un, ut, r, p, un, ut, F);
+    }
+}
+
+// A uniform tile (skip_uniform): every staged cell a face of the tile reads
+// (the tile's rows over the full halo width, its columns over the full halo
+// height, ghost cells included) holds the bits of tile cell (0, 0), and the
+// flux of that state is finite.  Then every face of one orientation has the
+// same flux, the update's flux differences are exactly zero, and only the
+// wave speeds of the two orientations are needed: returned in sz / sr
+// (valid in thread 0).  A barrier: called by all threads.
+template <typename R, int FLUX, int TZ, int TR, typename S>
+__device__ __forceinline__ bool tile_uniform(const S& sm, int b, const Gas<R>& g, R& sz, R& sr)
+{
+    constexpr int HZ = S::HZ, HR = S::HR, QX = S::QX;
+    using U = std::conditional_t<sizeof(R) == 4, unsigned int, unsigned long long>;
+    const auto& q = sm.qb[b];
+    auto bits = [](R v) { return *reinterpret_cast<const U*>(&v); };
+    const R s0 = q[0][2][2 + QX], s1 = q[1][2][2 + QX], s2 = q[2][2][2 + QX], s3 = q[3][2][2 + QX];
+    const U r0 = bits(s0), r1 = bits(s1), r2 = bits(s2), r3 = bits(s3);
+    bool same = true;
+    for (int idx = threadIdx.x; idx < HR * HZ; idx += kThreads) {
+        const int j = idx / HZ, i = idx - j * HZ;
+        const bool rin = (j >= 2 && j < TR + 2), cin = (i >= 2 && i < TZ + 2);
+        if (!rin && !cin) continue;   // the corners: read by no face
+        same = same && bits(q[0][j][i + QX]) == r0 && bits(q[1][j][i + QX]) == r1 && bits(q[2][j][i + QX]) == r2 &&
+               bits(q[3][j][i + QX]) == r3;
+    }
+    if (threadIdx.x == 0) {
+        R F[4], G[4];
+        sz = uniform_face<R, FLUX>(g, s0, s1, s2, s3, F);   // z faces: normal v_z
+        sr = uniform_face<R, FLUX>(g, s0, s1, s3, s2, G);   // r faces: normal v_r
+        for (int k = 0; k < 4; k++) same = same && isfinite(F[k]) && isfinite(G[k]);
+        same = same && isfinite(sz) && isfinite(sr);
+    }
+    return __syncthreads_and(same);
+}
+
 // faces, exact-solver queue and conservative update of the tile staged in
 // buffer b.  TO_SMEM: the updated cells go to sm.out (for a bulk store)
 // instead of global memory.  Ends without a barrier.
@@ -1008,7 +1067,25 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
         sm.ydrow[threadIdx.x] = P.y_min + m * P.dy;
         sm.yfrow[threadIdx.x] = P.y_minf + (float)m * P.dyf;
     }
-    face_pass<R, FLUX, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
+    R sz, sr;
+    if (P.skip_uniform && !P.region_select && !tile_near_fixed<TZ, TR>(P, n0, m0) &&
+        tile_uniform<R, FLUX, TZ, TR>(sm, b, g, sz, sr)) {
+        // zero fluxes (the same flux on every face of an orientation: its
+        // differences are exactly zero) and the two wave speeds
+        constexpr int NF4 = (TR * (TZ + 1) + (TR + 1) * TZ) * 4;
+        R* fz = &sm.Fz[0][0][0];
+        R* fr = &sm.Fr[0][0][0];
+        for (int w = threadIdx.x; w < NF4 / 4; w += kThreads) {
+            R* d = (w < TR * (TZ + 1)) ? fz + 4 * w : fr + 4 * (w - TR * (TZ + 1));
+            put4(d, R(0), R(0), R(0), R(0));
+        }
+        if (threadIdx.x == 0) {
+            acc.smz = fmax(acc.smz, sz);
+            acc.smr = fmax(acc.smr, sr);
+        }
+    } else {
+        face_pass<R, FLUX, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
+    }
     // persistent kernel: the previous tile's bulk store, issued by the copy
     // thread at the start of this face pass, has read sm.out before anything
     // overwrites it (the network's space in the queue phase, then the update)

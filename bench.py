@@ -10,6 +10,9 @@ Forms measured (each from the same initial state, warm-up steps first):
   fp64_godunov   plain FP64 path (the reference's solver; the oracle-comparable form)
   fp32_pvrs      FP32 form, Newton for p* from the acoustic (PVRS-type) start value
   fp32_learned   FP32 form, Newton from the learned start value (the headline)
+  fp32_learned_skip  the same with skip_uniform = 1: tiles whose staged cells are
+                 all bit-identical skip the face pass (identical results, checked
+                 bit for bit against fp32_learned; not the headline)
 The FP32 forms report their density and pressure L1 error against the FP64
 run after the same steps, and Newton statistics (mean/max iterations,
 fallback rate).  The headline `value` is the form named in config.form.
@@ -130,7 +133,7 @@ class ClockSampler:
 # Newton tolerance 1e-8 (clamped to 4 ulps of FP32)
 # (the HLL pair is the precision form of the small config's flux at full
 # size, timed for its own rate and %HBM)
-FORMS = ("fp64_godunov", "fp32_pvrs", "fp32_learned", "fp64_hll", "fp32_hll")
+FORMS = ("fp64_godunov", "fp32_pvrs", "fp32_learned", "fp32_learned_skip", "fp64_hll", "fp32_hll")
 
 
 def make_config(form):
@@ -142,7 +145,8 @@ def make_config(form):
     cfg.persistent = PERSISTENT
     if prec == A.PREC_FP32:
         cfg.riemann_tol = 1e-8
-        cfg.guess = A.GUESS_MLP if form == "fp32_learned" else A.GUESS_PVRS
+        cfg.guess = A.GUESS_MLP if form.startswith("fp32_learned") else A.GUESS_PVRS
+        cfg.skip_uniform = 1 if form.endswith("_skip") else 0
     return cfg
 
 
@@ -514,7 +518,7 @@ def main():
     s0, u0 = solver.fill_blast(cfg)
     cells = cfg.N * cfg.M
     params, params_src = (None, None)
-    if "fp32_learned" in ((args.form,) if args.no_forms else FORMS) or args.accuracy_steps:
+    if any(f.startswith("fp32_learned") for f in ((args.form,) if args.no_forms else FORMS)) or args.accuracy_steps:
         params, params_src = learned_params(s0, u0)
     # the timing window starts mid-run: the blast advanced start_step steps
     # from t = 0 (with the FP32 form, which is fast), the same start for all
@@ -528,7 +532,8 @@ def main():
         if form == args.form or args.no_forms:
             continue
         sec, s, u, st = time_form(form, start, args.steps, args.warmup, torch,
-                                  params if form == "fp32_learned" else None, stats_steps=0 if args.no_stats else 5)
+                                  params if form.startswith("fp32_learned") else None,
+                                  stats_steps=0 if args.no_stats else 5)
         forms[form] = {"value": cells * args.steps / sec, "ms_per_step": sec * 1e3 / args.steps}
         pf = "fp64" if form.startswith("fp64") else "fp32"
         forms[form]["hbm_frac"] = BYTES_PER_CELL[pf] * cells / (sec / args.steps) / 1e9 / peaks()[0]
@@ -544,7 +549,7 @@ def main():
     sampler = ClockSampler(local)
     sampler.start()
     sec, s, u, st = time_form(args.form, start, args.steps, args.warmup, torch,
-                              params if args.form == "fp32_learned" else None,
+                              params if args.form.startswith("fp32_learned") else None,
                               stats_steps=0 if args.no_stats else 5, sampler=sampler)
     clocks = sampler.stop()
     if ws > 1:
@@ -562,7 +567,8 @@ def main():
                                      "gated_mean_iters": st["strong_iters"] / max(1, st["strong_calls"])}
     # density / pressure L1 error of the FP32 forms against the FP64 run over
     # the timed window (same start, same steps)
-    for ref_form, pair in (("fp64_godunov", ("fp32_pvrs", "fp32_learned")), ("fp64_hll", ("fp32_hll",))):
+    for ref_form, pair in (("fp64_godunov", ("fp32_pvrs", "fp32_learned", "fp32_learned_skip")),
+                           ("fp64_hll", ("fp32_hll",))):
         if ref_form not in finals:
             continue
         ref = finals[ref_form]
@@ -575,7 +581,11 @@ def main():
         forms[args.form]["speedup_vs_fp64"] = forms[args.form]["value"] / forms["fp64_godunov"]["value"]
 
     e2e_steps = max(3, min(args.steps // 4, 50))
-    esec, bi, bo = time_e2e(args.form, start, e2e_steps, torch, params if args.form == "fp32_learned" else None)
+    if "fp32_learned_skip" in finals and "fp32_learned" in finals:
+        forms["fp32_learned_skip"]["bitwise_equal_to_fp32_learned"] = bool(
+            np.array_equal(finals["fp32_learned_skip"], finals["fp32_learned"]))
+    esec, bi, bo = time_e2e(args.form, start, e2e_steps, torch,
+                            params if args.form.startswith("fp32_learned") else None)
     hbm, src = peaks()
     prec = "fp64" if args.form.startswith("fp64") else "fp32"
     achieved = BYTES_PER_CELL[prec] * cells / (sec / args.steps) / 1e9

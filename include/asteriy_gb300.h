@@ -141,7 +141,16 @@ typedef struct ast_config {
        Same results; the FP64 solver and the raw entry points always use one
        CTA per tile (default 1)                                              */
     int32_t persistent;
-    int32_t reserved_i[5];
+    /* 1: tiles whose staged cells (tile and two-cell halo, ghosts included)
+       all hold the same four values, bit for bit, skip the face pass: every
+       face of such a tile has the same flux, so the flux differences of the
+       update are exactly zero, and the update runs on zero fluxes; the wave
+       speeds come from one face of each orientation.  The results are
+       identical to the full computation.  Tiles near the fixed region, runs
+       with region_select, and uniform states whose flux is not finite take
+       the full path (default 0)                                             */
+    int32_t skip_uniform;
+    int32_t reserved_i[4];
     /* wave strength above which the learned start value is used:
        max(|ln(p_R/p_L)|, |u_R - u_L| / min(c_L, c_R)); weaker faces start
        from the acoustic value, which is already close for them (0.2)        */

@@ -49,7 +49,8 @@ def test_config_default_matches_reference_macros():
 
 
 @pytest.mark.parametrize("field,value", [("N", 2), ("M", 0), ("gamma", 1.0), ("cfl", 0.0), ("flux", 7),
-                                         ("riemann_max_iter", 0), ("x_max", -5.0)])
+                                         ("riemann_max_iter", 0), ("x_max", -5.0),
+                                         ("persistent", 2), ("skip_uniform", 2), ("skip_uniform", -1)])
 def test_config_check_rejects(field, value):
     c = problems.blast_config(64, 32)
     setattr(c, field, value)
