@@ -238,6 +238,41 @@ int ast_set_stream(ast_solver* S, void* stream)
     return AST_OK;
 }
 
+// The device address of the host range [p, p + bytes) when the GPU can
+// read and write it in place: page-locked host memory (over NVLink-C2C on
+// GB300), the whole range inside one allocation.  Otherwise nullptr, and
+// the caller copies through its device staging buffers.
+static void* host_range_on_device(const void* p, size_t bytes)
+{
+    using GetAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+    static GetAttr get = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        looked = true;
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 4000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get = reinterpret_cast<GetAttr>(fn);
+        cudaGetLastError();
+    }
+    if (!get) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    const CUdeviceptr d = (CUdeviceptr)a.devicePointer;
+    if (get(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, d) != CUDA_SUCCESS) return nullptr;
+    if (get(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, d) != CUDA_SUCCESS) return nullptr;
+    if (d < start || d + bytes > start + size) return nullptr;
+    return a.devicePointer;
+}
+
 static int convert_in(ast_solver* S, const double* s, const double* u)
 {
     const long long K = (long long)S->cfg.N * S->cfg.M;
@@ -258,6 +293,15 @@ int ast_set_state(ast_solver* S, const double* s, const double* u, int on_device
     if (!S || !s || !u) return fail(AST_ERR_INVALID, "null argument");
     const size_t bytes = (size_t)S->cfg.N * S->cfg.M * 2 * sizeof(double);
     if (on_device) return convert_in(S, s, u);
+    // page-locked host arrays: the conversion kernel reads them in place
+    const void* ds = host_range_on_device(s, bytes);
+    const void* du = ds ? host_range_on_device(u, bytes) : nullptr;
+    if (ds && du) {
+        int rc = convert_in(S, (const double*)ds, (const double*)du);
+        if (rc != AST_OK) return rc;
+        AST_CUDA(cudaStreamSynchronize(S->stream));
+        return AST_OK;
+    }
     AST_CUDA(cudaMemcpyAsync(S->stage_s, s, bytes, cudaMemcpyHostToDevice, S->stream));
     AST_CUDA(cudaMemcpyAsync(S->stage_u, u, bytes, cudaMemcpyHostToDevice, S->stream));
     int rc = convert_in(S, S->stage_s, S->stage_u);
@@ -271,8 +315,13 @@ int ast_get_state(ast_solver* S, double* s, double* u, int on_device)
     if (!S || !s || !u) return fail(AST_ERR_INVALID, "null argument");
     const long long K = (long long)S->cfg.N * S->cfg.M;
     const int nb = (int)((K + 255) / 256);
-    double* ds = on_device ? s : S->stage_s;
-    double* du = on_device ? u : S->stage_u;
+    const size_t bytes = (size_t)K * 2 * sizeof(double);
+    // page-locked host arrays: the conversion kernel writes them in place
+    double* hs = on_device ? nullptr : (double*)host_range_on_device(s, bytes);
+    double* hu = hs ? (double*)host_range_on_device(u, bytes) : nullptr;
+    const bool direct = on_device || (hs && hu);
+    double* ds = on_device ? s : (direct ? hs : S->stage_s);
+    double* du = on_device ? u : (direct ? hu : S->stage_u);
     const void* src = S->buf[S->cur];
     if (S->elem == 8)
         soa_to_aos<double><<<nb, 256, 0, S->stream>>>((const double*)src, (double2*)ds, (double2*)du, S->cfg.N,
@@ -282,9 +331,10 @@ int ast_get_state(ast_solver* S, double* s, double* u, int on_device)
                                                      S->cfg.M, S->ld, S->plane);
     AST_CUDA(cudaGetLastError());
     if (!on_device) {
-        const size_t bytes = (size_t)K * 2 * sizeof(double);
-        AST_CUDA(cudaMemcpyAsync(s, ds, bytes, cudaMemcpyDeviceToHost, S->stream));
-        AST_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, S->stream));
+        if (!direct) {
+            AST_CUDA(cudaMemcpyAsync(s, ds, bytes, cudaMemcpyDeviceToHost, S->stream));
+            AST_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, S->stream));
+        }
         AST_CUDA(cudaStreamSynchronize(S->stream));
     }
     return AST_OK;
