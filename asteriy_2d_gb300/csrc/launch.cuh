@@ -52,12 +52,15 @@ template <int FLUX, bool RECON>
 int launch_tma_t(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int grid, cudaStream_t st,
                  bool launch, int* per_sm)
 {
-    auto k = step_kernel_tma<FLUX, RECON>;
+    // two variants: with the uniform-tile test (skip_uniform) and without it
+    auto k = P.skip_uniform ? step_kernel_tma<FLUX, RECON, true> : step_kernel_tma<FLUX, RECON, false>;
     constexpr size_t smem = tile_smem_bytes<float, FLUX, 32, 16, 2>();
     cudaError_t e;
     if (!launch) {
-        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+        for (auto kv : {step_kernel_tma<FLUX, RECON, true>, step_kernel_tma<FLUX, RECON, false>}) {
+            e = cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+        }
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, kThreads, smem);
         return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     }

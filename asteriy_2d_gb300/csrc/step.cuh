@@ -1054,7 +1054,8 @@ __device__ __forceinline__ bool tile_uniform(const S& sm, int b, const Gas<R>& g
 // faces, exact-solver queue and conservative update of the tile staged in
 // buffer b.  TO_SMEM: the updated cells go to sm.out (for a bulk store)
 // instead of global memory.  Ends without a barrier.
-template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR, bool TO_SMEM, typename S>
+template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR, bool TO_SMEM, bool SKIP = true,
+          typename S>
 __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
                                           const StepConsts& K, TileAcc<R>& acc)
 {
@@ -1067,9 +1068,14 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
         sm.ydrow[threadIdx.x] = P.y_min + m * P.dy;
         sm.yfrow[threadIdx.x] = P.y_minf + (float)m * P.dyf;
     }
+    // SKIP: the kernel carries the uniform-tile test (skip_uniform); the
+    // persistent kernel has a variant without it, so that the default path
+    // holds none of its code
+    bool skipped = false;
     R sz, sr;
-    if (P.skip_uniform && !P.region_select && !tile_near_fixed<TZ, TR>(P, n0, m0) &&
+    if (SKIP && P.skip_uniform && !P.region_select && !tile_near_fixed<TZ, TR>(P, n0, m0) &&
         tile_uniform<R, FLUX, TZ, TR>(sm, b, g, sz, sr)) {
+        skipped = true;
         // zero fluxes (the same flux on every face of an orientation: its
         // differences are exactly zero) and the two wave speeds
         constexpr int NF4 = (TR * (TZ + 1) + (TR + 1) * TZ) * 4;
@@ -1083,9 +1089,9 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
             acc.smz = fmax(acc.smz, sz);
             acc.smr = fmax(acc.smr, sr);
         }
-    } else {
-        face_pass<R, FLUX, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
     }
+    if (!skipped)
+        face_pass<R, FLUX, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
     // persistent kernel: the previous tile's bulk store, issued by the copy
     // thread at the start of this face pass, has read sm.out before anything
     // overwrites it (the network's space in the queue phase, then the update)
@@ -1395,7 +1401,7 @@ __global__ void __launch_bounds__(kThreads, min_ctas<R, FLUX>())
 // wave-speed maxima and counters accumulate over its tiles and are reported
 // once (one ticket per CTA).  A bulk copy that does not arrive within the
 // wait limit sets AST_ST_TIMEOUT and ends the CTA's loop.
-template <int FLUX, bool RECON>
+template <int FLUX, bool RECON, bool SKIP>
 __global__ void __launch_bounds__(kThreads, 4)
     step_kernel_tma(StepParams P, const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout)
 {
@@ -1483,7 +1489,7 @@ __global__ void __launch_bounds__(kThreads, 4)
             s_tile[b] = tnn;
             s_org[b] = make_int2((tnn % tiles_z) * TZ, (tnn / tiles_z) * TR);
         }
-        tile_body<R, FLUX, RECON, kSoA, TZ, TR, true>(P, sm, b, g, n0, m0, sK, acc);
+        tile_body<R, FLUX, RECON, kSoA, TZ, TR, true, SKIP>(P, sm, b, g, n0, m0, sK, acc);
         // this thread's shared-memory writes (sm.out, ghost cells) before
         // the bulk copies that read or overwrite them
         tma::fence_async_shared();
