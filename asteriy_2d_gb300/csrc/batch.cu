@@ -178,7 +178,8 @@ int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool l
             if (rc != AST_OK) return rc;
             BATCH_CUDA(cudaGetDevice(&dev));
             BATCH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            c.grid = std::min(c.tiles[shape], std::max(per_sm, 1) * sms);
+            // tiles go out in chunks of kChunk: no more CTAs than chunks
+            c.grid = std::min((c.tiles[shape] + kChunk - 1) / kChunk, std::max(per_sm, 1) * sms);
             return AST_OK;
         }
         BATCH_CUDA(cudaMemsetAsync(B->counters + ci, 0, sizeof(unsigned int), st));
