@@ -128,6 +128,51 @@ __device__ __forceinline__ R flux_hll(const Gas<R>& g, R rL, R pL, R unL, R utL,
     return S;
 }
 
+// ------------------------------------------------------------------ HLL, two faces in packed FP32
+// Two independent HLL faces (.x and .y) with each add, multiply and fused
+// multiply-add on the pair issued as one packed FP32 instruction (FADD2,
+// FMUL2, FFMA2); divisions, square roots, min/max and the selects stay per
+// element.  The same formula as flux_hll, with the multiply-adds fused
+// explicitly; each element rounds as a scalar evaluation with those fusions.
+__device__ __forceinline__ float2 pk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+
+__device__ __forceinline__ void flux_hll_x2(const Gas<float>& g, float2 rL, float2 pL, float2 unL, float2 utL,
+                                            float2 rR, float2 pR, float2 unR, float2 utR, float2 F[4], float2& S)
+{
+    const float2 ga = pk(g.ga, g.ga), ig1 = pk(g.inv_g1, g.inv_g1), half = pk(0.5f, 0.5f);
+    const float2 gpL = mul2(ga, pL), gpR = mul2(ga, pR);
+    const float2 cL = pk((rL.x <= 0.0f) ? 0.0f : sqrtf(gpL.x / rL.x), (rL.y <= 0.0f) ? 0.0f : sqrtf(gpL.y / rL.y));
+    const float2 cR = pk((rR.x <= 0.0f) ? 0.0f : sqrtf(gpR.x / rR.x), (rR.y <= 0.0f) ? 0.0f : sqrtf(gpR.y / rR.y));
+    const float2 eL = fma2(mul2(rL, fma2(utL, utL, mul2(unL, unL))), half, mul2(pL, ig1));
+    const float2 eR = fma2(mul2(rR, fma2(utR, utR, mul2(unR, unR))), half, mul2(pR, ig1));
+    const float2 mxc = pk(fmaxf(cL.x, cR.x), fmaxf(cL.y, cR.y));
+    const float2 DL = sub2(pk(fminf(unL.x, unR.x), fminf(unL.y, unR.y)), mxc);
+    const float2 DR = add2(pk(fmaxf(unL.x, unR.x), fmaxf(unL.y, unR.y)), mxc);
+    S = pk(fmaxf(fabsf(DL.x), fabsf(DR.x)), fmaxf(fabsf(DL.y), fabsf(DR.y)));
+    const float2 mL = mul2(rL, unL), mR = mul2(rR, unR);
+    const float2 fl1 = fma2(mL, unL, pL), fl2 = mul2(mL, utL), fl3 = mul2(add2(eL, pL), unL);
+    const float2 fr1 = fma2(mR, unR, pR), fr2 = mul2(mR, utR), fr3 = mul2(add2(eR, pR), unR);
+    const float2 d = sub2(DR, DL);
+    const float2 inv = pk(1.0f / d.x, 1.0f / d.y);
+    const float2 dd = mul2(DL, DR);
+    const float2 nDL = mul2(DL, pk(-1.0f, -1.0f));
+    F[0] = mul2(fma2(dd, sub2(rR, rL), fma2(nDL, mR, mul2(DR, mL))), inv);
+    F[1] = mul2(fma2(dd, sub2(mR, mL), fma2(nDL, fr1, mul2(DR, fl1))), inv);
+    F[2] = mul2(fma2(dd, fma2(rR, utR, mul2(mul2(rL, utL), pk(-1.0f, -1.0f))), fma2(nDL, fr2, mul2(DR, fl2))), inv);
+    F[3] = mul2(fma2(dd, sub2(eR, eL), fma2(nDL, fr3, mul2(DR, fl3))), inv);
+    // supersonic faces take one side's physical flux (rare: one branch for both)
+    if (DL.x > 0.0f || DR.x < 0.0f || DL.y > 0.0f || DR.y < 0.0f) {
+        if (DL.x > 0.0f) { F[0].x = mL.x; F[1].x = fl1.x; F[2].x = fl2.x; F[3].x = fl3.x; }
+        else if (DR.x < 0.0f) { F[0].x = mR.x; F[1].x = fr1.x; F[2].x = fr2.x; F[3].x = fr3.x; }
+        if (DL.y > 0.0f) { F[0].y = mL.y; F[1].y = fl1.y; F[2].y = fl2.y; F[3].y = fl3.y; }
+        else if (DR.y < 0.0f) { F[0].y = mR.y; F[1].y = fr1.y; F[2].y = fr2.y; F[3].y = fr3.y; }
+    }
+}
+
 // ------------------------------------------------------------------ HLLC (Aleksashov)
 // The reference's second HLLC (HLLC_Aleksashov, kernel.cu:767-1079), an MHD
 // HLLC solver it calls with zero magnetic field.  In the face frame (normal

@@ -663,15 +663,31 @@ __device__ __forceinline__ void face_two(const StepParams& P, S& sm, int b, cons
             }
         }
     }
-    // one flux call site for both faces (a smaller kernel)
+    if constexpr (FLUX == 0 && sizeof(R) == 4) {
+        // HLL in FP32: both faces in packed arithmetic
+        constexpr int NN = ZF ? 2 : 3, TT = ZF ? 3 : 2;
+        float2 F[4], Sp;
+        flux_hll_x2(g, pk(L0[0], L1[0]), pk(L0[1], L1[1]), pk(L0[NN], L1[NN]), pk(L0[TT], L1[TT]), pk(U0[0], U1[0]),
+                    pk(U0[1], U1[1]), pk(U0[NN], U1[NN]), pk(U0[TT], U1[TT]), F, Sp);
+        auto store = [&](int fa, int fc, bool act, float f0, float f1, float f2, float f3, float sp) {
+            if (!(sp == sp)) { rc.status |= 0x10u; sp = 0.0f; }
+            if (ZF) put4(sm.Fz[fa][fc], f0, f1, f2, f3);
+            else put4(sm.Fr[fa][fc], f0, f2, f1, f3);
+            if (act) smax = fmax(smax, (R)sp);
+        };
+        store(a, c, act0, F[0].x, F[1].x, F[2].x, F[3].x, Sp.x);
+        if (two) store(a1, c1, act1, F[0].y, F[1].y, F[2].y, F[3].y, Sp.y);
+    } else {
+        // one flux call site for both faces (a smaller kernel)
 #pragma unroll 1
-    for (int s = 0; s < (two ? 2 : 1); s++) {
-        face_flux<R, FLUX, TZ, TR, ZF>(P, sm, g, s ? a1 : a, s ? c1 : c, s ? act1 : act0, s ? hi1 : hi0, L0, U0, rc,
-                                       smax);
+        for (int s = 0; s < (two ? 2 : 1); s++) {
+            face_flux<R, FLUX, TZ, TR, ZF>(P, sm, g, s ? a1 : a, s ? c1 : c, s ? act1 : act0, s ? hi1 : hi0, L0, U0,
+                                           rc, smax);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            L0[k] = L1[k];
-            U0[k] = U1[k];
+            for (int k = 0; k < 4; k++) {
+                L0[k] = L1[k];
+                U0[k] = U1[k];
+            }
         }
     }
 }
