@@ -438,6 +438,23 @@ def cpu_baseline(cfg, s0, u0, nsteps, where="the initial state"):
             "sample": f"{nsteps} step(s) of the full {cfg.N}x{cfg.M} grid from {where}, FP64"}
 
 
+def reduce_max(value, torch):
+    """The largest of the ranks' values, on every rank (the value itself
+    without a process group): the slowest rank's time."""
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return value
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.item()
+
+
+def job_rate(ws, units_per_rank, sec):
+    """Whole-job throughput: the units all ranks processed (each rank an
+    independent replica of the same work) over the slowest rank's time."""
+    return ws * units_per_rank / sec
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -569,11 +586,8 @@ def main():
                               params if args.form.startswith("fp32_learned") else None,
                               stats_steps=0 if args.no_stats else 5, sampler=sampler)
     clocks = sampler.stop()
-    if ws > 1:
-        t = torch.tensor([sec], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        sec = t.item()
-    value = ws * cells * args.steps / sec
+    sec = reduce_max(sec, torch)
+    value = job_rate(ws, cells * args.steps, sec)
     forms[args.form] = {"value": cells * args.steps / sec, "ms_per_step": sec * 1e3 / args.steps}
     finals[args.form] = s
     if st and st["newton_calls"]:
