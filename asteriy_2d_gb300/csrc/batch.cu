@@ -178,8 +178,7 @@ int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool l
             if (rc != AST_OK) return rc;
             BATCH_CUDA(cudaGetDevice(&dev));
             BATCH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            // tiles go out in chunks of kChunk: no more CTAs than chunks
-            c.grid = std::min((c.tiles[shape] + kChunk - 1) / kChunk, std::max(per_sm, 1) * sms);
+            c.grid = std::min(c.tiles[shape], std::max(per_sm, 1) * sms);
             return AST_OK;
         }
         BATCH_CUDA(cudaMemsetAsync(B->counters + ci, 0, sizeof(unsigned int), st));
@@ -599,6 +598,9 @@ int ast_batch_synchronize(ast_batch* B)
     BATCH_CUDA(cudaMemcpy(c.data(), B->clocks, sizeof(DevClock) * B->nprob, cudaMemcpyDeviceToHost));
     for (const DevClock& k : c)
         if (k.status & AST_ST_NONFINITE) return set_error(AST_ERR_NUMERIC, "non-finite wave speed");
+    for (const DevClock& k : c) {
+        if (k.status & AST_ST_TIMEOUT) return set_error(AST_ERR_CUDA, "a bulk tile copy did not arrive in time");
+    }
     return AST_OK;
 }
 

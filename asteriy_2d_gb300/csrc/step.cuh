@@ -1524,19 +1524,14 @@ __global__ void __launch_bounds__(kThreads, 4)
 }
 
 // The persistent FP32 kernel of one batch class: tiles of all the class's
-// problems handed out by a counter in chunks of kChunk consecutive tiles of
-// the work list (problems in slot order, each problem's tiles in row-major
-// order), so a CTA's consecutive tiles mostly belong to one problem.  Each
-// tile's box arrives by a bulk-tensor copy through its problem's tensor map
-// while the CTA computes the previous tile, and leaves by a bulk-tensor
-// store; as in step_kernel_tma, one thread of the last warp issues the
-// copies, the store, the counter's atomic and the work-list search at the
-// start of the face pass.  The problem's parameters are copied to shared
-// memory when the problem changes, and the CTA reports to the problem's
-// clock once per run of consecutive tiles of one problem, with one ticket
-// per tile (the problem's last ticket shifts its dt).  The caller zeroes
-// *counter before each launch.
-constexpr int kChunk = 4;
+// problems handed out by a counter (the work list of the class, problems in
+// slot order, each problem's tiles in row-major order); each tile's box
+// arrives by a bulk-tensor copy through its problem's tensor map while the
+// CTA computes the previous tile, and leaves by a bulk-tensor store.  The
+// problem's parameters are copied to shared memory per tile; each tile
+// reports to its problem's clock (one ticket per tile; the problem's last
+// tile shifts that problem's dt).  The caller zeroes *counter before each
+// launch.
 template <int FLUX, bool RECON>
 __global__ void __launch_bounds__(kThreads, 4)
     batch_kernel_tma(const StepParams* __restrict__ Ps, const CUtensorMap* __restrict__ tin,
@@ -1550,143 +1545,89 @@ __global__ void __launch_bounds__(kThreads, 4)
     S& sm = tile_smem<S>();
     __shared__ __align__(16) StepParams sP;
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ int s_tile[2], s_prob[2];   // per buffer: work-list entry and problem
-    __shared__ int2 s_org[2];              // and the tile's origin
-    __shared__ int2 s_pend;                // copy thread: the tile whose cells wait in sm.out
-    __shared__ int s_pend_j;               // and its problem (-1: none)
-    __shared__ int s_cnext, s_cend, s_cprob;   // copy thread: its chunk (next entry, end) and problem
+    __shared__ int s_tile[2], s_prob[2];
+    __shared__ int2 s_org[2];
     __shared__ StepConsts sK;
     const int tid = threadIdx.x;
-    const bool copier = tid == kCopyThread;
     const int total = tile_start[nprob];
-    // copy thread: the CTA's next work-list entry (total when none is left),
-    // its problem and its tile's origin
-    auto schedule = [&](int& t, int& j, int2& org) {
-        if (s_cnext >= s_cend) {
-            const int c0 = (int)atomicAdd(counter, 1u) * kChunk;
-            s_cnext = c0;
-            s_cend = min(c0 + kChunk, total);
-            if (c0 < total) {
-                int lo = 0, hi = nprob - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (tile_start[mid] <= c0) lo = mid; else hi = mid - 1;
-                }
-                s_cprob = lo;
-            }
+    // problem j of work-list entry t and the tile's origin (x0, y0)
+    auto locate = [&](int t, int& j, int& x0, int& y0) {
+        int lo = 0, hi = nprob - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tile_start[mid] <= t) lo = mid; else hi = mid - 1;
         }
-        t = s_cnext;
-        j = 0;
-        org = make_int2(0, 0);
-        if (t >= s_cend) {
-            t = total;
-            return;
-        }
-        s_cnext = t + 1;
-        int jj = s_cprob;
-        while (tile_start[jj + 1] <= t) jj++;   // a chunk can run into the next problem
-        s_cprob = jj;
-        j = jj;
+        j = lo;
         const int tl = t - tile_start[j];
         const int tz = (Ps[j].N + TZ - 1) / TZ;
-        org = make_int2((tl % tz) * TZ, (tl / tz) * TR);
+        x0 = (tl % tz) * TZ;
+        y0 = (tl / tz) * TR;
     };
-    if (copier) {
+    if (tid == 0) {
         tma::mbar_init(&bar[0], 1);
         tma::mbar_init(&bar[1], 1);
         tma::fence_async_shared();
-        s_cnext = s_cend = 0;
-        s_pend_j = -1;
-        for (int q = 0; q < 2; q++) {
-            int t, j;
-            int2 org;
-            schedule(t, j, org);
-            s_tile[q] = t;
-            s_prob[q] = j;
-            s_org[q] = org;
-        }
-        if (s_tile[0] < total) {
+        const int t0 = (int)atomicAdd(counter, 1u);
+        s_tile[0] = t0;
+        if (t0 < total) {
+            int j, x0, y0;
+            locate(t0, j, x0, y0);
+            s_prob[0] = j;
+            s_org[0] = make_int2(x0, y0);
             tma::mbar_expect(&bar[0], kBoxBytes);
-            tma::load_3d(&tin[s_prob[0]], &sm.qb[0][0][0][0], &bar[0], s_org[0].x - 4, s_org[0].y - 2, 0);
+            tma::load_3d(&tin[j], &sm.qb[0][0][0][0], &bar[0], x0 - 4, y0 - 2, 0);
         }
     }
-    __syncthreads();
     TileAcc<R> acc;
-    acc.clear();
-    int cur_j = -1, run = 0;   // the problem whose parameters sP holds; its tiles since the last report
     for (int k = 0;; k++) {
+        // the previous tile is done with sP, the buffers and s_tile / s_prob
+        __syncthreads();
         const int b = k & 1;
         const int t = s_tile[b];
-        const int j = (t < total) ? s_prob[b] : -1;
-        if (j != cur_j) {
-            // the run of the previous problem ends: report it
-            if (cur_j >= 0) {
-                cta_epilogue<R>(sP, acc, (unsigned)(tile_start[cur_j + 1] - tile_start[cur_j]), false,
-                                (unsigned)run);
-                acc.clear();
-                run = 0;
-                cur_j = -1;
+        if (t >= total) break;
+        const int j = s_prob[b];
+        for (int w = tid; w < (int)(sizeof(StepParams) / 16); w += kThreads)
+            reinterpret_cast<int4*>(&sP)[w] = reinterpret_cast<const int4*>(Ps + j)[w];
+        if (tid == 0) {
+            const int tn = (int)atomicAdd(counter, 1u);
+            s_tile[b ^ 1] = tn;
+            if (tn < total) {
+                int jn, x0, y0;
+                locate(tn, jn, x0, y0);
+                s_prob[b ^ 1] = jn;
+                s_org[b ^ 1] = make_int2(x0, y0);
+                tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
+                tma::load_3d(&tin[jn], &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], x0 - 4, y0 - 2, 0);
             }
-            if (t >= total) break;
-            // the new problem's parameters (after every reader of the old
-            // ones, the epilogue's last thread included)
-            __syncthreads();
-            for (int w = tid; w < (int)(sizeof(StepParams) / 16); w += kThreads)
-                reinterpret_cast<int4*>(&sP)[w] = reinterpret_cast<const int4*>(Ps + j)[w];
-            __syncthreads();
-            if (tid == 0) step_consts(sP, sK);
-            cur_j = j;
         }
         const bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
         if (__syncthreads_or(!arrived)) {
-            // give up this step's remaining tiles; wait (bounded) for the
-            // copy in flight (the next one is not issued yet)
-            if (copier) {
+            if (tid == 0) {
                 atomicOr(&sP.clock->status, AST_ST_TIMEOUT);
                 tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+                if (s_tile[b ^ 1] < total) tma::mbar_wait(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
             }
             break;
         }
         const int n0 = s_org[b].x, m0 = s_org[b].y;
         patch_tile<R, TZ, TR>(sP, sm, b, n0, m0);
-        if (copier) sm.qn = 0u;
-        __syncthreads();
-        if (copier) {
-            // the previous tile's cells, the next tile's box, and the entry
-            // after it into this buffer's slots (every thread has read them)
-            if (s_pend_j >= 0) {
-                tma::store_3d(&tout[s_pend_j], &sm.out[0][0][0], s_pend.x, s_pend.y, 0);
-                tma::store_commit();
-            }
-            s_pend = make_int2(n0, m0);
-            s_pend_j = j;
-            if (s_tile[b ^ 1] < total) {
-                tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
-                tma::load_3d(&tin[s_prob[b ^ 1]], &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], s_org[b ^ 1].x - 4,
-                             s_org[b ^ 1].y - 2, 0);
-            }
-            int tn, jn;
-            int2 on;
-            schedule(tn, jn, on);
-            s_tile[b] = tn;
-            s_prob[b] = jn;
-            s_org[b] = on;
+        if (tid == 0) {
+            sm.qn = 0u;
+            step_consts(sP, sK);
+            tma::store_wait_read();   // the previous tile's store has read sm.out
         }
+        __syncthreads();
+        acc.clear();
         tile_body<R, FLUX, RECON, kSoA, TZ, TR, true>(sP, sm, b, sP.gf, n0, m0, sK, acc);
         tma::fence_async_shared();
         __syncthreads();
-        run++;
-    }
-    // a run cut short by a copy that did not arrive
-    if (cur_j >= 0 && run > 0)
-        cta_epilogue<R>(sP, acc, (unsigned)(tile_start[cur_j + 1] - tile_start[cur_j]), false, (unsigned)run);
-    if (copier) {
-        if (s_pend_j >= 0) {
-            tma::store_3d(&tout[s_pend_j], &sm.out[0][0][0], s_pend.x, s_pend.y, 0);
+        if (tid == 0) {
+            tma::store_3d(&tout[j], &sm.out[0][0][0], n0, m0, 0);
             tma::store_commit();
         }
-        tma::store_wait_all();
+        cta_epilogue<R>(sP, acc, (unsigned)(tile_start[j + 1] - tile_start[j]), false);
     }
+    if (tid == 0) tma::store_wait_all();
 }
 
 // Characteristic inflow at z_lo after a step (add2_bound, kernel.cu:1895-
