@@ -1118,6 +1118,11 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
     if constexpr (FLUX == 2) {
         queue_pass<R, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
         __syncthreads();
+        // persistent kernels: the next tile's queue starts empty (ordered
+        // before its face pass by the barrier between the tiles)
+        if constexpr (TO_SMEM) {
+            if (threadIdx.x == kCopyThread) sm.qn = 0u;
+        }
     }
 
     // ---- conservative update of the tile's cells
@@ -1445,6 +1450,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         tma::fence_async_shared();
         step_consts(P, sK);
         s_pend = make_int2(-1, -1);
+        sm.qn = 0u;   // later tiles: reset after the previous tile's queue
         // the first two tiles: the first is copied now, the second at the
         // start of the first tile's face pass
         const int t0 = (int)atomicAdd(&P.clock->next_tile, 1u);
@@ -1466,6 +1472,14 @@ __global__ void __launch_bounds__(kThreads, 4)
         const int b = k & 1;
         const int t = s_tile[b];
         if (t >= tiles) break;
+        // the origin the copy thread found (one integer division per tile,
+        // not one per thread), read before the barrier below, after which
+        // the copy thread overwrites this buffer's slots
+        const int n0 = s_org[b].x, m0 = s_org[b].y;
+        // The barrier after the copy's arrival is the one barrier between
+        // two tiles: every thread has finished the previous tile (its
+        // update and its reads of the other buffer and of the output tile)
+        // and fenced its shared-memory writes for the bulk copies.
         const bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
         if (__syncthreads_or(!arrived)) {
             // give up this step's remaining tiles; wait (bounded) for the
@@ -1477,12 +1491,12 @@ __global__ void __launch_bounds__(kThreads, 4)
             }
             break;
         }
-        // the origin the copy thread found (one integer division per tile,
-        // not one per thread)
-        const int n0 = s_org[b].x, m0 = s_org[b].y;
-        patch_tile<R, TZ, TR>(P, sm, b, n0, m0);
-        if (copier) sm.qn = 0u;
-        __syncthreads();
+        // ghost cells (tiles at the grid's edge or near the fixed region
+        // only: the others need no second barrier)
+        if (n0 - 2 < 0 || n0 + TZ + 2 > P.N || m0 - 2 < 0 || m0 + TR + 2 > P.M || P.fixed_region) {
+            patch_tile<R, TZ, TR>(P, sm, b, n0, m0);
+            __syncthreads();
+        }
         if (copier) {
             // the previous tile's cells (sm.out is not written again before
             // the store has read it: see tile_body)
@@ -1508,10 +1522,11 @@ __global__ void __launch_bounds__(kThreads, 4)
         }
         tile_body<R, FLUX, RECON, kSoA, TZ, TR, true, SKIP>(P, sm, b, g, n0, m0, sK, acc);
         // this thread's shared-memory writes (sm.out, ghost cells) before
-        // the bulk copies that read or overwrite them
+        // the bulk copies that read or overwrite them (ordered by the next
+        // tile's barrier, or the one below)
         tma::fence_async_shared();
-        __syncthreads();
     }
+    __syncthreads();
     if (copier) {
         const int2 pend = s_pend;
         if (pend.x >= 0) {
