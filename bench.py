@@ -151,6 +151,47 @@ def make_config(form):
     return cfg
 
 
+def time_config(cfg, s0, u0, steps, warmup, torch):
+    """Device-timed steps of one configuration from (s0, u0) at t = 0
+    (CUDA events on the solver's stream).  Returns seconds."""
+    from asteriy_2d_gb300 import solver
+    stream = torch.cuda.Stream()
+    with solver.Solver(cfg, stream=stream.cuda_stream) as S:
+        S.set_state(s0, u0)
+        S.step(warmup)
+        S.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        S.step(steps, sync=False)
+        e1.record(stream)
+        S.synchronize()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+
+def time_configs(warmup, torch):
+    """The other configurations of the scope table, each timed from t = 0
+    as its own run: C1, the blast at 256x128 with HLL + minmod in FP64 (the
+    small case, 500 steps; launch-bound at this size), and C2, the
+    wind-counterflow at 2048x1024 with HLLC + minmod (seeded density noise,
+    the wind sphere held fixed) in FP64 and in the FP32 form."""
+    from asteriy_2d_gb300 import abi as A
+    from asteriy_2d_gb300 import problems, solver
+    out = {}
+    runs = [("C1_blast_256x128_hll_fp64", problems.blast_config(256, 128, flux=A.FLUX_HLL), "blast", 500)]
+    for prec, tag in ((A.PREC_FP64, "fp64"), (A.PREC_FP32, "fp32")):
+        runs.append((f"C2_wind_2048x1024_hllc_{tag}", problems.wind_config(2048, 1024, precision=prec), "wind",
+                     200 if prec == A.PREC_FP64 else 1000))
+    for name, cfg, setup, steps in runs:
+        s0, u0 = solver.fill_blast(cfg) if setup == "blast" else solver.fill_wind(cfg)
+        sec = time_config(cfg, s0, u0, steps, warmup, torch)
+        out[name] = {"value": cfg.N * cfg.M * steps / sec, "unit": "cell-updates/s",
+                     "ms_per_step": sec * 1e3 / steps, "steps": steps}
+    return out
+
+
 def learned_params(s0, u0):
     """Trained parameters of the start-value network: the committed ones
     (asteriy_2d_gb300/train_guess.py) or, when absent, a quick training on
@@ -644,6 +685,8 @@ def main():
         "clocks": clocks,
     }
     line["config"]["start_step"] = args.start_step
+    if rank == 0 and not args.no_forms:
+        line["configs"] = time_configs(args.warmup, torch)
     if rank == 0 and args.batch_steps:
         line["batch"] = time_batch(args.batch_steps, args.warmup, torch)
         line["gpu_launches_batch_step"] = line["batch"]["launches_per_step"]
