@@ -28,17 +28,54 @@ int set_error(int code, const char* msg);
 int encode_planes(CUtensorMap* map, void* base, const ast_config& c, long long ld, long long plane, unsigned bx,
                   unsigned by);
 
+// the GPU's SM count (the current device when first asked)
+inline int sm_count()
+{
+    static int n = 0;
+    if (n <= 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            n = v;
+        else
+            return 1;
+    }
+    return n;
+}
+
 // launch=false only raises the kernel's dynamic shared-memory limit, which
-// must happen outside stream capture (ast_create, ast_step_raw)
+// must happen outside stream capture (ast_create, ast_step_raw).  The FP64
+// solver on a small grid (fewer 32x16 tiles than two per SM) steps with
+// 16x16 tiles: twice the CTAs with half the cells each, since there every
+// CTA runs alone on its SM at the FP64 rate.
 template <typename R, int FLUX, bool RECON, int LAYOUT>
 int launch_step_t(const StepParams& P, cudaStream_t st, bool launch)
 {
+    constexpr bool kSmallTiles = sizeof(R) == 8 && LAYOUT == kSoA;
+    constexpr int kSZ = 16, kSR = 16;
     auto k = step_kernel<R, FLUX, RECON, LAYOUT, kTZ, kTR>;
     constexpr size_t smem = tile_smem_bytes<R, FLUX, kTZ, kTR>();
     cudaError_t e;
     if (!launch) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaFuncSetAttribute");
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+        if constexpr (kSmallTiles) {
+            e = cudaFuncSetAttribute(step_kernel<R, FLUX, RECON, LAYOUT, kSZ, kSR>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tile_smem_bytes<R, FLUX, kSZ, kSR>());
+            if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+        }
+        return AST_OK;
+    }
+    const long long tiles = (long long)((P.N + kTZ - 1) / kTZ) * ((P.M + kTR - 1) / kTR);
+    if constexpr (kSmallTiles) {
+        if (tiles < 2LL * sm_count()) {
+            dim3 grid((P.N + kSZ - 1) / kSZ, (P.M + kSR - 1) / kSR);
+            step_kernel<R, FLUX, RECON, LAYOUT, kSZ, kSR>
+                <<<grid, kThreads, tile_smem_bytes<R, FLUX, kSZ, kSR>(), st>>>(P);
+            e = cudaGetLastError();
+            return e == cudaSuccess ? AST_OK : cuda_fail(e, "step kernel launch");
+        }
     }
     dim3 grid((P.N + kTZ - 1) / kTZ, (P.M + kTR - 1) / kTR);
     k<<<grid, kThreads, smem, st>>>(P);

@@ -90,6 +90,17 @@ def test_blast_hllc():
     assert_same_shock_cells(s, os_, cfg)
 
 
+@pytest.mark.parametrize("flux", [A.FLUX_HLLC, A.FLUX_GODUNOV])
+def test_fp64_32x16_tile_path_matches_oracle(flux):
+    # grids with at least two 32x16 tiles per SM step with 32x16 tiles;
+    # smaller FP64 grids (every other parity case here) use 16x16 tiles
+    cfg = problems.blast_config(640, 320, flux=flux)
+    cfg.riemann_tol = 1e-13
+    s0, u0 = solver.fill_blast(cfg)
+    s, u, os_, ou = assert_parity(cfg, s0, u0, 30)
+    assert_same_shock_cells(s, os_, cfg)
+
+
 # The exact solver's shock-rarefaction bisection stops on an absolute
 # residual of 10e-10 (devtwo, kernel.cu:685): which bisection iterate first
 # meets it depends on the last bits of pow(), which differ between CUDA and
