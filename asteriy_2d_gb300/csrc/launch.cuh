@@ -51,7 +51,7 @@ inline int sm_count()
 template <typename R, int FLUX, bool RECON, int LAYOUT>
 int launch_step_t(const StepParams& P, cudaStream_t st, bool launch)
 {
-    constexpr bool kSmallTiles = sizeof(R) == 8 && LAYOUT == kSoA;
+    constexpr bool kSmallTiles = sizeof(R) == 8;
     constexpr int kSZ = 16, kSR = 16;
     auto k = step_kernel<R, FLUX, RECON, LAYOUT, kTZ, kTR>;
     constexpr size_t smem = tile_smem_bytes<R, FLUX, kTZ, kTR>();
