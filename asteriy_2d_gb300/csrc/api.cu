@@ -119,6 +119,8 @@ struct ast_solver {
     bool tma = false;                // FP32 persistent kernel
     int tma_grid = 0;                // its CTAs
     CUtensorMap tin[2], tout[2];     // tile-box load and store maps of buf[0], buf[1]
+    cudaStream_t pipe[2] = {nullptr, nullptr};   // ast_step_host: copies in, copies out
+    cudaEvent_t pev[2 * 16 + 2] = {};            // its band events (created on first use)
 };
 
 extern "C" {
@@ -214,6 +216,10 @@ int ast_destroy(ast_solver* S)
 {
     if (!S) return AST_OK;
     if (S->graph) cudaGraphExecDestroy(S->graph);
+    for (cudaEvent_t& ev : S->pev)
+        if (ev) cudaEventDestroy(ev);
+    for (cudaStream_t& st : S->pipe)
+        if (st) cudaStreamDestroy(st);
     cudaFree(S->buf[0]);
     cudaFree(S->buf[1]);
     cudaFree(S->clock);
@@ -448,6 +454,140 @@ int ast_step(ast_solver* S, int nsteps)
         int rc = enqueue_one(S);
         if (rc != AST_OK) return rc;
     }
+    return AST_OK;
+}
+
+// ast_step_host: one step from host arrays to host arrays, pipelined over
+// bands of tile rows.  Two copy streams carry nothing but copies, so the
+// host link's two directions stay busy: `in` copies band b's s, u into the
+// device staging arrays, `out` copies band b of the new state back.  The
+// kernels run in order on the solver's stream: band b + 1 converted into
+// the state buffer (it holds band b's lower halo rows), band b stepped,
+// band b converted into staging for `out`.
+static constexpr int kHostBands = 16;
+
+static bool ranges_overlap(const void* a, const void* b, size_t bytes)
+{
+    const char *x = (const char*)a, *y = (const char*)b;
+    return x < y + bytes && y < x + bytes;
+}
+
+int ast_step_host(ast_solver* S, const double* s_in, const double* u_in, double* s_out, double* u_out)
+{
+    if (!S || !s_in || !u_in || !s_out || !u_out) return fail(AST_ERR_INVALID, "null argument");
+    if (S->cfg.flux == AST_FLUX_GODUNOV && S->cfg.guess == AST_GUESS_MLP && S->P.riemann_newton && !S->mlp)
+        return fail(AST_ERR_INVALID, "guess == MLP needs ast_set_mlp first");
+    const int N = S->cfg.N, M = S->cfg.M;
+    const size_t bytes = (size_t)N * M * 2 * sizeof(double);
+    // an output array is its input array (in place) or lies apart from both
+    // inputs: band b's results are written after the inputs of all bands up
+    // to b + 1 were read, but before those of later bands
+    for (const double* o : {(const double*)s_out, (const double*)u_out})
+        for (const double* i : {s_in, u_in})
+            if (o != i && ranges_overlap(o, i, bytes)) return fail(AST_ERR_INVALID, "overlapping host arrays");
+    if (ranges_overlap(s_out, u_out, bytes)) return fail(AST_ERR_INVALID, "overlapping host arrays");
+    const bool pinned = host_range_on_device(s_in, bytes) && host_range_on_device(u_in, bytes) &&
+                        host_range_on_device(s_out, bytes) && host_range_on_device(u_out, bytes);
+    if (!pinned || S->cfg.inflow_p > 0.0) {
+        // pageable arrays (the copies would not overlap) or the inflow rule
+        // (a pass over every row after the step): the three calls in turn
+        int rc = ast_set_state(S, s_in, u_in, 0);
+        if (rc == AST_OK) rc = ast_step(S, 1);
+        if (rc == AST_OK) rc = ast_get_state(S, s_out, u_out, 0);
+        return rc;
+    }
+    if (!S->pipe[0]) {
+        for (cudaStream_t& st : S->pipe) AST_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        for (cudaEvent_t& ev : S->pev) AST_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    const int rows = (M + kTR - 1) / kTR;   // tile rows
+    const int bands = std::min(rows, kHostBands);
+    cudaEvent_t* ev_in = S->pev;                  // band b in staging
+    cudaEvent_t* ev_out = S->pev + kHostBands;    // band b of the new state in staging
+    cudaEvent_t ev_start = S->pev[2 * kHostBands], ev_done = S->pev[2 * kHostBands + 1];
+    cudaStream_t cin = S->pipe[0], cst = S->stream, cout = S->pipe[1];
+    struct Band {
+        int t0, t1;          // tile rows
+        long long k0, k1;    // cells
+    };
+    Band bd[kHostBands];
+    const int tiles_z = (N + kTZ - 1) / kTZ;
+    int units = 0;   // CTAs of all bands' persistent launches
+    for (int b = 0; b < bands; b++) {
+        bd[b].t0 = (int)((long long)b * rows / bands);
+        bd[b].t1 = (int)((long long)(b + 1) * rows / bands);
+        bd[b].k0 = (long long)bd[b].t0 * kTR * N;
+        bd[b].k1 = (long long)std::min(bd[b].t1 * kTR, M) * N;
+        units += std::min((bd[b].t1 - bd[b].t0) * tiles_z, S->tma_grid);
+    }
+    AST_CUDA(cudaEventRecord(ev_start, cst));
+    AST_CUDA(cudaStreamWaitEvent(cin, ev_start, 0));
+    AST_CUDA(cudaStreamWaitEvent(cout, ev_start, 0));
+    for (int b = 0; b < bands; b++) {
+        const size_t off = (size_t)bd[b].k0 * 2, n = (size_t)(bd[b].k1 - bd[b].k0) * 2 * sizeof(double);
+        AST_CUDA(cudaMemcpyAsync(S->stage_s + off, s_in + off, n, cudaMemcpyHostToDevice, cin));
+        AST_CUDA(cudaMemcpyAsync(S->stage_u + off, u_in + off, n, cudaMemcpyHostToDevice, cin));
+        AST_CUDA(cudaEventRecord(ev_in[b], cin));
+    }
+    void* src = S->buf[S->cur];
+    void* dst = S->buf[S->cur ^ 1];
+    auto convert_band_in = [&](int b) -> int {
+        AST_CUDA(cudaStreamWaitEvent(cst, ev_in[b], 0));
+        const int nb = (int)((bd[b].k1 - bd[b].k0 + 255) / 256);
+        if (S->elem == 8)
+            aos_to_soa<double><<<nb, 256, 0, cst>>>((const double2*)S->stage_s, (const double2*)S->stage_u,
+                                                    (double*)src, N, M, S->ld, S->plane, bd[b].k0, bd[b].k1);
+        else
+            aos_to_soa<float><<<nb, 256, 0, cst>>>((const double2*)S->stage_s, (const double2*)S->stage_u,
+                                                   (float*)src, N, M, S->ld, S->plane, bd[b].k0, bd[b].k1);
+        AST_CUDA(cudaGetLastError());
+        return AST_OK;
+    };
+    int rc = convert_band_in(0);
+    for (int b = 0; b < bands && rc == AST_OK; b++) {
+        if (b + 1 < bands) rc = convert_band_in(b + 1);
+        if (rc != AST_OK) break;
+        StepParams P = S->P;
+        P.in = src;
+        P.out = dst;
+        P.band_lo = bd[b].t0;
+        P.band_hi = bd[b].t1;
+        if (S->tma) {
+            // each band hands out its tiles from a counter set to zero
+            P.units = units;
+            if (b > 0) AST_CUDA(cudaMemsetAsync(&S->clock->next_tile, 0, sizeof(unsigned int), cst));
+            rc = launch_step_tma(P, S->tin[S->cur], S->tout[S->cur ^ 1], S->cfg.flux, S->cfg.recon,
+                                 std::min((bd[b].t1 - bd[b].t0) * tiles_z, S->tma_grid), cst, true, nullptr);
+        } else {
+            rc = (S->elem == 8) ? launch_step_r<double, kSoA>(P, S->cfg.flux, S->cfg.recon, cst, true)
+                                : launch_step_r<float, kSoA>(P, S->cfg.flux, S->cfg.recon, cst, true);
+        }
+        if (rc != AST_OK) break;
+        const int nb = (int)((bd[b].k1 - bd[b].k0 + 255) / 256);
+        if (S->elem == 8)
+            soa_to_aos<double><<<nb, 256, 0, cst>>>((const double*)dst, (double2*)S->stage_s, (double2*)S->stage_u, N,
+                                                    M, S->ld, S->plane, bd[b].k0, bd[b].k1);
+        else
+            soa_to_aos<float><<<nb, 256, 0, cst>>>((const float*)dst, (double2*)S->stage_s, (double2*)S->stage_u, N,
+                                                   M, S->ld, S->plane, bd[b].k0, bd[b].k1);
+        AST_CUDA(cudaGetLastError());
+        AST_CUDA(cudaEventRecord(ev_out[b], cst));
+        const size_t off = (size_t)bd[b].k0 * 2, n = (size_t)(bd[b].k1 - bd[b].k0) * 2 * sizeof(double);
+        AST_CUDA(cudaStreamWaitEvent(cout, ev_out[b], 0));
+        AST_CUDA(cudaMemcpyAsync(s_out + off, S->stage_s + off, n, cudaMemcpyDeviceToHost, cout));
+        AST_CUDA(cudaMemcpyAsync(u_out + off, S->stage_u + off, n, cudaMemcpyDeviceToHost, cout));
+    }
+    // the copy streams rejoin the solver's stream even after a failed launch
+    AST_CUDA(cudaEventRecord(ev_done, cout));
+    AST_CUDA(cudaStreamWaitEvent(cst, ev_done, 0));
+    AST_CUDA(cudaEventRecord(ev_done, cin));
+    AST_CUDA(cudaStreamWaitEvent(cst, ev_done, 0));
+    if (rc != AST_OK) {
+        cudaStreamSynchronize(cst);
+        return rc;
+    }
+    S->cur ^= 1;
+    AST_CUDA(cudaStreamSynchronize(cst));
     return AST_OK;
 }
 

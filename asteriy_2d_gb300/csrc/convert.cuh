@@ -8,12 +8,13 @@
 namespace ast {
 // internal linkage: every translation unit that converts has its own copy
 
+// cells k0 <= k < k1 (k1 = 0: the whole grid)
 template <typename R>
 static __global__ void aos_to_soa(const double2* __restrict__ s, const double2* __restrict__ u, R* __restrict__ q,
-                           int N, int M, long long ld, long long plane)
+                           int N, int M, long long ld, long long plane, long long k0 = 0, long long k1 = 0)
 {
-    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (long long)N * M) return;
+    long long k = k0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (k1 > 0 ? k1 : (long long)N * M)) return;
     int m = (int)(k / N), n = (int)(k - (long long)m * N);
     long long o = (long long)m * ld + n;
     double2 a = s[k], b = u[k];
@@ -22,10 +23,10 @@ static __global__ void aos_to_soa(const double2* __restrict__ s, const double2* 
 
 template <typename R>
 static __global__ void soa_to_aos(const R* __restrict__ q, double2* __restrict__ s, double2* __restrict__ u, int N,
-                           int M, long long ld, long long plane)
+                           int M, long long ld, long long plane, long long k0 = 0, long long k1 = 0)
 {
-    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (long long)N * M) return;
+    long long k = k0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (k1 > 0 ? k1 : (long long)N * M)) return;
     int m = (int)(k / N), n = (int)(k - (long long)m * N);
     long long o = (long long)m * ld + n;
     s[k] = make_double2((double)q[o], (double)q[o + plane]);

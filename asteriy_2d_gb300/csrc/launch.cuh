@@ -47,7 +47,9 @@ inline int sm_count()
 // must happen outside stream capture (ast_create, ast_step_raw).  The FP64
 // solver on a small grid (fewer 32x16 tiles than two per SM) steps with
 // 16x16 tiles: twice the CTAs with half the cells each, since there every
-// CTA runs alone on its SM at the FP64 rate.
+// CTA runs alone on its SM at the FP64 rate.  P.band_hi > 0 launches the
+// tile rows [band_lo, band_hi) only (both tile shapes are 16 rows high), and
+// every tile of the grid counts towards the step's clock.
 template <typename R, int FLUX, bool RECON, int LAYOUT>
 int launch_step_t(const StepParams& P, cudaStream_t st, bool launch)
 {
@@ -67,18 +69,24 @@ int launch_step_t(const StepParams& P, cudaStream_t st, bool launch)
         }
         return AST_OK;
     }
-    const long long tiles = (long long)((P.N + kTZ - 1) / kTZ) * ((P.M + kTR - 1) / kTR);
+    static_assert(kSR == kTR, "bands are counted in tile rows of either shape");
+    const int rows = (P.M + kTR - 1) / kTR;
+    const int band = P.band_hi > 0 ? P.band_hi - P.band_lo : rows;
+    StepParams Q = P;
+    const long long tiles = (long long)((P.N + kTZ - 1) / kTZ) * rows;
     if constexpr (kSmallTiles) {
         if (tiles < 2LL * sm_count()) {
-            dim3 grid((P.N + kSZ - 1) / kSZ, (P.M + kSR - 1) / kSR);
+            dim3 grid((P.N + kSZ - 1) / kSZ, band);
+            if (P.band_hi > 0) Q.units = (int)grid.x * rows;
             step_kernel<R, FLUX, RECON, LAYOUT, kSZ, kSR>
-                <<<grid, kThreads, tile_smem_bytes<R, FLUX, kSZ, kSR>(), st>>>(P);
+                <<<grid, kThreads, tile_smem_bytes<R, FLUX, kSZ, kSR>(), st>>>(Q);
             e = cudaGetLastError();
             return e == cudaSuccess ? AST_OK : cuda_fail(e, "step kernel launch");
         }
     }
-    dim3 grid((P.N + kTZ - 1) / kTZ, (P.M + kTR - 1) / kTR);
-    k<<<grid, kThreads, smem, st>>>(P);
+    dim3 grid((P.N + kTZ - 1) / kTZ, band);
+    if (P.band_hi > 0) Q.units = (int)grid.x * rows;
+    k<<<grid, kThreads, smem, st>>>(Q);
     e = cudaGetLastError();
     return e == cudaSuccess ? AST_OK : cuda_fail(e, "step kernel launch");
 }

@@ -69,6 +69,10 @@ struct __align__(16) StepParams {
     int fixed_nlo, fixed_nhi, fixed_mhi;   // cells that can lie in the region (one cell of margin)
     int region_select;
     int skip_uniform;              // uniform tiles skip the face pass
+    // one step launched in bands of tile rows: this launch steps tile rows
+    // [band_lo, band_hi) (band_hi 0: all rows of the grid), and `units` CTAs
+    // of all the step's launches report to the clock (0: this launch's grid)
+    int band_lo, band_hi, units;
     // the high-order region as column intervals (found on the host from
     // the reference's FP64 face positions): z faces whose lower cell's
     // column lies in [region_zlo, region_zhi], r faces of the columns in
@@ -1375,7 +1379,8 @@ constexpr int min_ctas() { return sizeof(R) == 8 ? 2 : 4; }
 template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR>
 __global__ void __launch_bounds__(kThreads, min_ctas<R, FLUX>()) step_kernel(StepParams P)
 {
-    step_tile<R, FLUX, RECON, LAYOUT, TZ, TR>(P, blockIdx.x, blockIdx.y, gridDim.x * gridDim.y);
+    step_tile<R, FLUX, RECON, LAYOUT, TZ, TR>(P, blockIdx.x, blockIdx.y + P.band_lo,
+                                              P.units > 0 ? (unsigned)P.units : gridDim.x * gridDim.y);
 }
 
 // many problems of one (flux, recon) class: a CTA per (problem, tile) of the
@@ -1441,7 +1446,8 @@ __global__ void __launch_bounds__(kThreads, 4)
     const int tid = threadIdx.x;
     const bool copier = tid == kCopyThread;
     const int tiles_z = (P.N + TZ - 1) / TZ;
-    const int tiles = tiles_z * ((P.M + TR - 1) / TR);
+    const int t_lo = P.band_lo * tiles_z;   // this launch's tiles: t_lo <= t < tiles
+    const int tiles = tiles_z * (P.band_hi > 0 ? P.band_hi : (P.M + TR - 1) / TR);
     if (copier) {
         tma::prefetch_map(&tin);
         tma::prefetch_map(&tout);
@@ -1453,8 +1459,8 @@ __global__ void __launch_bounds__(kThreads, 4)
         sm.qn = 0u;   // later tiles: reset after the previous tile's queue
         // the first two tiles: the first is copied now, the second at the
         // start of the first tile's face pass
-        const int t0 = (int)atomicAdd(&P.clock->next_tile, 1u);
-        const int t1 = (t0 < tiles) ? (int)atomicAdd(&P.clock->next_tile, 1u) : tiles;
+        const int t0 = t_lo + (int)atomicAdd(&P.clock->next_tile, 1u);
+        const int t1 = (t0 < tiles) ? t_lo + (int)atomicAdd(&P.clock->next_tile, 1u) : tiles;
         s_tile[0] = t0;
         s_tile[1] = t1;
         s_org[1] = make_int2((t1 % tiles_z) * TZ, (t1 / tiles_z) * TR);
@@ -1515,7 +1521,7 @@ __global__ void __launch_bounds__(kThreads, 4)
                 tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
                 tma::load_3d(&tin, &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], s_org[b ^ 1].x - 4, s_org[b ^ 1].y - 2,
                              0);
-                tnn = (int)atomicAdd(&P.clock->next_tile, 1u);
+                tnn = t_lo + (int)atomicAdd(&P.clock->next_tile, 1u);
             }
             s_tile[b] = tnn;
             s_org[b] = make_int2((tnn % tiles_z) * TZ, (tnn / tiles_z) * TR);
@@ -1535,7 +1541,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         }
         tma::store_wait_all();
     }
-    cta_epilogue<R>(P, acc, gridDim.x, true);
+    cta_epilogue<R>(P, acc, P.units > 0 ? (unsigned)P.units : gridDim.x, true);
 }
 
 // The persistent FP32 kernel of one batch class: tiles of all the class's

@@ -31,6 +31,7 @@ SIGNATURES = {
     "ast_set_clock": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int64]),
     "ast_get_clock": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int64)]),
     "ast_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "ast_step_host": (C.c_int, [C.c_void_p] * 5),
     "ast_synchronize": (C.c_int, [C.c_void_p]),
     "ast_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.ast_stats), C.c_int]),
     "ast_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
@@ -288,6 +289,13 @@ class Solver:
         a, b, c = C.c_double(), C.c_double(), C.c_int64()
         check(self.lib.ast_get_clock(self.h, C.byref(a), C.byref(b), C.byref(c)), "ast_get_clock")
         return a.value, b.value, c.value
+
+    def step_host(self, s_in, u_in, s_out, u_out):
+        """One step from host arrays to host arrays (ast_step_host): the
+        addresses of four (K, 2) float64 arrays; page-locked arrays are
+        pipelined by bands, others are copied in, stepped and copied out."""
+        check(self.lib.ast_step_host(self.h, C.c_void_p(s_in), C.c_void_p(u_in), C.c_void_p(s_out),
+                                     C.c_void_p(u_out)), "ast_step_host")
 
     def step(self, n=1, sync=True):
         check(self.lib.ast_step(self.h, n), "ast_step")

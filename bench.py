@@ -343,9 +343,13 @@ def accuracy(nsteps, params):
     return out
 
 
-def time_e2e(form, start, steps, torch, params=None):
+def time_e2e(form, start, steps, torch, params=None, banded=True):
     """Through the public API with host buffers: every step copies the state
-    in from pinned host memory, steps once and reads the result back."""
+    in from pinned host memory, steps once and writes the result back to
+    pinned host memory.  banded: one ast_step_host call per step (the copies
+    in, the step and the copies out pipelined over bands of rows, ping-pong
+    between two pairs of host arrays); otherwise ast_set_state, ast_step(1),
+    ast_get_state."""
     from asteriy_2d_gb300 import solver
     s0, u0, clock = start
     cfg = make_config(form)
@@ -354,17 +358,26 @@ def time_e2e(form, start, steps, torch, params=None):
     hu = torch.empty((K, 2), dtype=torch.float64, pin_memory=True)
     hs.numpy()[:] = s0
     hu.numpy()[:] = u0
+    hs2 = torch.empty((K, 2), dtype=torch.float64, pin_memory=True) if banded else hs
+    hu2 = torch.empty((K, 2), dtype=torch.float64, pin_memory=True) if banded else hu
     lib = solver.load()
     with solver.Solver(cfg) as S:
         if params is not None:
             S.set_mlp(params)
         S.set_clock(*clock)
+        bufs = [(hs, hu), (hs2, hu2)]
 
         def one():
+            if banded:
+                (a_s, a_u), (b_s, b_u) = bufs
+                S.step_host(a_s.data_ptr(), a_u.data_ptr(), b_s.data_ptr(), b_u.data_ptr())
+                bufs.reverse()
+                return
             solver.check(lib.ast_set_state(S.h, hs.data_ptr(), hu.data_ptr(), 0), "set_state")
             S.step(1, sync=False)
             solver.check(lib.ast_get_state(S.h, hs.data_ptr(), hu.data_ptr(), 0), "get_state")
         one()
+        bufs.reverse()
         hs.numpy()[:] = s0
         hu.numpy()[:] = u0
         torch.cuda.synchronize()
@@ -658,6 +671,8 @@ def main():
             np.array_equal(finals["fp32_learned_skip"], finals["fp32_learned"]))
     esec, bi, bo = time_e2e(args.form, start, e2e_steps, torch,
                             params if args.form.startswith("fp32_learned") else None)
+    esec3, _, _ = time_e2e(args.form, start, e2e_steps, torch,
+                           params if args.form.startswith("fp32_learned") else None, banded=False)
     hbm, src = peaks()
     prec = "fp64" if args.form.startswith("fp64") else "fp32"
     achieved = BYTES_PER_CELL[prec] * cells / (sec / args.steps) / 1e9
@@ -680,7 +695,11 @@ def main():
         "forms": forms,
         "e2e": {"value": cells * e2e_steps / esec, "unit": "cell-updates/s", "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo,
-                "note": "per step: ast_set_state from pinned host, ast_step(1), ast_get_state to pinned host"},
+                "note": "per step: one ast_step_host call, pinned host arrays in and out (copies in, step and "
+                        "copies out pipelined over 16 bands of rows)",
+                "three_calls": {"value": cells * e2e_steps / esec3, "unit": "cell-updates/s",
+                                "note": "per step: ast_set_state from pinned host, ast_step(1), "
+                                        "ast_get_state to pinned host"}},
         "gpu_launches": args.steps,
         "clocks": clocks,
     }

@@ -220,6 +220,17 @@ int ast_get_clock(ast_solver* solver, double* T_do, double* TT, int64_t* step);
    returns without waiting; ast_synchronize waits and reports errors. */
 int ast_step(ast_solver* solver, int nsteps);
 int ast_synchronize(ast_solver* solver);
+/* One step from host arrays to host arrays, waiting for the result: the
+   reference's step between its host<->device state copies (the state
+   in, kernel.cu:3444-3445; the time loop, 3868-3947; the state out,
+   4075-4076).
+   s_in, u_in hold the state in the layout of ast_set_state; s_out, u_out
+   receive the new state in the layout of ast_get_state.  An output array
+   may be its input array (in place); any other overlap is AST_ERR_INVALID.
+   Page-locked arrays are moved in bands of rows, the copies in, the step
+   and the copies out overlapping; pageable arrays, or a configuration with
+   the inflow rule, take ast_set_state + ast_step + ast_get_state. */
+int ast_step_host(ast_solver* solver, const double* s_in, const double* u_in, double* s_out, double* u_out);
 int ast_get_stats(ast_solver* solver, ast_stats* out, int reset);
 /* Device view of the current state: four planes rho, p, v_z, v_r of M rows
    with row pitch *ld elements of *elem_bytes bytes (8 = FP64, 4 = FP32),
