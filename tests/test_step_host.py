@@ -70,6 +70,7 @@ def assert_same(ref, got):
 CASES = [
     # (precision, persistent, flux, grid)
     (A.PREC_FP32, 1, A.FLUX_HLL, (512, 384)),       # 24 tile rows: 16 bands of 1-2
+    (A.PREC_FP32, 1, A.FLUX_HLLC, (64, 3200)),      # 200 tile rows: 16 bands of 12-13
     (A.PREC_FP32, 1, A.FLUX_GODUNOV, (300, 130)),   # 9 tile rows, ragged edges
     (A.PREC_FP32, 0, A.FLUX_HLLC, (256, 272)),      # per-tile FP32 kernel, 17 tile rows
     (A.PREC_FP64, 0, A.FLUX_HLLC, (1024, 512)),     # FP64, 32x16 tiles
