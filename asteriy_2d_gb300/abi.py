@@ -63,7 +63,7 @@ class ast_config(C.Structure):
         ("collect_stats", C.c_int32), ("riemann_newton", C.c_int32), ("persistent", C.c_int32),
         ("skip_uniform", C.c_int32), ("reserved_i", C.c_int32 * 4),
         ("mlp_gate", C.c_double), ("inflow_p", C.c_double), ("inflow_v", C.c_double),
-        ("reserved_d", C.c_double * 5),
+        ("neutral_nh", C.c_double), ("neutral_kn", C.c_double), ("reserved_d", C.c_double * 3),
     ]
 
     def copy(self):
@@ -121,6 +121,7 @@ def default_config():
     c.persistent = 1
     c.mlp_gate = 0.2
     c.inflow_p, c.inflow_v = 0.0, 1.0
+    c.neutral_nh, c.neutral_kn = 3.0, 0.419231
     return c
 
 

@@ -119,6 +119,7 @@ struct ast_solver {
     bool tma = false;                // FP32 persistent kernel
     int tma_grid = 0;                // its CTAs
     CUtensorMap tin[2], tout[2];     // tile-box load and store maps of buf[0], buf[1]
+    void* nsrc = nullptr;            // neutral-coupling source planes (nn2.x, nn2.y), or null
     cudaStream_t pipe[2] = {nullptr, nullptr};   // ast_step_host: copies in, copies out
     cudaEvent_t pev[2 * 16 + 2] = {};            // its band events (created on first use)
 };
@@ -229,6 +230,7 @@ int ast_destroy(ast_solver* S)
     cudaFree(S->rec);
     cudaFree(S->rec_n);
     cudaFree(S->probe_buf);
+    cudaFree(S->nsrc);
     delete S;
     return AST_OK;
 }
@@ -386,6 +388,14 @@ static int enqueue_one(ast_solver* S)
     else
         rc = (S->elem == 8) ? launch_step_r<double, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true)
                             : launch_step_r<float, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true);
+    if (rc == AST_OK && S->elem == 4 && P.nsrc) {
+        // the FP32 form's neutral-coupling source, after the step
+        const long long K = (long long)S->cfg.N * S->cfg.M;
+        const int nb = (int)std::min<long long>((K + 255) / 256, 16LL * sm_count());
+        neutral_kernel<<<nb, 256, 0, S->stream>>>(P);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_fail(e, "neutral source kernel launch");
+    }
     if (rc == AST_OK && S->cfg.inflow_p > 0.0) {
         const int nb = (S->cfg.M + 127) / 128;
         if (S->elem == 8)
@@ -488,9 +498,10 @@ int ast_step_host(ast_solver* S, const double* s_in, const double* u_in, double*
     if (ranges_overlap(s_out, u_out, bytes)) return fail(AST_ERR_INVALID, "overlapping host arrays");
     const bool pinned = host_range_on_device(s_in, bytes) && host_range_on_device(u_in, bytes) &&
                         host_range_on_device(s_out, bytes) && host_range_on_device(u_out, bytes);
-    if (!pinned || S->cfg.inflow_p > 0.0) {
-        // pageable arrays (the copies would not overlap) or the inflow rule
-        // (a pass over every row after the step): the three calls in turn
+    if (!pinned || S->cfg.inflow_p > 0.0 || (S->elem == 4 && S->P.nsrc)) {
+        // pageable arrays (the copies would not overlap), or a pass over
+        // every row after the step (the inflow rule, the FP32 form's
+        // neutral-coupling source): the three calls in turn
         int rc = ast_set_state(S, s_in, u_in, 0);
         if (rc == AST_OK) rc = ast_step(S, 1);
         if (rc == AST_OK) rc = ast_get_state(S, s_out, u_out, 0);
@@ -648,6 +659,40 @@ int ast_set_mlp(ast_solver* S, const float* params)
     return AST_OK;
 }
 
+int ast_set_neutral(ast_solver* S, const double* nn2, int on_device)
+{
+    if (!S) return fail(AST_ERR_INVALID, "null solver");
+    drop_graph(S);   // captured steps hold the old parameters
+    if (!nn2) {
+        S->P.nsrc = nullptr;
+        return AST_OK;
+    }
+    const long long K = (long long)S->cfg.N * S->cfg.M;
+    if (!S->nsrc) AST_CUDA(cudaMalloc(&S->nsrc, (size_t)S->plane * 2 * S->elem));
+    const double* src = nn2;
+    double* tmp = nullptr;
+    if (!on_device) {
+        AST_CUDA(cudaMalloc(&tmp, (size_t)K * 3 * sizeof(double)));
+        cudaError_t e = cudaMemcpyAsync(tmp, nn2, (size_t)K * 3 * sizeof(double), cudaMemcpyHostToDevice, S->stream);
+        if (e != cudaSuccess) {
+            cudaFree(tmp);
+            return cuda_fail(e, "cudaMemcpyAsync nn2");
+        }
+        src = tmp;
+    }
+    const int nb = (int)((K + 255) / 256);
+    if (S->elem == 8)
+        nn2_to_planes<double><<<nb, 256, 0, S->stream>>>(src, (double*)S->nsrc, S->cfg.N, S->cfg.M, S->ld, S->plane);
+    else
+        nn2_to_planes<float><<<nb, 256, 0, S->stream>>>(src, (float*)S->nsrc, S->cfg.N, S->cfg.M, S->ld, S->plane);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail(e, "neutral source conversion");
+    S->P.nsrc = S->nsrc;
+    return AST_OK;
+}
+
 int ast_probe(ast_solver* S, const int64_t* cells, int n, double* rho, double* TT)
 {
     if (!S || n < 0 || (n > 0 && (!cells || !rho))) return fail(AST_ERR_INVALID, "bad argument");
@@ -735,11 +780,9 @@ int ast_device_state(ast_solver* S, void** planes, int64_t* ld, int* elem_bytes)
 }
 
 // ==================================================================== kernel-level drop-in
-int ast_step_raw(const double* s, const double* u, double* s2, double* u2, double* T, const double* T_do,
-                 const double* TT, int method, const ast_config* cfg, void* stream)
+static int step_raw(const double* s, const double* u, double* s2, double* u2, const double* nn2, double* T,
+                    const double* T_do, const ast_config* cfg, void* stream)
 {
-    (void)TT;
-    (void)method;
     if (!s || !u || !s2 || !u2 || !T || !T_do || !cfg) return fail(AST_ERR_INVALID, "null argument");
     int rc = ast_config_check(cfg);
     if (rc != AST_OK) return rc;
@@ -755,9 +798,29 @@ int ast_step_raw(const double* s, const double* u, double* s2, double* u2, doubl
     P.T_min = T;
     P.T_do_ptr = T_do;
     P.collect_stats = 0;
+    P.nsrc = nn2;
     rc = launch_step_r<double, kAoS>(P, cfg->flux, cfg->recon, (cudaStream_t)stream, false);
     if (rc != AST_OK) return rc;
     return launch_step_r<double, kAoS>(P, cfg->flux, cfg->recon, (cudaStream_t)stream, true);
+}
+
+int ast_step_raw(const double* s, const double* u, double* s2, double* u2, double* T, const double* T_do,
+                 const double* TT, int method, const ast_config* cfg, void* stream)
+{
+    (void)TT;
+    (void)method;
+    return step_raw(s, u, s2, u2, nullptr, T, T_do, cfg, stream);
+}
+
+int ast_add_mk_raw(const double* s, const double* u, double* s2, double* u2, const double* nn1, const double* nn2,
+                   const double* nn3, double* T, const double* T_do, int method, int step, const ast_config* cfg,
+                   void* stream)
+{
+    (void)nn1;
+    (void)nn3;
+    (void)method;
+    (void)step;
+    return step_raw(s, u, s2, u2, nn2, T, T_do, cfg, stream);
 }
 
 int ast_inflow_raw(const double* s, const double* u, double* s2, double* u2, const ast_config* cfg, void* stream)

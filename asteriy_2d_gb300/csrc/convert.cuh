@@ -33,4 +33,18 @@ static __global__ void soa_to_aos(const R* __restrict__ q, double2* __restrict__
     u[k] = make_double2((double)q[o + 2 * plane], (double)q[o + 3 * plane]);
 }
 
+// The reference's nn2 (K double3, k = m*N + n; x and y read) as two SoA
+// planes of the solver's precision and row pitch
+template <typename R>
+static __global__ void nn2_to_planes(const double* __restrict__ nn2, R* __restrict__ q, int N, int M, long long ld,
+                                     long long plane)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (long long)N * M) return;
+    const int m = (int)(k / N), n = (int)(k - (long long)m * N);
+    const long long j = (long long)m * ld + n;
+    q[j] = (R)nn2[3 * k];
+    q[j + plane] = (R)nn2[3 * k + 1];
+}
+
 }  // namespace ast

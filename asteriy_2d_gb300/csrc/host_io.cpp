@@ -57,6 +57,8 @@ void ast_config_default(ast_config* c)
     c->riemann_tol = 10e-10;            // Header.h:62
     c->mlp_gate = 0.2;
     c->inflow_v = 1.0;
+    c->neutral_nh = 3.0;        // n_H, Header.h:85
+    c->neutral_kn = 0.419231;   // Kn, Header.h:84
     c->persistent = 1;
 }
 
@@ -75,6 +77,7 @@ int ast_config_check(const ast_config* c)
     if (c->persistent < 0 || c->persistent > 1) return AST_ERR_INVALID;
     if (c->skip_uniform < 0 || c->skip_uniform > 1) return AST_ERR_INVALID;
     if (!(c->inflow_p >= 0.0)) return AST_ERR_INVALID;
+    if (!std::isfinite(c->neutral_nh) || !std::isfinite(c->neutral_kn)) return AST_ERR_INVALID;
     for (int s = 0; s < 4; s++) {
         if (c->bc[s].kind < AST_BC_REFLECT || c->bc[s].kind > AST_BC_NONREFLECT) return AST_ERR_INVALID;
         if (c->bc[s].kind == AST_BC_FIXED && !(c->bc[s].rho > 0.0 && c->bc[s].p > 0.0)) return AST_ERR_INVALID;

@@ -313,6 +313,8 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
     P.body_hi = c.body_hi;
     P.body_rsplit = c.body_rsplit;
     P.body_amp = c.body_amp;
+    P.nsrc = nullptr;   // set by ast_set_neutral / ast_add_mk_raw
+    P.nsrc_coef = (c.neutral_kn != 0.0) ? c.neutral_nh / c.neutral_kn : 0.0;
 }
 
 extern template int launch_step_r<double, kSoA>(const StepParams&, int, int, cudaStream_t, bool);

@@ -46,6 +46,7 @@ struct DevClock {
                                    // strong_calls, strong_iters
     unsigned int next_tile;        // persistent kernel: next tile to hand out
     unsigned int pad_;
+    double T_prev;                 // dt the last step used
 };
 
 enum Layout { kSoA = 0, kAoS = 1 };
@@ -80,6 +81,12 @@ struct __align__(16) StepParams {
     int region_zlo, region_zhi, region_rlo, region_rhi;
     int body_force;
     double body_lo, body_hi, body_rsplit, body_amp;
+    // the neutral-coupling momentum source of add_MK: null, or per cell
+    // (nn2.x, nn2.y) as two SoA planes of the state's precision and pitch
+    // (solver) or the reference's double3 array (raw entry points); the
+    // momentum gains T_do * (rho * nsrc_coef) * (nn2.x, nn2.y)
+    const void* nsrc;
+    double nsrc_coef;
     // state: SoA planes (in/out) or reference AoS (s, u, s2, u2)
     const void* in;
     void* out;
@@ -321,8 +328,8 @@ __device__ __forceinline__ S& tile_smem()
 // axisymmetric with the cylindrical source: add_MK, kernel.cu:2480-2509.
 template <typename C, typename R>
 __device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C inv_g1, const R in[4],
-                                            const R f[4][4], C T_do, C tdv, C ty, C dx, C dy, C Q2, int& nrho,
-                                            int& np, R out[4], C* E2o = nullptr, C* KE2o = nullptr)
+                                            const R f[4][4], C T_do, C tdv, C ty, C dx, C dy, C Q2, C Sz, C Sr,
+                                            int& nrho, int& np, R out[4], C* E2o = nullptr, C* KE2o = nullptr)
 {
     const C r1 = (C)in[0], p1 = (C)in[1], vz1 = (C)in[2], vr1 = (C)in[3];
     C ps[4];
@@ -338,14 +345,14 @@ __device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C i
     if (P.geom == 1) {
         rho2 = r1 - tdv * ps[0] - ty * r1 * vr1;
         if (rho2 <= C(0)) { nrho++; rho2 = r1; }
-        mz = r1 * vz1 - tdv * ps[1] - ty * r1 * vr1 * vz1;
-        mr = r1 * vr1 - tdv * ps[2] - ty * r1 * vr1 * vr1 + T_do * Q2;
+        mz = r1 * vz1 - tdv * ps[1] - ty * r1 * vr1 * vz1 + Sz;
+        mr = r1 * vr1 - tdv * ps[2] - ty * r1 * vr1 * vr1 + T_do * Q2 + Sr;
         E2 = (p1 * inv_g1 + ke1) - tdv * ps[3] - ty * vr1 * (ga * p1 * inv_g1 + ke1) + T_do * Q3;
     } else {
         rho2 = r1 - tdv * ps[0];
         if (rho2 <= C(0)) { nrho++; rho2 = r1; }
-        mz = r1 * vz1 - tdv * ps[1];
-        mr = r1 * vr1 - tdv * ps[2] + T_do * Q2;
+        mz = r1 * vz1 - tdv * ps[1] + Sz;
+        mr = r1 * vr1 - tdv * ps[2] + T_do * Q2 + Sr;
         E2 = (p1 * inv_g1 + ke1) - tdv * ps[3] + T_do * Q3;
     }
     const C irho = C(1) / rho2;
@@ -355,6 +362,23 @@ __device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C i
     if (p2 <= C(0)) { np++; p2 = sizeof(C) == 4 ? (C)P.p_floorf : (C)P.p_floor; }
     out[0] = (R)rho2; out[1] = (R)p2; out[2] = (R)vz2; out[3] = (R)vr2;
     if (E2o) { *E2o = E2; *KE2o = KE2; }
+}
+
+// The neutral-coupling source of cell (n, m): SoA planes of the state's
+// precision (the solver's copy) or the reference's double3 array (raw
+// entry points, AoS layout)
+template <typename R, int LAYOUT, bool TO_SMEM, typename C>
+__device__ __forceinline__ void neutral_at(const StepParams& P, int n, int m, C& az, C& ar)
+{
+    if constexpr (LAYOUT == kSoA || TO_SMEM) {
+        const R* q = (const R*)P.nsrc + (long long)m * P.ld + n;
+        az = (C)__ldg(q);
+        ar = (C)__ldg(q + P.plane);
+    } else {
+        const double* q = (const double*)P.nsrc + 3 * ((long long)m * P.N + n);
+        az = (C)__ldg(q);
+        ar = (C)__ldg(q + 1);
+    }
 }
 
 // The pressure of an updated FP32 cell recovered in FP64, for cells whose
@@ -1149,15 +1173,24 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
     auto update_fp64 = [&](int row, int n, const R in[4], const R f[4][4], R o[4]) {
         const double T_do = K.T_do, tdv_d = K.tdv;
         const double y = sm.ydrow[row];
-        double Q2 = 0.0;
+        double Q2 = 0.0, Sz = 0.0, Sr = 0.0;
         if (P.body_force) {
             const double x = P.x_min + n * P.dx;
             if (x > P.body_lo && x < P.body_hi)
                 Q2 = (y >= P.body_rsplit) ? -P.body_amp * (double)in[0] : P.body_amp * (double)in[0];
         }
+        // the neutral-coupling source in the update (FP64 kernels; the FP32
+        // form adds it in neutral_kernel after the step)
+        if (sizeof(R) == 8 && P.nsrc) {
+            double az, ar;
+            neutral_at<R, LAYOUT, TO_SMEM>(P, n, m0 + row, az, ar);
+            const double w = T_do * ((double)in[0] * P.nsrc_coef);
+            Sz = w * az;
+            Sr = w * ar;
+        }
         const double ty = (P.geom == 1) ? T_do / y : 0.0;
-        update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty, P.dx, P.dy, Q2, acc.nrho,
-                            acc.np, o);
+        update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty, P.dx, P.dy, Q2, Sz, Sr,
+                            acc.nrho, acc.np, o);
     };
     // the FP32 form's source terms of a cell: ty = T_do/r and the body force
     auto sources_fp32 = [&](int row, int n, const R in[4], float& ty, float& Q2) {
@@ -1214,8 +1247,8 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
                 float ty, Q2;
                 sources_fp32(row, n, in, ty, Q2);
                 float E2, KE2;
-                update_cell<float>(P, gaf, g1f, ig1f, in, f, Tf, tdv_f, ty, dxf, dyf, Q2, acc.nrho, acc.np, o, &E2,
-                                   &KE2);
+                update_cell<float>(P, gaf, g1f, ig1f, in, f, Tf, tdv_f, ty, dxf, dyf, Q2, 0.0f, 0.0f, acc.nrho, acc.np,
+                                   o, &E2, &KE2);
                 // pressure recovery p = (g-1)(E - rho v^2/2) in FP64 where
                 // the kinetic energy is more than 99% of the total
                 if (KE2 > 0.99f * E2) deferred |= 2u << (2 * it);
@@ -1336,6 +1369,7 @@ __device__ __forceinline__ void cta_epilogue(const StepParams& P, TileAcc<R>& ac
         double dt = P.dt_cap;
         if (a > 0.0) dt = fmin(dt, P.krit_dx / a);
         if (b > 0.0) dt = fmin(dt, P.krit_dy / b);
+        C->T_prev = C->T_do;
         C->T_do = dt;
         C->TT = C->TT + dt;
         C->step = C->step + 1;
@@ -1664,6 +1698,39 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+
+// The FP32 form's neutral-coupling source, after the step (P.in: the state
+// the step read, P.out: the state it wrote; SoA planes): the momentum
+// T_do * (rho * coef) * (nn2.x, nn2.y) of add_MK (kernel.cu:2495-2496),
+// rho the old density, T_do the step's dt, added to the new momentum at
+// fixed total energy (add_MK's energy term is zero), in FP64:
+// v += S / rho', p -= (gamma - 1) rho' (|v + S/rho'|^2 - |v|^2) / 2, then
+// the pressure floor.  Cells of the fixed region are left as they are.
+// In the kernel the source term would cost the FP32 update registers and
+// time (2% at 4096x2048) on every step, used or not.
+static __global__ void neutral_kernel(StepParams P)
+{
+    const long long K = (long long)P.N * P.M;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < K; k += (long long)gridDim.x * blockDim.x) {
+        const int m = (int)(k / P.N), n = (int)(k - (long long)m * P.N);
+        if (P.fixed_region && n >= P.fixed_nlo && n <= P.fixed_nhi && m <= P.fixed_mhi &&
+            cell_fixed(P, P.x_min + n * P.dx, P.y_min + m * P.dy))
+            continue;
+        const long long j = (long long)m * P.ld + n;
+        const float* q = (const float*)P.in;
+        float* o = (float*)P.out;
+        const float* src = (const float*)P.nsrc;
+        const double T = P.clock->T_prev;
+        const double rho2 = o[j], vz = o[j + 2 * P.plane], vr = o[j + 3 * P.plane];
+        const double w = T * ((double)q[j] * P.nsrc_coef) / rho2;
+        const double vz2 = vz + w * (double)src[j], vr2 = vr + w * (double)src[j + P.plane];
+        double p2 = (double)o[j + P.plane] - P.gd.g1 * 0.5 * rho2 * ((vz2 * vz2 + vr2 * vr2) - (vz * vz + vr * vr));
+        if (p2 <= 0.0) p2 = P.p_floor;
+        o[j + P.plane] = (float)p2;
+        o[j + 2 * P.plane] = (float)vz2;
+        o[j + 3 * P.plane] = (float)vr2;
+    }
+}
 
 template <typename R, int LAYOUT>
 __global__ void inflow_kernel(StepParams P, double p_in, double v_in)

@@ -32,6 +32,8 @@ SIGNATURES = {
     "ast_get_clock": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int64)]),
     "ast_step": (C.c_int, [C.c_void_p, C.c_int]),
     "ast_step_host": (C.c_int, [C.c_void_p] * 5),
+    "ast_set_neutral": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "ast_add_mk_raw": (C.c_int, [C.c_void_p] * 9 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "ast_synchronize": (C.c_int, [C.c_void_p]),
     "ast_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.ast_stats), C.c_int]),
     "ast_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
@@ -290,6 +292,18 @@ class Solver:
         check(self.lib.ast_get_clock(self.h, C.byref(a), C.byref(b), C.byref(c)), "ast_get_clock")
         return a.value, b.value, c.value
 
+    def set_neutral(self, nn2):
+        """The neutral-coupling momentum source (add_MK's nn2): K (x, y, z)
+        triples, or None to remove it."""
+        if nn2 is None:
+            check(self.lib.ast_set_neutral(self.h, None, 0), "ast_set_neutral")
+            return
+        a = np.ascontiguousarray(nn2, dtype=np.float64).reshape(self.K, 3)
+        check(self.lib.ast_set_neutral(self.h, a.ctypes.data, 0), "ast_set_neutral")
+
+    def set_neutral_device(self, ptr):
+        check(self.lib.ast_set_neutral(self.h, C.c_void_p(ptr), 1), "ast_set_neutral")
+
     def step_host(self, s_in, u_in, s_out, u_out):
         """One step from host arrays to host arrays (ast_step_host): the
         addresses of four (K, 2) float64 arrays; page-locked arrays are
@@ -348,6 +362,14 @@ def step_raw(s, u, s2, u2, T, T_do, TT, cfg, method=1, stream=None):
     check(load().ast_step_raw(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), C.c_void_p(T),
                               C.c_void_p(T_do), C.c_void_p(TT), method, C.byref(cfg),
                               C.c_void_p(stream) if stream else None), "ast_step_raw")
+
+
+def add_mk_raw(s, u, s2, u2, nn2, T, T_do, cfg, stream=None):
+    """ast_add_mk_raw on device pointers (ints; nn2 may be 0 for none), the
+    add_MK drop-in with its neutral-coupling source."""
+    check(load().ast_add_mk_raw(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), None,
+                                C.c_void_p(nn2) if nn2 else None, None, C.c_void_p(T), C.c_void_p(T_do), 0, 0,
+                                C.byref(cfg), C.c_void_p(stream) if stream else None), "ast_add_mk_raw")
 
 
 def inflow_raw(s, u, s2, u2, cfg, stream=None):

@@ -163,7 +163,14 @@ typedef struct ast_config {
        column 1, unprimed the old state of column 0.  0 disables (default);
        the reference's values are 7 and 1.                                  */
     double  inflow_p, inflow_v;
-    double  reserved_d[5];
+    /* neutral-atom coupling (add_MK, kernel.cu:2495-2496): with a source
+       array set (ast_set_neutral, ast_add_mk_raw) the momentum gains
+       T_do * (rho * neutral_nh / neutral_kn) * (nn2.x, nn2.y) per step;
+       the reference's n_H and Kn (Header.h:84-85) are the defaults, 3 and
+       0.419231 (neutral_kn = 0: no source).  The energy term of add_MK
+       multiplies its source by 0 and is left out.                           */
+    double  neutral_nh, neutral_kn;
+    double  reserved_d[3];
 } ast_config;
 
 typedef struct ast_stats {
@@ -228,9 +235,18 @@ int ast_synchronize(ast_solver* solver);
    receive the new state in the layout of ast_get_state.  An output array
    may be its input array (in place); any other overlap is AST_ERR_INVALID.
    Page-locked arrays are moved in bands of rows, the copies in, the step
-   and the copies out overlapping; pageable arrays, or a configuration with
-   the inflow rule, take ast_set_state + ast_step + ast_get_state. */
+   and the copies out overlapping; pageable arrays, a configuration with
+   the inflow rule, or the FP32 form with a neutral-coupling source take
+   ast_set_state + ast_step + ast_get_state. */
 int ast_step_host(ast_solver* solver, const double* s_in, const double* u_in, double* s_out, double* u_out);
+/* The neutral-coupling momentum source of add_MK (kernel.cu:2495-2496):
+   nn2 holds K (x, y, z) triples in the reference's double3 layout (only x
+   and y enter the update); on_device=1 means a device pointer.  The solver
+   keeps its own copy; nn2 = NULL removes the source.  See
+   ast_config.neutral_nh.  The FP64 solver adds the source inside the
+   update, as add_MK does; the FP32 form adds it in a pass after the step
+   (same terms, in FP64, at the step's total energy). */
+int ast_set_neutral(ast_solver* solver, const double* nn2, int on_device);
 int ast_get_stats(ast_solver* solver, ast_stats* out, int reset);
 /* Device view of the current state: four planes rho, p, v_z, v_r of M rows
    with row pitch *ld elements of *elem_bytes bytes (8 = FP64, 4 = FP32),
@@ -285,6 +301,17 @@ int ast_mlp_train(const float* samples, int64_t n, int epochs, int batch, float 
 int ast_step_raw(const double* s, const double* u, double* s2, double* u2,
                  double* T, const double* T_do, const double* TT, int method,
                  const ast_config* cfg, void* cuda_stream);
+/* The same for
+     add_MK<<<K/256,256>>>(s, u, s2, u2, nn1, nn2, nn3, T, T_do, method, step)
+   (kernel.cu:2293, launched at kernel.cu:3723 and 3747), with its
+   neutral-coupling momentum source from nn2 (K double3, device pointer;
+   NULL: none).  nn1 and nn3 are accepted and not read (add_MK reads nn1
+   nowhere and multiplies its nn3 term by 0); method and step are ignored
+   like ast_step_raw's method.  cfg->geom should be AST_GEOM_AXISYM for
+   add_MK's update. */
+int ast_add_mk_raw(const double* s, const double* u, double* s2, double* u2, const double* nn1,
+                   const double* nn2, const double* nn3, double* T, const double* T_do, int method, int step,
+                   const ast_config* cfg, void* cuda_stream);
 /* Replacement for add2_bound<<<K/256,256>>>(s, u, s2, u2, ...)
    (kernel.cu:1895-1925, launched after the step at kernel.cu:3565, 3590):
    column n = 0 of (s2, u2) from the old state (s, u) and the new column 1,

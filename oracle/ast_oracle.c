@@ -23,7 +23,10 @@
  *                                    kernel.cu:2328-2382 (add_MK)
  *   reconstruction + faces ......... kernel.cu:2701-2857
  *   planar update .................. kernel.cu:3027-3073
- *   axisymmetric update ............ kernel.cu:2480-2509
+ *   axisymmetric update ............ kernel.cu:2480-2509, with add_MK's
+ *                                    neutral-coupling momentum source
+ *                                    (nn2, kernel.cu:2495-2496; also applied
+ *                                    to the planar update when set)
  *   dt (exact min, lagged) ......... kernel.cu:3013-3017, funk_time :1525-1536
  *   characteristic inflow .......... add2_bound kernel.cu:1895-1925
  *   non-reflecting ghost ........... the commented rule of add2, kernel.cu:1979-1985
@@ -690,6 +693,13 @@ static int in_region(const ast_config* c, double xf)
     return !c->region_select || (xf > c->region_lo && xf < c->region_hi);
 }
 
+/* The neutral-coupling source nn2 (K x, y, z triples, the reference's
+   double3 layout) the steps use, or NULL for none.  The array is read, not
+   copied: it must outlive the steps. */
+static const double* g_nn2 = NULL;
+
+void ora_set_neutral(const double* nn2) { g_nn2 = nn2; }
+
 /* One cell of one step.  Returns the cell's tmin; a cell held fixed returns
    1e7, the reset value of T, because the reference's fixed cells never
    touch T (kernel.cu:2318-2324). */
@@ -803,6 +813,15 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
     }
     tmin = fmin(tmin, t);
 
+    /* neutral-coupling momentum source of add_MK (kernel.cu:2495-2496):
+       T_do * (rho * n_H / Kn) * nn2[index].(x, y), with the reference's
+       expression order; its energy term multiplies nn3 by 0 */
+    double NSx = 0.0, NSy = 0.0;
+    if (g_nn2 && c->neutral_kn != 0.0) {
+        NSx = T_do * (s_1.x * c->neutral_nh / c->neutral_kn) * g_nn2[3 * (size_t)index];
+        NSy = T_do * (s_1.x * c->neutral_nh / c->neutral_kn) * g_nn2[3 * (size_t)index + 1];
+    }
+
     /* body force (kernel.cu:3034-3056) */
     double Q2x = 0.0, Q2 = 0.0, Q3;
     if (c->body_force && x > c->body_lo && x < c->body_hi)
@@ -819,8 +838,8 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
         PU.y = (Pu12.y + Pu14.y) * dy + (Pu13.y + Pu15.y) * dx;
         rs2.x = s_1.x - (T_do / dV) * PS.x - (T_do / y) * s_1.x * u_1.y;
         if (rs2.x <= 0) { st->rho_floor++; rs2.x = s_1.x; }
-        ru2.x = (s_1.x * u_1.x - (T_do / dV) * PU.x - (T_do / y) * s_1.x * u_1.y * u_1.x + T_do * Q2x) / rs2.x;
-        ru2.y = (s_1.x * u_1.y - (T_do / dV) * PU.y - (T_do / y) * s_1.x * u_1.y * u_1.y + T_do * Q2) / rs2.x;
+        ru2.x = (s_1.x * u_1.x - (T_do / dV) * PU.x - (T_do / y) * s_1.x * u_1.y * u_1.x + T_do * Q2x + NSx) / rs2.x;
+        ru2.y = (s_1.x * u_1.y - (T_do / dV) * PU.y - (T_do / y) * s_1.x * u_1.y * u_1.y + T_do * Q2 + NSy) / rs2.x;
         rs2.y = (((s_1.y / (ggg - 1.0) + s_1.x * (u_1.x * u_1.x + u_1.y * u_1.y) * 0.5) - (T_do / dV) * PS.y -
                   (T_do / y) * u_1.y * (ggg * s_1.y / (ggg - 1.0) + s_1.x * (u_1.x * u_1.x + u_1.y * u_1.y) * 0.5) +
                   T_do * Q3) -
@@ -833,8 +852,8 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
         PU.y = Pu12.y * dy + Pu13.y * dx + Pu14.y * dy + Pu15.y * dx;
         rs2.x = s_1.x - (T_do / dV) * PS.x;
         if (rs2.x <= 0.0) { st->rho_floor++; rs2.x = s_1.x; }
-        ru2.x = (s_1.x * u_1.x - (T_do / dV) * PU.x + T_do * Q2x) / rs2.x;
-        ru2.y = (s_1.x * u_1.y - (T_do / dV) * PU.y + T_do * Q2) / rs2.x;
+        ru2.x = (s_1.x * u_1.x - (T_do / dV) * PU.x + T_do * Q2x + NSx) / rs2.x;
+        ru2.y = (s_1.x * u_1.y - (T_do / dV) * PU.y + T_do * Q2 + NSy) / rs2.x;
         rs2.y = (((s_1.y / (ggg - 1) + s_1.x * (u_1.x * u_1.x + u_1.y * u_1.y) * 0.5) - (T_do / dV) * PS.y + T_do * Q3) -
                  0.5 * rs2.x * (ru2.x * ru2.x + ru2.y * ru2.y)) * (ggg - 1);
     }

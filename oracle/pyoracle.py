@@ -49,6 +49,8 @@ def lib():
         L.ora_face.restype = C.c_double
         L.ora_face.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
                                _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_double, _dp, _i64p]
+        L.ora_set_neutral.restype = None
+        L.ora_set_neutral.argtypes = [C.c_void_p]
         L.ora_step.restype = C.c_double
         L.ora_step.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_int, _i64p]
         L.ora_run.restype = C.c_int
@@ -85,6 +87,8 @@ def ref():
                                      C.POINTER(C.c_longlong), C.c_int]
         R.ora_run.restype = C.c_int
         R.ora_run.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _i64p, C.c_int, _i64p]
+        R.ref_set_neutral.restype = None
+        R.ref_set_neutral.argtypes = [C.c_void_p]
         R.ref_bound.restype = None
         R.ref_bound.argtypes = [_dp, _dp, _dp, _dp]
         R.ref_diag_count.restype = C.c_longlong
@@ -120,16 +124,22 @@ def step(cfg, s, u, T_do, nthreads=1):
     return s2, u2, T, cnt
 
 
-def run(cfg, s, u, nsteps, T_do=None, TT=0.0, step_no=0, nthreads=1):
-    """nsteps steps with the lagged-dt protocol.  Returns (s, u, T_do, TT, step, counters)."""
+def run(cfg, s, u, nsteps, T_do=None, TT=0.0, step_no=0, nthreads=1, nn2=None):
+    """nsteps steps with the lagged-dt protocol.  Returns (s, u, T_do, TT, step, counters).
+    nn2: the neutral-coupling source, K (x, y, z) triples (add_MK's nn2), or None."""
     s = np.array(s, dtype=np.float64, order="C")
     u = np.array(u, dtype=np.float64, order="C")
     tdo = C.c_double(cfg.dt_first if T_do is None else T_do)
     tt = C.c_double(TT)
     st = C.c_int64(step_no)
     cnt = np.zeros(10, dtype=np.int64)
-    rc = lib().ora_run(C.byref(cfg), _ptr(s), _ptr(u), nsteps, C.byref(tdo), C.byref(tt),
-                       C.byref(st), nthreads, cnt.ctypes.data_as(_i64p))
+    src = None if nn2 is None else np.ascontiguousarray(nn2, dtype=np.float64).reshape(-1, 3)
+    lib().ora_set_neutral(None if src is None else src.ctypes.data)
+    try:
+        rc = lib().ora_run(C.byref(cfg), _ptr(s), _ptr(u), nsteps, C.byref(tdo), C.byref(tt),
+                           C.byref(st), nthreads, cnt.ctypes.data_as(_i64p))
+    finally:
+        lib().ora_set_neutral(None)
     if rc != 0:
         raise RuntimeError(f"ora_run failed: {rc}")
     return s, u, tdo.value, tt.value, st.value, cnt
@@ -155,15 +165,23 @@ def ref_face(which, sL, uL, sR, uR, n1, n2, rad):
     return t, out
 
 
-def ref_run(kernel, cfg, s, u, nsteps, method=0, nthreads=1):
+def ref_run(kernel, cfg, s, u, nsteps, method=0, nthreads=1, nn2=None):
+    """nsteps launches of the reference's own kernel (REF_KERNEL_TVD, REF_ADD_MK,
+    ...) + funk_time; nn2: add_MK's neutral source (K x, y, z triples) or None
+    for the zeros of the reference's main."""
     ref_set(cfg)
     s = np.array(s, dtype=np.float64, order="C")
     u = np.array(u, dtype=np.float64, order="C")
     tdo = C.c_double(cfg.dt_first)
     tt = C.c_double(0.0)
     st = C.c_longlong(0)
-    ref().ref_kernel_run(kernel, _ptr(s), _ptr(u), nsteps, method, C.byref(tdo), C.byref(tt),
-                         C.byref(st), nthreads)
+    src = None if nn2 is None else np.ascontiguousarray(nn2, dtype=np.float64).reshape(-1, 3)
+    ref().ref_set_neutral(None if src is None else src.ctypes.data)
+    try:
+        ref().ref_kernel_run(kernel, _ptr(s), _ptr(u), nsteps, method, C.byref(tdo), C.byref(tt),
+                             C.byref(st), nthreads)
+    finally:
+        ref().ref_set_neutral(None)
     return s, u, tdo.value, tt.value, st.value
 
 

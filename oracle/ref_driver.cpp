@@ -81,6 +81,12 @@ double ref_face(int which, const double* sL, const double* uL, const double* sR,
     return t;
 }
 
+/* nn2 of add_MK's launches (K double3), or NULL for the zeros of the
+   reference's main (kernel.cu:3338). */
+static const double3* g_ref_nn2 = nullptr;
+
+void ref_set_neutral(const double* nn2) { g_ref_nn2 = reinterpret_cast<const double3*>(nn2); }
+
 /*
  * One launch of a reference step kernel over all K cells.
  * kernel: 0 Kernel_TVD (kernel.cu:2513), 1 add_MK (kernel.cu:2293),
@@ -114,7 +120,9 @@ double ref_kernel_step(int kernel, const double* s, const double* u, double* s2,
         for (int k = 0; k < Kc; k++) {
             threadIdx.x = (unsigned int)k;
             if (kernel == 0) Kernel_TVD(S, U, S2, U2, &Tl, &Tdo, &TTl, method);
-            else if (kernel == 1) add_MK(S, U, S2, U2, nn1.data(), nn2.data(), nn3.data(), &Tl, &Tdo, method, 0);
+            else if (kernel == 1)
+                add_MK(S, U, S2, U2, nn1.data(), g_ref_nn2 ? const_cast<double3*>(g_ref_nn2) : nn2.data(),
+                       nn3.data(), &Tl, &Tdo, method, 0);
             else add2(S, U, S2, U2, &Tl, &Tdo, &TTl, method, 0);
         }
 #ifdef _OPENMP

@@ -16,7 +16,11 @@ records their outputs on seeded inputs:
                  method 1 (HLLC_Aleksashov) and method 2 (exact Godunov), on
                  a 48x24 axisymmetric grid;
   inflow.npz     one launch of add2_bound (kernel.cu:1895-1925, p_H = 7,
-                 inflow speed 1) on a random old and new state, 24x8.
+                 inflow speed 1) on a random old and new state, 24x8;
+  step_mk_neutral.npz
+                 20 launches of add_MK method 0 (HLL) on the 48x24 grid with
+                 a random neutral-coupling source nn2 (kernel.cu:2495-2496;
+                 the reference's main passes zeros).
 
 The configurations that reproduce those kernels live in golden_configs.py so
 the tests use exactly the same ones.  Usage:  python tests/golden/make_golden.py
@@ -96,6 +100,16 @@ def make_inflow(rng):
     np.savez_compressed(os.path.join(HERE, "inflow.npz"), s=s, u=u, s2=s2, u2=u2, s2_out=b2, u2_out=c2)
 
 
+def make_neutral(rng):
+    cfg = G.add_mk_config(0)
+    K = cfg.N * cfg.M
+    s, u = G.random_state(K, rng)
+    nn2 = rng.uniform(-0.5, 0.5, (K, 3))
+    s1, u1, tdo, tt, st = O.ref_run(O.REF_ADD_MK, cfg, s, u, 20, method=0, nn2=nn2)
+    np.savez_compressed(os.path.join(HERE, "step_mk_neutral.npz"), s0=s, u0=u, nn2=nn2, s=s1, u=u1, T_do=tdo,
+                        TT=tt, steps=st, nsteps=20)
+
+
 def main():
     make_ref.main([])
     rng = np.random.default_rng(20261203)
@@ -105,6 +119,7 @@ def main():
     make_step("step_mk_god.npz", G.add_mk_config(2), O.REF_ADD_MK, 2, 20, rng)
     make_step("step_mk_hllca.npz", G.add_mk_config(1), O.REF_ADD_MK, 1, 20, rng)
     make_inflow(np.random.default_rng(1895))
+    make_neutral(np.random.default_rng(2495))
     print("golden vectors written to", HERE)
 
 

@@ -50,13 +50,23 @@ def test_config_default_matches_reference_macros():
 
 @pytest.mark.parametrize("field,value", [("N", 2), ("M", 0), ("gamma", 1.0), ("cfl", 0.0), ("flux", 7),
                                          ("riemann_max_iter", 0), ("x_max", -5.0),
-                                         ("persistent", 2), ("skip_uniform", 2), ("skip_uniform", -1)])
+                                         ("persistent", 2), ("skip_uniform", 2), ("skip_uniform", -1),
+                                         ("neutral_nh", float("nan")), ("neutral_kn", float("inf"))])
 def test_config_check_rejects(field, value):
     c = problems.blast_config(64, 32)
     setattr(c, field, value)
     assert solver.load().ast_config_check(C.byref(c)) == A.AST_ERR_INVALID
     h = C.c_void_p()
     assert solver.load().ast_create(C.byref(c), C.byref(h)) == A.AST_ERR_INVALID
+
+
+def test_null_solver_is_refused():
+    L = solver.load()
+    assert L.ast_set_neutral(None, None, 0) == A.AST_ERR_INVALID
+    assert L.ast_step_host(None, None, None, None, None) == A.AST_ERR_INVALID
+    c = problems.blast_config(64, 32)
+    assert L.ast_add_mk_raw(None, None, None, None, None, None, None, None, None, 0, 0, C.byref(c), None) == \
+        A.AST_ERR_INVALID
 
 
 def test_fixed_side_needs_positive_state():

@@ -62,6 +62,15 @@ def test_steps_bitwise_against_reference_kernels(fname, cfg):
     assert tdo == float(d["T_do"]) and tt == float(d["TT"]) and st == int(d["steps"])
 
 
+def test_neutral_source_bitwise_against_reference_add_mk():
+    # add_MK with a random nn2 (its momentum source, kernel.cu:2495-2496)
+    d = golden("step_mk_neutral.npz")
+    s, u, tdo, tt, st, _ = O.run(G.add_mk_config(0), d["s0"], d["u0"], int(d["nsteps"]), nthreads=2, nn2=d["nn2"])
+    np.testing.assert_array_equal(s, d["s"])
+    np.testing.assert_array_equal(u, d["u"])
+    assert tdo == float(d["T_do"]) and tt == float(d["TT"]) and st == int(d["steps"])
+
+
 def test_step_is_deterministic_across_thread_counts():
     cfg = G.tvd_config()
     rng = np.random.default_rng(3)
