@@ -1699,39 +1699,6 @@ __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, 
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
 
-// The FP32 form's neutral-coupling source, after the step (P.in: the state
-// the step read, P.out: the state it wrote; SoA planes): the momentum
-// T_do * (rho * coef) * (nn2.x, nn2.y) of add_MK (kernel.cu:2495-2496),
-// rho the old density, T_do the step's dt, added to the new momentum at
-// fixed total energy (add_MK's energy term is zero), in FP64:
-// v += S / rho', p -= (gamma - 1) rho' (|v + S/rho'|^2 - |v|^2) / 2, then
-// the pressure floor.  Cells of the fixed region are left as they are.
-// In the kernel the source term would cost the FP32 update registers and
-// time (2% at 4096x2048) on every step, used or not.
-static __global__ void neutral_kernel(StepParams P)
-{
-    const long long K = (long long)P.N * P.M;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < K; k += (long long)gridDim.x * blockDim.x) {
-        const int m = (int)(k / P.N), n = (int)(k - (long long)m * P.N);
-        if (P.fixed_region && n >= P.fixed_nlo && n <= P.fixed_nhi && m <= P.fixed_mhi &&
-            cell_fixed(P, P.x_min + n * P.dx, P.y_min + m * P.dy))
-            continue;
-        const long long j = (long long)m * P.ld + n;
-        const float* q = (const float*)P.in;
-        float* o = (float*)P.out;
-        const float* src = (const float*)P.nsrc;
-        const double T = P.clock->T_prev;
-        const double rho2 = o[j], vz = o[j + 2 * P.plane], vr = o[j + 3 * P.plane];
-        const double w = T * ((double)q[j] * P.nsrc_coef) / rho2;
-        const double vz2 = vz + w * (double)src[j], vr2 = vr + w * (double)src[j + P.plane];
-        double p2 = (double)o[j + P.plane] - P.gd.g1 * 0.5 * rho2 * ((vz2 * vz2 + vr2 * vr2) - (vz * vz + vr * vr));
-        if (p2 <= 0.0) p2 = P.p_floor;
-        o[j + P.plane] = (float)p2;
-        o[j + 2 * P.plane] = (float)vz2;
-        o[j + 3 * P.plane] = (float)vr2;
-    }
-}
-
 template <typename R, int LAYOUT>
 __global__ void inflow_kernel(StepParams P, double p_in, double v_in)
 {
