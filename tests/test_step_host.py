@@ -89,6 +89,28 @@ def test_banded_host_step_equals_set_step_get(prec, persistent, flux, grid):
     assert_same(reference_run(cfg, s0, u0, 5), host_run(cfg, s0, u0, 5))
 
 
+def test_uniform_tile_variant_and_stats():
+    # the persistent kernel's skip_uniform variant in bands; the counters
+    # of the banded step equal those of the whole-grid step
+    cfg = problems.blast_config(640, 320, flux=A.FLUX_GODUNOV, precision=A.PREC_FP32)
+    cfg.skip_uniform, cfg.collect_stats = 1, 1
+    s0, u0 = solver.fill_blast(cfg)
+    ref = reference_run(cfg, s0, u0, 3)
+    assert_same(ref, host_run(cfg, s0, u0, 3))
+    K = cfg.N * cfg.M
+    a = [pinned((K, 2)) for _ in range(4)]
+    a[0].numpy()[:] = s0
+    a[1].numpy()[:] = u0
+    with solver.Solver(cfg) as S:
+        S.step_host(*(t.data_ptr() for t in a))
+        st_host = S.stats()
+    with solver.Solver(cfg) as S:
+        S.set_state(s0, u0)
+        S.step(1)
+        st_plain = S.stats()
+    assert st_host == st_plain
+
+
 @pytest.mark.parametrize("prec", [A.PREC_FP32, A.PREC_FP64])
 def test_in_place(prec):
     cfg = problems.wind_config(256, 160, precision=prec)
