@@ -32,6 +32,7 @@ SIGNATURES = {
     "ast_get_clock": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int64)]),
     "ast_step": (C.c_int, [C.c_void_p, C.c_int]),
     "ast_step_host": (C.c_int, [C.c_void_p] * 5),
+    "ast_step_host_n": (C.c_int, [C.c_void_p, C.c_int] + [C.c_void_p] * 4),
     "ast_set_neutral": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "ast_add_mk_raw": (C.c_int, [C.c_void_p] * 9 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "ast_synchronize": (C.c_int, [C.c_void_p]),
@@ -303,6 +304,12 @@ class Solver:
 
     def set_neutral_device(self, ptr):
         check(self.lib.ast_set_neutral(self.h, C.c_void_p(ptr), 1), "ast_set_neutral")
+
+    def step_host_n(self, n, s_a, u_a, s_b, u_b):
+        """n host-array steps ping-ponging between two pairs of (K, 2)
+        float64 arrays given by address (ast_step_host_n)."""
+        check(self.lib.ast_step_host_n(self.h, n, C.c_void_p(s_a), C.c_void_p(u_a), C.c_void_p(s_b),
+                                       C.c_void_p(u_b)), "ast_step_host_n")
 
     def step_host(self, s_in, u_in, s_out, u_out):
         """One step from host arrays to host arrays (ast_step_host): the

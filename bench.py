@@ -343,23 +343,19 @@ def accuracy(nsteps, params):
     return out
 
 
-def time_e2e(form, start, steps, torch, params=None, banded=True):
+def time_e2e(form, start, steps, torch, params=None, mode="chain"):
     """Through the public API with host buffers: every step copies the state
     in from pinned host memory, steps once and writes the result back to
-    pinned host memory.  banded: one ast_step_host call per step (the copies
-    in, the step and the copies out pipelined over bands of rows, ping-pong
-    between two pairs of host arrays); otherwise ast_set_state, ast_step(1),
-    ast_get_state."""
+    pinned host memory (ping-pong between two pairs of host arrays).
+    mode "chain": one ast_step_host_n call for all the steps (the copies in,
+    the step and the copies out pipelined over bands of rows, and the bands
+    of consecutive steps overlapping); "per_step": one ast_step_host call
+    per step; "three_calls": ast_set_state, ast_step(1), ast_get_state."""
     from asteriy_2d_gb300 import solver
     s0, u0, clock = start
     cfg = make_config(form)
     K = cfg.N * cfg.M
-    hs = torch.empty((K, 2), dtype=torch.float64, pin_memory=True)
-    hu = torch.empty((K, 2), dtype=torch.float64, pin_memory=True)
-    hs.numpy()[:] = s0
-    hu.numpy()[:] = u0
-    hs2 = torch.empty((K, 2), dtype=torch.float64, pin_memory=True) if banded else hs
-    hu2 = torch.empty((K, 2), dtype=torch.float64, pin_memory=True) if banded else hu
+    hs, hu, hs2, hu2 = (torch.empty((K, 2), dtype=torch.float64, pin_memory=True) for _ in range(4))
     lib = solver.load()
     with solver.Solver(cfg) as S:
         if params is not None:
@@ -367,23 +363,29 @@ def time_e2e(form, start, steps, torch, params=None, banded=True):
         S.set_clock(*clock)
         bufs = [(hs, hu), (hs2, hu2)]
 
-        def one():
-            if banded:
+        def run(n):
+            if mode == "chain":
                 (a_s, a_u), (b_s, b_u) = bufs
-                S.step_host(a_s.data_ptr(), a_u.data_ptr(), b_s.data_ptr(), b_u.data_ptr())
-                bufs.reverse()
+                S.step_host_n(n, a_s.data_ptr(), a_u.data_ptr(), b_s.data_ptr(), b_u.data_ptr())
                 return
-            solver.check(lib.ast_set_state(S.h, hs.data_ptr(), hu.data_ptr(), 0), "set_state")
-            S.step(1, sync=False)
-            solver.check(lib.ast_get_state(S.h, hs.data_ptr(), hu.data_ptr(), 0), "get_state")
-        one()
-        bufs.reverse()
+            for _ in range(n):
+                (a_s, a_u), (b_s, b_u) = bufs
+                if mode == "per_step":
+                    S.step_host(a_s.data_ptr(), a_u.data_ptr(), b_s.data_ptr(), b_u.data_ptr())
+                else:
+                    solver.check(lib.ast_set_state(S.h, a_s.data_ptr(), a_u.data_ptr(), 0), "set_state")
+                    S.step(1, sync=False)
+                    solver.check(lib.ast_get_state(S.h, b_s.data_ptr(), b_u.data_ptr(), 0), "get_state")
+                bufs.reverse()
         hs.numpy()[:] = s0
         hu.numpy()[:] = u0
+        run(1)   # warm-up (streams, events, graph-free launch path)
+        hs.numpy()[:] = s0
+        hu.numpy()[:] = u0
+        bufs[:] = [(hs, hu), (hs2, hu2)]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(steps):
-            one()
+        run(steps)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
     return dt, 2 * K * 16, 2 * K * 16
@@ -669,10 +671,10 @@ def main():
     if "fp32_learned_skip" in finals and "fp32_learned" in finals:
         forms["fp32_learned_skip"]["bitwise_equal_to_fp32_learned"] = bool(
             np.array_equal(finals["fp32_learned_skip"], finals["fp32_learned"]))
-    esec, bi, bo = time_e2e(args.form, start, e2e_steps, torch,
-                            params if args.form.startswith("fp32_learned") else None)
-    esec3, _, _ = time_e2e(args.form, start, e2e_steps, torch,
-                           params if args.form.startswith("fp32_learned") else None, banded=False)
+    eparams = params if args.form.startswith("fp32_learned") else None
+    esec, bi, bo = time_e2e(args.form, start, e2e_steps, torch, eparams)
+    esec1, _, _ = time_e2e(args.form, start, e2e_steps, torch, eparams, mode="per_step")
+    esec3, _, _ = time_e2e(args.form, start, e2e_steps, torch, eparams, mode="three_calls")
     hbm, src = peaks()
     prec = "fp64" if args.form.startswith("fp64") else "fp32"
     achieved = BYTES_PER_CELL[prec] * cells / (sec / args.steps) / 1e9
@@ -695,8 +697,12 @@ def main():
         "forms": forms,
         "e2e": {"value": cells * e2e_steps / esec, "unit": "cell-updates/s", "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo,
-                "note": "per step: one ast_step_host call, pinned host arrays in and out (copies in, step and "
-                        "copies out pipelined over 16 bands of rows)",
+                "steps": e2e_steps,
+                "note": "one ast_step_host_n call for all the steps; every step copies its whole input in from "
+                        "pinned host arrays and its whole result out to pinned host arrays (pipelined over 4 "
+                        "bands of rows, the bands of consecutive steps overlapping)",
+                "per_step": {"value": cells * e2e_steps / esec1, "unit": "cell-updates/s",
+                             "note": "one ast_step_host call per step (16 bands)"},
                 "three_calls": {"value": cells * e2e_steps / esec3, "unit": "cell-updates/s",
                                 "note": "per step: ast_set_state from pinned host, ast_step(1), "
                                         "ast_get_state to pinned host"}},

@@ -239,6 +239,15 @@ int ast_synchronize(ast_solver* solver);
    the inflow rule, or the FP32 form with a neutral-coupling source take
    ast_set_state + ast_step + ast_get_state. */
 int ast_step_host(ast_solver* solver, const double* s_in, const double* u_in, double* s_out, double* u_out);
+/* nsteps such steps between two pairs of host arrays: step k reads
+   (s_a, u_a) and writes (s_b, u_b) for even k, the reverse for odd k, so
+   the result is in (s_b, u_b) when nsteps is odd and in (s_a, u_a) when it
+   is even.  Every step copies its whole input in and its whole result
+   out; with page-locked arrays a band of step k + 1 goes in as soon as the
+   same band of step k is out, so the copies of consecutive steps overlap.
+   Same array rules and fallbacks as ast_step_host; the pairs may be the
+   same arrays (in place). */
+int ast_step_host_n(ast_solver* solver, int nsteps, double* s_a, double* u_a, double* s_b, double* u_b);
 /* The neutral-coupling momentum source of add_MK (kernel.cu:2495-2496):
    nn2 holds K (x, y, z) triples in the reference's double3 layout (only x
    and y enter the update); on_device=1 means a device pointer.  The solver

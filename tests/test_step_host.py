@@ -150,3 +150,32 @@ def test_overlapping_arrays_are_refused():
             S.step_host(p, p + K * 16, p + K * 8, p + 2 * K * 16)
         with pytest.raises(solver.AstError):
             S.step_host(p, p + K * 16, p + 2 * K * 16, p + 2 * K * 16)
+
+
+@pytest.mark.parametrize("prec,persistent,grid,in_place", [
+    (A.PREC_FP32, 1, (512, 384), False),
+    (A.PREC_FP32, 1, (300, 130), True),
+    (A.PREC_FP64, 0, (256, 160), False),
+])
+def test_n_steps_chain_equals_single_steps(prec, persistent, grid, in_place):
+    # ast_step_host_n: the copies of consecutive steps overlap; every step's
+    # result must still equal the step-by-step one, and the last result
+    # lies in the pair the step count's parity names
+    cfg = problems.blast_config(*grid, flux=A.FLUX_GODUNOV, precision=prec)
+    cfg.persistent = persistent
+    s0, u0 = solver.fill_blast(cfg)
+    u0[:, 0] = np.linspace(-0.3, 0.4, len(u0))
+    K = cfg.N * cfg.M
+    for n in (1, 4, 7):
+        ref = reference_run(cfg, s0, u0, n)[-1]
+        a_s, a_u, b_s, b_u = (pinned((K, 2)) for _ in range(4))
+        a_s.numpy()[:] = s0
+        a_u.numpy()[:] = u0
+        if in_place:
+            b_s, b_u = a_s, a_u
+        with solver.Solver(cfg) as S:
+            S.step_host_n(n, a_s.data_ptr(), a_u.data_ptr(), b_s.data_ptr(), b_u.data_ptr())
+            clk = S.clock()
+        s, u = (b_s, b_u) if n % 2 else (a_s, a_u)
+        assert np.array_equal(s.numpy(), ref[0]) and np.array_equal(u.numpy(), ref[1]), n
+        assert clk == ref[2]
