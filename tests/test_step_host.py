@@ -179,3 +179,20 @@ def test_n_steps_chain_equals_single_steps(prec, persistent, grid, in_place):
         s, u = (b_s, b_u) if n % 2 else (a_s, a_u)
         assert np.array_equal(s.numpy(), ref[0]) and np.array_equal(u.numpy(), ref[1]), n
         assert clk == ref[2]
+
+
+def test_n_steps_pageable_takes_the_plain_calls():
+    cfg = problems.blast_config(128, 64, flux=A.FLUX_HLLC, precision=A.PREC_FP32)
+    s0, u0 = solver.fill_blast(cfg)
+    ref = reference_run(cfg, s0, u0, 3)[-1]
+    a_s, a_u = s0.copy(), u0.copy()
+    b_s, b_u = np.empty_like(s0), np.empty_like(u0)
+    with solver.Solver(cfg) as S:
+        S.step_host_n(3, a_s.ctypes.data, a_u.ctypes.data, b_s.ctypes.data, b_u.ctypes.data)
+        clk = S.clock()
+    assert np.array_equal(b_s, ref[0]) and np.array_equal(b_u, ref[1]) and clk == ref[2]
+    with solver.Solver(cfg) as S:
+        S.step_host_n(0, a_s.ctypes.data, a_u.ctypes.data, b_s.ctypes.data, b_u.ctypes.data)
+        assert S.clock()[2] == 0
+        with pytest.raises(solver.AstError):
+            S.step_host_n(-1, a_s.ctypes.data, a_u.ctypes.data, b_s.ctypes.data, b_u.ctypes.data)
