@@ -97,6 +97,13 @@ struct ast_batch {
     std::vector<cudaStream_t> pstream;
     std::vector<cudaEvent_t> pev;
     cudaEvent_t pfork = nullptr;
+    // FP32, one reconstruction: every problem in one launch of the mixed
+    // kernel (32x16 tiles, slot order)
+    bool mix_ok = false;
+    int mixed = 0;                      // 1: steps are mixed launches
+    int* mix_start = nullptr;           // prefix sums of the problems' tiles (nprob + 1)
+    int mix_tiles = 0, mix_recon = 0;
+    float ms_mixed = 0.0f, ms_split = 0.0f;   // autotuner: ms per step, one launch / per class
 };
 
 namespace {
@@ -192,6 +199,15 @@ int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool l
 // streams, forked from and joined back into `st`
 int enqueue_steps(ast_batch* B, cudaStream_t st, int count)
 {
+    if (B->mixed) {
+        for (int i = 0; i < count; i++) {
+            const int rc = launch_batch_mixed(B->dP[B->cur], B->mix_start, B->nprob, B->mix_tiles, B->mix_recon, st,
+                                              true);
+            if (rc != AST_OK) return rc;
+            B->cur ^= 1;
+        }
+        return AST_OK;
+    }
     const int nc = (int)B->cls.size();
     BATCH_CUDA(cudaEventRecord(B->ev[0], st));   // the fork point
     const int cur0 = B->cur;
@@ -426,6 +442,21 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
     }
     for (size_t c = 0; c < B->cls.size() && rc == AST_OK; c++)
         for (int sh = 0; sh < B->schedules && rc == AST_OK; sh++) rc = launch_class(B, B->cls[c], sh, nullptr, false);
+    // the one-launch work list (FP32, when every problem has the same
+    // reconstruction): every slot's 32x16 tiles
+    B->mix_ok = B->elem == 4;
+    for (int i = 1; i < nprob; i++)
+        if (cfgs[i].recon != cfgs[0].recon) B->mix_ok = false;
+    if (rc == AST_OK && B->mix_ok) {
+        std::vector<int> ms(nprob + 1, 0);
+        for (int s = 0; s < nprob; s++) ms[s + 1] = ms[s] + tiles_of(B->cfg[order[s]], 0);
+        B->mix_tiles = ms[nprob];
+        B->mix_recon = cfgs[0].recon;
+        if ((e = cudaMalloc(&B->mix_start, sizeof(int) * ms.size())) != cudaSuccess ||
+            (e = cudaMemcpy(B->mix_start, ms.data(), sizeof(int) * ms.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            rc = cuda_fail(e, "batch work list");
+        if (rc == AST_OK) rc = launch_batch_mixed(nullptr, nullptr, 0, 0, B->mix_recon, nullptr, false);
+    }
     for (size_t c = 1; c < B->cls.size() && rc == AST_OK; c++) {
         cudaStream_t s;
         if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) {
@@ -467,6 +498,7 @@ int ast_batch_destroy(ast_batch* B)
     cudaFree(B->dP[0]);
     cudaFree(B->dP[1]);
     cudaFree(B->tile_start);
+    cudaFree(B->mix_start);
     cudaFree(B->stage_s);
     cudaFree(B->stage_u);
     cudaFree(B->mlp);
@@ -649,9 +681,36 @@ int ast_batch_info(ast_batch* B, int64_t* cells, int64_t* tiles, int* launches_p
     if (cells) *cells = B->cells;
     if (tiles) {
         *tiles = 0;
-        for (const BatchClass& k : B->cls) *tiles += k.tiles[k.shape];
+        if (B->mixed) *tiles = B->mix_tiles;
+        else
+            for (const BatchClass& k : B->cls) *tiles += k.tiles[k.shape];
     }
-    if (launches_per_step) *launches_per_step = (int)B->cls.size();
+    if (launches_per_step) *launches_per_step = B->mixed ? 1 : (int)B->cls.size();
+    return AST_OK;
+}
+
+int ast_batch_num_classes(ast_batch* B)
+{
+    if (!B) return set_error(AST_ERR_INVALID, "null batch");
+    return (int)B->cls.size();
+}
+
+int ast_batch_set_mixed(ast_batch* B, int on)
+{
+    if (!B || on < 0 || on > 1) return set_error(AST_ERR_INVALID, "bad argument");
+    if (on && !B->mix_ok)
+        return set_error(AST_ERR_UNSUPPORTED, "one launch needs FP32 problems with one reconstruction");
+    B->mixed = on;
+    drop_graph(B);
+    return AST_OK;
+}
+
+int ast_batch_get_mixed(ast_batch* B, int* on, float* ms_mixed, float* ms_split)
+{
+    if (!B) return set_error(AST_ERR_INVALID, "null batch");
+    if (on) *on = B->mixed;
+    if (ms_mixed) *ms_mixed = B->ms_mixed;
+    if (ms_split) *ms_split = B->ms_split;
     return AST_OK;
 }
 
@@ -720,6 +779,29 @@ int ast_batch_autotune(ast_batch* B, int trials)
                 k.shape = sh;
             }
         }
+    }
+    // then the whole step: the classes' chosen schedules (one launch per
+    // class, concurrent chains) against every problem in one launch
+    if (rc == AST_OK && B->mix_ok) {
+        const int cur0 = B->cur;
+        float ms2[2] = {0.0f, 0.0f};
+        for (int mode = 0; mode < 2 && rc == AST_OK; mode++) {
+            B->mixed = mode;
+            rc = enqueue_steps(B, B->stream, 1);   // warm-up
+            B->cur = cur0;
+            if (rc == AST_OK && (e = cudaEventRecord(e0, B->stream)) != cudaSuccess) rc = cuda_fail(e, "event");
+            for (int t = 0; t < trials && rc == AST_OK; t++) {
+                rc = enqueue_steps(B, B->stream, 1);
+                B->cur = cur0;
+            }
+            if (rc == AST_OK && (e = cudaEventRecord(e1, B->stream)) != cudaSuccess) rc = cuda_fail(e, "event");
+            if (rc == AST_OK && (e = cudaEventSynchronize(e1)) != cudaSuccess) rc = cuda_fail(e, "event");
+            if (rc == AST_OK && (e = cudaEventElapsedTime(&ms2[mode], e0, e1)) != cudaSuccess) rc = cuda_fail(e, "event");
+        }
+        B->cur = cur0;
+        B->ms_split = ms2[0] / trials;
+        B->ms_mixed = ms2[1] / trials;
+        B->mixed = (rc == AST_OK && B->ms_mixed < B->ms_split) ? 1 : 0;
     }
     e = cudaMemcpyAsync(B->clocks, B->clock_save, sizeof(DevClock) * B->nprob, cudaMemcpyDeviceToDevice,
                         B->stream);

@@ -1,0 +1,34 @@
+// batch_mixed.cu - the FP32 batch kernel over problems of every flux in
+// one launch (32x16 tiles).
+#include "launch.cuh"
+
+namespace ast {
+
+template <bool RECON>
+static int launch_mixed_t(const StepParams* Ps, const int* tile_start, int nprob, int tiles, cudaStream_t st,
+                          bool launch)
+{
+    constexpr int TZ = kShapeTZ[0], TR = kShapeTR[0];
+    auto k = batch_kernel_mixed<float, RECON, TZ, TR>;
+    constexpr size_t smem =
+        std::max(std::max(tile_smem_bytes<float, 0, TZ, TR>(), tile_smem_bytes<float, 1, TZ, TR>()),
+                 std::max(tile_smem_bytes<float, 2, TZ, TR>(), tile_smem_bytes<float, 3, TZ, TR>()));
+    cudaError_t e;
+    if (!launch) {
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaFuncSetAttribute");
+    }
+    if (tiles <= 0) return AST_OK;
+    k<<<tiles, kThreads, smem, st>>>(Ps, tile_start, nprob);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? AST_OK : cuda_fail(e, "mixed batch kernel launch");
+}
+
+int launch_batch_mixed(const StepParams* Ps, const int* tile_start, int nprob, int tiles, int recon, cudaStream_t st,
+                       bool launch)
+{
+    return recon ? launch_mixed_t<true>(Ps, tile_start, nprob, tiles, st, launch)
+                 : launch_mixed_t<false>(Ps, tile_start, nprob, tiles, st, launch);
+}
+
+}  // namespace ast

@@ -70,6 +70,7 @@ struct __align__(16) StepParams {
     int fixed_nlo, fixed_nhi, fixed_mhi;   // cells that can lie in the region (one cell of margin)
     int region_select;
     int skip_uniform;              // uniform tiles skip the face pass
+    int flux_kind;                 // the kernels' FLUX: 0 HLL, 1 HLLC, 2 exact Godunov, 3 HLLC_Aleksashov
     // one step launched in bands of tile rows: this launch steps tile rows
     // [band_lo, band_hi) (band_hi 0: all rows of the grid), and `units` CTAs
     // of all the step's launches report to the clock (0: this launch's grid)
@@ -1445,6 +1446,40 @@ __global__ void __launch_bounds__(kThreads, min_ctas<R, FLUX>())
     const int t = (int)blockIdx.x - tile_start[j];
     const int tz = (sP.N + TZ - 1) / TZ;
     step_tile<R, FLUX, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, (unsigned)(tile_start[j + 1] - tile_start[j]));
+}
+
+// Many problems of any fluxes (one reconstruction) in one launch: as
+// batch_kernel, each CTA then steps its tile with the tile code of its
+// problem's flux (a CTA runs one of the four; the dynamic shared memory is
+// the largest of their tile spaces)
+template <typename R, bool RECON, int TZ, int TR>
+__global__ void __launch_bounds__(kThreads, min_ctas<R, 2>())
+    batch_kernel_mixed(const StepParams* __restrict__ Ps, const int* __restrict__ tile_start, int nprob)
+{
+    __shared__ __align__(16) StepParams sP;
+    __shared__ int s_j;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nprob - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tile_start[mid] <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+        }
+        s_j = lo;
+    }
+    __syncthreads();
+    const int j = s_j;
+    for (int w = threadIdx.x; w < (int)(sizeof(StepParams) / 16); w += kThreads)
+        reinterpret_cast<int4*>(&sP)[w] = reinterpret_cast<const int4*>(Ps + j)[w];
+    __syncthreads();
+    const int t = (int)blockIdx.x - tile_start[j];
+    const int tz = (sP.N + TZ - 1) / TZ;
+    const unsigned tiles = (unsigned)(tile_start[j + 1] - tile_start[j]);
+    switch (sP.flux_kind) {
+    case 0: step_tile<R, 0, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, tiles); break;
+    case 1: step_tile<R, 1, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, tiles); break;
+    case 3: step_tile<R, 3, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, tiles); break;
+    default: step_tile<R, 2, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, tiles); break;
+    }
 }
 
 // The FP32 solver's persistent kernel: as many CTAs as fit on the GPU at

@@ -69,6 +69,9 @@ SIGNATURES = {
     "ast_batch_set_mlp": (C.c_int, [C.c_void_p, _fp]),
     "ast_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
     "ast_batch_autotune": (C.c_int, [C.c_void_p, C.c_int]),
+    "ast_batch_num_classes": (C.c_int, [C.c_void_p]),
+    "ast_batch_set_mixed": (C.c_int, [C.c_void_p, C.c_int]),
+    "ast_batch_get_mixed": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), _fp, _fp]),
     "ast_batch_class": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _fp]),
     "ast_batch_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
@@ -513,7 +516,7 @@ class Batch:
         """Per (flux, recon) class: problems, tile shape in use, and the
         autotuner's ms per step of each built shape."""
         out = []
-        for k in range(self.info()["launches_per_step"]):
+        for k in range(self.lib.ast_batch_num_classes(self.h)):
             v = [C.c_int() for _ in range(6)]
             ms = np.zeros(len(SCHEDULES), dtype=np.float32)
             check(self.lib.ast_batch_class(self.h, k, *[C.byref(x) for x in v], _fptr(ms)), "ast_batch_class")
@@ -525,6 +528,18 @@ class Batch:
     def autotune(self, trials=3):
         check(self.lib.ast_batch_autotune(self.h, trials), "ast_batch_autotune")
         return self.classes()
+
+    def set_mixed(self, on):
+        """One launch per step for the whole batch (ast_batch_set_mixed)."""
+        check(self.lib.ast_batch_set_mixed(self.h, int(on)), "ast_batch_set_mixed")
+
+    def mixed(self):
+        """(one-launch mode on, tuner ms per step one launch, per class)."""
+        on = C.c_int()
+        a = np.zeros(1, dtype=np.float32)
+        b = np.zeros(1, dtype=np.float32)
+        check(self.lib.ast_batch_get_mixed(self.h, C.byref(on), _fptr(a), _fptr(b)), "ast_batch_get_mixed")
+        return bool(on.value), float(a[0]), float(b[0])
 
     def set_tiles(self, cls, tile_z, tile_r):
         check(self.lib.ast_batch_set_tiles(self.h, cls, tile_z, tile_r), "ast_batch_set_tiles")

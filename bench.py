@@ -412,6 +412,7 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
         # tile shape per class, timed on the initial states (the tuner
         # leaves the state and clocks as they were)
         classes = B.autotune(3)
+        one_launch = B.mixed()
         info = B.info()
         B.step(warmup)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -465,6 +466,11 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
                      "schedule": solver.SCHEDULES[c["schedule"]], "tile": "%dx%d" % c["tile"],
                      "tuner_ms": {name: round(m, 4) for name, m in zip(solver.SCHEDULES, c["ms_per_schedule"])}}
                     for c in classes],
+        "one_launch": {"in_use": one_launch[0], "tuner_ms": round(one_launch[1], 4),
+                       "tuner_ms_per_class_launches": round(one_launch[2], 4),
+                       "note": "every problem in one launch of the mixed kernel (32x16 tiles, each CTA the tile "
+                               "code of its problem's flux) against one launch per class; the tuner keeps the "
+                               "faster"},
         "mix": {k: kinds.count(k) for k in sorted(set(kinds))},
         "solo_value": cells * solo_steps / solo_sec, "solo_steps": solo_steps,
         "l1_rho_vs_fp64": {"median": float(np.median(l1)), "max": float(l1.max()),

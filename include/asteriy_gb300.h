@@ -381,8 +381,11 @@ int ast_batch_synchronize(ast_batch* batch);
 int ast_batch_get_stats(ast_batch* batch, int prob, ast_stats* out, int reset);
 int ast_batch_set_mlp(ast_batch* batch, const float* params);
 /* cells of all problems, tiles of all problems (at the tile shapes in use),
-   and kernel launches per step (the number of (flux, recon) classes) */
+   and kernel launches per step (the number of (flux, recon) classes, or 1
+   in the one-launch mode) */
 int ast_batch_info(ast_batch* batch, int64_t* cells, int64_t* tiles, int* launches_per_step);
+/* the number of (flux, recon) classes */
+int ast_batch_num_classes(ast_batch* batch);
 /* Schedules.  Each class steps with one schedule: 0, 1, 2 = one CTA per
  * tile with tiles of 32x16, 16x16 or 64x8 (z x r) cells; 3 = the persistent
  * batch kernel (FP32 only; the class's tiles of 32x16 staged and stored by
@@ -405,6 +408,18 @@ int ast_batch_class(ast_batch* batch, int cls, int* flux, int* recon, int* nprob
                     int* tile_r, float* ms_per_schedule);
 int ast_batch_set_schedule(ast_batch* batch, int cls, int schedule);
 int ast_batch_set_tiles(ast_batch* batch, int cls, int tile_z, int tile_r);
+/* One launch per step for the whole batch (FP32 batches whose problems
+ * share one reconstruction): every problem's 32x16 tiles in one work list,
+ * each CTA running the tile code of its problem's flux, instead of one
+ * launch per class.  The results are those of schedule 0 for every class,
+ * bit for bit.  ast_batch_autotune, after the per-class schedules, times a
+ * whole step both ways (the classes' schedules as concurrent chains, and
+ * the one launch) and keeps the faster; ast_batch_get_mixed reports the
+ * mode in use and those two times (ms per step, 0 when not timed).
+ * ast_batch_set_mixed(batch, 1) on a batch that cannot run this way is
+ * AST_ERR_UNSUPPORTED. */
+int ast_batch_set_mixed(ast_batch* batch, int on);
+int ast_batch_get_mixed(ast_batch* batch, int* on, float* ms_mixed, float* ms_split);
 
 /* A seeded set of benchmark problems: problem i draws, in this order from
  * one std::mt19937_64(seed) stream (u = (draw >> 11) * 2^-53, b = draw >> 63):

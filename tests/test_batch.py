@@ -267,3 +267,58 @@ def test_autotune_leaves_the_run_unchanged():
         U.step(20)
         for i in range(len(cfgs)):
             assert_agree(A.PREC_FP32, T.get_state(i), U.get_state(i), T.clock(i), U.clock(i), i)
+
+
+@pytest.mark.gpu
+def test_one_launch_mode():
+    """Every problem in one launch (the mixed kernel: each CTA the tile code
+    of its problem's flux) steps as schedule 0 of every class does."""
+    probs = small_set(A.PREC_FP32, n=7)
+    probs[0].cfg.N, probs[0].cfg.M = 150, 70
+    probs[1].cfg.N, probs[1].cfg.M = 33, 17
+    probs[2].cfg.flux = A.FLUX_HLLC_A
+    probs[3].cfg.flux = A.FLUX_HLL
+    cfgs = [p.cfg for p in probs]
+    init = [solver.problem_fill(p) for p in probs]
+    states = []
+    for mixed in (True, False):
+        with solver.Batch(cfgs) as B:
+            if mixed:
+                B.set_mixed(True)
+                assert B.info()["launches_per_step"] == 1 and B.mixed()[0]
+            else:
+                for k in range(B.info()["launches_per_step"]):
+                    B.set_schedule(k, 0)
+            for i, (s0, u0) in enumerate(init):
+                B.set_state(i, s0, u0)
+            B.step(21)
+            states.append([(B.get_state(i), B.clock(i)) for i in range(len(cfgs))])
+    bitwise = True
+    for i in range(len(cfgs)):
+        (s, u), clk = states[0][i]
+        (rs, ru), rclk = states[1][i]
+        assert_agree(A.PREC_FP32, (s, u), (rs, ru), clk, rclk, i)
+        bitwise = bitwise and np.array_equal(s, rs) and np.array_equal(u, ru) and clk == rclk
+    # the same tile code for each flux as schedule 0's kernels
+    assert bitwise
+    # the tuner times both ways and keeps the faster
+    with solver.Batch(cfgs) as B:
+        for i, (s0, u0) in enumerate(init):
+            B.set_state(i, s0, u0)
+        B.autotune(2)
+        on, ms_mixed, ms_split = B.mixed()
+        assert ms_mixed > 0 and ms_split > 0 and on == (ms_mixed < ms_split)
+        assert B.info()["launches_per_step"] == (1 if on else B.lib.ast_batch_num_classes(B.h))
+    # FP64 batches, and problems of different reconstructions, keep one
+    # launch per class
+    c64 = [c.copy() for c in cfgs[:2]]
+    for c in c64:
+        c.precision = A.PREC_FP64
+    with solver.Batch(c64) as B:
+        with pytest.raises(solver.AstError):
+            B.set_mixed(True)
+    two = [cfgs[0].copy(), cfgs[1].copy()]
+    two[1].recon = A.RECON_NONE
+    with solver.Batch(two) as B:
+        with pytest.raises(solver.AstError):
+            B.set_mixed(True)
