@@ -101,7 +101,8 @@ struct ast_batch {
     // kernel (32x16 tiles, slot order)
     bool mix_ok = false;
     int mixed = 0;                      // 1: steps are mixed launches
-    int* mix_start = nullptr;           // prefix sums of the problems' tiles (nprob + 1)
+    int* mix_start = nullptr;           // prefix sums of the problems' tiles (nprob + 1), then
+                                        // per slot the kernels' FLUX (nprob)
     int mix_tiles = 0, mix_recon = 0;
     float ms_mixed = 0.0f, ms_split = 0.0f;   // autotuner: ms per step, one launch / per class
 };
@@ -201,8 +202,8 @@ int enqueue_steps(ast_batch* B, cudaStream_t st, int count)
 {
     if (B->mixed) {
         for (int i = 0; i < count; i++) {
-            const int rc = launch_batch_mixed(B->dP[B->cur], B->mix_start, B->nprob, B->mix_tiles, B->mix_recon, st,
-                                              true);
+            const int rc = launch_batch_mixed(B->dP[B->cur], B->mix_start, B->mix_start + B->nprob + 1, B->nprob,
+                                              B->mix_tiles, B->mix_recon, st, true);
             if (rc != AST_OK) return rc;
             B->cur ^= 1;
         }
@@ -448,14 +449,19 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
     for (int i = 1; i < nprob; i++)
         if (cfgs[i].recon != cfgs[0].recon) B->mix_ok = false;
     if (rc == AST_OK && B->mix_ok) {
-        std::vector<int> ms(nprob + 1, 0);
-        for (int s = 0; s < nprob; s++) ms[s + 1] = ms[s] + tiles_of(B->cfg[order[s]], 0);
+        std::vector<int> ms(2 * nprob + 1, 0);
+        for (int s = 0; s < nprob; s++) {
+            const ast_config& c = B->cfg[order[s]];
+            ms[s + 1] = ms[s] + tiles_of(c, 0);
+            ms[nprob + 1 + s] =
+                (c.flux == AST_FLUX_HLL) ? 0 : (c.flux == AST_FLUX_HLLC) ? 1 : (c.flux == AST_FLUX_HLLC_A) ? 3 : 2;
+        }
         B->mix_tiles = ms[nprob];
         B->mix_recon = cfgs[0].recon;
         if ((e = cudaMalloc(&B->mix_start, sizeof(int) * ms.size())) != cudaSuccess ||
             (e = cudaMemcpy(B->mix_start, ms.data(), sizeof(int) * ms.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
             rc = cuda_fail(e, "batch work list");
-        if (rc == AST_OK) rc = launch_batch_mixed(nullptr, nullptr, 0, 0, B->mix_recon, nullptr, false);
+        if (rc == AST_OK) rc = launch_batch_mixed(nullptr, nullptr, nullptr, 0, 0, B->mix_recon, nullptr, false);
     }
     for (size_t c = 1; c < B->cls.size() && rc == AST_OK; c++) {
         cudaStream_t s;

@@ -5,8 +5,8 @@
 namespace ast {
 
 template <bool RECON>
-static int launch_mixed_t(const StepParams* Ps, const int* tile_start, int nprob, int tiles, cudaStream_t st,
-                          bool launch)
+static int launch_mixed_t(const StepParams* Ps, const int* tile_start, const int* flux_of, int nprob, int tiles,
+                          cudaStream_t st, bool launch)
 {
     constexpr int TZ = kShapeTZ[0], TR = kShapeTR[0];
     auto k = batch_kernel_mixed<float, RECON, TZ, TR>;
@@ -19,16 +19,16 @@ static int launch_mixed_t(const StepParams* Ps, const int* tile_start, int nprob
         return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaFuncSetAttribute");
     }
     if (tiles <= 0) return AST_OK;
-    k<<<tiles, kThreads, smem, st>>>(Ps, tile_start, nprob);
+    k<<<tiles, kThreads, smem, st>>>(Ps, tile_start, flux_of, nprob);
     e = cudaGetLastError();
     return e == cudaSuccess ? AST_OK : cuda_fail(e, "mixed batch kernel launch");
 }
 
-int launch_batch_mixed(const StepParams* Ps, const int* tile_start, int nprob, int tiles, int recon, cudaStream_t st,
-                       bool launch)
+int launch_batch_mixed(const StepParams* Ps, const int* tile_start, const int* flux_of, int nprob, int tiles,
+                       int recon, cudaStream_t st, bool launch)
 {
-    return recon ? launch_mixed_t<true>(Ps, tile_start, nprob, tiles, st, launch)
-                 : launch_mixed_t<false>(Ps, tile_start, nprob, tiles, st, launch);
+    return recon ? launch_mixed_t<true>(Ps, tile_start, flux_of, nprob, tiles, st, launch)
+                 : launch_mixed_t<false>(Ps, tile_start, flux_of, nprob, tiles, st, launch);
 }
 
 }  // namespace ast

@@ -225,8 +225,8 @@ inline int launch_batch(size_t elem, int shape, const StepParams* Ps, const int*
 // the FP32 batch kernel over problems of every flux (32x16 tiles, one
 // reconstruction) over `tiles` work-list entries; launch=false raises its
 // shared-memory limit
-int launch_batch_mixed(const StepParams* Ps, const int* tile_start, int nprob, int tiles, int recon, cudaStream_t st,
-                       bool launch);
+int launch_batch_mixed(const StepParams* Ps, const int* tile_start, const int* flux_of, int nprob, int tiles,
+                       int recon, cudaStream_t st, bool launch);
 
 // kernel parameters of a configuration (grid spacing, constants, boundaries)
 inline void fill_step_params(StepParams& P, const ast_config& c)
@@ -320,7 +320,6 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
     P.body_rsplit = c.body_rsplit;
     P.body_amp = c.body_amp;
     P.nsrc = nullptr;   // set by ast_set_neutral / ast_add_mk_raw
-    P.flux_kind = (c.flux == AST_FLUX_HLL) ? 0 : (c.flux == AST_FLUX_HLLC) ? 1 : (c.flux == AST_FLUX_HLLC_A) ? 3 : 2;
     P.nsrc_coef = (c.neutral_kn != 0.0) ? c.neutral_nh / c.neutral_kn : 0.0;
 }
 

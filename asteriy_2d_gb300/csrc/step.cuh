@@ -70,7 +70,6 @@ struct __align__(16) StepParams {
     int fixed_nlo, fixed_nhi, fixed_mhi;   // cells that can lie in the region (one cell of margin)
     int region_select;
     int skip_uniform;              // uniform tiles skip the face pass
-    int flux_kind;                 // the kernels' FLUX: 0 HLL, 1 HLLC, 2 exact Godunov, 3 HLLC_Aleksashov
     // one step launched in bands of tile rows: this launch steps tile rows
     // [band_lo, band_hi) (band_hi 0: all rows of the grid), and `units` CTAs
     // of all the step's launches report to the clock (0: this launch's grid)
@@ -1450,11 +1449,13 @@ __global__ void __launch_bounds__(kThreads, min_ctas<R, FLUX>())
 
 // Many problems of any fluxes (one reconstruction) in one launch: as
 // batch_kernel, each CTA then steps its tile with the tile code of its
-// problem's flux (a CTA runs one of the four; the dynamic shared memory is
-// the largest of their tile spaces)
+// problem's flux, flux_of[j] = the kernels' FLUX (0 HLL, 1 HLLC, 2 exact
+// Godunov, 3 HLLC_Aleksashov); a CTA runs one of the four, and the dynamic
+// shared memory is the largest of their tile spaces
 template <typename R, bool RECON, int TZ, int TR>
 __global__ void __launch_bounds__(kThreads, min_ctas<R, 2>())
-    batch_kernel_mixed(const StepParams* __restrict__ Ps, const int* __restrict__ tile_start, int nprob)
+    batch_kernel_mixed(const StepParams* __restrict__ Ps, const int* __restrict__ tile_start,
+                       const int* __restrict__ flux_of, int nprob)
 {
     __shared__ __align__(16) StepParams sP;
     __shared__ int s_j;
@@ -1474,7 +1475,7 @@ __global__ void __launch_bounds__(kThreads, min_ctas<R, 2>())
     const int t = (int)blockIdx.x - tile_start[j];
     const int tz = (sP.N + TZ - 1) / TZ;
     const unsigned tiles = (unsigned)(tile_start[j + 1] - tile_start[j]);
-    switch (sP.flux_kind) {
+    switch (flux_of[j]) {
     case 0: step_tile<R, 0, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, tiles); break;
     case 1: step_tile<R, 1, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, tiles); break;
     case 3: step_tile<R, 3, RECON, kSoA, TZ, TR>(sP, t % tz, t / tz, tiles); break;
