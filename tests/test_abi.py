@@ -64,6 +64,10 @@ def test_null_solver_is_refused():
     L = solver.load()
     assert L.ast_set_neutral(None, None, 0) == A.AST_ERR_INVALID
     assert L.ast_step_host(None, None, None, None, None) == A.AST_ERR_INVALID
+    assert L.ast_step_host_n(None, 1, None, None, None, None) == A.AST_ERR_INVALID
+    assert L.ast_batch_set_mixed(None, 1) == A.AST_ERR_INVALID
+    assert L.ast_batch_get_mixed(None, None, None, None) == A.AST_ERR_INVALID
+    assert L.ast_batch_num_classes(None) == A.AST_ERR_INVALID
     c = problems.blast_config(64, 32)
     assert L.ast_add_mk_raw(None, None, None, None, None, None, None, None, None, 0, 0, C.byref(c), None) == \
         A.AST_ERR_INVALID
