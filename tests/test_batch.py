@@ -322,3 +322,37 @@ def test_one_launch_mode():
     with solver.Batch(two) as B:
         with pytest.raises(solver.AstError):
             B.set_mixed(True)
+
+
+@pytest.mark.gpu
+def test_one_launch_mode_with_learned_guess():
+    """The mixed kernel with exact-Godunov problems on the learned start
+    value next to HLLC problems: bit for bit schedule 0, counters included."""
+    probs = small_set(A.PREC_FP32, n=8)
+    params = np.load(os.path.join(os.path.dirname(solver.__file__), "data", "guess_blast.npy"))
+    cfgs = []
+    for p in probs:
+        c = p.cfg.copy()
+        c.collect_stats = 1
+        if c.flux == A.FLUX_GODUNOV:
+            c.guess, c.riemann_tol = A.GUESS_MLP, 1e-8
+        cfgs.append(c)
+    assert any(c.guess == A.GUESS_MLP for c in cfgs) and any(c.flux == A.FLUX_HLLC for c in cfgs)
+    init = [solver.problem_fill(p) for p in probs]
+    out = []
+    for mixed in (True, False):
+        with solver.Batch(cfgs) as B:
+            B.set_mlp(params)
+            if mixed:
+                B.set_mixed(True)
+            else:
+                for k in range(B.lib.ast_batch_num_classes(B.h)):
+                    B.set_schedule(k, 0)
+            for i, (s0, u0) in enumerate(init):
+                B.set_state(i, s0, u0)
+            B.step(18)
+            out.append([(B.get_state(i), B.clock(i), B.stats(i)) for i in range(len(cfgs))])
+    for i in range(len(cfgs)):
+        (s, u), clk, st = out[0][i]
+        (rs, ru), rclk, rst = out[1][i]
+        assert np.array_equal(s, rs) and np.array_equal(u, ru) and clk == rclk and st == rst, i
