@@ -28,19 +28,17 @@ int set_error(int code, const char* msg);
 int encode_planes(CUtensorMap* map, void* base, const ast_config& c, long long ld, long long plane, unsigned bx,
                   unsigned by);
 
-// the GPU's SM count (the current device when first asked)
+// the SM count of the current device (looked up once per device)
 inline int sm_count()
 {
-    static int n = 0;
-    if (n <= 0) {
-        int dev = 0, v = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
-            n = v;
-        else
-            return 1;
-    }
-    return n;
+    constexpr int kMaxDev = 64;
+    static int n[kMaxDev] = {};
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (dev >= 0 && dev < kMaxDev && n[dev] > 0) return n[dev];
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return 1;
+    if (dev >= 0 && dev < kMaxDev) n[dev] = v;
+    return v;
 }
 
 // launch=false only raises the kernel's dynamic shared-memory limit, which

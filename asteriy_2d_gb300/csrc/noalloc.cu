@@ -1,23 +1,26 @@
-// noalloc.cu - one fused step (Kernel_TVD + funk_time) that allocates nothing.
+// noalloc.cu - a step with the dt shift (Kernel_TVD + funk_time) that
+// allocates nothing.
 //
-// Who needs it: code that must not call cudaMalloc while it steps - a host
-// loop running inside another framework's stream capture, a process whose
-// device memory is carved up by a different allocator with a fixed budget,
-// or a real-time loop where an allocation's latency or failure is not
-// acceptable.  ast_step_raw already needs no scratch, but it leaves the dt
-// shift to a second launch (ast_funk_time); the solver object does both in
-// one launch but owns device memory that ast_create allocates.  This entry
-// point does both in one step-kernel launch on the caller's reference-layout
-// arrays, with the cross-CTA reduction state (the device clock: wave-speed
-// maxima, CTA ticket, status) in a file-scope device array instead of
-// allocated memory.
+// Who needs it: code that must not call cudaMalloc while it steps - a
+// process whose device memory is carved up by a different allocator under a
+// fixed budget, or a real-time loop where an allocation's latency or failure
+// is not acceptable.  ast_step_raw already needs no scratch, but it leaves
+// the dt shift to a second call (ast_funk_time); the solver object shifts dt
+// inside its step kernel but owns device memory that ast_create allocates.
+// This entry point does the step and the shift on the caller's
+// reference-layout arrays with the cross-CTA reduction state (the device
+// clock: wave-speed maxima, CTA ticket, status, counters) in a file-scope
+// device array instead of allocated memory.  It enqueues three kernels on
+// the caller's stream: a one-thread kernel that clears the array and copies
+// T_do, TT and step in, the step kernel, and a one-thread kernel that copies
+// the shifted T_do, TT and step (and the status bits) back out.
 //
 // Limits and sharing:
 //   - the scratch is a fixed AST_NOALLOC_SCRATCH_BYTES block per device,
 //     held from library load until process exit; it does not grow with the
 //     grid, so every grid that ast_config_check accepts fits;
 //   - every call shares the block and it keeps the last call's contents:
-//     each call clears the counters first; calls that overlap on the GPU
+//     each call clears all of it first; calls that overlap on the GPU
 //     (other streams, other host threads) race on it and must be serialised
 //     by the caller;
 //   - the first call on a device looks up the block's device address
@@ -43,7 +46,7 @@ constexpr int kMaxDevices = 64;
 DevClock* g_scratch_ptr[kMaxDevices] = {};
 std::mutex g_setup_mu;
 
-// clock in: step counters cleared, T_do / TT / step taken from the caller
+// clock in: every field cleared, then T_do / TT / step taken from the caller
 __global__ void clock_in(DevClock* C, const double* T_do, const double* TT, const int64_t* step)
 {
     C->T_do = *T_do;
@@ -53,7 +56,10 @@ __global__ void clock_in(DevClock* C, const double* T_do, const double* TT, cons
     C->smax_r = 0ull;
     C->done = 0u;
     C->status = 0u;
-    for (int i = 0; i < 8; i++) C->cnt[i] = 0ull;
+    for (int i = 0; i < (int)(sizeof(C->cnt) / sizeof(C->cnt[0])); i++) C->cnt[i] = 0ull;
+    C->next_tile = 0u;
+    C->pad_ = 0u;
+    C->T_prev = 0.0;
 }
 
 // clock out: the shifted T_do, TT and step back to the caller

@@ -333,21 +333,22 @@ int ast_inflow_raw(const double* s, const double* u, double* s2, double* u2, con
 int ast_funk_time(double* T, double* T_do, double* TT, int* i, void* cuda_stream);
 
 /* ---- a step that allocates nothing (no counterpart in the reference) -----
- * For callers that must not call cudaMalloc while they step: a loop that runs
- * inside another framework's stream capture, a process whose device memory
- * is handed out by a different allocator under a fixed budget, or a
- * real-time loop that cannot absorb an allocation's latency or failure.
- * One launch does what ast_step_raw + ast_funk_time do: reads s, u and
+ * For callers that must not call cudaMalloc while they step: a process whose
+ * device memory is handed out by a different allocator under a fixed
+ * budget, or a real-time loop that cannot absorb an allocation's latency or
+ * failure.  It does what ast_step_raw + ast_funk_time do: reads s, u and
  * *T_do, writes s2, u2, then *T_do = the new dt, *TT += *T_do, *step += 1
- * (and *status = the step's AST_ST_* bits when status is not NULL).  All
- * pointers are device pointers, FP64 reference layout; guess must be PVRS.
- * Its cross-CTA reduction state lives in a file-scope device array of
- * AST_NOALLOC_SCRATCH_BYTES per device, held from library load to process
- * exit; it does not grow with the grid.  Every call shares that array and
- * clears it first, so calls that overlap on the GPU (other streams or host
- * threads) race and must be serialised by the caller.  The first call on a
- * device looks the array up and sets kernel attributes: make it before any
- * stream capture. */
+ * (and *status = the step's AST_ST_* bits when status is not NULL).  It
+ * enqueues three kernels on cuda_stream: a one-thread copy of T_do, TT and
+ * step into the scratch array below, the step kernel, and a one-thread copy
+ * back out.  All pointers are device pointers, FP64 reference layout; guess
+ * must be PVRS.  Its cross-CTA reduction state lives in a file-scope device
+ * array of AST_NOALLOC_SCRATCH_BYTES per device, held from library load to
+ * process exit; it does not grow with the grid.  Every call shares that
+ * array and clears all of it first, so calls that overlap on the GPU (other
+ * streams or host threads) race and must be serialised by the caller.  The
+ * first call on a device looks the array up and sets kernel attributes:
+ * make it before any stream capture. */
 #define AST_NOALLOC_SCRATCH_BYTES 256
 int ast_step_noalloc(const double* s, const double* u, double* s2, double* u2, double* T_do, double* TT,
                      int64_t* step, unsigned int* status, const ast_config* cfg, void* cuda_stream);

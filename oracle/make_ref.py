@@ -16,6 +16,7 @@ is called at kernel.cu:3652, 3676), and it needs nvcc -rdc plus a GPU; only
 its functions are compiled here, for the host.
 
 Usage:  python oracle/make_ref.py [--src /path/to/reference] [--extract-only]
+(or ASTERIY_REF_SRC=/path/to/reference in the environment)
 With --extract-only the .inc is written but not compiled; build() on a
 machine without the reference sources compiles an existing .inc.
 """
@@ -26,7 +27,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_SRC = "/root/reference"
+# the reference checkout: $ASTERIY_REF_SRC, else --src, else the checkout
+# location of the machine this recipe was written on
+DEFAULT_SRC = os.environ.get("ASTERIY_REF_SRC") or "/root/reference"
 
 # (file, first line, last line, text the first line must contain)
 RANGES = [

@@ -1,13 +1,13 @@
 """The step that allocates nothing (ast_step_noalloc).
 
-Some callers cannot call cudaMalloc while they step (a loop inside another
-framework's stream capture, a device-memory budget owned by a different
-allocator, a real-time loop).  ast_step_noalloc does one step and the dt
-shift in one launch with its reduction state in a static device array.
-Here it is called twice in a row through the C ABI and compared with the
-existing entry points ast_step_raw + ast_funk_time on the same inputs: the
-states within the parity tolerance, the clock (T_do, TT, step) equal.
-This file is collected last; it passes alone in a fresh process too.
+Some callers cannot call cudaMalloc while they step (a device-memory budget
+owned by a different allocator, a real-time loop).  ast_step_noalloc does
+one step and the dt shift with its reduction state in a static device array
+(three kernels: clock in, step, clock out).  Here it is called twice in a
+row through the C ABI and compared with the existing entry points
+ast_step_raw + ast_funk_time on the same inputs: the states within the
+parity tolerance, the clock (T_do, TT, step) equal.  This file is collected
+last; it passes alone in a fresh process too.
 """
 import numpy as np
 import pytest
