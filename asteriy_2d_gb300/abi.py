@@ -61,7 +61,7 @@ class ast_config(C.Structure):
         ("dt_first", C.c_double), ("dt_cap", C.c_double), ("p_floor", C.c_double),
         ("riemann_tol", C.c_double),
         ("collect_stats", C.c_int32), ("riemann_newton", C.c_int32), ("persistent", C.c_int32),
-        ("skip_uniform", C.c_int32), ("reserved_i", C.c_int32 * 4),
+        ("skip_uniform", C.c_int32), ("copy_wait_polls", C.c_int32), ("reserved_i", C.c_int32 * 3),
         ("mlp_gate", C.c_double), ("inflow_p", C.c_double), ("inflow_v", C.c_double),
         ("neutral_nh", C.c_double), ("neutral_kn", C.c_double), ("reserved_d", C.c_double * 3),
     ]

@@ -118,6 +118,8 @@ struct ast_solver {
     int probe_cap = 0;
     bool tma = false;                // FP32 persistent kernel
     int tma_grid = 0;                // its CTAs
+    bool sweep = false;              // FP32 strip kernel
+    int sweep_grid = 0;              // its CTAs (at most)
     CUtensorMap tin[2], tout[2];     // tile-box load and store maps of buf[0], buf[1]
     void* nsrc = nullptr;            // neutral-coupling source planes (nn2.x, nn2.y), or null
     cudaStream_t pipe[2] = {nullptr, nullptr};   // ast_step_host: copies in, copies out
@@ -187,7 +189,21 @@ int ast_create(const ast_config* cfg, ast_solver** out)
     }
     rc = (S->elem == 8) ? launch_step_r<double, kSoA>(S->P, cfg->flux, cfg->recon, nullptr, false)
                         : launch_step_r<float, kSoA>(S->P, cfg->flux, cfg->recon, nullptr, false);
-    if (rc == AST_OK && S->elem == 4 && cfg->persistent) {
+    // FP32: the strip kernel (persistent = 2) or the persistent tile kernel (1)
+    const bool want_sweep = S->elem == 4 && cfg->persistent == 2;
+    if (rc == AST_OK && want_sweep) {
+        int per_sm = 0, dev = 0, sms = 0;
+        rc = launch_step_sweep(S->P, cfg->flux, cfg->recon, 0, nullptr, false, &per_sm);
+        if (rc == AST_OK && (e = cudaGetDevice(&dev)) != cudaSuccess) rc = cuda_fail(e, "cudaGetDevice");
+        if (rc == AST_OK && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            rc = cuda_fail(e, "cudaDeviceGetAttribute");
+        if (rc == AST_OK) {
+            const int strips = sweep_strips(cfg->N, cfg->M, 0, 0);
+            S->sweep_grid = std::min((strips + kThreads / 32 - 1) / (kThreads / 32), std::max(per_sm, 1) * sms);
+            S->sweep = true;
+        }
+    }
+    if (rc == AST_OK && S->elem == 4 && cfg->persistent && !want_sweep) {
         // box loads of tile + halo (TZ+8 x TR+4), stores of the tile (TZ x TR)
         for (int b = 0; b < 2 && rc == AST_OK; b++) {
             rc = encode_planes(&S->tin[b], S->buf[b], *cfg, S->ld, S->plane, kTZ + 8, kTR + 4);
@@ -409,13 +425,23 @@ static __global__ void neutral_kernel(StepParams P)
     }
 }
 
+// CTAs of the strip kernel for tile rows [t0, t1): one per 8 strips, at
+// most the solver's grid
+static int band_sweep_grid(const ast_solver* S, int t0, int t1)
+{
+    const int strips = sweep_strips(S->cfg.N, S->cfg.M, t0, t1);
+    return std::min((strips + kThreads / 32 - 1) / (kThreads / 32), S->sweep_grid);
+}
+
 static int enqueue_one(ast_solver* S)
 {
     StepParams P = S->P;
     P.in = S->buf[S->cur];
     P.out = S->buf[S->cur ^ 1];
     int rc;
-    if (S->tma)
+    if (S->sweep)
+        rc = launch_step_sweep(P, S->cfg.flux, S->cfg.recon, S->sweep_grid, S->stream, true, nullptr);
+    else if (S->tma)
         rc = launch_step_tma(P, S->tin[S->cur], S->tout[S->cur ^ 1], S->cfg.flux, S->cfg.recon, S->tma_grid,
                              S->stream, true, nullptr);
     else
@@ -580,7 +606,8 @@ static int host_steps(ast_solver* S, int nsteps, double* s_a, double* u_a, doubl
         bd[b].t1 = (int)((long long)(b + 1) * rows / bands);
         bd[b].k0 = (long long)bd[b].t0 * kTR * N;
         bd[b].k1 = (long long)std::min(bd[b].t1 * kTR, M) * N;
-        units += std::min((bd[b].t1 - bd[b].t0) * tiles_z, S->tma_grid);
+        units += S->sweep ? band_sweep_grid(S, bd[b].t0, bd[b].t1)
+                          : std::min((bd[b].t1 - bd[b].t0) * tiles_z, S->tma_grid);
     }
     AST_CUDA(cudaEventRecord(ev_start, cst));
     AST_CUDA(cudaStreamWaitEvent(cin, ev_start, 0));
@@ -624,7 +651,13 @@ static int host_steps(ast_solver* S, int nsteps, double* s_a, double* u_a, doubl
             P.out = dst;
             P.band_lo = bd[b].t0;
             P.band_hi = bd[b].t1;
-            if (S->tma) {
+            if (S->sweep) {
+                // each band hands out its strips from a counter set to zero
+                P.units = units;
+                if (b > 0) AST_CUDA(cudaMemsetAsync(&S->clock->next_tile, 0, sizeof(unsigned int), cst));
+                rc = launch_step_sweep(P, S->cfg.flux, S->cfg.recon, band_sweep_grid(S, bd[b].t0, bd[b].t1), cst,
+                                       true, nullptr);
+            } else if (S->tma) {
                 // each band hands out its tiles from a counter set to zero
                 P.units = units;
                 if (b > 0) AST_CUDA(cudaMemsetAsync(&S->clock->next_tile, 0, sizeof(unsigned int), cst));

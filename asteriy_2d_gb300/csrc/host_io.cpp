@@ -74,7 +74,8 @@ int ast_config_check(const ast_config* c)
     if (c->geom < AST_GEOM_PLANAR || c->geom > AST_GEOM_AXISYM) return AST_ERR_INVALID;
     if (c->precision < AST_PREC_FP64 || c->precision > AST_PREC_FP32) return AST_ERR_INVALID;
     if (c->guess < AST_GUESS_PVRS || c->guess > AST_GUESS_MLP) return AST_ERR_INVALID;
-    if (c->persistent < 0 || c->persistent > 1) return AST_ERR_INVALID;
+    if (c->copy_wait_polls < 0) return AST_ERR_INVALID;
+    if (c->persistent < 0 || c->persistent > 2) return AST_ERR_INVALID;
     if (c->skip_uniform < 0 || c->skip_uniform > 1) return AST_ERR_INVALID;
     if (!(c->inflow_p >= 0.0)) return AST_ERR_INVALID;
     if (!std::isfinite(c->neutral_nh) || !std::isfinite(c->neutral_kn)) return AST_ERR_INVALID;

@@ -11,8 +11,11 @@
 #include <cmath>
 #include <cstring>
 
+#include <algorithm>
+
 #include "../../include/asteriy_gb300.h"
 #include "step.cuh"
+#include "sweep.cuh"
 
 namespace ast {
 
@@ -114,6 +117,33 @@ int launch_tma_t(const StepParams& P, const CUtensorMap& tin, const CUtensorMap&
 
 int launch_step_tma(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int flux, int recon,
                     int grid, cudaStream_t st, bool launch, int* per_sm);
+
+// the FP32 strip kernel over `grid` CTAs; launch=false returns the CTAs per
+// SM it reaches in *per_sm
+template <int FLUX, bool RECON>
+int launch_sweep_t(const StepParams& P, int grid, cudaStream_t st, bool launch, int* per_sm)
+{
+    auto k = sweep_kernel<FLUX, RECON>;
+    cudaError_t e;
+    if (!launch) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, kThreads, 0);
+        return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    }
+    k<<<grid, kThreads, 0, st>>>(P);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? AST_OK : cuda_fail(e, "strip kernel launch");
+}
+
+// the FP32 strip kernel of a flux and reconstruction (every flux but the
+// exact solver's); AST_ERR_UNSUPPORTED for the exact solver
+int launch_step_sweep(const StepParams& P, int flux, int recon, int grid, cudaStream_t st, bool launch, int* per_sm);
+// strips of the strip kernel in tile rows [band_lo, band_hi) (all rows when
+// band_hi is 0) of an N x M grid
+inline int sweep_strips(int N, int M, int band_lo, int band_hi)
+{
+    const int r_lo = band_lo * kTR, r_hi = band_hi > 0 ? std::min(band_hi * kTR, M) : M;
+    return ((N + kSW - 1) / kSW) * ((r_hi - r_lo + kSH - 1) / kSH);
+}
 
 // the persistent FP32 batch kernel of one class (maps and parameters in
 // device memory, indexed by the class's problem); launch=false as above
@@ -263,6 +293,7 @@ inline void fill_step_params(StepParams& P, const ast_config& c)
     P.guess = c.guess;
     P.mlp_gate = (float)c.mlp_gate;
     P.rec_every = 1;
+    P.wait_polls = c.copy_wait_polls > 0 ? c.copy_wait_polls : tma::kWaitLimit;
     P.rec_gate = 0.0;
     for (int sd = 0; sd < 4; sd++) {
         P.bc_kind[sd] = c.bc[sd].kind;

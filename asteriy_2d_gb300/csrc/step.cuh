@@ -74,6 +74,9 @@ struct __align__(16) StepParams {
     // [band_lo, band_hi) (band_hi 0: all rows of the grid), and `units` CTAs
     // of all the step's launches report to the clock (0: this launch's grid)
     int band_lo, band_hi, units;
+    // polls of a bulk copy's mbarrier before a persistent kernel reports
+    // AST_ST_TIMEOUT (it then waits on with the long default limit)
+    int wait_polls;
     // the high-order region as column intervals (found on the host from
     // the reference's FP64 face positions): z faces whose lower cell's
     // column lies in [region_zlo, region_zhi], r faces of the columns in
@@ -121,15 +124,36 @@ __device__ __forceinline__ const Gas<R>& gas_of(const StepParams& P)
 // leaves commented in add2, kernel.cu:1979-1985, written there for the z_hi
 // side; w is the velocity along the side's outward normal)
 template <typename R>
+__device__ __forceinline__ void ghost_nonreflect_s(const Gas<R>& g, bool low, R& rho, R& p, R& vn)
+{
+    const R w = low ? -vn : vn;
+    const R cc = sqrt(g.ga * p / rho);
+    const R cg = g.g1 / g.g2 * (w + R(2) / g.g1 * cc);
+    rho = rho * pow(cg / cc, R(2) / g.g1);
+    p = rho * cg * cg / g.ga;
+    vn = low ? -cg : cg;
+}
+// (the element chosen by branches, not by a reference to a runtime-chosen
+// element, which would put the array in local memory)
+template <typename R>
 __device__ __forceinline__ void ghost_nonreflect(const Gas<R>& g, bool zside, bool low, R v[4])
 {
-    R& vn = zside ? v[2] : v[3];
-    const R w = low ? -vn : vn;
-    const R cc = sqrt(g.ga * v[1] / v[0]);
-    const R cg = g.g1 / g.g2 * (w + R(2) / g.g1 * cc);
-    v[0] = v[0] * pow(cg / cc, R(2) / g.g1);
-    v[1] = v[0] * cg * cg / g.ga;
-    vn = low ? -cg : cg;
+    if (zside) ghost_nonreflect_s(g, low, v[0], v[1], v[2]);
+    else ghost_nonreflect_s(g, low, v[0], v[1], v[3]);
+}
+
+// the SUCTION rule on v's normal velocity: on a low side v_n = min(v_n,
+// lim), on a high side v_n = max(v_n, lim)
+template <typename R>
+__device__ __forceinline__ void ghost_suction(bool zside, bool low, R lim, R v[4])
+{
+    if (zside) {
+        if (low) { if (v[2] > lim) v[2] = lim; }
+        else     { if (v[2] < lim) v[2] = lim; }
+    } else {
+        if (low) { if (v[3] > lim) v[3] = lim; }
+        else     { if (v[3] < lim) v[3] = lim; }
+    }
 }
 
 // ------------------------------------------------------------------ loads
@@ -184,10 +208,7 @@ __device__ __forceinline__ void fetch_cell(const StepParams& P, int n, int m, R 
     } else {                    // OUTFLOW, SUCTION, NONREFLECT
         read_cell<R, LAYOUT>(P, bn, bm, v);
         if (kind == 3) {
-            R lim = (R)(zside ? P.bc_val[side][2] : P.bc_val[side][3]);
-            R& vn = zside ? v[2] : v[3];
-            if (low) { if (vn > lim) vn = lim; }
-            else     { if (vn < lim) vn = lim; }
+            ghost_suction(zside, low, (R)(zside ? P.bc_val[side][2] : P.bc_val[side][3]), v);
         } else if (kind == 4) {
             ghost_nonreflect(gas_of<R>(P), zside, low, v);
         }
@@ -329,7 +350,8 @@ __device__ __forceinline__ S& tile_smem()
 template <typename C, typename R>
 __device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C inv_g1, const R in[4],
                                             const R f[4][4], C T_do, C tdv, C ty, C dx, C dy, C Q2, C Sz, C Sr,
-                                            int& nrho, int& np, R out[4], C* E2o = nullptr, C* KE2o = nullptr)
+                                            int& nrho, int& np, unsigned& status, R out[4], C* E2o = nullptr,
+                                            C* KE2o = nullptr)
 {
     const C r1 = (C)in[0], p1 = (C)in[1], vz1 = (C)in[2], vr1 = (C)in[3];
     C ps[4];
@@ -360,6 +382,9 @@ __device__ __forceinline__ void update_cell(const StepParams& P, C ga, C g1, C i
     const C KE2 = C(0.5) * rho2 * (vz2 * vz2 + vr2 * vr2);
     C p2 = (E2 - KE2) * g1;
     if (p2 <= C(0)) { np++; p2 = sizeof(C) == 4 ? (C)P.p_floorf : (C)P.p_floor; }
+    // a non-finite flux or state reaches p2 through the energy or 1/rho
+    // (a NaN sound speed can leave the wave speed finite: fmax drops NaN)
+    if (!(p2 == p2)) status |= 0x10u;
     out[0] = (R)rho2; out[1] = (R)p2; out[2] = (R)vz2; out[3] = (R)vr2;
     if (E2o) { *E2o = E2; *KE2o = KE2; }
 }
@@ -1025,10 +1050,7 @@ __device__ __forceinline__ void patch_tile(const StepParams& P, S& sm, int b, in
             const int si = bn - n0 + 2 + QX, sj = bm - m0 + 2;
             v[0] = q[0][sj][si]; v[1] = q[1][sj][si]; v[2] = q[2][sj][si]; v[3] = q[3][sj][si];
             if (kind == 3) {
-                R lim = (R)(zside ? P.bc_val[side][2] : P.bc_val[side][3]);
-                R& vn = zside ? v[2] : v[3];
-                if (low) { if (vn > lim) vn = lim; }
-                else     { if (vn < lim) vn = lim; }
+                ghost_suction(zside, low, (R)(zside ? P.bc_val[side][2] : P.bc_val[side][3]), v);
             } else if (kind == 4) {
                 ghost_nonreflect(gas_of<R>(P), zside, low, v);
             }
@@ -1190,7 +1212,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
         }
         const double ty = (P.geom == 1) ? T_do / y : 0.0;
         update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty, P.dx, P.dy, Q2, Sz, Sr,
-                            acc.nrho, acc.np, o);
+                            acc.nrho, acc.np, acc.rc.status, o);
     };
     // the FP32 form's source terms of a cell: ty = T_do/r and the body force
     auto sources_fp32 = [&](int row, int n, const R in[4], float& ty, float& Q2) {
@@ -1248,7 +1270,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
                 sources_fp32(row, n, in, ty, Q2);
                 float E2, KE2;
                 update_cell<float>(P, gaf, g1f, ig1f, in, f, Tf, tdv_f, ty, dxf, dyf, Q2, 0.0f, 0.0f, acc.nrho, acc.np,
-                                   o, &E2, &KE2);
+                                   acc.rc.status, o, &E2, &KE2);
                 // pressure recovery p = (g-1)(E - rho v^2/2) in FP64 where
                 // the kinetic energy is more than 99% of the total
                 if (KE2 > 0.99f * E2) deferred |= 2u << (2 * it);
@@ -1497,7 +1519,8 @@ __global__ void __launch_bounds__(kThreads, min_ctas<R, 2>())
 // tile, and the counter's atomic for the tile after it.  The CTA's
 // wave-speed maxima and counters accumulate over its tiles and are reported
 // once (one ticket per CTA).  A bulk copy that does not arrive within the
-// wait limit sets AST_ST_TIMEOUT and ends the CTA's loop.
+// wait limit (P.wait_polls) sets AST_ST_TIMEOUT and is waited for with the
+// long limit; one that does not arrive even then ends the CTA's loop.
 template <int FLUX, bool RECON, bool SKIP>
 __global__ void __launch_bounds__(kThreads, 4)
     step_kernel_tma(StepParams P, const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout)
@@ -1556,16 +1579,16 @@ __global__ void __launch_bounds__(kThreads, 4)
         // two tiles: every thread has finished the previous tile (its
         // update and its reads of the other buffer and of the output tile)
         // and fenced its shared-memory writes for the bulk copies.
-        const bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+        bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1), P.wait_polls);
         if (__syncthreads_or(!arrived)) {
-            // give up this step's remaining tiles; wait (bounded) for the
-            // copy in flight before leaving (the next tile's copy is not
-            // issued yet)
-            if (copier) {
-                acc.rc.status |= AST_ST_TIMEOUT;
-                tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
-            }
-            break;
+            // the copy did not arrive within the wait limit: reported, then
+            // waited for with the long limit (every CTA leaves with no copy
+            // in flight; the next tile's copy is not issued yet), and the
+            // tile is computed when it has arrived.  A copy that does not
+            // arrive even then ends this CTA's tiles.
+            if (copier) acc.rc.status |= AST_ST_TIMEOUT;
+            arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+            if (__syncthreads_or(!arrived)) break;
         }
         // ghost cells (tiles at the grid's edge or near the fixed region
         // only: the others need no second barrier)
@@ -1691,14 +1714,20 @@ __global__ void __launch_bounds__(kThreads, 4)
                 tma::load_3d(&tin[jn], &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], x0 - 4, y0 - 2, 0);
             }
         }
-        const bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+        // (the wait limit from global memory: sP is being written by other
+        // threads until the barrier below)
+        bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1), Ps[j].wait_polls);
         if (__syncthreads_or(!arrived)) {
-            if (tid == 0) {
-                atomicOr(&sP.clock->status, AST_ST_TIMEOUT);
-                tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
-                if (s_tile[b ^ 1] < total) tma::mbar_wait(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
+            // reported, then waited for with the long limit and computed
+            // (as in step_kernel_tma); a copy that does not arrive even then
+            // ends this CTA's tiles after the next tile's copy, already
+            // issued, has been waited for (long limit)
+            if (tid == 0) atomicOr(&sP.clock->status, AST_ST_TIMEOUT);
+            arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+            if (__syncthreads_or(!arrived)) {
+                if (tid == 0 && s_tile[b ^ 1] < total) tma::mbar_wait(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
+                break;
             }
-            break;
         }
         const int n0 = s_org[b].x, m0 = s_org[b].y;
         patch_tile<R, TZ, TR>(sP, sm, b, n0, m0);

@@ -18,4 +18,18 @@ int launch_step_tma(const StepParams& P, const CUtensorMap& tin, const CUtensorM
     if (flux == AST_FLUX_HLLC_A) return launch_tma_t<3, false>(P, tin, tout, grid, st, launch, per_sm);
     return launch_tma_t<2, false>(P, tin, tout, grid, st, launch, per_sm);
 }
+
+int launch_step_sweep(const StepParams& P, int flux, int recon, int grid, cudaStream_t st, bool launch, int* per_sm)
+{
+    if (recon) {
+        if (flux == AST_FLUX_HLL) return launch_sweep_t<0, true>(P, grid, st, launch, per_sm);
+        if (flux == AST_FLUX_HLLC) return launch_sweep_t<1, true>(P, grid, st, launch, per_sm);
+        if (flux == AST_FLUX_HLLC_A) return launch_sweep_t<3, true>(P, grid, st, launch, per_sm);
+        return launch_sweep_t<2, true>(P, grid, st, launch, per_sm);
+    }
+    if (flux == AST_FLUX_HLL) return launch_sweep_t<0, false>(P, grid, st, launch, per_sm);
+    if (flux == AST_FLUX_HLLC) return launch_sweep_t<1, false>(P, grid, st, launch, per_sm);
+    if (flux == AST_FLUX_HLLC_A) return launch_sweep_t<3, false>(P, grid, st, launch, per_sm);
+    return launch_sweep_t<2, false>(P, grid, st, launch, per_sm);
+}
 }  // namespace ast

@@ -5,7 +5,7 @@
 // z = the four state planes) into shared memory, completion signalled on an
 // mbarrier with an expected byte count.  Stores: the updated tile from
 // shared memory back to the state planes through a bulk group.  Every wait
-// is bounded: after kWaitLimit failed polls the caller gets `false` and
+// is bounded: after its limit of failed polls the caller gets `false` and
 // must report the failure instead of waiting on.
 #pragma once
 
@@ -44,10 +44,29 @@ __device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes)
 }
 
 // waits for the completion of phase `parity` of the barrier; false after
-// kWaitLimit polls
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// `limit` polls.  The default limit polls with try_wait, which may suspend
+// the thread between polls (about a second in all); a shorter limit (a
+// configured copy_wait_polls, the failure tests' setting) polls with the
+// non-blocking test_wait, so that it runs out within microseconds
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = kWaitLimit)
 {
     const uint32_t a = smem_addr(bar);
+    if (limit < kWaitLimit) {
+        for (int i = 0; i < limit; i++) {
+            uint32_t done;
+            asm volatile(
+                "{\n"
+                ".reg .pred p;\n"
+                "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                "selp.u32 %0, 1, 0, p;\n"
+                "}\n"
+                : "=r"(done)
+                : "r"(a), "r"(parity)
+                : "memory");
+            if (done) return true;
+        }
+        return false;
+    }
     for (int i = 0; i < kWaitLimit; i++) {
         uint32_t done;
         asm volatile(

@@ -45,6 +45,8 @@ REF_BUDGET_S = 150.0    # reference arm: seconds of timed host work
 #   bench.py --steps 2 --warmup 1 --no-forms --no-stats --no-cpu --accuracy-steps 0 --batch-steps 0 [--form F]
 # (dram__bytes_read.sum + dram__bytes_write.sum); the default grid only
 MEASURED_TRAFFIC = {"fp32_learned": 134.55e6 + 94.62e6, "fp32_hll": 134.45e6 + 93.56e6}
+MEASURED_TRAFFIC_SOURCE = ("a constant, not measured in this run: ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                           "of one launch (profiles/step_kernel_tma_fp32_learned_godunov_4096x2048.md)")
 
 
 def peaks():
@@ -272,74 +274,108 @@ def axis_shock_z(s):
     return -1.0 + (i + 0.5) * dx
 
 
-def accuracy(nsteps, params):
-    """Error of the FP32 forms against the FP64 path after nsteps from t = 0:
-    the precision form (HLL + minmod) and the learned form (exact Godunov).
-    Two comparisons: at the same step count, and at the same simulated time
-    (the FP64 solution linearly interpolated in time to the FP32 run's final
-    time: the two runs' lagged time steps differ by ~1e-3 after 2000 steps,
-    which moves every shock by a fraction of a cell)."""
+def _errs(r32, r64):
+    d = np.abs(r32 - r64)
+    return {"l1_rho": float(d[:, 0].sum() / np.abs(r64[:, 0]).sum()),
+            "l1_p": float(d[:, 1].sum() / np.abs(r64[:, 1]).sum()),
+            "linf_rho": float(d[:, 0].max() / np.abs(r64[:, 0]).max()),
+            "linf_p": float(d[:, 1].max() / np.abs(r64[:, 1]).max())}
+
+
+def _timed_steps(S, n, stream, torch):
+    """n steps of solver S in one call, device-timed on its stream: seconds."""
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    S.step(n, sync=False)
+    e1.record(stream)
+    S.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def run_from_t0(flux, nsteps, params, torch, fp32_forms):
+    """The blast from t = 0 over nsteps steps: the FP64 run and the given
+    FP32 forms ((name, guess) pairs), each form's average rate over the run
+    (device-timed, one call of all its steps: the FP64 run over its first
+    nsteps - 16 steps, after which it continues step by step), and each FP32
+    form's error against the FP64 run at the same step count and at the same
+    simulated time (the FP64 solution linearly interpolated in time to the
+    FP32 run's final time: the runs' lagged time steps drift apart, which
+    moves every shock by a fraction of a cell)."""
     from asteriy_2d_gb300 import abi as A
     from asteriy_2d_gb300 import problems, solver
-
-    def errs(r32, r64):
-        d = np.abs(r32 - r64)
-        return {"l1_rho": float(d[:, 0].sum() / np.abs(r64[:, 0]).sum()),
-                "l1_p": float(d[:, 1].sum() / np.abs(r64[:, 1]).sum()),
-                "linf_rho": float(d[:, 0].max() / np.abs(r64[:, 0]).max()),
-                "linf_p": float(d[:, 1].max() / np.abs(r64[:, 1]).max())}
-
-    out = {}
-    for name, flux, guess in (("precision_hll", A.FLUX_HLL, None), ("learned_godunov", A.FLUX_GODUNOV, params)):
+    cells = N_Z * M_R
+    cfg64 = problems.blast_config(N_Z, M_R, flux=flux, precision=A.PREC_FP64)
+    s0, u0 = solver.fill_blast(cfg64)
+    stream = torch.cuda.Stream()
+    out, finals = {}, {}
+    for name, guess in fp32_forms:
         cfg32 = problems.blast_config(N_Z, M_R, flux=flux, precision=A.PREC_FP32)
         if flux == A.FLUX_GODUNOV:
             cfg32.riemann_tol = 1e-8
-            cfg32.guess = A.GUESS_MLP
-        cfg64 = problems.blast_config(N_Z, M_R, flux=flux, precision=A.PREC_FP64)
-        s0, u0 = solver.fill_blast(cfg64)
-        with solver.Solver(cfg32) as S:
-            if guess is not None:
-                S.set_mlp(guess)
+            cfg32.guess = guess
+        with solver.Solver(cfg32, stream=stream.cuda_stream) as S:
+            if guess == A.GUESS_MLP:
+                S.set_mlp(params)
             S.set_state(s0, u0)
-            S.step(nsteps)
-            r32 = S.get_state()[0]
-            tt32 = S.clock()[1]
-        # FP64: to nsteps - 8, then single steps, keeping the two states that
-        # bracket tt32 in time (at most 16 more steps)
-        with solver.Solver(cfg64) as S:
-            S.set_state(s0, u0)
-            S.step(nsteps - 8)
-            prev = (S.clock()[1], S.get_state()[0])
-            r64, bracket = None, None
-            for k in range(nsteps - 8, nsteps + 8):
-                S.step(1)
-                cur = (S.clock()[1], S.get_state()[0])
-                if k + 1 == nsteps:
-                    r64, tt64 = cur[1], cur[0]
-                if bracket is None and prev[0] <= tt32 <= cur[0]:
-                    bracket = (prev, cur)
-                if r64 is not None and bracket is not None:
-                    break
-                prev = cur
-        res = {"steps": nsteps, "same_step": errs(r32, r64), "tt_fp32": tt32, "tt_fp64": tt64,
-               "axis_shock_z_fp64": axis_shock_z(r64), "axis_shock_z_fp32": axis_shock_z(r32)}
-        if bracket is not None:
-            (ta, sa), (tb, sb) = bracket
-            w = (tt32 - ta) / (tb - ta) if tb > ta else 0.0
-            res["same_time"] = errs(r32, (1.0 - w) * sa + w * sb)
-        out[name] = res
-        if name == "precision_hll":
-            # the flow's own sensitivity: FP64 from an initial density
-            # perturbed by 1e-12 relative, against the unperturbed FP64 run
-            sp = s0.copy()
-            sp[:, 0] *= 1.0 + 1e-12 * np.random.default_rng(1).uniform(-1.0, 1.0, len(sp))
-            with solver.Solver(cfg64) as S:
-                S.set_state(sp, u0)
-                S.step(nsteps)
-                rp = S.get_state()[0]
-            d = np.abs(rp - r64)
-            out["fp64_sensitivity_1e-12"] = {"steps": nsteps, "l1_rho": float(d[:, 0].sum() / np.abs(r64[:, 0]).sum()),
-                                             "linf_rho": float(d[:, 0].max() / np.abs(r64[:, 0]).max())}
+            sec = _timed_steps(S, nsteps, stream, torch)
+            finals[name] = (S.get_state()[0], S.clock()[1])
+        out[name] = {"rate": cells * nsteps / sec, "ms_per_step": sec * 1e3 / nsteps}
+    # FP64: nsteps - 16 steps in one timed call, then single steps to
+    # nsteps + 8, keeping the states around the FP32 runs' final times
+    k0 = nsteps - 16
+    with solver.Solver(cfg64, stream=stream.cuda_stream) as S:
+        S.set_state(s0, u0)
+        sec = _timed_steps(S, k0, stream, torch)
+        out["fp64"] = {"rate": cells * k0 / sec, "ms_per_step": sec * 1e3 / k0, "timed_steps": k0}
+        hist = [(S.clock()[1], S.get_state()[0])]
+        for _ in range(24):
+            S.step(1)
+            hist.append((S.clock()[1], S.get_state()[0]))
+    r64, tt64 = hist[16][1], hist[16][0]
+    out["fp64"]["tt"] = tt64
+    out["fp64"]["axis_shock_z"] = axis_shock_z(r64)
+    for name, (r32, tt32) in finals.items():
+        res = out[name]
+        res.update({"steps": nsteps, "same_step": _errs(r32, r64), "tt": tt32,
+                    "tt_rel_drift": (tt32 - tt64) / tt64, "axis_shock_z": axis_shock_z(r32)})
+        for (ta, sa), (tb, sb) in zip(hist[:-1], hist[1:]):
+            if ta <= tt32 <= tb:
+                w = (tt32 - ta) / (tb - ta) if tb > ta else 0.0
+                res["same_time"] = _errs(r32, (1.0 - w) * sa + w * sb)
+                break
+    return out
+
+
+def accuracy(nsteps, params, torch):
+    """Error of the FP32 forms against the FP64 path after nsteps from t = 0,
+    and every form's average rate over that run: the precision form (HLL +
+    minmod) and, on the exact solver's problem (the learned form's run), the
+    FP32 form from the acoustic start value and from the learned one."""
+    from asteriy_2d_gb300 import abi as A
+    from asteriy_2d_gb300 import problems, solver
+    out = {"precision_hll": run_from_t0(A.FLUX_HLL, nsteps, None, torch, [("fp32_hll", A.GUESS_PVRS)]),
+           "godunov": run_from_t0(A.FLUX_GODUNOV, nsteps, params, torch,
+                                  [("fp32_pvrs", A.GUESS_PVRS), ("fp32_learned", A.GUESS_MLP)])}
+    # the flow's own sensitivity: FP64 from an initial density perturbed by
+    # 1e-12 relative, against the unperturbed FP64 run (HLL, nsteps)
+    cfg64 = problems.blast_config(N_Z, M_R, flux=A.FLUX_HLL, precision=A.PREC_FP64)
+    s0, u0 = solver.fill_blast(cfg64)
+    sp = s0.copy()
+    sp[:, 0] *= 1.0 + 1e-12 * np.random.default_rng(1).uniform(-1.0, 1.0, len(sp))
+    with solver.Solver(cfg64) as S:
+        S.set_state(s0, u0)
+        S.step(nsteps)
+        r64 = S.get_state()[0]
+        S.set_state(sp, u0)
+        S.set_clock(cfg64.dt_first, 0.0, 0)
+        S.step(nsteps)
+        rp = S.get_state()[0]
+    d = np.abs(rp - r64)
+    out["fp64_sensitivity_1e-12"] = {"steps": nsteps, "l1_rho": float(d[:, 0].sum() / np.abs(r64[:, 0]).sum()),
+                                     "linf_rho": float(d[:, 0].max() / np.abs(r64[:, 0]).max())}
     return out
 
 
@@ -479,25 +515,79 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
     }
 
 
-def cpu_baseline(cfg, s0, u0, nsteps, where="the initial state"):
+def cpu_baseline(cfg, s0, u0, nsteps, clock, where):
     """The reference's face functions compiled for the host (oracle/_ref) in
     the oracle's step loop, on all host threads; the oracle port if the
     reference build is absent."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     nt = os.cpu_count() or 1
+    T_do, TT, step = clock
     if O.have_ref():
         kind = "reference"
-        fn = lambda: O.ref_run_composed(cfg, s0, u0, nsteps, nthreads=nt)  # noqa: E731
+        fn = lambda: O.ref_run_composed(cfg, s0, u0, nsteps, nthreads=nt, T_do=T_do, TT=TT, step_no=step)  # noqa: E731
     else:
         kind = "port"
-        fn = lambda: O.run(cfg, s0, u0, nsteps, nthreads=nt)  # noqa: E731
+        fn = lambda: O.run(cfg, s0, u0, nsteps, T_do=T_do, TT=TT, step_no=step, nthreads=nt)  # noqa: E731
     t0 = time.perf_counter()
     fn()
     dt = time.perf_counter() - t0
     cells = cfg.N * cfg.M * nsteps
     return {"value": cells / dt, "unit": "cell-updates/s", "cores": nt, "kind": kind,
             "sample": f"{nsteps} step(s) of the full {cfg.N}x{cfg.M} grid from {where}, FP64"}
+
+
+def blast_host(cfg, p_in=10.0, p_out=0.1, radius=0.2):
+    """The blast's initial state by numpy, the values ast_fill_blast writes
+    (the reference arm does not load the CUDA library)."""
+    x = cfg.x_min + np.arange(cfg.N) * ((cfg.x_max - cfg.x_min) / (cfg.N - 1))
+    y = (cfg.y_max / (2.0 * cfg.M)) + np.arange(cfg.M) * (cfg.y_max / cfg.M)
+    dist = np.sqrt(x[None, :] * x[None, :] + y[:, None] * y[:, None])
+    s = np.empty((cfg.M * cfg.N, 2))
+    s[:, 0] = 1.0
+    s[:, 1] = np.where(dist < radius, p_in, p_out).reshape(-1)
+    return s, np.zeros((cfg.M * cfg.N, 2))
+
+
+def blast_host_advanced(cfg, nsteps, run, margin=64, radius=0.2):
+    """The blast advanced nsteps steps from t = 0 on the host: `run(sub, s, u,
+    n)` (the reference's functions or the oracle port) steps only the part of
+    the grid the solution can have reached, and the rest keeps the ambient
+    state.  That part is the half z >= 0 (the blast is symmetric about z = 0,
+    the face between the two middle columns, which a reflecting side
+    reproduces) and the rows and columns within the blast radius plus the
+    distance a wave travels in nsteps steps (at most cfl cells per step)
+    plus `margin` cells.  The sub-grid keeps the cell size and positions of
+    the full grid (its dx may differ from the full grid's in the last bit).
+    Returns (s, u, (T_do, TT, step))."""
+    from asteriy_2d_gb300 import abi as A
+    N, M = cfg.N, cfg.M
+    assert N % 2 == 0 and cfg.x_min == -cfg.x_max
+    dx = (cfg.x_max - cfg.x_min) / (N - 1)
+    dy = cfg.y_max / M
+    reach = cfg.cfl * nsteps + margin
+    nz = min(N // 2, int(np.ceil(radius / dx + reach)))
+    mr = min(M, int(np.ceil(radius / dy + reach)))
+    s, u = blast_host(cfg)
+    if nsteps == 0:
+        return s, u, (cfg.dt_first, 0.0, 0)
+    sub = cfg.copy()
+    sub.N, sub.M = nz, mr
+    sub.x_min = cfg.x_min + (N // 2) * dx
+    sub.x_max = cfg.x_min + (N // 2 + nz - 1) * dx
+    sub.y_max = cfg.y_max * mr / M
+    A.set_bc(sub, A.Z_LO, A.BC_REFLECT)
+    g = s.reshape(M, N, 2)
+    h = u.reshape(M, N, 2)
+    ss = np.ascontiguousarray(g[:mr, N // 2:N // 2 + nz]).reshape(-1, 2)
+    us = np.ascontiguousarray(h[:mr, N // 2:N // 2 + nz]).reshape(-1, 2)
+    ss, us, T_do, TT, step, _ = run(sub, ss, us, nsteps)
+    ss, us = ss.reshape(mr, nz, 2), us.reshape(mr, nz, 2)
+    g[:mr, N // 2:N // 2 + nz] = ss
+    h[:mr, N // 2:N // 2 + nz] = us
+    g[:mr, N // 2 - nz:N // 2] = ss[:, ::-1]
+    h[:mr, N // 2 - nz:N // 2] = us[:, ::-1] * np.array([-1.0, 1.0])
+    return s, u, (T_do, TT, step)
 
 
 def reduce_max(value, torch):
@@ -524,6 +614,80 @@ def dist_setup():
     return ws, rank, local
 
 
+def shared_config(args):
+    """The workload, identical in both arms' lines."""
+    return {"workload": f"blast {N_Z}x{M_R}, exact Godunov + minmod, axisymmetric, CFL 0.4",
+            "start_step": args.start_step,
+            "l2": "state larger than L2 (ping-pong of 2x134 MB in FP32, 2x268 MB in FP64)"}
+
+
+def reference_arm(args):
+    """The reference's own functions compiled for the host (oracle/_ref; the
+    oracle port when they are absent) on all host threads, FP64, from the
+    same start as the GPU arm: the blast advanced args.start_step steps,
+    computed here on the host (blast_host_advanced), so that this process
+    never loads the CUDA library.  One full-grid step first (warm-up, and
+    the time of a full step), then the remaining warm-up steps and the
+    timed steps on a band of the grid's first rows (the blast's centre and
+    the axis, all columns) sized so the timed steps take about REF_BUDGET_S
+    seconds, or the full grid when that fits."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    nt = os.cpu_count() or 1
+    kind = "reference" if O.have_ref() else "port"
+
+    def run(c, s, u, n, clock=None):
+        T_do, TT, step = clock if clock else (None, 0.0, 0)
+        if kind == "reference":
+            return O.ref_run_composed(c, s, u, n, nthreads=nt, T_do=T_do, TT=TT, step_no=step)
+        return O.run(c, s, u, n, T_do=T_do, TT=TT, step_no=step, nthreads=nt)
+
+    cfg = make_config("fp64_godunov")
+    t0 = time.perf_counter()
+    s0, u0, clock = blast_host_advanced(cfg, args.start_step, run)
+    t_prep = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s1, u1, T_do, TT, step, _ = run(cfg, s0, u0, 1, clock)
+    t_full = time.perf_counter() - t0
+    rows = cfg.M
+    if args.steps * t_full > REF_BUDGET_S:
+        rows = max(16, int(cfg.M * REF_BUDGET_S / (args.steps * t_full)))
+    band = cfg.copy()
+    band.M = rows
+    band.y_max = cfg.y_max * rows / cfg.M
+    sb, ub = s1[:rows * cfg.N], u1[:rows * cfg.N]
+    bclock = (T_do, TT, step)
+    if args.warmup > 1:
+        sb, ub, T_do, TT, step, _ = run(band, sb, ub, args.warmup - 1, bclock)
+        bclock = (T_do, TT, step)
+    t0 = time.perf_counter()
+    run(band, sb, ub, args.steps, bclock)
+    dt = time.perf_counter() - t0
+    v = band.N * band.M * args.steps / dt
+    sample = (f"{args.steps} steps of rows 0..{rows - 1} of the {N_Z}x{M_R} grid ({N_Z}x{rows} cells per step) "
+              f"from the blast advanced {args.start_step} steps (computed on the host by the same functions in "
+              f"{t_prep:.0f} s on the part of the grid the blast can reach), after {args.warmup} warm-up "
+              f"step(s), the first on the full grid ({t_full:.2f} s)")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic", "scaling": "weak", "vs_baseline": None,
+            "config": shared_config(args), "form": "fp64_godunov", "parallelism": "host threads",
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nt, "kind": kind, "sample": sample},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+METRIC = "cell-updates/s at 4096x2048 (exact Godunov + minmod)"
+
+
+def newton_summary(st):
+    return {"mean_iters": st["newton_iters"] / st["newton_calls"], "max_iters": st["newton_max_iters"],
+            "fallback_rate": st["mlp_fallback"] / max(1, st["strong_calls"]), "gated_faces": st["strong_calls"],
+            "gated_mean_iters": st["strong_iters"] / max(1, st["strong_calls"])}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -536,7 +700,8 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="time only --form")
     ap.add_argument("--grid", default=None, help="NxM instead of 4096x2048 (profiling runs)")
     ap.add_argument("--start-step", type=int, default=1000, help="timed window starts at this step of the run")
-    ap.add_argument("--accuracy-steps", type=int, default=2000, help="FP32 vs FP64 error after these steps (0: skip)")
+    ap.add_argument("--accuracy-steps", type=int, default=2000,
+                    help="whole runs from t = 0 of this many steps: rates and FP32 error vs FP64 (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=1000, help="steps of the 64-problem batch (0: skip)")
     ap.add_argument("--per-tile", action="store_true", help="FP32 forms with one CTA per tile, not the persistent kernel")
     args = ap.parse_args()
@@ -545,67 +710,14 @@ def main():
     if args.grid:
         N_Z, M_R = (int(v) for v in args.grid.lower().split("x"))
     ws, rank, local = dist_setup()
-    from asteriy_2d_gb300 import solver
 
     if args.impl == "reference":
         if rank != 0:
             return 0
-        cfg = make_config("fp64_godunov")
-        s0, u0 = solver.fill_blast(cfg)
-        where = "the initial state"
-        if args.start_step:
-            # the same mid-run start state as the GPU arm: prepared once (on
-            # the GPU when there is one), outside the timed region; only the
-            # reference's own code is timed
-            try:
-                import torch
-                if torch.cuda.is_available():
-                    s0, u0, _ = advance("fp32_pvrs", s0, u0, args.start_step)
-                    where = f"the state at step {args.start_step}"
-            except Exception as e:  # noqa: BLE001
-                where = f"the initial state ({type(e).__name__} preparing step {args.start_step})"
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import pyoracle as O
-        nt = os.cpu_count() or 1
-        kind = "reference" if O.have_ref() else "port"
-        run = (lambda n: O.ref_run_composed(cfg, s0, u0, n, nthreads=nt)) if kind == "reference" else \
-            (lambda n: O.run(cfg, s0, u0, n, nthreads=nt))
-        # one full step untimed (warm-up, and the time of a full step); then
-        # each timed step runs on a band of the grid's first rows (the
-        # blast's centre and the axis), sized so that the timed steps take
-        # about REF_BUDGET_S seconds
-        t0 = time.perf_counter()
-        run(1)
-        t_full = time.perf_counter() - t0
-        rows = cfg.M
-        if args.steps * t_full > REF_BUDGET_S:
-            rows = max(16, int(cfg.M * REF_BUDGET_S / (args.steps * t_full)))
-        band = cfg.copy()
-        band.M = rows
-        band.y_max = cfg.y_max * rows / cfg.M
-        sb, ub = s0[:rows * cfg.N], u0[:rows * cfg.N]
-        run = (lambda n: O.ref_run_composed(band, sb, ub, n, nthreads=nt)) if kind == "reference" else \
-            (lambda n: O.run(band, sb, ub, n, nthreads=nt))
-        t0 = time.perf_counter()
-        run(args.steps)
-        dt = time.perf_counter() - t0
-        v = band.N * band.M * args.steps / dt
-        line = {"impl": "reference", "metric": "cell-updates/s at 4096x2048 (exact Godunov + minmod)", "value": v,
-                "unit": "cell-updates/s",
-                "n_gpus": args.gpus, "steps": args.steps, "warmup": 1,
-                "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "dtype": "f64",
-                "data": "synthetic", "scaling": "weak", "vs_baseline": None,
-                "config": {"workload": f"blast {N_Z}x{M_R}, exact Godunov + minmod, axisymmetric",
-                           "form": "fp64_godunov", "parallelism": "host threads"},
-                "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nt, "kind": kind,
-                                 "sample": (f"{args.steps} steps of rows 0..{rows - 1} of the {N_Z}x{M_R} grid "
-                                            f"({N_Z}x{rows} cells per step) from {where}; one full untimed step "
-                                            f"first ({t_full:.2f} s)")},
-                "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        return 0
+        return reference_arm(args)
 
     import torch
+    from asteriy_2d_gb300 import solver
     torch.cuda.set_device(local)
     if ws > 1:
         import torch.distributed as dist
@@ -617,9 +729,10 @@ def main():
     if any(f.startswith("fp32_learned") for f in ((args.form,) if args.no_forms else FORMS)) or args.accuracy_steps:
         params, params_src = learned_params(s0, u0)
     # the timing window starts mid-run: the blast advanced start_step steps
-    # from t = 0 (with the FP32 form, which is fast), the same start for all
+    # from t = 0 by the FP64 path (the reference arm computes the same start
+    # with the reference's functions on the host), the same start for all
     # forms
-    start = advance("fp32_pvrs", s0, u0, args.start_step) if args.start_step else (s0, u0, (cfg.dt_first, 0.0, 0))
+    start = advance("fp64_godunov", s0, u0, args.start_step) if args.start_step else (s0, u0, (cfg.dt_first, 0.0, 0))
 
     # side-by-side forms (same start state, same step count); the headline
     # form is timed last, under the clock sampler and the rank barrier
@@ -635,11 +748,7 @@ def main():
         forms[form]["hbm_frac"] = BYTES_PER_CELL[pf] * cells / (sec / args.steps) / 1e9 / peaks()[0]
         finals[form] = s
         if st and st["newton_calls"]:
-            forms[form]["newton"] = {"mean_iters": st["newton_iters"] / st["newton_calls"],
-                                     "max_iters": st["newton_max_iters"],
-                                     "fallback_rate": st["mlp_fallback"] / max(1, st["strong_calls"]),
-                                     "gated_faces": st["strong_calls"],
-                                     "gated_mean_iters": st["strong_iters"] / max(1, st["strong_calls"])}
+            forms[form]["newton"] = newton_summary(st)
     if ws > 1:
         torch.distributed.barrier()
     sampler = ClockSampler(local)
@@ -653,11 +762,7 @@ def main():
     forms[args.form] = {"value": cells * args.steps / sec, "ms_per_step": sec * 1e3 / args.steps}
     finals[args.form] = s
     if st and st["newton_calls"]:
-        forms[args.form]["newton"] = {"mean_iters": st["newton_iters"] / st["newton_calls"],
-                                      "max_iters": st["newton_max_iters"],
-                                      "fallback_rate": st["mlp_fallback"] / max(1, st["strong_calls"]),
-                                     "gated_faces": st["strong_calls"],
-                                     "gated_mean_iters": st["strong_iters"] / max(1, st["strong_calls"])}
+        forms[args.form]["newton"] = newton_summary(st)
     # density / pressure L1 error of the FP32 forms against the FP64 run over
     # the timed window (same start, same steps)
     for ref_form, pair in (("fp64_godunov", ("fp32_pvrs", "fp32_learned", "fp32_learned_skip")),
@@ -672,6 +777,8 @@ def main():
             forms[form]["l1_p_vs_fp64"] = float(np.sum(np.abs(sf[:, 1] - ref[:, 1])) / np.sum(np.abs(ref[:, 1])))
     if "fp64_godunov" in forms and args.form != "fp64_godunov":
         forms[args.form]["speedup_vs_fp64"] = forms[args.form]["value"] / forms["fp64_godunov"]["value"]
+    if "fp32_pvrs" in forms and args.form == "fp32_learned":
+        forms["fp32_learned"]["speedup_vs_fp32_pvrs"] = forms["fp32_learned"]["value"] / forms["fp32_pvrs"]["value"]
 
     e2e_steps = max(3, min(args.steps // 4, 50))
     if "fp32_learned_skip" in finals and "fp32_learned" in finals:
@@ -684,21 +791,19 @@ def main():
     hbm, src = peaks()
     prec = "fp64" if args.form.startswith("fp64") else "fp32"
     achieved = BYTES_PER_CELL[prec] * cells / (sec / args.steps) / 1e9
+    traffic = MEASURED_TRAFFIC.get(args.form) if (N_Z, M_R) == (4096, 2048) and PERSISTENT else None
     line = {
-        "metric": "cell-updates/s at 4096x2048 (exact Godunov + minmod)",
+        "metric": METRIC,
         "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
-        "config": {"workload": f"blast {N_Z}x{M_R}, exact Godunov + minmod, axisymmetric, CFL 0.4",
-                   "form": args.form, "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "fp32_kernel": "persistent, bulk-tensor staged" if PERSISTENT else "one CTA per tile",
-                   "mlp_params": params_src,
-                   "l2": "inputs larger than L2 (state ping-pong 2x%d MB)" % (cells * BYTES_PER_CELL[prec] // 2 // 2**20)},
+        "config": shared_config(args),
+        "form": args.form, "parallelism": "replicas" if ws > 1 else "single GPU",
+        "fp32_kernel": "persistent, bulk-tensor staged" if PERSISTENT else "one CTA per tile",
+        "mlp_params": params_src,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src,
-                     "traffic": (MEASURED_TRAFFIC.get(args.form) if (N_Z, M_R) == (4096, 2048) and PERSISTENT
-                                 else None),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch",
+                     "peak_source": src, "traffic": traffic,
+                     "traffic_source": (MEASURED_TRAFFIC_SOURCE if traffic is not None else None),
                      "note": "algorithmic bytes = %d B/cell-update (one state read + one write)" % BYTES_PER_CELL[prec]},
         "forms": forms,
         "e2e": {"value": cells * e2e_steps / esec, "unit": "cell-updates/s", "h2d_bytes_per_step": bi,
@@ -715,17 +820,31 @@ def main():
         "gpu_launches": args.steps,
         "clocks": clocks,
     }
-    line["config"]["start_step"] = args.start_step
     if rank == 0 and not args.no_forms:
         line["configs"] = time_configs(args.warmup, torch)
     if rank == 0 and args.batch_steps:
         line["batch"] = time_batch(args.batch_steps, args.warmup, torch)
         line["gpu_launches_batch_step"] = line["batch"]["launches_per_step"]
     if rank == 0 and args.accuracy_steps:
-        line["accuracy_vs_fp64"] = accuracy(args.accuracy_steps, params)
+        acc = accuracy(args.accuracy_steps, params, torch)
+        line["accuracy_vs_fp64"] = acc
+        g = acc["godunov"]
+        line["run_average"] = {
+            "steps": args.accuracy_steps, "unit": "cell-updates/s",
+            "fp32_learned": g["fp32_learned"]["rate"], "fp32_pvrs": g["fp32_pvrs"]["rate"],
+            "fp64_godunov": g["fp64"]["rate"],
+            "fp32_learned_over_fp64": g["fp32_learned"]["rate"] / g["fp64"]["rate"],
+            "note": "the whole run of the learned form's workload from t = 0, one timed call per form (FP64 over "
+                    "its first %d steps)" % (args.accuracy_steps - 16)}
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(make_config("fp64_godunov"), start[0], start[1], 1,
-                                            where=f"the state at step {args.start_step}")
+        cb = cpu_baseline(make_config("fp64_godunov"), start[0], start[1], 1, start[2],
+                          where=f"the blast advanced {args.start_step} steps")
+        line["cpu_baseline"] = cb
+        if "fp64_godunov" in forms:
+            # the same-precision comparison: the FP64 GPU path against the
+            # reference's functions on the host cores, same state, FP64
+            line["fp64_vs_cpu_reference"] = {"gpu_fp64": forms["fp64_godunov"]["value"], "cpu_fp64": cb["value"],
+                                             "ratio": forms["fp64_godunov"]["value"] / cb["value"]}
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:

@@ -136,10 +136,14 @@ typedef struct ast_config {
        always uses 1 (the reference's absolute tolerance is below FP32
        resolution).                                                          */
     int32_t riemann_newton;
-    /* 1: the FP32 solver steps with the persistent kernel (tiles staged and
-       stored by bulk-tensor copies, double-buffered); 0: one CTA per tile.
-       Same results; the FP64 solver and the raw entry points always use one
-       CTA per tile (default 1)                                              */
+    /* the FP32 solver's step kernel: 2 = strips of 30 columns swept up
+       their rows by one warp each, the stencil, fluxes and update in
+       registers (the learned start value by the whole warp, in FP32);
+       1 = the persistent tile kernel (tiles staged and stored by
+       bulk-tensor copies, double-buffered; the learned start value by f16
+       tensor-core tiles); 0 = one CTA per tile.  The same arithmetic per
+       face and cell; the FP64 solver and the raw entry points always use
+       one CTA per tile (default 1)                                          */
     int32_t persistent;
     /* 1: tiles whose staged cells (tile and two-cell halo, ghosts included)
        all hold the same four values, bit for bit, skip the face pass: every
@@ -150,7 +154,13 @@ typedef struct ast_config {
        with region_select, and uniform states whose flux is not finite take
        the full path (default 0)                                             */
     int32_t skip_uniform;
-    int32_t reserved_i[4];
+    /* polls of a bulk tile copy's barrier before the FP32 persistent kernels
+       report AST_ST_TIMEOUT (the copy is then waited for with the long
+       default limit and the tile computed, so the step's result is the
+       same; ast_synchronize returns AST_ERR_CUDA).  0: the default, about a
+       second; small values make the failure path run (tests)            */
+    int32_t copy_wait_polls;
+    int32_t reserved_i[3];
     /* wave strength above which the learned start value is used:
        max(|ln(p_R/p_L)|, |u_R - u_L| / min(c_L, c_R)); weaker faces start
        from the acoustic value, which is already close for them (0.2)        */

@@ -63,6 +63,12 @@ typedef struct ora_stats {
     int64_t bisect_calls, bisect_iters, bisect_cap;
     int64_t vacuum;
     int64_t newton_max;
+    /* smallest | |residual| - tol | / tol over the bisection's stopping
+       tests since the cell began (the per-cell margin diagnostic) */
+    double margin;
+    /* smallest distance of Udf to a wave-pattern threshold (Uvk, Urz,
+       Uud), relative to cI + cII, over the faces with unequal states */
+    double pmargin;
 } ora_stats;
 
 /* physical constants of one configuration (Header.h:17-26, 47, 62-63) */
@@ -267,6 +273,14 @@ static void lev(const ora_phys* ph, double enI, double pI, double rI, double enI
     *fee = f1 - f2;
 }
 
+/* the margin diagnostic: how close one stopping test |res| <= tol came to
+   the other outcome, relative to tol (not part of the reference) */
+static void ora_margin(ora_stats* st, double res, double tol)
+{
+    const double m = fabs(fabs(res) - tol) / tol;
+    if (m < st->margin) st->margin = m;
+}
+
 /* bisection on [pI, pII] for the shock-rarefaction pattern (kernel.cu:682-749) */
 static void devtwo(const ora_phys* ph, ora_stats* st, double enI, double pI, double rI,
                    double enII, double pII, double rII, double* p)
@@ -277,12 +291,15 @@ static void devtwo(const ora_phys* ph, ora_stats* st, double enI, double pI, dou
     lev(ph, enI, pI, rI, enII, pII, rII, kl, &ksi);
     lev(ph, enI, pI, rI, enII, pII, rII, kp, &ksir);
     st->bisect_calls++;
+    ora_margin(st, ksi, epsil);
     if (fabs(ksi) <= epsil) { *p = kl; return; }
+    ora_margin(st, ksir, epsil);
     if (fabs(ksir) <= epsil) { *p = kp; return; }
     for (;;) {
         it++;
         kc = (kl + kp) / 2.0;
         lev(ph, enI, pI, rI, enII, pII, rII, kc, &ksit);
+        ora_margin(st, ksit, epsil);
         if (fabs(ksit) <= epsil) break;
         if (it >= ph->max_iter) { st->bisect_cap++; break; }
         if ((ksi * ksit) <= 0.0) { kp = kc; ksir = ksit; }
@@ -358,6 +375,11 @@ static double godunov(const ora_phys* ph, ora_stats* st, d2 Ls, d2 Lu, d2 Rs, d2
     double Uvk = -2.0 * (cII + cI) / g1;
     double Udf = enI - enII;
     int il = -2, ip = -2;
+    if (!(pI == pII && rI == rII && enI == enII)) {
+        const double sc = (cI + cII > 0.0) ? cI + cII : 1.0;
+        const double pm = fmin(fabs(Udf - Urz), fmin(fabs(Udf - Uud), fabs(Udf - Uvk))) / sc;
+        if (pm < st->pmargin) st->pmargin = pm;
+    }
     double p = 0.0, r = 0.0, te2 = 0.0, te3 = 0.0, en = 0.0;
 
     if (Udf < Uvk) { il = -1; ip = -1; }
@@ -700,6 +722,21 @@ static const double* g_nn2 = NULL;
 
 void ora_set_neutral(const double* nn2) { g_nn2 = nn2; }
 
+/* Per-cell margin diagnostic (not part of the reference): when set, every
+   step writes, for each cell k, the smallest | |res| - tol | / tol over the
+   bisection stopping tests of its four faces (devtwo, kernel.cu:682-749),
+   or a large value when none ran.  A cell whose margin is small can take one
+   bisection iterate more or less under rounding of its inputs. */
+static double* g_margin = NULL;
+static double* g_pmargin = NULL;
+
+/* per_cell: the bisection margins; pattern (may be NULL): per cell the
+   smallest distance of Udf to a wave-pattern threshold of its faces
+   (Uvk, Urz, Uud of kernel.cu:186-231) relative to cI + cII, over the faces
+   with unequal states (a cell whose faces sit on a threshold can change
+   pattern under rounding of its inputs) */
+void ora_set_margin(double* per_cell, double* pattern) { g_margin = per_cell; g_pmargin = pattern; }
+
 /* One cell of one step.  Returns the cell's tmin; a cell held fixed returns
    1e7, the reset value of T, because the reference's fixed cells never
    touch T (kernel.cu:2318-2324). */
@@ -714,6 +751,8 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
     const double ggg = ph->ga;
     double tmin = c->dt_cap;
     d2 s_1 = s[index], u_1 = u[index];
+    st->margin = 1e300;
+    st->pmargin = 1e300;
 
     if (c->fixed_region) {
         double xz = x - c->fixed_zc;
@@ -909,6 +948,8 @@ double ora_step(const ast_config* c, const double* s, const double* u, double* s
             for (int n = 0; n < g.N; n++) {
                 double tm = ora_cell(&g, c, &ph, &st, S, U, S2, U2, n, m, T_do);
                 if (Tl > tm) Tl = tm;
+                if (g_margin) g_margin[(size_t)m * g.N + n] = st.margin;
+                if (g_pmargin) g_pmargin[(size_t)m * g.N + n] = st.pmargin;
             }
         }
 #ifdef _OPENMP

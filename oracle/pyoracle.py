@@ -56,6 +56,8 @@ def lib():
         L.ora_run.restype = C.c_int
         L.ora_run.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _i64p, C.c_int, _i64p]
         L.ora_max_threads.restype = C.c_int
+        L.ora_set_margin.restype = None
+        L.ora_set_margin.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_inflow.restype = None
         L.ora_inflow.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         _lib = L
@@ -145,6 +147,23 @@ def run(cfg, s, u, nsteps, T_do=None, TT=0.0, step_no=0, nthreads=1, nn2=None):
     return s, u, tdo.value, tt.value, st.value, cnt
 
 
+def step_margin(cfg, s, u, T_do, nthreads=1):
+    """One step like step(), plus two per-cell diagnostics of the exact
+    solver's faces: the bisection margin, the smallest | |res| - tol | / tol
+    over the bisection stopping tests (devtwo), and the pattern margin, the
+    smallest distance of Udf to a wave-pattern threshold relative to
+    cI + cII, over faces with unequal states (1e300 where none applies).
+    Returns (s2, u2, new_dt, bisect_margin[K], pattern_margin[K])."""
+    margin = np.empty(cfg.N * cfg.M)
+    pmargin = np.empty(cfg.N * cfg.M)
+    lib().ora_set_margin(margin.ctypes.data, pmargin.ctypes.data)
+    try:
+        s2, u2, T, _ = step(cfg, s, u, T_do, nthreads)
+    finally:
+        lib().ora_set_margin(None, None)
+    return s2, u2, T, margin, pmargin
+
+
 def max_threads():
     return lib().ora_max_threads()
 
@@ -206,15 +225,16 @@ def ref_bound(cfg, s, u, s2, u2):
     return s2, u2
 
 
-def ref_run_composed(cfg, s, u, nsteps, nthreads=1):
+def ref_run_composed(cfg, s, u, nsteps, nthreads=1, T_do=None, TT=0.0, step_no=0):
     """The oracle's step loop with every face evaluated by the reference's own
-    HLL / HLLC / Godunov functions (any configuration).  Returns like run()."""
+    HLL / HLLC / Godunov functions (any configuration), from the clock
+    (T_do, TT, step_no) (T_do None: cfg.dt_first).  Returns like run()."""
     ref_set(cfg)
     s = np.array(s, dtype=np.float64, order="C")
     u = np.array(u, dtype=np.float64, order="C")
-    tdo = C.c_double(cfg.dt_first)
-    tt = C.c_double(0.0)
-    st = C.c_int64(0)
+    tdo = C.c_double(cfg.dt_first if T_do is None else T_do)
+    tt = C.c_double(TT)
+    st = C.c_int64(step_no)
     cnt = np.zeros(10, dtype=np.int64)
     rc = ref().ora_run(C.byref(cfg), _ptr(s), _ptr(u), nsteps, C.byref(tdo), C.byref(tt), C.byref(st),
                        nthreads, cnt.ctypes.data_as(_i64p))

@@ -50,7 +50,7 @@ def test_config_default_matches_reference_macros():
 
 @pytest.mark.parametrize("field,value", [("N", 2), ("M", 0), ("gamma", 1.0), ("cfl", 0.0), ("flux", 7),
                                          ("riemann_max_iter", 0), ("x_max", -5.0),
-                                         ("persistent", 2), ("skip_uniform", 2), ("skip_uniform", -1),
+                                         ("persistent", 3), ("copy_wait_polls", -1), ("skip_uniform", 2), ("skip_uniform", -1),
                                          ("neutral_nh", float("nan")), ("neutral_kn", float("inf"))])
 def test_config_check_rejects(field, value):
     c = problems.blast_config(64, 32)

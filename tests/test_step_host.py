@@ -76,6 +76,9 @@ CASES = [
     (A.PREC_FP64, 0, A.FLUX_HLLC, (1024, 512)),     # FP64, 32x16 tiles
     (A.PREC_FP64, 0, A.FLUX_GODUNOV, (97, 45)),     # FP64, 16x16 tiles, 3 tile rows
     (A.PREC_FP32, 1, A.FLUX_HLLC_A, (40, 7)),       # one tile row: one band
+    (A.PREC_FP32, 2, A.FLUX_HLL, (512, 384)),       # strip kernel, 16 bands (strips cut at band edges)
+    (A.PREC_FP32, 2, A.FLUX_HLLC, (64, 3200)),      # strip kernel, bands of 12-13 tile rows
+    (A.PREC_FP32, 2, A.FLUX_HLLC_A, (300, 130)),    # strip kernel, ragged edges
 ]
 
 
