@@ -106,10 +106,13 @@ __device__ __forceinline__ R flux_hll(const Gas<R>& g, R rL, R pL, R unL, R utL,
     R cR = (rR <= R(0)) ? R(0) : sqrt(g.ga * pR / rR);
     R eL = pL * g.inv_g1 + rL * (unL * unL + utL * utL) * R(0.5);
     R eR = pR * g.inv_g1 + rR * (unR * unR + utR * utR) * R(0.5);
-    R mxc = fmax(cL, cR);
-    R DL = fmin(unL, unR) - mxc;
-    R DR = fmax(unL, unR) + mxc;
-    R S = fmax(fabs(DL), fabs(DR));
+    // the reference's selects, not fmin/fmax: they give the same values,
+    // and a NaN (the sound speed of a negative pressure) propagates or not
+    // as in the reference (kernel.cu:1399-1523)
+    R mxc = (cL >= cR) ? cL : cR;
+    R DL = ((unL <= unR) ? unL : unR) - mxc;
+    R DR = ((unL >= unR) ? unL : unR) + mxc;
+    R S = (fabs(DL) >= fabs(DR)) ? fabs(DL) : fabs(DR);
     R mL = rL * unL, mR = rR * unR;
     if (DL > R(0)) {
         F[0] = mL; F[1] = mL * unL + pL; F[2] = mL * utL; F[3] = (eL + pL) * unL;

@@ -32,22 +32,39 @@
 namespace ast {
 
 constexpr int kSW = 30;   // columns a strip updates
-constexpr int kSH = 64;   // rows of a strip (a multiple of the 16-row band unit)
+constexpr int kSH = 32;   // rows of a strip (a multiple of the 16-row band unit)
 constexpr unsigned kFull = 0xffffffffu;
 
+// the four planes of a column: base pointers of its cell in row 0; cell
+// (n, m) of the plane is base[k][m * ld] (32-bit row offsets: the planes
+// of a grid that ast_config_check accepts hold fewer than 2^32 elements)
+struct SwCol {
+    const float* q[4];
+    __device__ __forceinline__ void init(const StepParams& P, int n)
+    {
+        const float* b = (const float*)P.in + n;
+        q[0] = b;
+        q[1] = b + P.plane;
+        q[2] = b + 2 * P.plane;
+        q[3] = b + 3 * P.plane;
+    }
+};
+
 // cell (n, m) of the FP32 input planes; strips at the grid's edge take the
-// ghost rules (fetch_cell), the others plain loads
-__device__ __forceinline__ void sw_load(const StepParams& P, bool edge, int n, int m, float v[4])
+// ghost rules (fetch_cell), the others plain loads through the column's
+// plane bases (col: column n)
+__device__ __forceinline__ void sw_load(const StepParams& P, bool edge, const SwCol& col, int n, int m, float v[4],
+                                        int dn = 0)
 {
     if (edge) {
-        fetch_cell<float, kSoA>(P, n, m, v);
+        fetch_cell<float, kSoA>(P, n + dn, m, v);
         return;
     }
-    const float* q = (const float*)P.in + (long long)m * P.ld + n;
-    v[0] = __ldg(q);
-    v[1] = __ldg(q + P.plane);
-    v[2] = __ldg(q + 2 * P.plane);
-    v[3] = __ldg(q + 3 * P.plane);
+    const long long o = (long long)((unsigned)m * (unsigned)P.ld) + dn;
+    v[0] = __ldg(col.q[0] + o);
+    v[1] = __ldg(col.q[1] + o);
+    v[2] = __ldg(col.q[2] + o);
+    v[3] = __ldg(col.q[3] + o);
 }
 
 // the two face values of a cell t from its neighbours a (lower) and b
@@ -233,9 +250,11 @@ __device__ __forceinline__ void sweep_strip(const StepParams& P, const StepConst
     const bool near = P.fixed_region && n0 - 2 <= P.fixed_nhi && n0 + kSW + 1 >= P.fixed_nlo && m0 - 2 <= P.fixed_mhi;
     const bool cin = c >= 0 && c < N;
     const bool owner = lane >= 1 && lane <= kSW && c < N;
-    // the outer z neighbour of lanes 0 and 31 (the other lanes load their
-    // own cell again, an L1 hit, and do not use it)
-    const int cx = (lane == 0) ? c - 1 : (lane == 31 ? c + 1 : c);
+    // the outer z neighbour of lanes 0 and 31, column c + dx (the other
+    // lanes load their own cell again, an L1 hit, and do not use it)
+    const int dx = (lane == 0) ? -1 : (lane == 31 ? 1 : 0);
+    SwCol cc;
+    if (!edge) cc.init(P, c);
     // region test of this lane's faces (lower cell's column, as face_meta)
     const bool hz = !P.region_select || (c >= P.region_zlo && c <= P.region_zhi);
     const bool hr = !P.region_select || (c >= P.region_rlo && c <= P.region_rhi);
@@ -246,12 +265,12 @@ __device__ __forceinline__ void sweep_strip(const StepParams& P, const StepConst
     {
         // warm-up: rows m0-2 .. m0+2, the r face below row m0
         float a[4], b[4];
-        sw_load(P, edge, c, m0 - 2, a);
-        sw_load(P, edge, c, m0 - 1, b);
-        sw_load(P, edge, c, m0, w0);
-        sw_load(P, edge, c, m0 + 1, w1);
-        sw_load(P, edge, c, m0 + 2, w2);
-        sw_load(P, edge, cx, m0, ex);
+        sw_load(P, edge, cc, c, m0 - 2, a);
+        sw_load(P, edge, cc, c, m0 - 1, b);
+        sw_load(P, edge, cc, c, m0, w0);
+        sw_load(P, edge, cc, c, m0 + 1, w1);
+        sw_load(P, edge, cc, c, m0 + 2, w2);
+        sw_load(P, edge, cc, c, m0, ex, dx);
         float lo[4], Rm[4];
         sw_recon<RECON>(P, a, b, w0, lo, Rm);   // cell m0-1: its top value
         sw_recon<RECON>(P, b, w0, w1, lo, Rr);  // cell m0: bottom (lo), top (Rr)
@@ -285,11 +304,12 @@ __device__ __forceinline__ void sweep_strip(const StepParams& P, const StepConst
         }
     }
     const float gaf = g.ga, g1f = g.g1, ig1f = g.inv_g1;
+#pragma unroll 1
     for (int m = m0; m < m1; m++) {
         // row m+3 and the outer neighbour of row m+1, one step ahead
         float nx[4], exn[4];
-        sw_load(P, edge, c, m + 3, nx);
-        sw_load(P, edge, cx, m + 1, exn);
+        sw_load(P, edge, cc, c, m + 3, nx);
+        sw_load(P, edge, cc, c, m + 1, exn, dx);
         fx1 = sw_fixed(P, near, c, m + 1);
         // r: cell m+1 (rows m, m+1, m+2)
         float Lr1[4], Rr1[4];
@@ -311,10 +331,20 @@ __device__ __forceinline__ void sweep_strip(const StepParams& P, const StepConst
         }
         // the two faces: z face right of cell m (zL | zU) and r face above it
         float zL[4], zU[4], rL[4], rU[4];
-        sw_sel(hz, Rz, w0, zL);
-        sw_sel(hz, Un, Uc, zU);
-        sw_sel(hr, Rr, w0, rL);
-        sw_sel(hr, Lr1, w1, rU);
+        if (P.region_select) {
+            sw_sel(hz, Rz, w0, zL);
+            sw_sel(hz, Un, Uc, zU);
+            sw_sel(hr, Rr, w0, rL);
+            sw_sel(hr, Lr1, w1, rU);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                zL[k] = Rz[k];
+                zU[k] = Un[k];
+                rL[k] = Rr[k];
+                rU[k] = Lr1[k];
+            }
+        }
         float Fz[4], Ft[4], Sz, Sr;
         if constexpr (FLUX == 0) {
             float2 F[4], S;
