@@ -3,7 +3,9 @@
 TEST INFRASTRUCTURE ONLY.  Recipe:
   1. copy the listed line ranges of the reference, byte for byte, into
      oracle/_ref/ref_extract.inc (each range preceded by a #line directive
-     naming its origin, and checked against the function it must start with);
+     naming its origin, and checked against the function it must start with),
+     and the reference's file writers into oracle/_ref/ref_pfm.inc and
+     ref_endrun.inc (compiled by oracle/ref_writers.cpp);
   2. compile oracle/ref_driver.cpp, which includes oracle/ref_shim.h and that
      file, with g++ -fopenmp -ffp-contract=off into oracle/_ref/libastref.so,
      together with the oracle's step loop (oracle/ast_oracle.c built with
@@ -49,8 +51,36 @@ RANGES = [
 ]
 
 
+# the reference's writers (host C++), for pinning the library's file writers:
+# print_file_mini (the snapshot with Mach and vorticity) and the end-of-run
+# block of main that writes the .bin dump, the mini Tecplot file with T and
+# Zav, the axis line and the run summary; written to their own files
+WRITER_RANGES = {
+    "ref_pfm.inc": [("kernel.cu", 3109, 3173, "void print_file_mini(")],
+    "ref_endrun.inc": [("kernel.cu", 4109, 4221, "ofstream fout;")],
+}
+
+
+def _copy_ranges(src, ranges, dst):
+    chunks = []
+    for fname, a, b, must in ranges:
+        path = os.path.join(src, fname)
+        with open(path, "rb") as f:
+            lines = f.read().decode("latin-1").splitlines()
+        first = lines[a - 1]
+        if must not in first:
+            raise RuntimeError(f"{fname}:{a} does not start {must!r}: {first!r}")
+        chunks.append(f'#line {a} "{fname}"')
+        chunks.extend(lines[a - 1:b])
+    with open(dst, "wb") as f:
+        f.write(("\n".join(chunks) + "\n").encode("latin-1"))
+    return dst
+
+
 def extract(src):
     os.makedirs(OUT, exist_ok=True)
+    for name, ranges in WRITER_RANGES.items():
+        _copy_ranges(src, ranges, os.path.join(OUT, name))
     chunks = []
     for fname, a, b, must in RANGES:
         path = os.path.join(src, fname)
@@ -77,8 +107,11 @@ def compile_ref(cxx="g++"):
     # the oracle's step loop, with every face evaluated by the reference's functions
     subprocess.run(["gcc", "-O2", "-std=c99", "-fopenmp", "-ffp-contract=off", "-fPIC", "-DORA_WITH_REF", "-c",
                     os.path.join(HERE, "ast_oracle.c"), "-o", obj], check=True)
+    srcs = [os.path.join(HERE, "ref_driver.cpp")]
+    if all(os.path.exists(os.path.join(OUT, n)) for n in WRITER_RANGES):
+        srcs.append(os.path.join(HERE, "ref_writers.cpp"))
     cmd = [cxx, "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-w",
-           "-I", HERE, os.path.join(HERE, "ref_driver.cpp"), obj, "-o", so]
+           "-I", HERE] + srcs + [obj, "-o", so]
     subprocess.run(cmd, check=True)
     return so
 

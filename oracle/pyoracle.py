@@ -94,6 +94,11 @@ def ref():
         R.ref_bound.restype = None
         R.ref_bound.argtypes = [_dp, _dp, _dp, _dp]
         R.ref_diag_count.restype = C.c_longlong
+        if hasattr(R, "ref_print_file_mini"):
+            R.ref_print_file_mini.restype = None
+            R.ref_print_file_mini.argtypes = [_dp, _dp, C.c_int, C.c_double, C.c_char_p]
+            R.ref_end_of_run.restype = None
+            R.ref_end_of_run.argtypes = [_dp, _dp, C.c_double, C.c_int, C.c_double, C.c_double, C.c_char_p]
         R.ref_max_threads.restype = C.c_int
         _ref = R
     return _ref
@@ -223,6 +228,26 @@ def ref_bound(cfg, s, u, s2, u2):
     ref().ref_bound(_ptr(np.ascontiguousarray(s, dtype=np.float64)), _ptr(np.ascontiguousarray(u, dtype=np.float64)),
                     _ptr(s2), _ptr(u2))
     return s2, u2
+
+
+def have_ref_writers():
+    return have_ref() and hasattr(ref(), "ref_print_file_mini")
+
+
+def ref_print_file_mini(cfg, s, u, stride, soltime, path):
+    """The reference's print_file_mini (kernel.cu:3109-3173) of (s, u) to path."""
+    ref_set(cfg)
+    ref().ref_print_file_mini(_ptr(np.ascontiguousarray(s, dtype=np.float64)),
+                              _ptr(np.ascontiguousarray(u, dtype=np.float64)), stride, soltime, path.encode())
+
+
+def ref_end_of_run(cfg, s, u, TT, stride, mach_inf, chi, name):
+    """The end-of-run files of the reference's main (kernel.cu:4109-4221):
+    name.bin, name_param_for_texplot.txt, name_param_for_texplot_mini.txt,
+    name_param_y=0.txt, name_inform.txt."""
+    ref_set(cfg)
+    ref().ref_end_of_run(_ptr(np.ascontiguousarray(s, dtype=np.float64)),
+                         _ptr(np.ascontiguousarray(u, dtype=np.float64)), TT, stride, mach_inf, chi, name.encode())
 
 
 def ref_run_composed(cfg, s, u, nsteps, nthreads=1, T_do=None, TT=0.0, step_no=0):

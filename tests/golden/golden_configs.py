@@ -64,3 +64,11 @@ def inflow_config(N=24, M=8):
     c.N, c.M = N, M
     c.inflow_p, c.inflow_v = 7.0, 1.0
     return c
+
+
+def writer_config(N=24, M=12):
+    """The grid of the writer fixtures: z in [-1, 1], r in [0, 1], gamma 5/3."""
+    c = A.default_config()
+    c.N, c.M = N, M
+    c.x_min, c.x_max, c.y_max = -1.0, 1.0, 1.0
+    return c

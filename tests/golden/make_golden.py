@@ -20,10 +20,15 @@ records their outputs on seeded inputs:
   step_mk_neutral.npz
                  20 launches of add_MK method 0 (HLL) on the 48x24 grid with
                  a random neutral-coupling source nn2 (kernel.cu:2495-2496;
-                 the reference's main passes zeros).
+                 the reference's main passes zeros);
+  writers.npz    the bytes of the files the reference's writers produce for a
+                 random 24x12 state: print_file_mini (kernel.cu:3109-3173)
+                 with every 2nd and every 3rd cell, and the end-of-run block of
+                 main (kernel.cu:4109-4221: the .bin dump, the mini Tecplot
+                 file with T and Zav, the axis line, the run summary).
 
 The configurations that reproduce those kernels live in golden_configs.py so
-the tests use exactly the same ones.  Usage:  python tests/golden/make_golden.py
+the tests use exactly the same ones.  Usage:  python tests/golden/make_golden.py [writers]   (writers: that file only)
 """
 import os
 import sys
@@ -110,8 +115,36 @@ def make_neutral(rng):
                         TT=tt, steps=st, nsteps=20)
 
 
+def make_writers(rng):
+    import tempfile
+    cfg = G.writer_config()
+    K = cfg.N * cfg.M
+    s, u = G.random_state(K, rng)
+    u[:, 0] -= 0.5
+    TT, mach_inf, chi, soltime = 0.0123456789, 0.5, 17.0, 0.25
+    files = {}
+    with tempfile.TemporaryDirectory() as d:
+        for stride in (2, 3):
+            p = os.path.join(d, f"pfm{stride}.txt")
+            O.ref_print_file_mini(cfg, s, u, stride, soltime, p)
+            files[f"pfm{stride}"] = open(p, "rb").read()
+            name = os.path.join(d, f"run{stride}")
+            O.ref_end_of_run(cfg, s, u, TT, stride, mach_inf, chi, name)
+            files[f"final{stride}"] = open(name + "_param_for_texplot_mini.txt", "rb").read()
+            if stride == 2:
+                files["bin"] = open(name + ".bin", "rb").read()
+                files["axis"] = open(name + "_param_y=0.txt", "rb").read()
+                files["inform"] = open(name + "_inform.txt", "rb").read()
+    np.savez_compressed(os.path.join(HERE, "writers.npz"), s=s, u=u, TT=TT, mach_inf=mach_inf, chi=chi,
+                        soltime=soltime, **{k: np.frombuffer(v, dtype=np.uint8) for k, v in files.items()})
+
+
 def main():
     make_ref.main([])
+    if sys.argv[1:] == ["writers"]:
+        make_writers(np.random.default_rng(3109))
+        print("writers.npz written to", HERE)
+        return
     rng = np.random.default_rng(20261203)
     make_faces(rng)
     make_step("step_tvd.npz", G.tvd_config(), O.REF_KERNEL_TVD, 1, 20, rng)
@@ -120,6 +153,7 @@ def main():
     make_step("step_mk_hllca.npz", G.add_mk_config(1), O.REF_ADD_MK, 1, 20, rng)
     make_inflow(np.random.default_rng(1895))
     make_neutral(np.random.default_rng(2495))
+    make_writers(np.random.default_rng(3109))
     print("golden vectors written to", HERE)
 
 
