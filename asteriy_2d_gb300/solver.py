@@ -41,6 +41,7 @@ SIGNATURES = {
     "ast_step_raw": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_int, C.POINTER(A.ast_config), C.c_void_p]),
     "ast_funk_time": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ast_add2_raw": (C.c_int, [C.c_void_p] * 7 + [C.c_int, C.c_int, C.POINTER(A.ast_config), C.c_void_p]),
     "ast_inflow_raw": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(A.ast_config),
                                  C.c_void_p]),
     "ast_step_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -380,6 +381,13 @@ def add_mk_raw(s, u, s2, u2, nn2, T, T_do, cfg, stream=None):
     check(load().ast_add_mk_raw(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), None,
                                 C.c_void_p(nn2) if nn2 else None, None, C.c_void_p(T), C.c_void_p(T_do), 0, 0,
                                 C.byref(cfg), C.c_void_p(stream) if stream else None), "ast_add_mk_raw")
+
+
+def add2_raw(s, u, s2, u2, T, T_do, TT, cfg, method=1, stream=None):
+    """ast_add2_raw on device pointers (ints), the add2 drop-in."""
+    check(load().ast_add2_raw(C.c_void_p(s), C.c_void_p(u), C.c_void_p(s2), C.c_void_p(u2), C.c_void_p(T),
+                              C.c_void_p(T_do), C.c_void_p(TT), method, 0, C.byref(cfg),
+                              C.c_void_p(stream) if stream else None), "ast_add2_raw")
 
 
 def inflow_raw(s, u, s2, u2, cfg, stream=None):

@@ -331,6 +331,23 @@ int ast_step_raw(const double* s, const double* u, double* s2, double* u2,
 int ast_add_mk_raw(const double* s, const double* u, double* s2, double* u2, const double* nn1,
                    const double* nn2, const double* nn3, double* T, const double* T_do, int method, int step,
                    const ast_config* cfg, void* cuda_stream);
+/* The same for the first-order planar step
+     add2<<<K/256,256>>>(s, u, s2, u2, T, T_do, TT, method, step)
+   (kernel.cu:1928-2291, launched at kernel.cu:3488, 3512, 3564, 3589),
+   reproduced as the reference evaluates it: each cell its own four faces,
+   HLLC on its right and r faces inside the region (region_lo, region_hi)
+   and HLL outside, and on its LEFT face HLL inside the region and HLLC
+   outside (kernel.cu:2078-2085: the two cells of one face use different
+   fluxes there); right side outflow, left side the z_lo FIXED state with
+   its density perturbed by 1 + 0.01 sin(2 pi *TT) for y < 0.5 while
+   *TT < 3 when method != 0; reflecting r sides; the body force of
+   ast_config (the reference's is 2.5 rho for 20 < z < 30).  Lowers *T to
+   the cells' smallest dt candidate (atomic).  cfg must be FP64, first
+   order (recon NONE), planar, with a FIXED z_lo side; region_select 0
+   means no region (HLL right and r faces, HLLC left faces).  step is
+   ignored.  Device pointers. */
+int ast_add2_raw(const double* s, const double* u, double* s2, double* u2, double* T, const double* T_do,
+                 const double* TT, int method, int step, const ast_config* cfg, void* cuda_stream);
 /* Replacement for add2_bound<<<K/256,256>>>(s, u, s2, u2, ...)
    (kernel.cu:1895-1925, launched after the step at kernel.cu:3565, 3590):
    column n = 0 of (s2, u2) from the old state (s, u) and the new column 1,

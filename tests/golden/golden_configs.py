@@ -72,3 +72,21 @@ def writer_config(N=24, M=12):
     c.N, c.M = N, M
     c.x_min, c.x_max, c.y_max = -1.0, 1.0, 1.0
     return c
+
+
+def add2_config(N=96, M=12):
+    """add2 (kernel.cu:1928-2291) with Header.h's domain [0,80]x[0,1]: the
+    region 10.000001 < x < 40.000001 of its flux rule, inflow (1, p_H)
+    (1, 0) at n=0 (p_H = 7), outflow at n=N-1, reflecting r sides, body
+    force +-2.5 rho for 20.000001 < x < 30.000001 (split at r = 0.5),
+    first order, planar."""
+    c = A.default_config()
+    c.N, c.M = N, M
+    c.flux, c.recon, c.geom = A.FLUX_HLLC, A.RECON_NONE, A.GEOM_PLANAR
+    c.region_select, c.region_lo, c.region_hi = 1, 10.000001, 40.000001
+    A.set_bc(c, A.Z_LO, A.BC_FIXED, 1.0, 7.0, 1.0, 0.0)
+    A.set_bc(c, A.Z_HI, A.BC_OUTFLOW)
+    A.set_bc(c, A.R_LO, A.BC_REFLECT)
+    A.set_bc(c, A.R_HI, A.BC_REFLECT)
+    c.body_force, c.body_lo, c.body_hi, c.body_rsplit, c.body_amp = 1, 20.000001, 30.000001, 0.5, 2.5
+    return c

@@ -21,6 +21,10 @@ records their outputs on seeded inputs:
                  20 launches of add_MK method 0 (HLL) on the 48x24 grid with
                  a random neutral-coupling source nn2 (kernel.cu:2495-2496;
                  the reference's main passes zeros);
+  step_add2_m0.npz, step_add2_m1.npz
+                 20 launches of add2 (kernel.cu:1928) + funk_time, method 0
+                 and method 1 (the time-dependent inflow density), on a
+                 96x12 grid with a random state;
   writers.npz    the bytes of the files the reference's writers produce for a
                  random 24x12 state: print_file_mini (kernel.cu:3109-3173)
                  with every 2nd and every 3rd cell, and the end-of-run block of
@@ -28,7 +32,7 @@ records their outputs on seeded inputs:
                  file with T and Zav, the axis line, the run summary).
 
 The configurations that reproduce those kernels live in golden_configs.py so
-the tests use exactly the same ones.  Usage:  python tests/golden/make_golden.py [writers]   (writers: that file only)
+the tests use exactly the same ones.  Usage:  python tests/golden/make_golden.py [writers | add2]   (that fixture only)
 """
 import os
 import sys
@@ -115,6 +119,12 @@ def make_neutral(rng):
                         TT=tt, steps=st, nsteps=20)
 
 
+def make_add2():
+    rng = np.random.default_rng(1928)
+    for method in (0, 1):
+        make_step(f"step_add2_m{method}.npz", G.add2_config(), O.REF_ADD2, method, 20, rng)
+
+
 def make_writers(rng):
     import tempfile
     cfg = G.writer_config()
@@ -145,6 +155,10 @@ def main():
         make_writers(np.random.default_rng(3109))
         print("writers.npz written to", HERE)
         return
+    if sys.argv[1:] == ["add2"]:
+        make_add2()
+        print("add2 fixtures written to", HERE)
+        return
     rng = np.random.default_rng(20261203)
     make_faces(rng)
     make_step("step_tvd.npz", G.tvd_config(), O.REF_KERNEL_TVD, 1, 20, rng)
@@ -154,6 +168,7 @@ def main():
     make_inflow(np.random.default_rng(1895))
     make_neutral(np.random.default_rng(2495))
     make_writers(np.random.default_rng(3109))
+    make_add2()
     print("golden vectors written to", HERE)
 
 
