@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_Z, M_R = 4096, 2048   # overridable with --grid for profiling runs
-PERSISTENT = 1          # FP32 kernel: persistent (bulk-tensor staging) or one CTA per tile
+PERSISTENT = 1          # FP32 kernel: 1 persistent tile kernel (bulk-tensor staging), 0 one CTA per tile, 2 strips
 BYTES_PER_CELL = {"fp64": 64, "fp32": 32}   # one read + one write of 4 state values
 REF_BUDGET_S = 150.0    # reference arm: seconds of timed host work
 # DRAM bytes (read + write) per launch of the FP32 persistent kernel at
@@ -704,9 +704,11 @@ def main():
                     help="whole runs from t = 0 of this many steps: rates and FP32 error vs FP64 (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=1000, help="steps of the 64-problem batch (0: skip)")
     ap.add_argument("--per-tile", action="store_true", help="FP32 forms with one CTA per tile, not the persistent kernel")
+    ap.add_argument("--fp32-kernel", type=int, default=1, choices=[0, 1, 2],
+                    help="FP32 step kernel: 1 persistent tile kernel, 0 one CTA per tile, 2 strip kernel")
     args = ap.parse_args()
     global N_Z, M_R, PERSISTENT
-    PERSISTENT = 0 if args.per_tile else 1
+    PERSISTENT = 0 if args.per_tile else args.fp32_kernel
     if args.grid:
         N_Z, M_R = (int(v) for v in args.grid.lower().split("x"))
     ws, rank, local = dist_setup()
@@ -798,7 +800,7 @@ def main():
     hbm, src = peaks()
     prec = "fp64" if args.form.startswith("fp64") else "fp32"
     achieved = BYTES_PER_CELL[prec] * cells / (sec / args.steps) / 1e9
-    traffic = MEASURED_TRAFFIC.get(args.form) if (N_Z, M_R) == (4096, 2048) and PERSISTENT else None
+    traffic = MEASURED_TRAFFIC.get(args.form) if (N_Z, M_R) == (4096, 2048) and PERSISTENT == 1 else None
     line = {
         "metric": METRIC,
         "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -806,7 +808,7 @@ def main():
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
         "config": shared_config(args),
         "form": args.form, "parallelism": "replicas" if ws > 1 else "single GPU",
-        "fp32_kernel": "persistent, bulk-tensor staged" if PERSISTENT else "one CTA per tile",
+        "fp32_kernel": {0: "one CTA per tile", 1: "persistent, bulk-tensor staged", 2: "strips swept by warps"}[PERSISTENT],
         "mlp_params": params_src,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": src, "traffic": traffic,
