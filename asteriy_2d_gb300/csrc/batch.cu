@@ -46,6 +46,7 @@ struct BatchClass {
     int ts_off[kNumSchedules];    // offset of its count+1 prefix sums in the tile_start array
     float ms[kNumSchedules];      // autotuner: ms per step per schedule (0: not timed)
     int grid;                     // persistent kernel: CTAs
+    int work0;                    // persistent kernel: its first entry of the batch's work list
 };
 
 #define BATCH_CUDA(call)                                    \
@@ -88,7 +89,11 @@ struct ast_batch {
     DevClock* clock_save = nullptr;     // autotuner: clocks saved around the trials
     int schedules = kNumShapes;         // schedules built for this precision
     CUtensorMap* maps = nullptr;        // FP32: per parity, load maps then store maps, slot order
-    unsigned int* counters = nullptr;   // FP32: per class, the persistent kernel's tile counter
+    unsigned int* counters = nullptr;   // FP32: per class, then for the one-launch kernel, the persistent
+                                        // kernel's two counters (claims, CTAs that left)
+    int4* work = nullptr;               // FP32: the persistent kernels' work list (every slot's 32x16 tiles,
+                                        // slot order: {slot | FLUX << 24, n0, m0, tiles of the slot})
+    int wait_polls = 0;                 // FP32: the shortest configured copy wait of the batch
     // FP32, per-problem schedule (slot order): host copies of the maps and
     // of each parity's parameters, CTAs, streams and join events
     std::vector<CUtensorMap> hmaps;
@@ -100,11 +105,12 @@ struct ast_batch {
     // FP32, one reconstruction: every problem in one launch of the mixed
     // kernel (32x16 tiles, slot order)
     bool mix_ok = false;
-    int mixed = 0;                      // 1: steps are mixed launches
+    int mixed = 0;                      // 1: steps are mixed launches, 2: persistent mixed launches
+    int mix_grid = 0;                   // the persistent mixed kernel's CTAs
     int* mix_start = nullptr;           // prefix sums of the problems' tiles (nprob + 1), then
                                         // per slot the kernels' FLUX (nprob)
     int mix_tiles = 0, mix_recon = 0;
-    float ms_mixed = 0.0f, ms_split = 0.0f;   // autotuner: ms per step, one launch / per class
+    float ms_mixed = 0.0f, ms_split = 0.0f;   // autotuner: ms per step, one launch (the faster mode) / per class
 };
 
 namespace {
@@ -176,22 +182,23 @@ int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool l
         return AST_OK;
     }
     if (shape == kPersistent) {
+        // the class's run of the batch's work list; parameters and maps
+        // indexed by slot
         const int ci = (int)(&c - B->cls.data());
-        const CUtensorMap* tin = B->maps + (size_t)(2 * B->cur) * B->nprob + c.first;
-        const CUtensorMap* tout = B->maps + (size_t)(2 * B->cur + 1) * B->nprob + c.first;
+        const CUtensorMap* tin = B->maps + (size_t)(2 * B->cur) * B->nprob;
+        const CUtensorMap* tout = B->maps + (size_t)(2 * B->cur + 1) * B->nprob;
         if (!launch) {
             int per_sm = 0, dev = 0, sms = 0;
-            int rc = launch_batch_tma(Ps, tin, tout, ts, c.count, B->counters + ci, c.flux, c.recon, 0, st, false,
-                                      &per_sm);
+            int rc = launch_batch_tma(nullptr, nullptr, nullptr, nullptr, 0, nullptr, 0, c.flux, c.recon, 0, st,
+                                      false, &per_sm);
             if (rc != AST_OK) return rc;
             BATCH_CUDA(cudaGetDevice(&dev));
             BATCH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
             c.grid = std::min(c.tiles[shape], std::max(per_sm, 1) * sms);
             return AST_OK;
         }
-        BATCH_CUDA(cudaMemsetAsync(B->counters + ci, 0, sizeof(unsigned int), st));
-        return launch_batch_tma(Ps, tin, tout, ts, c.count, B->counters + ci, c.flux, c.recon, c.grid, st, true,
-                                nullptr);
+        return launch_batch_tma(B->dP[B->cur], tin, tout, B->work + c.work0, c.tiles[shape], B->counters + 2 * ci,
+                                B->wait_polls, c.flux, c.recon, c.grid, st, true, nullptr);
     }
     return launch_batch(B->elem, shape, Ps, ts, c.count, c.tiles[shape], c.flux, c.recon, st, launch);
 }
@@ -200,6 +207,19 @@ int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool l
 // streams, forked from and joined back into `st`
 int enqueue_steps(ast_batch* B, cudaStream_t st, int count)
 {
+    if (B->mixed == 2) {
+        // the persistent one-launch kernel over every problem's tiles
+        const size_t n = (size_t)B->nprob;
+        unsigned int* counter = B->counters + 2 * B->cls.size();
+        for (int i = 0; i < count; i++) {
+            const int rc = launch_batch_tma_mixed(B->dP[B->cur], B->maps + (2 * B->cur) * n,
+                                                  B->maps + (2 * B->cur + 1) * n, B->work, B->mix_tiles, counter,
+                                                  B->wait_polls, B->mix_recon, B->mix_grid, st, true, nullptr);
+            if (rc != AST_OK) return rc;
+            B->cur ^= 1;
+        }
+        return AST_OK;
+    }
     if (B->mixed) {
         for (int i = 0; i < count; i++) {
             const int rc = launch_batch_mixed(B->dP[B->cur], B->mix_start, B->mix_start + B->nprob + 1, B->nprob,
@@ -415,6 +435,23 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
             }
         }
         B->hmaps = maps;
+        // the persistent kernels' work list: every slot's 32x16 tiles in
+        // slot order (each class a contiguous run of it)
+        std::vector<int4> work;
+        for (BatchClass& k : B->cls) {
+            k.work0 = (int)work.size();
+            for (int s = k.first; s < k.first + k.count; s++) {
+                const ast_config& c = B->cfg[order[s]];
+                const int fk = (c.flux == AST_FLUX_HLL) ? 0 : (c.flux == AST_FLUX_HLLC) ? 1
+                                                          : (c.flux == AST_FLUX_HLLC_A) ? 3 : 2;
+                const int tz = (c.N + kShapeTZ[0] - 1) / kShapeTZ[0], nt = tiles_of(c, 0);
+                for (int t = 0; t < nt; t++)
+                    work.push_back(make_int4(s | (fk << 24), (t % tz) * kShapeTZ[0], (t / tz) * kShapeTR[0], nt));
+            }
+        }
+        B->wait_polls = tma::kWaitLimit;
+        for (int i = 0; i < nprob; i++)
+            if (B->cfg[i].copy_wait_polls > 0) B->wait_polls = std::min(B->wait_polls, B->cfg[i].copy_wait_polls);
         B->pgrid.assign(nprob, 0);
         for (int s = 0; s < nprob && rc == AST_OK; s++) {
             cudaStream_t ps;
@@ -432,11 +469,15 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
         }
         if (rc == AST_OK && (e = cudaEventCreateWithFlags(&B->pfork, cudaEventDisableTiming)) != cudaSuccess)
             rc = cuda_fail(e, "batch fork event");
+        const size_t ncnt = 2 * (B->cls.size() + 1);
         if (rc == AST_OK && ((e = cudaMalloc(&B->maps, sizeof(CUtensorMap) * maps.size())) != cudaSuccess ||
-                             (e = cudaMalloc(&B->counters, sizeof(unsigned int) * B->cls.size())) != cudaSuccess ||
+                             (e = cudaMalloc(&B->counters, sizeof(unsigned int) * ncnt)) != cudaSuccess ||
+                             (e = cudaMalloc(&B->work, sizeof(int4) * work.size())) != cudaSuccess ||
                              (e = cudaMemcpy(B->maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
                                              cudaMemcpyHostToDevice)) != cudaSuccess ||
-                             (e = cudaMemset(B->counters, 0, sizeof(unsigned int) * B->cls.size())) != cudaSuccess))
+                             (e = cudaMemcpy(B->work, work.data(), sizeof(int4) * work.size(),
+                                             cudaMemcpyHostToDevice)) != cudaSuccess ||
+                             (e = cudaMemset(B->counters, 0, sizeof(unsigned int) * ncnt)) != cudaSuccess))
             rc = cuda_fail(e, "batch tensor maps");
         // the persistent kernel is the FP32 default
         for (BatchClass& k : B->cls) k.shape = kPersistent;
@@ -462,6 +503,17 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
             (e = cudaMemcpy(B->mix_start, ms.data(), sizeof(int) * ms.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
             rc = cuda_fail(e, "batch work list");
         if (rc == AST_OK) rc = launch_batch_mixed(nullptr, nullptr, nullptr, 0, 0, B->mix_recon, nullptr, false);
+        if (rc == AST_OK) {
+            // the persistent one-launch kernel: as many CTAs as fit, at most
+            // one per tile
+            int per_sm = 0, dev = 0, sms = 0;
+            rc = launch_batch_tma_mixed(nullptr, nullptr, nullptr, nullptr, 0, nullptr, 0, B->mix_recon, 0, nullptr,
+                                        false, &per_sm);
+            if (rc == AST_OK && (e = cudaGetDevice(&dev)) != cudaSuccess) rc = cuda_fail(e, "cudaGetDevice");
+            if (rc == AST_OK && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+                rc = cuda_fail(e, "cudaDeviceGetAttribute");
+            if (rc == AST_OK) B->mix_grid = std::min(B->mix_tiles, std::max(per_sm, 1) * sms);
+        }
     }
     for (size_t c = 1; c < B->cls.size() && rc == AST_OK; c++) {
         cudaStream_t s;
@@ -501,6 +553,7 @@ int ast_batch_destroy(ast_batch* B)
     cudaFree(B->clock_save);
     cudaFree(B->maps);
     cudaFree(B->counters);
+    cudaFree(B->work);
     cudaFree(B->dP[0]);
     cudaFree(B->dP[1]);
     cudaFree(B->tile_start);
@@ -703,7 +756,7 @@ int ast_batch_num_classes(ast_batch* B)
 
 int ast_batch_set_mixed(ast_batch* B, int on)
 {
-    if (!B || on < 0 || on > 1) return set_error(AST_ERR_INVALID, "bad argument");
+    if (!B || on < 0 || on > 2) return set_error(AST_ERR_INVALID, "bad argument");
     if (on && !B->mix_ok)
         return set_error(AST_ERR_UNSUPPORTED, "one launch needs FP32 problems with one reconstruction");
     B->mixed = on;
@@ -790,8 +843,8 @@ int ast_batch_autotune(ast_batch* B, int trials)
     // class, concurrent chains) against every problem in one launch
     if (rc == AST_OK && B->mix_ok) {
         const int cur0 = B->cur;
-        float ms2[2] = {0.0f, 0.0f};
-        for (int mode = 0; mode < 2 && rc == AST_OK; mode++) {
+        float ms2[3] = {0.0f, 0.0f, 0.0f};
+        for (int mode = 0; mode < 3 && rc == AST_OK; mode++) {
             B->mixed = mode;
             rc = enqueue_steps(B, B->stream, 1);   // warm-up
             B->cur = cur0;
@@ -806,8 +859,10 @@ int ast_batch_autotune(ast_batch* B, int trials)
         }
         B->cur = cur0;
         B->ms_split = ms2[0] / trials;
-        B->ms_mixed = ms2[1] / trials;
-        B->mixed = (rc == AST_OK && B->ms_mixed < B->ms_split) ? 1 : 0;
+        // the faster of the two one-launch modes against the classes' launches
+        const int one = (ms2[2] < ms2[1]) ? 2 : 1;
+        B->ms_mixed = ms2[one] / trials;
+        B->mixed = (rc == AST_OK && B->ms_mixed < B->ms_split) ? one : 0;
     }
     e = cudaMemcpyAsync(B->clocks, B->clock_save, sizeof(DevClock) * B->nprob, cudaMemcpyDeviceToDevice,
                         B->stream);

@@ -1,5 +1,5 @@
-// batch_mixed.cu - the FP32 batch kernel over problems of every flux in
-// one launch (32x16 tiles).
+// batch_mixed.cu - the FP32 batch kernels over problems of every flux in
+// one launch (32x16 tiles): a CTA per tile, and the persistent kernel.
 #include "launch.cuh"
 
 namespace ast {
@@ -29,6 +29,16 @@ int launch_batch_mixed(const StepParams* Ps, const int* tile_start, const int* f
 {
     return recon ? launch_mixed_t<true>(Ps, tile_start, flux_of, nprob, tiles, st, launch)
                  : launch_mixed_t<false>(Ps, tile_start, flux_of, nprob, tiles, st, launch);
+}
+
+int launch_batch_tma_mixed(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
+                           int total, unsigned int* counter, int wait_polls, int recon, int grid, cudaStream_t st,
+                           bool launch, int* per_sm)
+{
+    return recon ? launch_batch_tma_t<2, true, true>(Ps, tin, tout, work, total, counter, wait_polls, grid, st,
+                                                     launch, per_sm)
+                 : launch_batch_tma_t<2, false, true>(Ps, tin, tout, work, total, counter, wait_polls, grid, st,
+                                                      launch, per_sm);
 }
 
 }  // namespace ast

@@ -134,8 +134,7 @@ int launch_sweep_t(const StepParams& P, int grid, cudaStream_t st, bool launch, 
     return e == cudaSuccess ? AST_OK : cuda_fail(e, "strip kernel launch");
 }
 
-// the FP32 strip kernel of a flux and reconstruction (every flux but the
-// exact solver's); AST_ERR_UNSUPPORTED for the exact solver
+// the FP32 strip kernel of a flux and reconstruction
 int launch_step_sweep(const StepParams& P, int flux, int recon, int grid, cudaStream_t st, bool launch, int* per_sm);
 // strips of the strip kernel in tile rows [band_lo, band_hi) (all rows when
 // band_hi is 0) of an N x M grid
@@ -145,14 +144,18 @@ inline int sweep_strips(int N, int M, int band_lo, int band_hi)
     return ((N + kSW - 1) / kSW) * ((r_hi - r_lo + kSH - 1) / kSH);
 }
 
-// the persistent FP32 batch kernel of one class (maps and parameters in
-// device memory, indexed by the class's problem); launch=false as above
-template <int FLUX, bool RECON>
-int launch_batch_tma_t(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int* tile_start,
-                       int nprob, unsigned int* counter, int grid, cudaStream_t st, bool launch, int* per_sm)
+// the persistent FP32 batch kernel (one class, or MIXED: every problem)
+// over `total` work-list entries with `grid` CTAs (maps and parameters in
+// device memory, indexed by slot; counter[0..1] zero before the first
+// launch, rewound by each launch); launch=false raises its shared-memory
+// limit and returns the CTAs per SM it reaches in *per_sm
+template <int FLUX, bool RECON, bool MIXED>
+int launch_batch_tma_t(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
+                       int total, unsigned int* counter, int wait_polls, int grid, cudaStream_t st, bool launch,
+                       int* per_sm)
 {
-    auto k = batch_kernel_tma<FLUX, RECON>;
-    constexpr size_t smem = tile_smem_bytes<float, FLUX, 32, 16, 2>();
+    auto k = batch_kernel_tma<FLUX, RECON, MIXED>;
+    constexpr size_t smem = tile_smem_bytes<float, MIXED ? 2 : FLUX, 32, 16, 2>();
     cudaError_t e;
     if (!launch) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -160,14 +163,15 @@ int launch_batch_tma_t(const StepParams* Ps, const CUtensorMap* tin, const CUten
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, kThreads, smem);
         return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     }
-    k<<<grid, kThreads, smem, st>>>(Ps, tin, tout, tile_start, nprob, counter);
+    if (grid <= 0 || total <= 0) return AST_OK;
+    k<<<grid, kThreads, smem, st>>>(Ps, tin, tout, work, total, counter, wait_polls);
     e = cudaGetLastError();
     return e == cudaSuccess ? AST_OK : cuda_fail(e, "persistent batch kernel launch");
 }
 
-int launch_batch_tma(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int* tile_start,
-                     int nprob, unsigned int* counter, int flux, int recon, int grid, cudaStream_t st, bool launch,
-                     int* per_sm);
+int launch_batch_tma(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
+                     int total, unsigned int* counter, int wait_polls, int flux, int recon, int grid, cudaStream_t st,
+                     bool launch, int* per_sm);
 
 template <typename R, int LAYOUT>
 int launch_step_r(const StepParams& P, int flux, int recon, cudaStream_t st, bool launch)
@@ -255,6 +259,12 @@ inline int launch_batch(size_t elem, int shape, const StepParams* Ps, const int*
 // shared-memory limit
 int launch_batch_mixed(const StepParams* Ps, const int* tile_start, const int* flux_of, int nprob, int tiles,
                        int recon, cudaStream_t st, bool launch);
+
+// the one-launch persistent FP32 batch kernel (every problem, one
+// reconstruction), as launch_batch_tma
+int launch_batch_tma_mixed(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
+                           int total, unsigned int* counter, int wait_polls, int recon, int grid, cudaStream_t st,
+                           bool launch, int* per_sm);
 
 // kernel parameters of a configuration (grid spacing, constants, boundaries)
 inline void fill_step_params(StepParams& P, const ast_config& c)

@@ -608,7 +608,13 @@ __device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<
     R F[4];
     R Sp;
     if constexpr (FLUX == 2) {
-        if (hi && L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]) {
+        if (!active) {
+            // no updated cell uses this face (both cells outside the grid or
+            // held fixed): not solved, so the solver's counters see the same
+            // faces however the tile was staged
+            F[0] = F[1] = F[2] = F[3] = R(0);
+            Sp = R(0);
+        } else if (hi && L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]) {
             // identical states: the exact solution is that state (the
             // reference reaches it through the two-rarefaction branch with
             // p* = p, u* = u_n, up to rounding), its flux the physical flux
@@ -1637,117 +1643,169 @@ __global__ void __launch_bounds__(kThreads, 4)
     cta_epilogue<R>(P, acc, P.units > 0 ? (unsigned)P.units : gridDim.x, true);
 }
 
-// The persistent FP32 kernel of one batch class: tiles of all the class's
-// problems handed out by a counter (the work list of the class, problems in
-// slot order, each problem's tiles in row-major order); each tile's box
-// arrives by a bulk-tensor copy through its problem's tensor map while the
-// CTA computes the previous tile, and leaves by a bulk-tensor store.  The
-// problem's parameters are copied to shared memory per tile; each tile
-// reports to its problem's clock (one ticket per tile; the problem's last
-// tile shifts that problem's dt).  The caller zeroes *counter before each
-// launch.
-template <int FLUX, bool RECON>
+// The persistent FP32 batch kernel: the tiles of many problems handed out by
+// one counter over a work list (`work`: per tile {slot | FLUX << 24, n0, m0,
+// tiles of the slot}; each problem's 32x16 tiles in row-major order, the
+// problems in slot order).  One class of problems (MIXED false: every tile
+// has the kernel's FLUX), or every problem of the batch in one launch (MIXED
+// true: each tile is stepped with the tile code of its own FLUX, all in the
+// exact solver's shared-memory layout).
+//
+// The copy thread claims the tile after next while the CTA computes the
+// current one, and stages the next tile's box by a bulk-tensor copy through
+// its problem's tensor map together with the problem's parameters (a bulk
+// copy of its StepParams) on the buffer's mbarrier; the step constants of a
+// tile (dt from its problem's clock) are formed by the copy thread during
+// the tile's face pass.  As in step_kernel_tma there is one barrier between
+// two tiles (the copy's arrival), and the previous tile's cells leave by a
+// bulk-tensor store issued after it.  The wave-speed maxima and counters of
+// consecutive tiles of one problem are reported together (one report of
+// `held` tickets when the next tile is another problem's), so the block
+// reduction runs once per run of tiles, not once per tile; the problem's
+// last ticket shifts its dt.  The last CTA to leave rewinds the counter
+// (counter[0] the claims, counter[1] the CTAs that left), so launches follow
+// one another with no reset between them.  Copies wait at most `wait_polls`
+// polls (the batch's shortest configured wait), then report AST_ST_TIMEOUT
+// to the problem and wait with the long limit.
+template <int FLUX, bool RECON, bool MIXED>
 __global__ void __launch_bounds__(kThreads, 4)
     batch_kernel_tma(const StepParams* __restrict__ Ps, const CUtensorMap* __restrict__ tin,
-                     const CUtensorMap* __restrict__ tout, const int* __restrict__ tile_start, int nprob,
-                     unsigned int* counter)
+                     const CUtensorMap* __restrict__ tout, const int4* __restrict__ work, int total,
+                     unsigned int* counter, int wait_polls)
 {
     using R = float;
     constexpr int TZ = 32, TR = 16;
-    using S = TileSmem<R, FLUX, TZ, TR, 2>;
+    using S = TileSmem<R, MIXED ? 2 : FLUX, TZ, TR, 2>;
     constexpr uint32_t kBoxBytes = 4u * S::HR * S::HZP * sizeof(R);
+    constexpr uint32_t kParBytes = sizeof(StepParams);
+    static_assert(kParBytes % 16 == 0, "StepParams is copied in 16-byte units");
     S& sm = tile_smem<S>();
-    __shared__ __align__(16) StepParams sP;
+    __shared__ __align__(16) StepParams sP[2];
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ int s_tile[2], s_prob[2];
-    __shared__ int2 s_org[2];
-    __shared__ StepConsts sK;
+    __shared__ int s_tile[2];
+    __shared__ int4 s_work[2];
+    __shared__ int4 s_pend;
+    __shared__ StepConsts sK[2];
     const int tid = threadIdx.x;
-    const int total = tile_start[nprob];
-    // problem j of work-list entry t and the tile's origin (x0, y0)
-    auto locate = [&](int t, int& j, int& x0, int& y0) {
-        int lo = 0, hi = nprob - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (tile_start[mid] <= t) lo = mid; else hi = mid - 1;
-        }
-        j = lo;
-        const int tl = t - tile_start[j];
-        const int tz = (Ps[j].N + TZ - 1) / TZ;
-        x0 = (tl % tz) * TZ;
-        y0 = (tl / tz) * TR;
+    const bool copier = tid == kCopyThread;
+    // the box and the parameters of work entry w into buffer bb
+    auto issue = [&](int bb, const int4 w) {
+        const int jn = w.x & 0xffffff;
+        tma::mbar_expect(&bar[bb], kBoxBytes + kParBytes);
+        tma::load_3d(&tin[jn], &sm.qb[bb][0][0][0], &bar[bb], w.y - 4, w.z - 2, 0);
+        tma::load_bulk(&sP[bb], Ps + jn, kParBytes, &bar[bb]);
     };
-    if (tid == 0) {
+    if (copier) {
         tma::mbar_init(&bar[0], 1);
         tma::mbar_init(&bar[1], 1);
         tma::fence_async_shared();
+        sm.qn = 0u;
+        s_pend = make_int4(-1, 0, 0, 0);
         const int t0 = (int)atomicAdd(counter, 1u);
         s_tile[0] = t0;
         if (t0 < total) {
-            int j, x0, y0;
-            locate(t0, j, x0, y0);
-            s_prob[0] = j;
-            s_org[0] = make_int2(x0, y0);
-            tma::mbar_expect(&bar[0], kBoxBytes);
-            tma::load_3d(&tin[j], &sm.qb[0][0][0][0], &bar[0], x0 - 4, y0 - 2, 0);
+            const int4 w = work[t0];
+            s_work[0] = w;
+            issue(0, w);
+        }
+        s_tile[1] = (t0 < total) ? (int)atomicAdd(counter, 1u) : total;
+    }
+    __syncthreads();
+    TileAcc<R> acc;
+    acc.clear();
+    unsigned held = 0u;   // tiles in acc (all of one problem, the one of buffer hb)
+    int hb = 0;
+    for (int k = 0;; k++) {
+        const int b = k & 1;
+        if (s_tile[b] >= total) break;
+        const int4 w = s_work[b];
+        const int j = w.x & 0xffffff, n0 = w.y, m0 = w.z;
+        // the one barrier between two tiles: every thread has finished the
+        // previous tile (its update, its reads of this buffer's slots) and
+        // fenced its shared-memory writes for the bulk copies
+        bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1), wait_polls);
+        if (__syncthreads_or(!arrived)) {
+            // reported (from global memory: the parameters come with the
+            // copy), then waited for with the long limit and computed; the
+            // next tile's copy is not issued yet, so a copy that does not
+            // arrive even then ends this CTA's tiles with none in flight
+            if (copier) atomicOr(&Ps[j].clock->status, AST_ST_TIMEOUT);
+            arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
+            if (__syncthreads_or(!arrived)) break;
+        }
+        const StepParams& P = sP[b];
+        if (n0 - 2 < 0 || n0 + TZ + 2 > P.N || m0 - 2 < 0 || m0 + TR + 2 > P.M || P.fixed_region) {
+            patch_tile<R, TZ, TR>(P, sm, b, n0, m0);
+            __syncthreads();
+        }
+        if (copier) {
+            // the previous tile's cells (sm.out is not written again before
+            // the store has read it: see tile_body)
+            const int4 pend = s_pend;
+            if (pend.x >= 0) {
+                tma::store_3d(&tout[pend.x], &sm.out[0][0][0], pend.y, pend.z, 0);
+                tma::store_commit();
+            }
+            s_pend = make_int4(j, n0, m0, 0);
+            // the next tile's box and parameters into the other buffer (last
+            // read by the previous tile), then the claim of the tile after
+            // it into this buffer's slot (every thread has read it)
+            const int tn = s_tile[b ^ 1];
+            int tnn = total;
+            if (tn < total) {
+                const int4 wn = work[tn];
+                s_work[b ^ 1] = wn;
+                issue(b ^ 1, wn);
+                tnn = (int)atomicAdd(counter, 1u);
+            }
+            s_tile[b] = tnn;
+            // this tile's step constants (read after the face pass's barrier)
+            step_consts(P, sK[b]);
+        }
+        if constexpr (MIXED) {
+            switch (w.x >> 24) {
+            case 0: tile_body<R, 0, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
+            case 1: tile_body<R, 1, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
+            case 3: tile_body<R, 3, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
+            default: tile_body<R, 2, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
+            }
+        } else {
+            tile_body<R, FLUX, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc);
+        }
+        // this thread's shared-memory writes before the bulk copies that
+        // read or overwrite them (ordered by the next barrier)
+        tma::fence_async_shared();
+        held++;
+        hb = b;
+        // the next tile's problem: s_tile[b ^ 1] was written before the
+        // previous barrier, s_work[b ^ 1] before this tile's face-pass
+        // barrier, so every thread takes the same branch
+        const int tn = s_tile[b ^ 1];
+        if (tn >= total || (s_work[b ^ 1].x & 0xffffff) != j) {
+            cta_epilogue<R>(P, acc, (unsigned)w.w, false, held);
+            acc.clear();
+            held = 0u;
         }
     }
-    TileAcc<R> acc;
-    for (int k = 0;; k++) {
-        // the previous tile is done with sP, the buffers and s_tile / s_prob
-        __syncthreads();
-        const int b = k & 1;
-        const int t = s_tile[b];
-        if (t >= total) break;
-        const int j = s_prob[b];
-        for (int w = tid; w < (int)(sizeof(StepParams) / 16); w += kThreads)
-            reinterpret_cast<int4*>(&sP)[w] = reinterpret_cast<const int4*>(Ps + j)[w];
-        if (tid == 0) {
-            const int tn = (int)atomicAdd(counter, 1u);
-            s_tile[b ^ 1] = tn;
-            if (tn < total) {
-                int jn, x0, y0;
-                locate(tn, jn, x0, y0);
-                s_prob[b ^ 1] = jn;
-                s_org[b ^ 1] = make_int2(x0, y0);
-                tma::mbar_expect(&bar[b ^ 1], kBoxBytes);
-                tma::load_3d(&tin[jn], &sm.qb[b ^ 1][0][0][0], &bar[b ^ 1], x0 - 4, y0 - 2, 0);
-            }
-        }
-        // (the wait limit from global memory: sP is being written by other
-        // threads until the barrier below)
-        bool arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1), Ps[j].wait_polls);
-        if (__syncthreads_or(!arrived)) {
-            // reported, then waited for with the long limit and computed
-            // (as in step_kernel_tma); a copy that does not arrive even then
-            // ends this CTA's tiles after the next tile's copy, already
-            // issued, has been waited for (long limit)
-            if (tid == 0) atomicOr(&sP.clock->status, AST_ST_TIMEOUT);
-            arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
-            if (__syncthreads_or(!arrived)) {
-                if (tid == 0 && s_tile[b ^ 1] < total) tma::mbar_wait(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
-                break;
-            }
-        }
-        const int n0 = s_org[b].x, m0 = s_org[b].y;
-        patch_tile<R, TZ, TR>(sP, sm, b, n0, m0);
-        if (tid == 0) {
-            sm.qn = 0u;
-            step_consts(sP, sK);
-            tma::store_wait_read();   // the previous tile's store has read sm.out
-        }
-        __syncthreads();
-        acc.clear();
-        tile_body<R, FLUX, RECON, kSoA, TZ, TR, true>(sP, sm, b, sP.gf, n0, m0, sK, acc);
-        tma::fence_async_shared();
-        __syncthreads();
-        if (tid == 0) {
-            tma::store_3d(&tout[j], &sm.out[0][0][0], n0, m0, 0);
+    // tiles held when a copy never arrived: reported with their own
+    // problem's parameters
+    if (held) cta_epilogue<R>(sP[hb], acc, (unsigned)s_work[hb].w, false, held);
+    __syncthreads();
+    if (copier) {
+        const int4 pend = s_pend;
+        if (pend.x >= 0) {
+            tma::store_3d(&tout[pend.x], &sm.out[0][0][0], pend.y, pend.z, 0);
             tma::store_commit();
         }
-        cta_epilogue<R>(sP, acc, (unsigned)(tile_start[j + 1] - tile_start[j]), false);
+        tma::store_wait_all();
+        // every claim of this CTA is made: the last CTA to leave rewinds the
+        // counter for the next launch
+        __threadfence();
+        if (atomicAdd(counter + 1, 1u) == gridDim.x - 1) {
+            counter[0] = 0u;
+            counter[1] = 0u;
+        }
     }
-    if (tid == 0) tma::store_wait_all();
 }
 
 // Characteristic inflow at z_lo after a step (add2_bound, kernel.cu:1895-

@@ -92,6 +92,15 @@ __device__ __forceinline__ void load_3d(const CUtensorMap* map, void* dst, uint6
         : "memory");
 }
 
+// `bytes` contiguous bytes from global memory into shared memory,
+// completing on bar (both addresses 16-byte aligned, bytes a multiple of 16)
+__device__ __forceinline__ void load_bulk(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 // shared-memory box to the tensor at (x, y, z); parts outside the tensor
 // are not written
 __device__ __forceinline__ void store_3d(const CUtensorMap* map, const void* src, int x, int y, int z)

@@ -537,17 +537,20 @@ class Batch:
         check(self.lib.ast_batch_autotune(self.h, trials), "ast_batch_autotune")
         return self.classes()
 
-    def set_mixed(self, on):
-        """One launch per step for the whole batch (ast_batch_set_mixed)."""
-        check(self.lib.ast_batch_set_mixed(self.h, int(on)), "ast_batch_set_mixed")
+    def set_mixed(self, mode):
+        """One launch per step for the whole batch (ast_batch_set_mixed):
+        0 one launch per class, 1 (or True) a CTA per tile, 2 the persistent
+        kernel."""
+        check(self.lib.ast_batch_set_mixed(self.h, int(mode)), "ast_batch_set_mixed")
 
     def mixed(self):
-        """(one-launch mode on, tuner ms per step one launch, per class)."""
+        """(one-launch mode: 0 off, 1 CTA per tile, 2 persistent; tuner ms per
+        step of the faster one-launch mode; of the per-class launches)."""
         on = C.c_int()
         a = np.zeros(1, dtype=np.float32)
         b = np.zeros(1, dtype=np.float32)
         check(self.lib.ast_batch_get_mixed(self.h, C.byref(on), _fptr(a), _fptr(b)), "ast_batch_get_mixed")
-        return bool(on.value), float(a[0]), float(b[0])
+        return int(on.value), float(a[0]), float(b[0])
 
     def set_tiles(self, cls, tile_z, tile_r):
         check(self.lib.ast_batch_set_tiles(self.h, cls, tile_z, tile_r), "ast_batch_set_tiles")

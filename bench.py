@@ -453,13 +453,28 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
         B.step(warmup)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        # events between windows of whole 16-step graph blocks: the step's
+        # cost as the run goes on (the tuner sees only the initial states)
+        win = 16 * max(1, steps // 160)
+        marks = []
         torch.cuda.synchronize()
         e0.record(stream)
-        B.step(steps, sync=False)
+        done = 0
+        while done < steps:
+            k = min(win, steps - done)
+            B.step(k, sync=False)
+            done += k
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(stream)
+            marks.append((done, ev))
         e1.record(stream)
         B.synchronize()
         torch.cuda.synchronize()
         sec = e0.elapsed_time(e1) / 1e3
+        windows, prev, prev_ev = [], 0, e0
+        for d, ev in marks:
+            windows.append([prev, d, round(prev_ev.elapsed_time(ev) / (d - prev), 4)])
+            prev, prev_ev = d, ev
         fp32 = [B.get_state(i)[0] for i in range(nprob)]
     # unbatched: one solver per problem, stepped in turn on one stream
     solos = []
@@ -502,11 +517,15 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
                      "schedule": solver.SCHEDULES[c["schedule"]], "tile": "%dx%d" % c["tile"],
                      "tuner_ms": {name: round(m, 4) for name, m in zip(solver.SCHEDULES, c["ms_per_schedule"])}}
                     for c in classes],
-        "one_launch": {"in_use": one_launch[0], "tuner_ms": round(one_launch[1], 4),
+        "one_launch": {"in_use": ["no", "a CTA per tile", "persistent"][one_launch[0]],
+                       "tuner_ms": round(one_launch[1], 4),
                        "tuner_ms_per_class_launches": round(one_launch[2], 4),
-                       "note": "every problem in one launch of the mixed kernel (32x16 tiles, each CTA the tile "
-                               "code of its problem's flux) against one launch per class; the tuner keeps the "
-                               "faster"},
+                       "note": "every problem in one launch (32x16 tiles, each tile the code of its problem's "
+                               "flux), a CTA per tile or the persistent kernel, against one launch per class; "
+                               "tuner_ms is the faster one-launch mode's; the tuner keeps the fastest"},
+        "ms_per_step_by_window": {"windows": windows,
+                                  "note": "[first step, end step, ms per step] of the timed run, counted from "
+                                          "the end of the warm-up; the tuner timed the initial states"},
         "mix": {k: kinds.count(k) for k in sorted(set(kinds))},
         "solo_value": cells * solo_steps / solo_sec, "solo_steps": solo_steps,
         "l1_rho_vs_fp64": {"median": float(np.median(l1)), "max": float(l1.max()),

@@ -437,15 +437,19 @@ int ast_batch_class(ast_batch* batch, int cls, int* flux, int* recon, int* nprob
 int ast_batch_set_schedule(ast_batch* batch, int cls, int schedule);
 int ast_batch_set_tiles(ast_batch* batch, int cls, int tile_z, int tile_r);
 /* One launch per step for the whole batch (FP32 batches whose problems
- * share one reconstruction): every problem's 32x16 tiles in one work list,
- * each CTA running the tile code of its problem's flux, instead of one
- * launch per class.  The results are those of schedule 0 for every class,
- * bit for bit.  ast_batch_autotune, after the per-class schedules, times a
- * whole step both ways (the classes' schedules as concurrent chains, and
- * the one launch) and keeps the faster; ast_batch_get_mixed reports the
- * mode in use and those two times (ms per step, 0 when not timed).
- * ast_batch_set_mixed(batch, 1) on a batch that cannot run this way is
- * AST_ERR_UNSUPPORTED. */
+ * share one reconstruction): every problem's 32x16 tiles in one work list
+ * (slot order: the exact solver's problems first, larger problems first),
+ * each tile stepped with the tile code of its problem's flux, instead of
+ * one launch per class.  on = 1: a CTA per tile; on = 2: the persistent
+ * kernel (as many CTAs as fit take tiles from one counter, each tile staged
+ * by a bulk-tensor copy through its problem's tensor map while the previous
+ * tile computes); 0: one launch per class.  The results are those of
+ * schedule 0 for every class, bit for bit.  ast_batch_autotune, after the
+ * per-class schedules, times a whole step all three ways and keeps the
+ * fastest; ast_batch_get_mixed reports the mode in use, the faster
+ * one-launch mode's time and the per-class launches' (ms per step, 0 when
+ * not timed).  ast_batch_set_mixed(batch, 1 or 2) on a batch that cannot
+ * run this way is AST_ERR_UNSUPPORTED. */
 int ast_batch_set_mixed(ast_batch* batch, int on);
 int ast_batch_get_mixed(ast_batch* batch, int* on, float* ms_mixed, float* ms_split);
 

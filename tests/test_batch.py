@@ -271,8 +271,10 @@ def test_autotune_leaves_the_run_unchanged():
 
 @pytest.mark.gpu
 def test_one_launch_mode():
-    """Every problem in one launch (the mixed kernel: each CTA the tile code
-    of its problem's flux) steps as schedule 0 of every class does."""
+    """Every problem in one launch, with a CTA per tile (mode 1) and with the
+    persistent kernel (mode 2; tiles from one counter, staged by bulk-tensor
+    copies): each tile stepped by the tile code of its problem's flux, as
+    schedule 0 of every class steps it, bit for bit."""
     probs = small_set(A.PREC_FP32, n=7)
     probs[0].cfg.N, probs[0].cfg.M = 150, 70
     probs[1].cfg.N, probs[1].cfg.M = 33, 17
@@ -281,11 +283,11 @@ def test_one_launch_mode():
     cfgs = [p.cfg for p in probs]
     init = [solver.problem_fill(p) for p in probs]
     states = []
-    for mixed in (True, False):
+    for mode in (1, 2, 0):
         with solver.Batch(cfgs) as B:
-            if mixed:
-                B.set_mixed(True)
-                assert B.info()["launches_per_step"] == 1 and B.mixed()[0]
+            if mode:
+                B.set_mixed(mode)
+                assert B.info()["launches_per_step"] == 1 and B.mixed()[0] == mode
             else:
                 for k in range(B.info()["launches_per_step"]):
                     B.set_schedule(k, 0)
@@ -293,21 +295,22 @@ def test_one_launch_mode():
                 B.set_state(i, s0, u0)
             B.step(21)
             states.append([(B.get_state(i), B.clock(i)) for i in range(len(cfgs))])
-    bitwise = True
-    for i in range(len(cfgs)):
-        (s, u), clk = states[0][i]
-        (rs, ru), rclk = states[1][i]
-        assert_agree(A.PREC_FP32, (s, u), (rs, ru), clk, rclk, i)
-        bitwise = bitwise and np.array_equal(s, rs) and np.array_equal(u, ru) and clk == rclk
-    # the same tile code for each flux as schedule 0's kernels
-    assert bitwise
+    for run in states[:2]:
+        bitwise = True
+        for i in range(len(cfgs)):
+            (s, u), clk = run[i]
+            (rs, ru), rclk = states[2][i]
+            assert_agree(A.PREC_FP32, (s, u), (rs, ru), clk, rclk, i)
+            bitwise = bitwise and np.array_equal(s, rs) and np.array_equal(u, ru) and clk == rclk
+        # the same tile code for each flux as schedule 0's kernels
+        assert bitwise
     # the tuner times both ways and keeps the faster
     with solver.Batch(cfgs) as B:
         for i, (s0, u0) in enumerate(init):
             B.set_state(i, s0, u0)
         B.autotune(2)
         on, ms_mixed, ms_split = B.mixed()
-        assert ms_mixed > 0 and ms_split > 0 and on == (ms_mixed < ms_split)
+        assert ms_mixed > 0 and ms_split > 0 and bool(on) == (ms_mixed < ms_split)
         assert B.info()["launches_per_step"] == (1 if on else B.lib.ast_batch_num_classes(B.h))
     # FP64 batches, and problems of different reconstructions, keep one
     # launch per class
@@ -340,11 +343,11 @@ def test_one_launch_mode_with_learned_guess():
     assert any(c.guess == A.GUESS_MLP for c in cfgs) and any(c.flux == A.FLUX_HLLC for c in cfgs)
     init = [solver.problem_fill(p) for p in probs]
     out = []
-    for mixed in (True, False):
+    for mode in (1, 2, 0):
         with solver.Batch(cfgs) as B:
             B.set_mlp(params)
-            if mixed:
-                B.set_mixed(True)
+            if mode:
+                B.set_mixed(mode)
             else:
                 for k in range(B.lib.ast_batch_num_classes(B.h)):
                     B.set_schedule(k, 0)
@@ -352,7 +355,8 @@ def test_one_launch_mode_with_learned_guess():
                 B.set_state(i, s0, u0)
             B.step(18)
             out.append([(B.get_state(i), B.clock(i), B.stats(i)) for i in range(len(cfgs))])
-    for i in range(len(cfgs)):
-        (s, u), clk, st = out[0][i]
-        (rs, ru), rclk, rst = out[1][i]
-        assert np.array_equal(s, rs) and np.array_equal(u, ru) and clk == rclk and st == rst, i
+    for run in out[:2]:
+        for i in range(len(cfgs)):
+            (s, u), clk, st = run[i]
+            (rs, ru), rclk, rst = out[2][i]
+            assert np.array_equal(s, rs) and np.array_equal(u, ru) and clk == rclk and st == rst, i

@@ -190,7 +190,10 @@ def test_copy_wait_timeout_reported_and_result_unchanged(flux):
     assert np.array_equal(again[0], ref[0])
 
 
-def test_batch_copy_wait_timeout_reported_and_result_unchanged():
+@pytest.mark.parametrize("one_launch", [False, True])
+def test_batch_copy_wait_timeout_reported_and_result_unchanged(one_launch):
+    """The persistent batch kernel, per class and in one launch for the whole
+    batch: a copy wait that runs out is reported and the step completes."""
     probs = solver.problem_set(64, 6, A.PREC_FP32)
     init = [solver.problem_fill(p) for p in probs]
 
@@ -203,8 +206,11 @@ def test_batch_copy_wait_timeout_reported_and_result_unchanged():
         with solver.Batch(cfgs) as B:
             for i, (s0, u0) in enumerate(init):
                 B.set_state(i, s0, u0)
-            for cls in range(B.info()["launches_per_step"]):
-                B.set_schedule(cls, 3)   # the persistent batch kernel
+            if one_launch:
+                B.set_mixed(2)   # the persistent kernel over every problem
+            else:
+                for cls in range(B.info()["launches_per_step"]):
+                    B.set_schedule(cls, solver.PERSISTENT)
             B.step(2, sync=False)
             err = None
             try:
