@@ -43,6 +43,10 @@ def _flags(ptxas_verbose=False):
                 "-I", os.path.join(ROOT, "include"), "-I", CSRC]
     if ptxas_verbose:
         f += ["-Xptxas", "-v"]
+    # profiling build: per-phase SM cycle counters in the persistent
+    # kernels (ast_get_phase_clocks); off in the product build
+    if os.environ.get("AST_PHASE_CLOCKS", "0") == "1":
+        f += ["-DAST_PHASE_CLOCKS"]
     return f
 
 

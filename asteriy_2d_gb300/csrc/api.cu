@@ -722,6 +722,26 @@ int ast_synchronize(ast_solver* S)
     return AST_OK;
 }
 
+int ast_get_phase_clocks(ast_solver* S, uint64_t out[8], int reset)
+{
+    if (!S || !out) return fail(AST_ERR_INVALID, "null argument");
+#ifdef AST_PHASE_CLOCKS
+    DevClock c;
+    AST_CUDA(cudaMemcpyAsync(&c, S->clock, sizeof c, cudaMemcpyDeviceToHost, S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    for (int i = 0; i < 8; i++) out[i] = c.phase[i];
+    if (reset) {
+        std::memset(c.phase, 0, sizeof c.phase);
+        AST_CUDA(cudaMemcpyAsync(S->clock, &c, sizeof c, cudaMemcpyHostToDevice, S->stream));
+        AST_CUDA(cudaStreamSynchronize(S->stream));
+    }
+    return AST_OK;
+#else
+    (void)reset;
+    return fail(AST_ERR_UNSUPPORTED, "the library was built without AST_PHASE_CLOCKS");
+#endif
+}
+
 int ast_get_stats(ast_solver* S, ast_stats* out, int reset)
 {
     if (!S || !out) return fail(AST_ERR_INVALID, "null argument");

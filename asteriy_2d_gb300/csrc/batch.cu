@@ -8,7 +8,8 @@
 // array per ping-pong parity) and one tile prefix sum, and steps with one
 // launch of batch_kernel over all of its problems' tiles.  Each problem has
 // its own DevClock, so its dt reduction and funk_time shift stay its own
-// (the last of its tiles to finish performs them).
+// (the last of its tiles to finish performs them; in the persistent batch
+// kernel, the last CTA of the launch performs every problem's).
 //
 // Blocks of 16 steps are captured into one CUDA graph in which every class
 // is an independent chain of launches: classes are forked from the caller's
@@ -91,8 +92,8 @@ struct ast_batch {
     CUtensorMap* maps = nullptr;        // FP32: per parity, load maps then store maps, slot order
     unsigned int* counters = nullptr;   // FP32: per class, then for the one-launch kernel, the persistent
                                         // kernel's two counters (claims, CTAs that left)
-    int4* work = nullptr;               // FP32: the persistent kernels' work list (every slot's 32x16 tiles,
-                                        // slot order: {slot | FLUX << 24, n0, m0, tiles of the slot})
+    BatchTile* work = nullptr;          // FP32: the persistent kernels' work list (every slot's 32x16 tiles,
+                                        // slot order)
     int wait_polls = 0;                 // FP32: the shortest configured copy wait of the batch
     // FP32, per-problem schedule (slot order): host copies of the maps and
     // of each parity's parameters, CTAs, streams and join events
@@ -189,16 +190,16 @@ int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool l
         const CUtensorMap* tout = B->maps + (size_t)(2 * B->cur + 1) * B->nprob;
         if (!launch) {
             int per_sm = 0, dev = 0, sms = 0;
-            int rc = launch_batch_tma(nullptr, nullptr, nullptr, nullptr, 0, nullptr, 0, c.flux, c.recon, 0, st,
-                                      false, &per_sm);
+            int rc = launch_batch_tma(nullptr, nullptr, nullptr, nullptr, 0, 0, 0, nullptr, 0, c.flux, c.recon, 0,
+                                      st, false, &per_sm);
             if (rc != AST_OK) return rc;
             BATCH_CUDA(cudaGetDevice(&dev));
             BATCH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
             c.grid = std::min(c.tiles[shape], std::max(per_sm, 1) * sms);
             return AST_OK;
         }
-        return launch_batch_tma(B->dP[B->cur], tin, tout, B->work + c.work0, c.tiles[shape], B->counters + 2 * ci,
-                                B->wait_polls, c.flux, c.recon, c.grid, st, true, nullptr);
+        return launch_batch_tma(B->dP[B->cur], tin, tout, B->work + c.work0, c.tiles[shape], c.first, c.count,
+                                B->counters + 2 * ci, B->wait_polls, c.flux, c.recon, c.grid, st, true, nullptr);
     }
     return launch_batch(B->elem, shape, Ps, ts, c.count, c.tiles[shape], c.flux, c.recon, st, launch);
 }
@@ -213,8 +214,9 @@ int enqueue_steps(ast_batch* B, cudaStream_t st, int count)
         unsigned int* counter = B->counters + 2 * B->cls.size();
         for (int i = 0; i < count; i++) {
             const int rc = launch_batch_tma_mixed(B->dP[B->cur], B->maps + (2 * B->cur) * n,
-                                                  B->maps + (2 * B->cur + 1) * n, B->work, B->mix_tiles, counter,
-                                                  B->wait_polls, B->mix_recon, B->mix_grid, st, true, nullptr);
+                                                  B->maps + (2 * B->cur + 1) * n, B->work, B->mix_tiles, B->nprob,
+                                                  counter, B->wait_polls, B->mix_recon, B->mix_grid, st, true,
+                                                  nullptr);
             if (rc != AST_OK) return rc;
             B->cur ^= 1;
         }
@@ -437,7 +439,7 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
         B->hmaps = maps;
         // the persistent kernels' work list: every slot's 32x16 tiles in
         // slot order (each class a contiguous run of it)
-        std::vector<int4> work;
+        std::vector<BatchTile> work;
         for (BatchClass& k : B->cls) {
             k.work0 = (int)work.size();
             for (int s = k.first; s < k.first + k.count; s++) {
@@ -445,8 +447,15 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
                 const int fk = (c.flux == AST_FLUX_HLL) ? 0 : (c.flux == AST_FLUX_HLLC) ? 1
                                                           : (c.flux == AST_FLUX_HLLC_A) ? 3 : 2;
                 const int tz = (c.N + kShapeTZ[0] - 1) / kShapeTZ[0], nt = tiles_of(c, 0);
-                for (int t = 0; t < nt; t++)
-                    work.push_back(make_int4(s | (fk << 24), (t % tz) * kShapeTZ[0], (t / tz) * kShapeTR[0], nt));
+                for (int t = 0; t < nt; t++) {
+                    BatchTile e;
+                    std::memset(&e, 0, sizeof e);
+                    e.sf = s | (fk << 24);
+                    e.n0 = (t % tz) * kShapeTZ[0];
+                    e.m0 = (t / tz) * kShapeTR[0];
+                    e.clock = B->clocks + order[s];
+                    work.push_back(e);
+                }
             }
         }
         B->wait_polls = tma::kWaitLimit;
@@ -472,10 +481,10 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
         const size_t ncnt = 2 * (B->cls.size() + 1);
         if (rc == AST_OK && ((e = cudaMalloc(&B->maps, sizeof(CUtensorMap) * maps.size())) != cudaSuccess ||
                              (e = cudaMalloc(&B->counters, sizeof(unsigned int) * ncnt)) != cudaSuccess ||
-                             (e = cudaMalloc(&B->work, sizeof(int4) * work.size())) != cudaSuccess ||
+                             (e = cudaMalloc(&B->work, sizeof(BatchTile) * work.size())) != cudaSuccess ||
                              (e = cudaMemcpy(B->maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
                                              cudaMemcpyHostToDevice)) != cudaSuccess ||
-                             (e = cudaMemcpy(B->work, work.data(), sizeof(int4) * work.size(),
+                             (e = cudaMemcpy(B->work, work.data(), sizeof(BatchTile) * work.size(),
                                              cudaMemcpyHostToDevice)) != cudaSuccess ||
                              (e = cudaMemset(B->counters, 0, sizeof(unsigned int) * ncnt)) != cudaSuccess))
             rc = cuda_fail(e, "batch tensor maps");
@@ -507,8 +516,8 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
             // the persistent one-launch kernel: as many CTAs as fit, at most
             // one per tile
             int per_sm = 0, dev = 0, sms = 0;
-            rc = launch_batch_tma_mixed(nullptr, nullptr, nullptr, nullptr, 0, nullptr, 0, B->mix_recon, 0, nullptr,
-                                        false, &per_sm);
+            rc = launch_batch_tma_mixed(nullptr, nullptr, nullptr, nullptr, 0, 0, nullptr, 0, B->mix_recon, 0,
+                                        nullptr, false, &per_sm);
             if (rc == AST_OK && (e = cudaGetDevice(&dev)) != cudaSuccess) rc = cuda_fail(e, "cudaGetDevice");
             if (rc == AST_OK && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
                 rc = cuda_fail(e, "cudaDeviceGetAttribute");

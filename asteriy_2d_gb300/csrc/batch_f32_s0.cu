@@ -2,12 +2,13 @@
 #include "launch.cuh"
 
 namespace ast {
-int launch_batch_tma(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
-                     int total, unsigned int* counter, int wait_polls, int flux, int recon, int grid, cudaStream_t st,
-                     bool launch, int* per_sm)
+int launch_batch_tma(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const BatchTile* work,
+                     int total, int slot0, int nslots, unsigned int* counter, int wait_polls, int flux, int recon,
+                     int grid, cudaStream_t st, bool launch, int* per_sm)
 {
-#define AST_BTMA(F, RC) \
-    return launch_batch_tma_t<F, RC, false>(Ps, tin, tout, work, total, counter, wait_polls, grid, st, launch, per_sm)
+#define AST_BTMA(F, RC)                                                                                            \
+    return launch_batch_tma_t<F, RC, false>(Ps, tin, tout, work, total, slot0, nslots, counter, wait_polls, grid, \
+                                            st, launch, per_sm)
     if (recon) {
         if (flux == AST_FLUX_HLL) AST_BTMA(0, true);
         if (flux == AST_FLUX_HLLC) AST_BTMA(1, true);

@@ -31,14 +31,14 @@ int launch_batch_mixed(const StepParams* Ps, const int* tile_start, const int* f
                  : launch_mixed_t<false>(Ps, tile_start, flux_of, nprob, tiles, st, launch);
 }
 
-int launch_batch_tma_mixed(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
-                           int total, unsigned int* counter, int wait_polls, int recon, int grid, cudaStream_t st,
-                           bool launch, int* per_sm)
+int launch_batch_tma_mixed(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout,
+                           const BatchTile* work, int total, int nslots, unsigned int* counter, int wait_polls,
+                           int recon, int grid, cudaStream_t st, bool launch, int* per_sm)
 {
-    return recon ? launch_batch_tma_t<2, true, true>(Ps, tin, tout, work, total, counter, wait_polls, grid, st,
-                                                     launch, per_sm)
-                 : launch_batch_tma_t<2, false, true>(Ps, tin, tout, work, total, counter, wait_polls, grid, st,
-                                                      launch, per_sm);
+    return recon ? launch_batch_tma_t<2, true, true>(Ps, tin, tout, work, total, 0, nslots, counter, wait_polls,
+                                                     grid, st, launch, per_sm)
+                 : launch_batch_tma_t<2, false, true>(Ps, tin, tout, work, total, 0, nslots, counter, wait_polls,
+                                                      grid, st, launch, per_sm);
 }
 
 }  // namespace ast

@@ -145,14 +145,15 @@ inline int sweep_strips(int N, int M, int band_lo, int band_hi)
 }
 
 // the persistent FP32 batch kernel (one class, or MIXED: every problem)
-// over `total` work-list entries with `grid` CTAs (maps and parameters in
-// device memory, indexed by slot; counter[0..1] zero before the first
-// launch, rewound by each launch); launch=false raises its shared-memory
-// limit and returns the CTAs per SM it reaches in *per_sm
+// over `total` work-list entries with `grid` CTAs; its problems are the
+// slots [slot0, slot0 + nslots) (maps and parameters in device memory,
+// indexed by slot; counter[0..1] zero before the first launch, rewound by
+// each launch); launch=false raises its shared-memory limit and returns the
+// CTAs per SM it reaches in *per_sm
 template <int FLUX, bool RECON, bool MIXED>
-int launch_batch_tma_t(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
-                       int total, unsigned int* counter, int wait_polls, int grid, cudaStream_t st, bool launch,
-                       int* per_sm)
+int launch_batch_tma_t(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const BatchTile* work,
+                       int total, int slot0, int nslots, unsigned int* counter, int wait_polls, int grid,
+                       cudaStream_t st, bool launch, int* per_sm)
 {
     auto k = batch_kernel_tma<FLUX, RECON, MIXED>;
     constexpr size_t smem = tile_smem_bytes<float, MIXED ? 2 : FLUX, 32, 16, 2>();
@@ -164,14 +165,14 @@ int launch_batch_tma_t(const StepParams* Ps, const CUtensorMap* tin, const CUten
         return e == cudaSuccess ? AST_OK : cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     }
     if (grid <= 0 || total <= 0) return AST_OK;
-    k<<<grid, kThreads, smem, st>>>(Ps, tin, tout, work, total, counter, wait_polls);
+    k<<<grid, kThreads, smem, st>>>(Ps, tin, tout, work, total, slot0, nslots, counter, wait_polls);
     e = cudaGetLastError();
     return e == cudaSuccess ? AST_OK : cuda_fail(e, "persistent batch kernel launch");
 }
 
-int launch_batch_tma(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
-                     int total, unsigned int* counter, int wait_polls, int flux, int recon, int grid, cudaStream_t st,
-                     bool launch, int* per_sm);
+int launch_batch_tma(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const BatchTile* work,
+                     int total, int slot0, int nslots, unsigned int* counter, int wait_polls, int flux, int recon,
+                     int grid, cudaStream_t st, bool launch, int* per_sm);
 
 template <typename R, int LAYOUT>
 int launch_step_r(const StepParams& P, int flux, int recon, cudaStream_t st, bool launch)
@@ -262,9 +263,9 @@ int launch_batch_mixed(const StepParams* Ps, const int* tile_start, const int* f
 
 // the one-launch persistent FP32 batch kernel (every problem, one
 // reconstruction), as launch_batch_tma
-int launch_batch_tma_mixed(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout, const int4* work,
-                           int total, unsigned int* counter, int wait_polls, int recon, int grid, cudaStream_t st,
-                           bool launch, int* per_sm);
+int launch_batch_tma_mixed(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout,
+                           const BatchTile* work, int total, int nslots, unsigned int* counter, int wait_polls,
+                           int recon, int grid, cudaStream_t st, bool launch, int* per_sm);
 
 // kernel parameters of a configuration (grid spacing, constants, boundaries)
 inline void fill_step_params(StepParams& P, const ast_config& c)

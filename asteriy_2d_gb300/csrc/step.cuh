@@ -47,7 +47,44 @@ struct DevClock {
     unsigned int next_tile;        // persistent kernel: next tile to hand out
     unsigned int pad_;
     double T_prev;                 // dt the last step used
+    unsigned long long phase[8];   // builds with AST_PHASE_CLOCKS: SM cycles per phase (phase_mark)
 };
+
+// ------------------------------------------------------------------ phase clocks
+// Builds with AST_PHASE_CLOCKS only (a profiling build; otherwise every
+// mark is empty): thread 0 of each CTA of the persistent kernels adds the
+// SM cycles between consecutive marks to one counter per phase, and at the
+// CTA's end adds them to its problem's clock.  Each mark follows the
+// CTA-wide barrier that ends its phase, so a phase's cycles include the
+// wait for the CTA's slowest warp.  Phases: 0 tile arrival (the barrier
+// after the copy's arrival: the previous tile's slowest update and any copy
+// wait), 1 ghost cells, 2 face pass, 3 exact-solver queue, 4 update (thread
+// 0's own cells), 5 the final store and report; counters 6 and 7 count the
+// CTAs and the tiles.
+constexpr int kPhaseStart = -1, kPhaseFlush = -2;
+#ifdef AST_PHASE_CLOCKS
+__device__ __forceinline__ void phase_mark(int k, DevClock* C = nullptr)
+{
+    __shared__ long long s_t;
+    __shared__ unsigned long long s_acc[8];
+    if (threadIdx.x != 0) return;
+    const long long now = clock64();
+    if (k == kPhaseStart) {
+        for (int i = 0; i < 8; i++) s_acc[i] = 0ull;
+    } else if (k == kPhaseFlush) {
+        if (C != nullptr) {
+            s_acc[6] = 1ull;
+            for (int i = 0; i < 8; i++) atomicAdd(&C->phase[i], s_acc[i]);
+        }
+    } else {
+        s_acc[k] += (unsigned long long)(now - s_t);
+        if (k == 0) s_acc[7] += 1ull;
+    }
+    s_t = now;
+}
+#else
+__device__ __forceinline__ void phase_mark(int, DevClock* = nullptr) {}
+#endif
 
 enum Layout { kSoA = 0, kAoS = 1 };
 
@@ -964,13 +1001,19 @@ struct StepConsts {
     int step;
 };
 
-__device__ __forceinline__ void step_consts(const StepParams& P, StepConsts& K)
+__device__ __forceinline__ void step_consts_of(const StepParams& P, double T_do, int step, StepConsts& K)
 {
-    K.T_do = (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr;
-    K.step = (P.clock != nullptr) ? (int)P.clock->step : 0;
+    K.T_do = T_do;
+    K.step = step;
     K.tdv = K.T_do / (P.dx * P.dy);
     K.tdv_f = (float)K.tdv;
     K.T_f = (float)K.T_do;
+}
+
+__device__ __forceinline__ void step_consts(const StepParams& P, StepConsts& K)
+{
+    step_consts_of(P, (P.clock != nullptr) ? *(volatile double*)&P.clock->T_do : *P.T_do_ptr,
+                   (P.clock != nullptr) ? (int)P.clock->step : 0, K);
 }
 
 // the fixed region's exact test (FP64 divisions, as the reference evaluates
@@ -1171,9 +1214,11 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
         if (threadIdx.x == kCopyThread) tma::store_wait_read();
     }
     __syncthreads();
+    phase_mark(2);
     if constexpr (FLUX == 2) {
         queue_pass<R, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
         __syncthreads();
+        phase_mark(3);
         // persistent kernels: the next tile's queue starts empty (ordered
         // before its face pass by the barrier between the tiles)
         if constexpr (TO_SMEM) {
@@ -1307,6 +1352,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
             }
         }
     }
+    phase_mark(4);
 }
 
 // Block reduction of the CTA's accumulators and the step epilogue.  `units`
@@ -1570,6 +1616,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         }
     }
     __syncthreads();
+    phase_mark(kPhaseStart);
     TileAcc<R> acc;
     acc.clear();
     const Gas<R>& g = P.gf;
@@ -1596,12 +1643,14 @@ __global__ void __launch_bounds__(kThreads, 4)
             arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
             if (__syncthreads_or(!arrived)) break;
         }
+        phase_mark(0);
         // ghost cells (tiles at the grid's edge or near the fixed region
         // only: the others need no second barrier)
         if (n0 - 2 < 0 || n0 + TZ + 2 > P.N || m0 - 2 < 0 || m0 + TR + 2 > P.M || P.fixed_region) {
             patch_tile<R, TZ, TR>(P, sm, b, n0, m0);
             __syncthreads();
         }
+        phase_mark(1);
         if (copier) {
             // the previous tile's cells (sm.out is not written again before
             // the store has read it: see tile_body)
@@ -1641,37 +1690,110 @@ __global__ void __launch_bounds__(kThreads, 4)
         tma::store_wait_all();
     }
     cta_epilogue<R>(P, acc, P.units > 0 ? (unsigned)P.units : gridDim.x, true);
+    phase_mark(5);
+    phase_mark(kPhaseFlush, P.clock);
+}
+
+// A tile of the persistent batch kernels' work list: its problem's slot and
+// tile code (slot | FLUX << 24), origin and clock.
+struct __align__(16) BatchTile {
+    int sf;
+    int n0, m0;
+    int rsv_;
+    DevClock* clock;
+    long long rsv2_;
+};
+
+// One run of consecutive tiles of one problem, reported by every warp
+// without a barrier: the warp's wave-speed maxima (atomic maxima on the
+// clock), floor and fallback counts, status bits and solver counters.
+template <typename R>
+__device__ __forceinline__ void warp_report(const StepParams& P, const TileAcc<R>& acc)
+{
+    DevClock* C = P.clock;
+    const R a = warp_max(acc.smz), b = warp_max(acc.smr);
+    const int c0 = __reduce_add_sync(0xffffffffu, acc.nrho), c1 = __reduce_add_sync(0xffffffffu, acc.np);
+    const int c2 = __reduce_add_sync(0xffffffffu, acc.fallback);
+    unsigned st = __reduce_or_sync(0xffffffffu, acc.rc.status);
+    const RiemannCount& rc = acc.rc;
+    int n1 = 0, n2 = 0, b1 = 0, b2 = 0, s1 = 0, s2 = 0;
+    unsigned nm = 0;
+    if (P.collect_stats) {
+        n1 = __reduce_add_sync(0xffffffffu, rc.newton_calls);
+        n2 = __reduce_add_sync(0xffffffffu, rc.newton_iters);
+        b1 = __reduce_add_sync(0xffffffffu, rc.bisect_calls);
+        b2 = __reduce_add_sync(0xffffffffu, rc.bisect_iters);
+        nm = __reduce_max_sync(0xffffffffu, (unsigned)rc.newton_max);
+        s1 = __reduce_add_sync(0xffffffffu, rc.strong_calls);
+        s2 = __reduce_add_sync(0xffffffffu, rc.strong_iters);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (c0) st |= 0x01u;
+        if (c1) st |= 0x02u;
+        if (c2) st |= 0x40u;
+        const double da = (double)a, db = (double)b;
+        if (da > 0.0) atomicMax(&C->smax_z, (unsigned long long)__double_as_longlong(da));
+        if (db > 0.0) atomicMax(&C->smax_r, (unsigned long long)__double_as_longlong(db));
+        if (c0) atomicAdd(&C->cnt[0], (unsigned long long)c0);
+        if (c1) atomicAdd(&C->cnt[1], (unsigned long long)c1);
+        if (c2) atomicAdd(&C->cnt[6], (unsigned long long)c2);
+        if (st) atomicOr(&C->status, st);
+        if (n1) atomicAdd(&C->cnt[2], (unsigned long long)n1);
+        if (n2) atomicAdd(&C->cnt[3], (unsigned long long)n2);
+        if (b1) atomicAdd(&C->cnt[4], (unsigned long long)b1);
+        if (b2) atomicAdd(&C->cnt[5], (unsigned long long)b2);
+        if (nm) atomicMax(&C->cnt[7], (unsigned long long)nm);
+        if (s1) atomicAdd(&C->cnt[8], (unsigned long long)s1);
+        if (s2) atomicAdd(&C->cnt[9], (unsigned long long)s2);
+    }
+}
+
+// funk_time (kernel.cu:1525-1536) of one problem after every tile of its
+// step has reported: T_do <- min dt, TT += T_do, step + 1
+__device__ __forceinline__ void clock_shift(const StepParams& P)
+{
+    DevClock* C = P.clock;
+    const double a = __longlong_as_double((long long)atomicExch(&C->smax_z, 0ull));
+    const double b = __longlong_as_double((long long)atomicExch(&C->smax_r, 0ull));
+    double dt = P.dt_cap;
+    if (a > 0.0) dt = fmin(dt, P.krit_dx / a);
+    if (b > 0.0) dt = fmin(dt, P.krit_dy / b);
+    C->T_prev = C->T_do;
+    C->T_do = dt;
+    C->TT = C->TT + dt;
+    C->step = C->step + 1;
+    C->done = 0u;
 }
 
 // The persistent FP32 batch kernel: the tiles of many problems handed out by
-// one counter over a work list (`work`: per tile {slot | FLUX << 24, n0, m0,
-// tiles of the slot}; each problem's 32x16 tiles in row-major order, the
-// problems in slot order).  One class of problems (MIXED false: every tile
-// has the kernel's FLUX), or every problem of the batch in one launch (MIXED
-// true: each tile is stepped with the tile code of its own FLUX, all in the
-// exact solver's shared-memory layout).
+// one counter over a work list (`work`: every problem's 32x16 tiles in
+// row-major order, the problems in slot order).  One class of problems
+// (MIXED false: every tile has the kernel's FLUX), or every problem of the
+// batch in one launch (MIXED true: each tile is stepped with the tile code of
+// its own FLUX, all in the exact solver's shared-memory layout).
 //
-// The copy thread claims the tile after next while the CTA computes the
-// current one, and stages the next tile's box by a bulk-tensor copy through
+// The copy thread stages the next tile's box by a bulk-tensor copy through
 // its problem's tensor map together with the problem's parameters (a bulk
-// copy of its StepParams) on the buffer's mbarrier; the step constants of a
-// tile (dt from its problem's clock) are formed by the copy thread during
-// the tile's face pass.  As in step_kernel_tma there is one barrier between
+// copy of its StepParams) on the buffer's mbarrier, fetches that tile's dt
+// and step from its clock and the work-list entry of the tile after it
+// (asynchronous copies into shared memory) and claims that tile, all while
+// the CTA computes the current tile; each is used one tile later, so their
+// latency is hidden and no register holds them through the tile.  As in step_kernel_tma there is one barrier between
 // two tiles (the copy's arrival), and the previous tile's cells leave by a
-// bulk-tensor store issued after it.  The wave-speed maxima and counters of
-// consecutive tiles of one problem are reported together (one report of
-// `held` tickets when the next tile is another problem's), so the block
-// reduction runs once per run of tiles, not once per tile; the problem's
-// last ticket shifts its dt.  The last CTA to leave rewinds the counter
-// (counter[0] the claims, counter[1] the CTAs that left), so launches follow
-// one another with no reset between them.  Copies wait at most `wait_polls`
-// polls (the batch's shortest configured wait), then report AST_ST_TIMEOUT
-// to the problem and wait with the long limit.
+// bulk-tensor store issued after it.  Each run of consecutive tiles of one
+// problem is reported by every warp on its own (warp_report: atomic maxima
+// and counts on the problem's clock, no barrier); the last CTA to leave
+// performs the dt shift of every problem of the launch (slots [slot0,
+// slot0 + nslots)) and rewinds the counter (counter[0] the claims,
+// counter[1] the CTAs that left), so launches follow one another with no
+// reset between them.  Copies wait at most `wait_polls` polls (the batch's
+// shortest configured wait), then report AST_ST_TIMEOUT to the problem and
+// wait with the long limit.
 template <int FLUX, bool RECON, bool MIXED>
 __global__ void __launch_bounds__(kThreads, 4)
     batch_kernel_tma(const StepParams* __restrict__ Ps, const CUtensorMap* __restrict__ tin,
-                     const CUtensorMap* __restrict__ tout, const int4* __restrict__ work, int total,
-                     unsigned int* counter, int wait_polls)
+                     const CUtensorMap* __restrict__ tout, const BatchTile* __restrict__ work, int total, int slot0,
+                     int nslots, unsigned int* counter, int wait_polls)
 {
     using R = float;
     constexpr int TZ = 32, TR = 16;
@@ -1683,17 +1805,31 @@ __global__ void __launch_bounds__(kThreads, 4)
     __shared__ __align__(16) StepParams sP[2];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int s_tile[2];
-    __shared__ int4 s_work[2];
+    __shared__ int4 s_work[2];     // {slot | FLUX << 24, n0, m0, 0} of the buffer's tile
     __shared__ int4 s_pend;
     __shared__ StepConsts sK[2];
+    __shared__ int s_last;
+    // copy thread only: the entry of the next tile to be issued, and per
+    // buffer the dt and step of its tile's problem (asynchronous copies)
+    __shared__ __align__(16) BatchTile s_next;
+    __shared__ double s_tdo[2];
+    __shared__ long long s_step[2];
     const int tid = threadIdx.x;
     const bool copier = tid == kCopyThread;
-    // the box and the parameters of work entry w into buffer bb
-    auto issue = [&](int bb, const int4 w) {
-        const int jn = w.x & 0xffffff;
+    // the box and the parameters of entry w into buffer bb; its dt and step
+    auto issue = [&](int bb, const BatchTile& w) {
+        const int jn = w.sf & 0xffffff;
+        s_work[bb] = make_int4(w.sf, w.n0, w.m0, 0);
         tma::mbar_expect(&bar[bb], kBoxBytes + kParBytes);
-        tma::load_3d(&tin[jn], &sm.qb[bb][0][0][0], &bar[bb], w.y - 4, w.z - 2, 0);
+        tma::load_3d(&tin[jn], &sm.qb[bb][0][0][0], &bar[bb], w.n0 - 4, w.m0 - 2, 0);
         tma::load_bulk(&sP[bb], Ps + jn, kParBytes, &bar[bb]);
+        tma::async_copy8(&s_tdo[bb], &w.clock->T_do);
+        tma::async_copy8(&s_step[bb], &w.clock->step);
+    };
+    // the entry of work-list tile t into s_next
+    auto fetch = [&](int t) {
+        tma::async_copy16(&s_next, &work[t]);
+        tma::async_copy16(reinterpret_cast<char*>(&s_next) + 16, reinterpret_cast<const char*>(&work[t]) + 16);
     };
     if (copier) {
         tma::mbar_init(&bar[0], 1);
@@ -1703,18 +1839,21 @@ __global__ void __launch_bounds__(kThreads, 4)
         s_pend = make_int4(-1, 0, 0, 0);
         const int t0 = (int)atomicAdd(counter, 1u);
         s_tile[0] = t0;
+        int t1 = total;
         if (t0 < total) {
-            const int4 w = work[t0];
-            s_work[0] = w;
-            issue(0, w);
+            const BatchTile w0 = work[t0];
+            issue(0, w0);
+            t1 = (int)atomicAdd(counter, 1u);
+            if (t1 < total) fetch(t1);
         }
-        s_tile[1] = (t0 < total) ? (int)atomicAdd(counter, 1u) : total;
+        tma::async_commit();
+        s_tile[1] = t1;
     }
     __syncthreads();
+    phase_mark(kPhaseStart);
     TileAcc<R> acc;
     acc.clear();
-    unsigned held = 0u;   // tiles in acc (all of one problem, the one of buffer hb)
-    int hb = 0;
+    int hb = -1;   // buffer of the last tile computed while its run is not reported yet
     for (int k = 0;; k++) {
         const int b = k & 1;
         if (s_tile[b] >= total) break;
@@ -1733,12 +1872,18 @@ __global__ void __launch_bounds__(kThreads, 4)
             arrived = tma::mbar_wait(&bar[b], (uint32_t)((k >> 1) & 1));
             if (__syncthreads_or(!arrived)) break;
         }
+        phase_mark(0);
         const StepParams& P = sP[b];
         if (n0 - 2 < 0 || n0 + TZ + 2 > P.N || m0 - 2 < 0 || m0 + TR + 2 > P.M || P.fixed_region) {
             patch_tile<R, TZ, TR>(P, sm, b, n0, m0);
             __syncthreads();
         }
+        phase_mark(1);
+        int claim = total;
         if (copier) {
+            // the asynchronous copies of the previous tile: this tile's dt
+            // and step, the next tile's entry
+            tma::async_wait_all();
             // the previous tile's cells (sm.out is not written again before
             // the store has read it: see tile_body)
             const int4 pend = s_pend;
@@ -1747,20 +1892,15 @@ __global__ void __launch_bounds__(kThreads, 4)
                 tma::store_commit();
             }
             s_pend = make_int4(j, n0, m0, 0);
-            // the next tile's box and parameters into the other buffer (last
-            // read by the previous tile), then the claim of the tile after
-            // it into this buffer's slot (every thread has read it)
-            const int tn = s_tile[b ^ 1];
-            int tnn = total;
-            if (tn < total) {
-                const int4 wn = work[tn];
-                s_work[b ^ 1] = wn;
-                issue(b ^ 1, wn);
-                tnn = (int)atomicAdd(counter, 1u);
+            // the next tile's box, parameters, dt and step into the other
+            // buffer (last read by the previous tile), and the claim of the
+            // tile after it (its slot written after this tile)
+            if (s_tile[b ^ 1] < total) {
+                issue(b ^ 1, s_next);
+                claim = (int)atomicAdd(counter, 1u);
             }
-            s_tile[b] = tnn;
             // this tile's step constants (read after the face pass's barrier)
-            step_consts(P, sK[b]);
+            step_consts_of(P, s_tdo[b], (int)s_step[b], sK[b]);
         }
         if constexpr (MIXED) {
             switch (w.x >> 24) {
@@ -1775,37 +1915,53 @@ __global__ void __launch_bounds__(kThreads, 4)
         // this thread's shared-memory writes before the bulk copies that
         // read or overwrite them (ordered by the next barrier)
         tma::fence_async_shared();
-        held++;
+        if (copier) {
+            // read at the top of the iteration after next, after barriers
+            s_tile[b] = claim;
+            if (claim < total) fetch(claim);
+            tma::async_commit();
+        }
         hb = b;
-        // the next tile's problem: s_tile[b ^ 1] was written before the
-        // previous barrier, s_work[b ^ 1] before this tile's face-pass
-        // barrier, so every thread takes the same branch
-        const int tn = s_tile[b ^ 1];
-        if (tn >= total || (s_work[b ^ 1].x & 0xffffff) != j) {
-            cta_epilogue<R>(P, acc, (unsigned)w.w, false, held);
+        // the run ends when the next tile is another problem's: s_tile[b ^ 1]
+        // was written before the previous barrier, s_work[b ^ 1] before this
+        // tile's face-pass barrier, so every thread takes the same branch
+        if (s_tile[b ^ 1] >= total || (s_work[b ^ 1].x & 0xffffff) != j) {
+            warp_report<R>(P, acc);
             acc.clear();
-            held = 0u;
+            hb = -1;
+            phase_mark(5);
         }
     }
-    // tiles held when a copy never arrived: reported with their own
-    // problem's parameters
-    if (held) cta_epilogue<R>(sP[hb], acc, (unsigned)s_work[hb].w, false, held);
+    // a run left unreported when a copy never arrived
+    if (hb >= 0) warp_report<R>(sP[hb], acc);
+    phase_mark(5);
     __syncthreads();
     if (copier) {
+        // (asynchronous copies still in flight when a copy never arrived)
+        tma::async_wait_all();
         const int4 pend = s_pend;
         if (pend.x >= 0) {
             tma::store_3d(&tout[pend.x], &sm.out[0][0][0], pend.y, pend.z, 0);
             tma::store_commit();
         }
         tma::store_wait_all();
-        // every claim of this CTA is made: the last CTA to leave rewinds the
-        // counter for the next launch
+        // every claim and report of this CTA is made: the last CTA to leave
+        // shifts the problems' clocks and rewinds the counter
         __threadfence();
-        if (atomicAdd(counter + 1, 1u) == gridDim.x - 1) {
+        s_last = (atomicAdd(counter + 1, 1u) == gridDim.x - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (int p = slot0 + tid; p < slot0 + nslots; p += kThreads) clock_shift(Ps[p]);
+        if (tid == 0) {
             counter[0] = 0u;
             counter[1] = 0u;
         }
     }
+#ifdef AST_PHASE_CLOCKS
+    phase_mark(kPhaseFlush, Ps[slot0].clock);
+#endif
 }
 
 // Characteristic inflow at z_lo after a step (add2_bound, kernel.cu:1895-

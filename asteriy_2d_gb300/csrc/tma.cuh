@@ -101,6 +101,19 @@ __device__ __forceinline__ void load_bulk(void* dst, const void* src, uint32_t b
                  : "memory");
 }
 
+// asynchronous copies of 8 / 16 bytes from global to shared memory with no
+// register staging (cp.async, completed by async_wait_all in this thread)
+__device__ __forceinline__ void async_copy8(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void async_copy16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // shared-memory box to the tensor at (x, y, z); parts outside the tensor
 // are not written
 __device__ __forceinline__ void store_3d(const CUtensorMap* map, const void* src, int x, int y, int z)

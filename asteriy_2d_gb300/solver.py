@@ -37,6 +37,7 @@ SIGNATURES = {
     "ast_add_mk_raw": (C.c_int, [C.c_void_p] * 9 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "ast_synchronize": (C.c_int, [C.c_void_p]),
     "ast_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.ast_stats), C.c_int]),
+    "ast_get_phase_clocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int]),
     "ast_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
     "ast_step_raw": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_int, C.POINTER(A.ast_config), C.c_void_p]),
@@ -334,6 +335,15 @@ class Solver:
         st = A.ast_stats()
         check(self.lib.ast_get_stats(self.h, C.byref(st), int(reset)), "ast_get_stats")
         return {name: getattr(st, name) for name, _ in st._fields_ if name != "reserved"}
+
+    def phase_clocks(self, reset=False):
+        """Profiling builds (AST_PHASE_CLOCKS=1 at build time): SM cycles per
+        phase of the persistent FP32 kernel, summed over CTAs, with the CTA
+        and tile counts (ast_get_phase_clocks)."""
+        out = (C.c_uint64 * 8)()
+        check(self.lib.ast_get_phase_clocks(self.h, out, int(reset)), "ast_get_phase_clocks")
+        names = ("arrival", "ghost", "faces", "queue", "update", "report", "ctas", "tiles")
+        return dict(zip(names, (int(v) for v in out)))
 
     def set_mlp(self, params):
         params = _f32(params)

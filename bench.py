@@ -136,6 +136,10 @@ class ClockSampler:
 # Newton tolerance 1e-8 (clamped to 4 ulps of FP32)
 # (the HLL pair is the precision form of the small config's flux at full
 # size, timed for its own rate and %HBM)
+# profiling builds (--phase-clocks): per form, the persistent kernel's SM
+# cycles per phase
+PHASES = None
+
 FORMS = ("fp64_godunov", "fp32_pvrs", "fp32_learned", "fp32_learned_skip", "fp64_hll", "fp32_hll")
 
 
@@ -207,6 +211,23 @@ def learned_params(s0, u0):
     return params, "trained in this run on faces of 200 FP64 steps"
 
 
+def phase_breakdown(phases):
+    """Per form: each phase's share of the CTAs' cycles and its cycles per
+    tile, from ast_get_phase_clocks counters."""
+    out = {}
+    for form, p in phases.items():
+        names = ("arrival", "ghost", "faces", "queue", "update", "report")
+        total = sum(p[k] for k in names)
+        if not total or not p["tiles"]:
+            continue
+        out[form] = {"share": {k: round(p[k] / total, 4) for k in names},
+                     "cycles_per_tile": {k: round(p[k] / p["tiles"], 1) for k in names},
+                     "tiles": p["tiles"], "ctas": p["ctas"],
+                     "note": "thread 0 of each CTA: SM cycles between the barriers that end each phase, summed over "
+                             "CTAs, warm-up and timed steps"}
+    return out
+
+
 def time_form(form, start, steps, warmup, torch, params=None, stats_steps=0, sampler=None):
     """Device-timed steps of one form from the start state `start` = (s, u,
     (T_do, TT, step)): inputs resident in HBM, CUDA events on the solver's
@@ -236,6 +257,10 @@ def time_form(form, start, steps, warmup, torch, params=None, stats_steps=0, sam
             sampler.end()
         ms = e0.elapsed_time(e1)
         s, u = S.get_state()
+        if PHASES is not None:
+            # profiling build: this form's cycles per phase over warm-up and
+            # timed steps (the counters start at zero with the solver)
+            PHASES[form] = S.phase_clocks()
     st = None
     if stats_steps:
         # Newton statistics from a separate run with the counters on
@@ -725,8 +750,12 @@ def main():
     ap.add_argument("--per-tile", action="store_true", help="FP32 forms with one CTA per tile, not the persistent kernel")
     ap.add_argument("--fp32-kernel", type=int, default=1, choices=[0, 1, 2],
                     help="FP32 step kernel: 1 persistent tile kernel, 0 one CTA per tile, 2 strip kernel")
+    ap.add_argument("--phase-clocks", action="store_true",
+                    help="report the persistent kernel's cycles per phase (library built with AST_PHASE_CLOCKS=1)")
     args = ap.parse_args()
-    global N_Z, M_R, PERSISTENT
+    global N_Z, M_R, PERSISTENT, PHASES
+    if args.phase_clocks:
+        PHASES = {}
     PERSISTENT = 0 if args.per_tile else args.fp32_kernel
     if args.grid:
         N_Z, M_R = (int(v) for v in args.grid.lower().split("x"))
@@ -850,6 +879,8 @@ def main():
     }
     if rank == 0 and not args.no_forms:
         line["configs"] = time_configs(args.warmup, torch)
+    if PHASES:
+        line["phase_clocks"] = phase_breakdown(PHASES)
     if rank == 0 and args.batch_steps:
         line["batch"] = time_batch(args.batch_steps, args.warmup, torch)
         line["gpu_launches_batch_step"] = line["batch"]["launches_per_step"]

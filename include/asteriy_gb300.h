@@ -267,6 +267,14 @@ int ast_step_host_n(ast_solver* solver, int nsteps, double* s_a, double* u_a, do
    (same terms, in FP64, at the step's total energy). */
 int ast_set_neutral(ast_solver* solver, const double* nn2, int on_device);
 int ast_get_stats(ast_solver* solver, ast_stats* out, int reset);
+/* Profiling builds only (the library compiled with AST_PHASE_CLOCKS;
+   otherwise AST_ERR_UNSUPPORTED): SM cycles the FP32 persistent kernel's
+   CTAs spent per phase of their tiles since the last reset, summed over
+   CTAs: out[0] tile arrival (the barrier after a tile's bulk copy
+   arrives), [1] ghost cells, [2] face pass, [3] exact-solver queue, [4]
+   update, [5] final store and report, [6] CTAs, [7] tiles.  reset = 1
+   zeroes the counters after reading. */
+int ast_get_phase_clocks(ast_solver* solver, uint64_t out[8], int reset);
 /* Device view of the current state: four planes rho, p, v_z, v_r of M rows
    with row pitch *ld elements of *elem_bytes bytes (8 = FP64, 4 = FP32),
    plane stride ld*M.  Valid until the next ast_step / ast_set_state. */
