@@ -452,11 +452,13 @@ def time_e2e(form, start, steps, torch, params=None, mode="chain"):
     return dt, 2 * K * 16, 2 * K * 16
 
 
-def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
+def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32, tune_at=200):
     """The batched form: the seeded set of nprob problems (ast_problem_set:
     128x64 .. 1024x512, blast or wind, HLLC or exact Godunov, gamma 5/3 or
-    1.4, Mach 1.5-6), FP32, all advanced together by ast_batch_step.  Timed
-    with CUDA events over `steps` steps after `warmup`; the same problems
+    1.4, Mach 1.5-6), FP32, all advanced together by ast_batch_step.  The
+    schedules are tuned after `tune_at` steps (the initial states are cheaper
+    than the run's: the blasts have not spread yet), then timed with CUDA
+    events over `steps` steps after `warmup`; the same problems
     stepped one solver after another (each its own graph) for solo_steps
     steps give the unbatched rate; every problem's density L1 error against
     the FP64 run of the same steps (an FP64 batch: bitwise the FP64 solo
@@ -470,9 +472,10 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
     with solver.Batch([p.cfg for p in probs], stream=stream.cuda_stream) as B:
         for i, (s0, u0) in enumerate(init):
             B.set_state(i, s0, u0)
-        # tile shape per class, timed on the initial states (the tuner
-        # leaves the state and clocks as they were)
-        classes = B.autotune(3)
+        # schedule per class and one-launch mode, timed on the states after
+        # tune_at steps (the tuner leaves the state and clocks as they were)
+        B.step(tune_at)
+        classes = B.autotune(10)
         one_launch = B.mixed()
         info = B.info()
         B.step(warmup)
@@ -527,7 +530,7 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
     with solver.Batch(cfg64) as B:
         for i, (s0, u0) in enumerate(init):
             B.set_state(i, s0, u0)
-        B.step(warmup + steps)
+        B.step(tune_at + warmup + steps)
         for i in range(nprob):
             r64 = B.get_state(i)[0][:, 0]
             l1.append(float(np.sum(np.abs(fp32[i][:, 0] - r64)) / np.sum(np.abs(r64))))
@@ -536,7 +539,8 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
              ("wind" if p.setup == A.SETUP_WIND else "blast") for p in probs]
     return {
         "value": cells * steps / sec, "unit": "cell-updates/s", "ms_per_step": sec * 1e3 / steps,
-        "steps": steps, "warmup": warmup, "problems": nprob, "seed": seed, "cells": cells,
+        "steps": steps, "warmup": warmup, "tuned_after_steps": tune_at, "problems": nprob, "seed": seed,
+        "cells": cells,
         "tiles": info["tiles"], "launches_per_step": info["launches_per_step"],
         "classes": [{"flux": ["hll", "hllc", "godunov", "hllc_a"][c["flux"]], "problems": c["problems"],
                      "schedule": solver.SCHEDULES[c["schedule"]], "tile": "%dx%d" % c["tile"],
@@ -550,7 +554,8 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32):
                                "tuner_ms is the faster one-launch mode's; the tuner keeps the fastest"},
         "ms_per_step_by_window": {"windows": windows,
                                   "note": "[first step, end step, ms per step] of the timed run, counted from "
-                                          "the end of the warm-up; the tuner timed the initial states"},
+                                          "the end of the warm-up; the tuner timed the states after "
+                                          "tuned_after_steps steps"},
         "mix": {k: kinds.count(k) for k in sorted(set(kinds))},
         "solo_value": cells * solo_steps / solo_sec, "solo_steps": solo_steps,
         "l1_rho_vs_fp64": {"median": float(np.median(l1)), "max": float(l1.max()),
