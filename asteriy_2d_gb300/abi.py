@@ -28,7 +28,7 @@ AST_ST_TIMEOUT = 0x80
 AST_MLP_NPARAM = 1325
 AST_RECORD_FLOATS = 10
 
-FLUX_HLL, FLUX_HLLC, FLUX_GODUNOV, FLUX_HLLC_A = 0, 1, 2, 3
+FLUX_HLL, FLUX_HLLC, FLUX_GODUNOV, FLUX_HLLC_A, FLUX_HLLCQ = 0, 1, 2, 3, 4
 RECON_NONE, RECON_MINMOD = 0, 1
 GEOM_PLANAR, GEOM_AXISYM = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
@@ -63,7 +63,8 @@ class ast_config(C.Structure):
         ("collect_stats", C.c_int32), ("riemann_newton", C.c_int32), ("persistent", C.c_int32),
         ("skip_uniform", C.c_int32), ("copy_wait_polls", C.c_int32), ("reserved_i", C.c_int32 * 3),
         ("mlp_gate", C.c_double), ("inflow_p", C.c_double), ("inflow_v", C.c_double),
-        ("neutral_nh", C.c_double), ("neutral_kn", C.c_double), ("reserved_d", C.c_double * 3),
+        ("neutral_nh", C.c_double), ("neutral_kn", C.c_double), ("scalar_in", C.c_double),
+        ("reserved_d", C.c_double * 2),
     ]
 
     def copy(self):

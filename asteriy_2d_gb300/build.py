@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libasteriy_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "step_f64.cu", "step_f32.cu", "step_raw.cu", "batch.cu",
            "batch_f64_s0.cu", "batch_f64_s1.cu", "batch_f64_s2.cu", "batch_f32_s0.cu", "batch_f32_s1.cu",
-           "batch_f32_s2.cu", "batch_mixed.cu", "mlp_train.cu", "noalloc.cu", "add2.cu", "host_io.cpp"]
+           "batch_f32_s2.cu", "batch_mixed.cu", "mlp_train.cu", "noalloc.cu", "add2.cu", "scalar.cu", "host_io.cpp"]
 # per-file extra flags: the FP32 form uses the fast single-precision
 # intrinsics (division, sqrt, pow); double-precision code is not affected
 EXTRA = {"step_f32.cu": ["--use_fast_math"], "batch_f32_s0.cu": ["--use_fast_math"],

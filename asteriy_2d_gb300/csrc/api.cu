@@ -122,6 +122,8 @@ struct ast_solver {
     int sweep_grid = 0;              // its CTAs (at most)
     CUtensorMap tin[2], tout[2];     // tile-box load and store maps of buf[0], buf[1]
     void* nsrc = nullptr;            // neutral-coupling source planes (nn2.x, nn2.y), or null
+    double* q[2] = {nullptr, nullptr};   // the passive scalar, per time level (N*M, row-major), or null
+    bool has_q = false;
     cudaStream_t pipe[2] = {nullptr, nullptr};   // ast_step_host: copies in, copies out
     cudaEvent_t pev[3 * 16 + 2] = {};            // its band events (created on first use)
 };
@@ -247,6 +249,8 @@ int ast_destroy(ast_solver* S)
     cudaFree(S->rec_n);
     cudaFree(S->probe_buf);
     cudaFree(S->nsrc);
+    cudaFree(S->q[0]);
+    cudaFree(S->q[1]);
     delete S;
     return AST_OK;
 }
@@ -439,6 +443,12 @@ static int enqueue_one(ast_solver* S)
     P.in = S->buf[S->cur];
     P.out = S->buf[S->cur ^ 1];
     int rc;
+    // the passive scalar first: it reads the old state and this step's dt,
+    // which the gas step's epilogue replaces
+    if (S->has_q) {
+        rc = launch_scalar(P, S->q[S->cur], S->q[S->cur ^ 1], S->cfg.flux, S->cfg.recon, S->cfg.scalar_in, S->stream);
+        if (rc != AST_OK) return rc;
+    }
     if (S->sweep)
         rc = launch_step_sweep(P, S->cfg.flux, S->cfg.recon, S->sweep_grid, S->stream, true, nullptr);
     else if (S->tma)
@@ -551,6 +561,7 @@ static int host_steps(ast_solver* S, int nsteps, double* s_a, double* u_a, doubl
     if (!S || !s_a || !u_a || !s_b || !u_b || nsteps < 0) return fail(AST_ERR_INVALID, "bad argument");
     if (S->cfg.flux == AST_FLUX_GODUNOV && S->cfg.guess == AST_GUESS_MLP && S->P.riemann_newton && !S->mlp)
         return fail(AST_ERR_INVALID, "guess == MLP needs ast_set_mlp first");
+    if (S->has_q) return fail(AST_ERR_UNSUPPORTED, "the host-array steps do not carry the passive scalar");
     const int N = S->cfg.N, M = S->cfg.M;
     const size_t bytes = (size_t)N * M * 2 * sizeof(double);
     // a pair's arrays lie apart; an array of one pair is an array of the
@@ -819,6 +830,39 @@ int ast_set_neutral(ast_solver* S, const double* nn2, int on_device)
     cudaFree(tmp);
     if (e != cudaSuccess) return cuda_fail(e, "neutral source conversion");
     S->P.nsrc = S->nsrc;
+    return AST_OK;
+}
+
+int ast_set_scalar(ast_solver* S, const double* q, int on_device)
+{
+    if (!S) return fail(AST_ERR_INVALID, "null solver");
+    drop_graph(S);   // captured steps do not hold the scalar's launches
+    if (!q) {
+        S->has_q = false;
+        return AST_OK;
+    }
+    if (S->elem != 8) return fail(AST_ERR_UNSUPPORTED, "the passive scalar is carried by the FP64 solver");
+    if (S->cfg.flux != AST_FLUX_HLLC && S->cfg.flux != AST_FLUX_HLLCQ)
+        return fail(AST_ERR_UNSUPPORTED, "the passive scalar needs the HLLC or HLLCQ flux");
+    if (S->cfg.region_select) return fail(AST_ERR_UNSUPPORTED, "the passive scalar has no first-order region");
+    const size_t bytes = (size_t)S->cfg.N * S->cfg.M * sizeof(double);
+    for (int i = 0; i < 2; i++)
+        if (!S->q[i]) AST_CUDA(cudaMalloc(&S->q[i], bytes));
+    AST_CUDA(cudaMemcpyAsync(S->q[S->cur], q, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
+    S->has_q = true;
+    return AST_OK;
+}
+
+int ast_get_scalar(ast_solver* S, double* q, int on_device)
+{
+    if (!S || !q) return fail(AST_ERR_INVALID, "null argument");
+    if (!S->has_q) return fail(AST_ERR_INVALID, "no passive scalar set");
+    const size_t bytes = (size_t)S->cfg.N * S->cfg.M * sizeof(double);
+    AST_CUDA(cudaMemcpyAsync(q, S->q[S->cur], bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             S->stream));
+    AST_CUDA(cudaStreamSynchronize(S->stream));
     return AST_OK;
 }
 

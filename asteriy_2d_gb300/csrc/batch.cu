@@ -320,6 +320,8 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
             return set_error(AST_ERR_INVALID, "all problems of a batch share one precision");
         if (cfgs[i].inflow_p > 0.0)
             return set_error(AST_ERR_UNSUPPORTED, "the characteristic inflow is a single-problem option");
+        if (cfgs[i].flux == AST_FLUX_HLLCQ)
+            return set_error(AST_ERR_UNSUPPORTED, "the HLLCQ flux is a single-problem option");
     }
     ast_batch* B = new (std::nothrow) ast_batch();
     if (!B) return set_error(AST_ERR_NOMEM, "host allocation");

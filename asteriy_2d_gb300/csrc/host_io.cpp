@@ -69,7 +69,8 @@ int ast_config_check(const ast_config* c)
     if (c->M > 65535 * 16) return AST_ERR_INVALID;
     if (!(c->x_max > c->x_min) || !(c->y_max > 0.0)) return AST_ERR_INVALID;
     if (!(c->gamma > 1.0) || !(c->cfl > 0.0)) return AST_ERR_INVALID;
-    if (c->flux < AST_FLUX_HLL || c->flux > AST_FLUX_HLLC_A) return AST_ERR_INVALID;
+    if (c->flux < AST_FLUX_HLL || c->flux > AST_FLUX_HLLCQ) return AST_ERR_INVALID;
+    if (c->flux == AST_FLUX_HLLCQ && c->precision != AST_PREC_FP64) return AST_ERR_INVALID;
     if (c->recon < AST_RECON_NONE || c->recon > AST_RECON_MINMOD) return AST_ERR_INVALID;
     if (c->geom < AST_GEOM_PLANAR || c->geom > AST_GEOM_AXISYM) return AST_ERR_INVALID;
     if (c->precision < AST_PREC_FP64 || c->precision > AST_PREC_FP32) return AST_ERR_INVALID;

@@ -177,6 +177,14 @@ int launch_batch_tma(const StepParams* Ps, const CUtensorMap* tin, const CUtenso
 template <typename R, int LAYOUT>
 int launch_step_r(const StepParams& P, int flux, int recon, cudaStream_t st, bool launch)
 {
+    if (flux == AST_FLUX_HLLCQ) {
+        // HLLCQ_Korolkov_2D: FP64 only
+        if constexpr (sizeof(R) == 8)
+            return recon ? launch_step_t<R, 4, true, LAYOUT>(P, st, launch)
+                         : launch_step_t<R, 4, false, LAYOUT>(P, st, launch);
+        else
+            return set_error(AST_ERR_UNSUPPORTED, "HLLCQ is an FP64 flux");
+    }
     if (recon) {
         if (flux == AST_FLUX_HLL) return launch_step_t<R, 0, true, LAYOUT>(P, st, launch);
         if (flux == AST_FLUX_HLLC) return launch_step_t<R, 1, true, LAYOUT>(P, st, launch);
@@ -266,6 +274,11 @@ int launch_batch_mixed(const StepParams* Ps, const int* tile_start, const int* f
 int launch_batch_tma_mixed(const StepParams* Ps, const CUtensorMap* tin, const CUtensorMap* tout,
                            const BatchTile* work, int total, int nslots, unsigned int* counter, int wait_polls,
                            int recon, int grid, cudaStream_t st, bool launch, int* per_sm);
+
+// the passive scalar's step (FP64, HLLC or HLLCQ): q (time level of P.in)
+// -> q2, before the gas step of the same time level
+int launch_scalar(const StepParams& P, const double* q, double* q2, int flux, int recon, double q_fixed,
+                  cudaStream_t st);
 
 // kernel parameters of a configuration (grid spacing, constants, boundaries)
 inline void fill_step_params(StepParams& P, const ast_config& c)

@@ -276,6 +276,104 @@ __device__ __forceinline__ R flux_hllc(const Gas<R>& g, R rL, R pL, R u1, R v1, 
     return S;
 }
 
+// The passive-scalar flux of the HLLC solver above (the Q channel of
+// HLLC_2d_Korolkov_b_s, Gas_Dinamic.cu:1660-1808, metod 2, W = 0): Q is a
+// density carried by the flow, its flux Q u on the upwind side and, in a
+// star region, the side's flux corrected by S (Q* - Q) with
+// Q* = Q (S - u)/(S - SM).  The wave speeds and the contact speed are
+// flux_hllc's, formed by the same expressions, so the scalar moves with
+// that solver's mass flux.
+template <typename R>
+__device__ __forceinline__ R flux_hllc_q(const Gas<R>& g, R rL, R pL, R u1, R QL, R rR, R pR, R u2, R QR)
+{
+    R cL = sqrt(g.ga * pL / rL);
+    R cR = sqrt(g.ga * pR / rR);
+    R mxc = fmax(cL, cR);
+    R SL = fmin(u1, u2) - mxc;
+    R SR = fmax(u1, u2) + mxc;
+    if (SL >= R(0)) return QL * u1;
+    if (SR <= R(0)) return QR * u2;
+    R suR = SR - u2, suL = SL - u1;
+    R SM = (suR * rR * u2 - suL * rL * u1 - pR + pL) / (suR * rR - suL * rL);
+    if (SM >= R(0)) {
+        R inv = R(1) / (SL - SM);
+        R qs = QL * suL * inv;
+        return QL * u1 + SL * qs - SL * QL;
+    }
+    R inv = R(1) / (SR - SM);
+    R qs = QR * suR * inv;
+    return QR * u2 + SR * qs - SR * QR;
+}
+
+// ------------------------------------------------------------------ HLLC with a passive scalar (Korolkov)
+// HLLCQ_Korolkov_2D (Gas_Dinamic.cu:249-353): an HLLC solver whose wave
+// bounds are min(u_L - c_L, u_R - c_R) and max(u_L + c_L, u_R + c_R), with a
+// passive scalar Q (a density: flux Q u upwind, Q rr/rho in a star region),
+// in the face frame (normal un, tangential ut; each side's kinetic energy
+// from its own components).  The tangential flux is odd in ut, so one
+// evaluation serves z faces (tangent +v_r) and r faces (the reference's
+// tangent there is -v_z, its flux rotated back by the same sign).  F = (mass,
+// normal momentum, tangential momentum, energy), FQ the scalar's flux;
+// returns max(|S_L|, |S_R|), whose dt candidate the reference forms as
+// krit*rad/that.  Expression order as the reference's.
+template <typename R>
+__device__ __forceinline__ R flux_hllcq(const Gas<R>& g, R ro1, R p1, R u_L, R v_L, R Q_L, R ro2, R p2, R u_R, R v_R,
+                                        R Q_R, R F[4], R& FQ)
+{
+    const R cL = sqrt(g.ga * p1 / ro1);
+    const R cR = sqrt(g.ga * p2 / ro2);
+    const R SL = fmin((u_L - cL), (u_R - cR));
+    const R SR = fmax((u_L + cL), (u_R + cR));
+    const R UU = fmax(fabs(SL), fabs(SR));
+    const R FL1 = ro1 * u_L * u_L + p1;
+    const R FL2 = ro1 * u_L * v_L;
+    const R FR1 = ro2 * u_R * u_R + p2;
+    const R FR2 = ro2 * u_R * v_R;
+    if (SL >= R(0)) {
+        FQ = Q_L * u_L;
+        F[0] = ro1 * u_L;
+        F[3] = (g.ga * p1 / (g.g1) + R(0.5) * ro1 * (u_L * u_L + v_L * v_L)) * u_L;
+        F[1] = FL1;
+        F[2] = FL2;
+        return UU;
+    }
+    if (SR <= R(0)) {
+        FQ = Q_R * u_R;
+        F[0] = ro2 * u_R;
+        F[3] = (g.ga * p2 / (g.g1) + R(0.5) * ro2 * (u_R * u_R + v_R * v_R)) * u_R;
+        F[1] = FR1;
+        F[2] = FR2;
+        return UU;
+    }
+    const R SM = ((SR - u_R) * ro2 * u_R - (SL - u_L) * ro1 * u_L - p2 + p1) / ((SR - u_R) * ro2 - (SL - u_L) * ro1);
+    const R pp = p1 + ro1 * (SL - u_L) * (SM - u_L);
+    if (SM <= R(0)) {
+        const R rr = ro2 * (SR - u_R) / (SR - SM);
+        const R e = p2 / g.g1 + R(0.5) * ro2 * (u_R * u_R + v_R * v_R);
+        const R ee = ((SR - u_R) * e - p2 * u_R + pp * SM) / (SR - SM);
+        FQ = SR * (rr * Q_R / ro2 - Q_R) + Q_R * u_R;
+        F[0] = SR * (rr - ro2) + ro2 * u_R;
+        F[3] = SR * (ee - e) + (g.ga * p2 / (g.g1) + R(0.5) * ro2 * (u_R * u_R + v_R * v_R)) * u_R;
+        F[1] = (ro2 * u_R * u_R + p2) + SR * (rr * SM - ro2 * u_R);
+        F[2] = (ro2 * u_R * v_R) + SR * (rr * v_R - ro2 * v_R);
+    } else if (SM >= R(0)) {
+        const R rr = ro1 * (SL - u_L) / (SL - SM);
+        const R e = p1 / g.g1 + R(0.5) * ro1 * (u_L * u_L + v_L * v_L);
+        const R ee = ((SL - u_L) * e - p1 * u_L + pp * SM) / (SL - SM);
+        FQ = SL * (rr * Q_L / ro1 - Q_L) + Q_L * u_L;
+        F[0] = SL * (rr - ro1) + ro1 * u_L;
+        F[3] = SL * (ee - e) + (g.ga * p1 / (g.g1) + R(0.5) * ro1 * (u_L * u_L + v_L * v_L)) * u_L;
+        F[1] = FL1 + SL * (rr * SM - ro1 * u_L);
+        F[2] = FL2 + SL * (rr * v_L - ro1 * v_L);
+    } else {
+        // SM is not a number (the reference prints an error and leaves the
+        // flux unset): a non-finite flux, reported by the caller
+        FQ = R(NAN);
+        F[0] = F[1] = F[2] = F[3] = R(NAN);
+    }
+    return UU;
+}
+
 // ------------------------------------------------------------------ exact Riemann solver
 // residual of the shock-rarefaction pattern (lev, kernel.cu:751-765)
 template <typename R>

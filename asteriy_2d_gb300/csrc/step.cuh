@@ -686,6 +686,11 @@ __device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<
     } else if constexpr (FLUX == 3) {
         if (hi) Sp = flux_hllc_a(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
         else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
+    } else if constexpr (FLUX == 4) {
+        // HLLCQ_Korolkov_2D's gas part (the FP64 solver only)
+        R FQ;
+        if (hi) Sp = flux_hllcq(g, L[0], L[1], L[NN], L[TT], R(0), U[0], U[1], U[NN], U[TT], R(0), F, FQ);
+        else Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
     } else {
         Sp = flux_hll(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT], F);
     }
@@ -1127,6 +1132,9 @@ __device__ __forceinline__ R uniform_face(const Gas<R>& g, R r, R p, R un, R ut,
         return flux_hllc(g, r, p, un, ut, r, p, un, ut, F);
     } else if constexpr (FLUX == 3) {
         return flux_hllc_a(g, r, p, un, ut, r, p, un, ut, F);
+    } else if constexpr (FLUX == 4) {
+        R FQ;
+        return flux_hllcq(g, r, p, un, ut, R(0), r, p, un, ut, R(0), F, FQ);
     } else {
         return flux_hll(g, r, p, un, ut, r, p, un, ut, F);
     }

@@ -38,6 +38,8 @@ SIGNATURES = {
     "ast_synchronize": (C.c_int, [C.c_void_p]),
     "ast_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.ast_stats), C.c_int]),
     "ast_get_phase_clocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int]),
+    "ast_set_scalar": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "ast_get_scalar": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "ast_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
     "ast_step_raw": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_int, C.POINTER(A.ast_config), C.c_void_p]),
@@ -335,6 +337,21 @@ class Solver:
         st = A.ast_stats()
         check(self.lib.ast_get_stats(self.h, C.byref(st), int(reset)), "ast_get_stats")
         return {name: getattr(st, name) for name, _ in st._fields_ if name != "reserved"}
+
+    def set_scalar(self, q):
+        """The passive scalar (K = N*M FP64 values, index m*N + n), or None
+        to remove it (ast_set_scalar)."""
+        if q is None:
+            check(self.lib.ast_set_scalar(self.h, None, 0), "ast_set_scalar")
+            return
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1)
+        assert q.size == self.cfg.N * self.cfg.M
+        check(self.lib.ast_set_scalar(self.h, q.ctypes.data, 0), "ast_set_scalar")
+
+    def get_scalar(self):
+        q = np.empty(self.cfg.N * self.cfg.M, dtype=np.float64)
+        check(self.lib.ast_get_scalar(self.h, q.ctypes.data, 0), "ast_get_scalar")
+        return q
 
     def phase_clocks(self, reset=False):
         """Profiling builds (AST_PHASE_CLOCKS=1 at build time): SM cycles per

@@ -504,6 +504,7 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32, tune_at=2
             windows.append([prev, d, round(prev_ev.elapsed_time(ev) / (d - prev), 4)])
             prev, prev_ev = d, ev
         fp32 = [B.get_state(i)[0] for i in range(nprob)]
+        tt32 = [B.clock(i)[1] for i in range(nprob)]
     # unbatched: one solver per problem, stepped in turn on one stream
     solos = []
     for p, (s0, u0) in zip(probs, init):
@@ -526,15 +527,32 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32, tune_at=2
         c = p.cfg.copy()
         c.precision = A.PREC_FP64
         cfg64.append(c)
-    l1 = []
+    # at the same step count, and at the same simulated time (the FP64
+    # density linearly interpolated in time to each FP32 problem's final
+    # time, from single FP64 steps around it)
+    def rel_l1(a, ref):
+        return float(np.sum(np.abs(a - ref)) / np.sum(np.abs(ref)))
+    l1, l1t, drift = [], [None] * nprob, []
+    total = tune_at + warmup + steps
     with solver.Batch(cfg64) as B:
         for i, (s0, u0) in enumerate(init):
             B.set_state(i, s0, u0)
-        B.step(tune_at + warmup + steps)
-        for i in range(nprob):
-            r64 = B.get_state(i)[0][:, 0]
-            l1.append(float(np.sum(np.abs(fp32[i][:, 0] - r64)) / np.sum(np.abs(r64))))
+        B.step(total - 8)
+        prev = [(B.clock(i)[1], B.get_state(i)[0][:, 0]) for i in range(nprob)]
+        for k in range(16):
+            B.step(1)
+            for i in range(nprob):
+                tb, rb = B.clock(i)[1], B.get_state(i)[0][:, 0]
+                ta, ra = prev[i]
+                if k == 7:
+                    l1.append(rel_l1(fp32[i][:, 0], rb))
+                    drift.append((tt32[i] - tb) / tb)
+                if l1t[i] is None and ta <= tt32[i] <= tb:
+                    w = (tt32[i] - ta) / (tb - ta) if tb > ta else 0.0
+                    l1t[i] = rel_l1(fp32[i][:, 0], (1.0 - w) * ra + w * rb)
+                prev[i] = (tb, rb)
     l1 = np.array(l1)
+    found = np.array([v for v in l1t if v is not None])
     kinds = [("godunov" if p.cfg.flux == A.FLUX_GODUNOV else "hllc") + "/" +
              ("wind" if p.setup == A.SETUP_WIND else "blast") for p in probs]
     return {
@@ -559,7 +577,16 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32, tune_at=2
         "mix": {k: kinds.count(k) for k in sorted(set(kinds))},
         "solo_value": cells * solo_steps / solo_sec, "solo_steps": solo_steps,
         "l1_rho_vs_fp64": {"median": float(np.median(l1)), "max": float(l1.max()),
+                           "above_1e-4": int(np.sum(l1 > 1e-4)),
                            "per_problem": [float("%.3g" % v) for v in l1]},
+        "l1_rho_vs_fp64_same_time": {"median": float(np.median(found)) if found.size else None,
+                                     "max": float(found.max()) if found.size else None,
+                                     "above_1e-4": int(np.sum(found > 1e-4)), "problems": int(found.size),
+                                     "tt_rel_drift_median": float(np.median(drift)),
+                                     "tt_rel_drift_max_abs": float(np.max(np.abs(drift))),
+                                     "note": "each FP32 problem against its FP64 run interpolated in time to the "
+                                             "FP32 run's final time (problems whose time lies within 8 steps "
+                                             "of the FP64 run's)"},
         "dtype": "f32",
     }
 

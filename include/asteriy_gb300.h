@@ -61,7 +61,8 @@ extern "C" {
 /* HLLC is the Korolkov solver (HLLC_2d_Korolkov, Gas_Dinamic.cu:1814);
    HLLC_A the reference's second HLLC (HLLC_Aleksashov, kernel.cu:767), an
    MHD formulation it calls with zero magnetic field (add_MK method 1). */
-enum ast_flux   { AST_FLUX_HLL = 0, AST_FLUX_HLLC = 1, AST_FLUX_GODUNOV = 2, AST_FLUX_HLLC_A = 3 };
+enum ast_flux   { AST_FLUX_HLL = 0, AST_FLUX_HLLC = 1, AST_FLUX_GODUNOV = 2, AST_FLUX_HLLC_A = 3,
+                  AST_FLUX_HLLCQ = 4 /* HLLCQ_Korolkov_2D (Gas_Dinamic.cu:249-353), FP64 solver only */ };
 enum ast_recon  { AST_RECON_NONE = 0, AST_RECON_MINMOD = 1 };
 enum ast_geom   { AST_GEOM_PLANAR = 0, AST_GEOM_AXISYM = 1 };
 enum ast_prec   { AST_PREC_FP64 = 0, AST_PREC_FP32 = 1 };
@@ -180,7 +181,11 @@ typedef struct ast_config {
        0.419231 (neutral_kn = 0: no source).  The energy term of add_MK
        multiplies its source by 0 and is left out.                           */
     double  neutral_nh, neutral_kn;
-    double  reserved_d[3];
+    /* the passive scalar's value in the ghost cells of FIXED sides
+       (ast_set_scalar; other sides copy or mirror the scalar as the
+       state's ghost rules do) */
+    double  scalar_in;
+    double  reserved_d[2];
 } ast_config;
 
 typedef struct ast_stats {
@@ -267,6 +272,21 @@ int ast_step_host_n(ast_solver* solver, int nsteps, double* s_a, double* u_a, do
    (same terms, in FP64, at the step's total energy). */
 int ast_set_neutral(ast_solver* solver, const double* nn2, int on_device);
 int ast_get_stats(ast_solver* solver, ast_stats* out, int reset);
+/* ---- passive scalar (FP64 solver; flux AST_FLUX_HLLC or AST_FLUX_HLLCQ;
+   no region_select).  The reference's HLLC solvers compute a passive
+   scalar's face flux beside the gas flux (the Q channel of
+   HLLC_2d_Korolkov_b_s, Gas_Dinamic.cu:1660-1808; HLLCQ_Korolkov_2D,
+   Gas_Dinamic.cu:249-353) but its steps never carry one.  With a scalar set,
+   every ast_step also advances Q, a density carried by the flow: from the
+   same old state, with the same reconstruction (the density's rule) and
+   solver as the gas step, Q' = Q - T_do/(dx dy) * (sum of its face fluxes)
+   [- T_do/r * Q * v_r on the axisymmetric grid]; cells held fixed keep Q;
+   ghost values as the state's (FIXED sides: cfg.scalar_in).  The gas step
+   is unchanged.  q holds K = N*M values, index m*N + n; on_device = 1
+   means a device pointer.  q = NULL removes the scalar.  The host-array
+   steps (ast_step_host*) refuse a solver that carries one. */
+int ast_set_scalar(ast_solver* solver, const double* q, int on_device);
+int ast_get_scalar(ast_solver* solver, double* q, int on_device);
 /* Profiling builds only (the library compiled with AST_PHASE_CLOCKS;
    otherwise AST_ERR_UNSUPPORTED): SM cycles the FP32 persistent kernel's
    CTAs spent per phase of their tiles since the last reset, summed over

@@ -15,7 +15,13 @@
  *
  *   minmod / linear / linear2 ...... kernel.cu:22-50, sign Gas_Dinamic.cu:858-872
  *   HLL ............................ kernel.cu:1399-1523
- *   HLLC (Korolkov, metod 2, W=0) .. Gas_Dinamic.cu:1604-1826
+ *   HLLC (Korolkov, metod 2, W=0) .. Gas_Dinamic.cu:1604-1826, with its
+ *                                    passive-scalar channel (PQ)
+ *   HLLCQ (Korolkov) ............... Gas_Dinamic.cu:249-353
+ *   passive scalar step ............ not in the reference (its steps do not
+ *                                    carry Q): the density's update form
+ *                                    with the solvers' PQ, as the library
+ *                                    carries it
  *   HLLC (Aleksashov, B = 0) ....... kernel.cu:767-1079
  *   exact Godunov .................. kernel.cu:128-570, newton :635-680,
  *                                    devtwo :682-749, lev :751-765
@@ -176,11 +182,11 @@ static double hll(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double n1, dou
 
 /* ------------------------------------------------------------------------ */
 /* HLLC, HLLC_2d_Korolkov_b_s with metod=2, W=0 (Gas_Dinamic.cu:1604-1826). */
-/* The passive scalar Q of the reference does not feed the other outputs    */
-/* and is left out.                                                          */
+/* The passive scalar Q does not feed the other outputs; its flux goes to   */
+/* *PQ when PQ is not NULL (Q_L, Q_R its values on the two sides).          */
 /* ------------------------------------------------------------------------ */
-static double hllc(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double n1, double n2,
-                   d2* Ps, d2* Pu, double rad, int nul_potok)
+static double hllc_q(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double Q_L, double Q_R, double n1,
+                     double n2, d2* Ps, d2* Pu, double* PQ, double rad, int nul_potok)
 {
     const double ggg = ph->ga, g1 = ph->g1, W = 0.0;
     double ro_L = Ls.x, p_L = Ls.y, v1_L = Lu.x, v2_L = Lu.y;
@@ -208,20 +214,26 @@ static double hllc(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double n1, do
     FR[0] = ro_R * u2; FR[1] = ro_R * u2 * u2 + p_R; FR[2] = ro_R * u2 * v2; FR[3] = (e2 + p_R) * u2;
     UL[0] = ro_L; UL[1] = ro_L * u1; UL[2] = ro_L * v1; UL[3] = e1;
     UR[0] = ro_R; UR[1] = ro_R * u2; UR[2] = ro_R * v2; UR[3] = e2;
+    /* the scalar's column (index 4 of the reference's arrays) */
+    double FL4 = Q_L * u1, FR4 = Q_R * u2, UL4 = Q_L, UR4 = Q_R, PQ4;
 
     if (SL >= W) {
         P[1] = n1 * (FL[1] - W * UL[1]) + t1 * (FL[2] - W * UL[2]);
         P[2] = n2 * (FL[1] - W * UL[1]) + t2 * (FL[2] - W * UL[2]);
         P[0] = FL[0] - W * UL[0];
         P[3] = FL[3] - W * UL[3];
+        PQ4 = FL4 - W * UL4;
     } else if (SR <= W) {
         P[1] = n1 * (FR[1] - W * UR[1]) + t1 * (FR[2] - W * UR[2]);
         P[2] = n2 * (FR[1] - W * UR[1]) + t2 * (FR[2] - W * UR[2]);
         P[0] = FR[0] - W * UR[0];
         P[3] = FR[3] - W * UR[3];
+        PQ4 = FR4 - W * UR4;
     } else {
         double ro_LL = ro_L * (SL - u1) / (SL - SM);
         double ro_RR = ro_R * (SR - u2) / (SR - SM);
+        double Q_LL = Q_L * (SL - u1) / (SL - SM);
+        double Q_RR = Q_R * (SR - u2) / (SR - SM);
         double suRm = suR / (SR - SM);
         double suLm = suL / (SL - SM);
         double ptzR = p_R + ro_R * suR * (SM - u2);
@@ -244,10 +256,13 @@ static double hllc(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double n1, do
         URR[0] = ro_RR; URR[1] = ro_RR * SM; URR[2] = ro_RR * vRR; URR[3] = ee2;
         if (SL < W && SM >= W) {
             for (int i = 0; i < 4; i++) PO[i] = FL[i] + SL * ULL[i] - SL * UL[i] - W * ULL[i];
+            PQ4 = FL4 + SL * Q_LL - SL * UL4 - W * Q_LL;
         } else if (SR > W && SM < W) {
             for (int i = 0; i < 4; i++) PO[i] = FR[i] + SR * URR[i] - SR * UR[i] - W * URR[i];
+            PQ4 = FR4 + SR * Q_RR - SR * UR4 - W * Q_RR;
         } else {
             for (int i = 0; i < 4; i++) PO[i] = NAN;
+            PQ4 = NAN;
         }
         P[1] = n1 * PO[1] + t1 * PO[2];
         P[2] = n2 * PO[1] + t2 * PO[2];
@@ -255,6 +270,87 @@ static double hllc(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double n1, do
         P[3] = PO[3];
     }
     Ps->x = P[0]; Ps->y = P[3]; Pu->x = P[1]; Pu->y = P[2];
+    if (PQ) *PQ = PQ4;
+    return time;
+}
+
+static double hllc(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double n1, double n2,
+                   d2* Ps, d2* Pu, double rad, int nul_potok)
+{
+    return hllc_q(ph, Ls, Lu, Rs, Ru, 1.0, 1.0, n1, n2, Ps, Pu, NULL, rad, nul_potok);
+}
+
+/* ------------------------------------------------------------------------ */
+/* HLLCQ_Korolkov_2D (Gas_Dinamic.cu:249-353): HLLC with the bounds         */
+/* min(u_L - c_L, u_R - c_R), max(u_L + c_L, u_R + c_R) and the passive     */
+/* scalar Q; tangent t = (-n2, n1).  A non-number contact speed leaves the  */
+/* reference's outputs unset: NaN here.                                     */
+/* ------------------------------------------------------------------------ */
+static double hllcq(const ora_phys* ph, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double LQ, double RQ, double n1, double n2,
+                    d2* Ps, d2* Pu, double* PQ, double rad)
+{
+    const double ga = ph->ga, g1 = ph->g1;
+    double ro1 = Ls.x, u1 = Lu.x, v1 = Lu.y, p1 = Ls.y, Q_L = LQ;
+    double ro2 = Rs.x, u2 = Ru.x, v2 = Ru.y, p2 = Rs.y, Q_R = RQ;
+    double t1 = -n2, t2 = n1;
+    double u_L = u1 * n1 + v1 * n2;
+    double v_L = u1 * t1 + v1 * t2;
+    double u_R = u2 * n1 + v2 * n2;
+    double v_R = u2 * t1 + v2 * t2;
+    double cL = sqrt(ga * p1 / ro1);
+    double cR = sqrt(ga * p2 / ro2);
+    double SL = fmin((u_L - cL), (u_R - cR));
+    double SR = fmax((u_L + cL), (u_R + cR));
+    double UU = fmax(fabs(SL), fabs(SR));
+    double time = ph->krit * rad / UU;
+    double FL1 = ro1 * u_L * u_L + p1;
+    double FL2 = ro1 * u_L * v_L;
+    double FR1 = ro2 * u_R * u_R + p2;
+    double FR2 = ro2 * u_R * v_R;
+    double q;
+    if (SL >= 0.0) {
+        q = Q_L * u_L;
+        Ps->x = ro1 * u_L;
+        Ps->y = (ga * p1 / (g1) + 0.5 * ro1 * (u1 * u1 + v1 * v1)) * u_L;
+        Pu->x = (FL1) * n1 + (FL2) * t1;
+        Pu->y = (FL1) * n2 + (FL2) * t2;
+    } else if (SR <= 0.0) {
+        q = Q_R * u_R;
+        Ps->x = ro2 * u_R;
+        Ps->y = (ga * p2 / (g1) + 0.5 * ro2 * (u2 * u2 + v2 * v2)) * u_R;
+        Pu->x = (FR1) * n1 + (FR2) * t1;
+        Pu->y = (FR1) * n2 + (FR2) * t2;
+    } else {
+        double SM = ((SR - u_R) * ro2 * u_R - (SL - u_L) * ro1 * u_L - p2 + p1) / ((SR - u_R) * ro2 - (SL - u_L) * ro1);
+        double pp = p1 + ro1 * (SL - u_L) * (SM - u_L);
+        if (SM <= 0.0) {
+            double rr = ro2 * (SR - u_R) / (SR - SM);
+            double e = p2 / g1 + 0.5 * ro2 * (u2 * u2 + v2 * v2);
+            double ee = ((SR - u_R) * e - p2 * u_R + pp * SM) / (SR - SM);
+            q = SR * (rr * Q_R / ro2 - Q_R) + Q_R * u_R;
+            Ps->x = SR * (rr - ro2) + ro2 * u_R;
+            Ps->y = SR * (ee - e) + (ga * p2 / (g1) + 0.5 * ro2 * (u2 * u2 + v2 * v2)) * u_R;
+            double F1 = (ro2 * u_R * u_R + p2) + SR * (rr * SM - ro2 * u_R);
+            double F2 = (ro2 * u_R * v_R) + SR * (rr * v_R - ro2 * v_R);
+            Pu->x = F1 * n1 + F2 * t1;
+            Pu->y = F1 * n2 + F2 * t2;
+        } else if (SM >= 0.0) {
+            double rr = ro1 * (SL - u_L) / (SL - SM);
+            double e = p1 / g1 + 0.5 * ro1 * (u1 * u1 + v1 * v1);
+            double ee = ((SL - u_L) * e - p1 * u_L + pp * SM) / (SL - SM);
+            q = SL * (rr * Q_L / ro1 - Q_L) + Q_L * u_L;
+            Ps->x = SL * (rr - ro1) + ro1 * u_L;
+            Ps->y = SL * (ee - e) + (ga * p1 / (g1) + 0.5 * ro1 * (u1 * u1 + v1 * v1)) * u_L;
+            double F1 = FL1 + SL * (rr * SM - ro1 * u_L);
+            double F2 = FL2 + SL * (rr * v_L - ro1 * v_L);
+            Pu->x = F1 * n1 + F2 * t1;
+            Pu->y = F1 * n2 + F2 * t2;
+        } else {
+            q = NAN;
+            Ps->x = Ps->y = Pu->x = Pu->y = NAN;
+        }
+    }
+    if (PQ) *PQ = q;
     return time;
 }
 
@@ -586,6 +682,7 @@ double ora_face(int flux, double gamma, double krit, double tol, int max_iter,
     if (flux == AST_FLUX_HLL) t = hll(&ph, Ls, Lu, Rs, Ru, n1, n2, &Ps, &Pu, rad);
     else if (flux == AST_FLUX_HLLC) t = hllc(&ph, Ls, Lu, Rs, Ru, n1, n2, &Ps, &Pu, rad, 0);
     else if (flux == AST_FLUX_HLLC_A) t = hllc_a(&ph, Ls, Lu, Rs, Ru, n1, n2, &Ps, &Pu, rad);
+    else if (flux == AST_FLUX_HLLCQ) t = hllcq(&ph, Ls, Lu, Rs, Ru, 0.0, 0.0, n1, n2, &Ps, &Pu, NULL, rad);
     else t = godunov(&ph, &st, Ls, Lu, Rs, Ru, n1, n2, &Ps, &Pu, rad);
     pack_out(Ps, Pu, out);
     if (counters) {
@@ -593,6 +690,24 @@ double ora_face(int flux, double gamma, double krit, double tol, int max_iter,
         counters[3] = st.bisect_calls; counters[4] = st.bisect_iters; counters[5] = st.bisect_cap;
         counters[6] = st.vacuum;
     }
+    return t;
+}
+
+/* One face of the passive-scalar solvers (flux AST_FLUX_HLLC: the Q channel
+   of HLLC_2d_Korolkov_b_s; AST_FLUX_HLLCQ: HLLCQ_Korolkov_2D): out[0..3] as
+   ora_face, out[4] the scalar's flux; returns the face dt. */
+double ora_face_q(int flux, double gamma, double krit, const double* sL, const double* uL, const double* sR,
+                  const double* uR, double QL, double QR, double n1, double n2, double rad, double* out)
+{
+    ora_phys ph;
+    ora_phys_init(&ph, gamma, krit, 10e-10, 200);
+    d2 Ls = {sL[0], sL[1]}, Lu = {uL[0], uL[1]}, Rs = {sR[0], sR[1]}, Ru = {uR[0], uR[1]};
+    d2 Ps = {0, 0}, Pu = {0, 0};
+    double PQ = 0.0, t;
+    if (flux == AST_FLUX_HLLCQ) t = hllcq(&ph, Ls, Lu, Rs, Ru, QL, QR, n1, n2, &Ps, &Pu, &PQ, rad);
+    else t = hllc_q(&ph, Ls, Lu, Rs, Ru, QL, QR, n1, n2, &Ps, &Pu, &PQ, rad, 0);
+    pack_out(Ps, Pu, out);
+    out[4] = PQ;
     return t;
 }
 
@@ -668,10 +783,14 @@ static void ora_get(const ora_grid* g, const ast_config* c, const d2* s, const d
 #ifdef ORA_WITH_REF
 /* Built into oracle/_ref/libastref.so: every face is evaluated by the
    reference's own function (HLL kernel.cu:1399, HLLC_2d_Korolkov
-   Gas_Dinamic.cu:1814, Godunov_Solver_Alexashov kernel.cu:128), compiled for
-   the host by oracle/ref_driver.cpp; gamma and CFL come from ref_set_params. */
+   Gas_Dinamic.cu:1814, Godunov_Solver_Alexashov kernel.cu:128,
+   HLLCQ_Korolkov_2D Gas_Dinamic.cu:249), compiled for the host by
+   oracle/ref_driver.cpp; gamma and CFL come from ref_set_params. */
 double ref_face(int which, const double* sL, const double* uL, const double* sR, const double* uR,
                 double n1, double n2, double rad, double* out);
+double ref_face_q(int which, const double* sL, const double* uL, const double* sR, const double* uR, double QL,
+                  double QR, double n1, double n2, double rad, double* out);
+#define REF_WHICH(flux) ((flux) == AST_FLUX_HLLCQ ? 5 : (flux))
 #endif
 
 static double ora_flux(int flux, const ora_phys* ph, ora_stats* st, d2 Ls, d2 Lu, d2 Rs, d2 Ru,
@@ -680,14 +799,32 @@ static double ora_flux(int flux, const ora_phys* ph, ora_stats* st, d2 Ls, d2 Lu
 #ifdef ORA_WITH_REF
     (void)ph; (void)st;
     double sl[2] = {Ls.x, Ls.y}, ul[2] = {Lu.x, Lu.y}, sr[2] = {Rs.x, Rs.y}, ur[2] = {Ru.x, Ru.y}, out[4];
-    double t = ref_face(flux, sl, ul, sr, ur, n1, n2, rad, out);
+    double t = ref_face(REF_WHICH(flux), sl, ul, sr, ur, n1, n2, rad, out);
     Ps->x = out[0]; Pu->x = out[1]; Pu->y = out[2]; Ps->y = out[3];
     return t;
 #endif
     if (flux == AST_FLUX_HLLC) return hllc(ph, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad, 0);
+    if (flux == AST_FLUX_HLLCQ) return hllcq(ph, Ls, Lu, Rs, Ru, 0.0, 0.0, n1, n2, Ps, Pu, NULL, rad);
     if (flux == AST_FLUX_HLLC_A) return hllc_a(ph, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
     if (flux == AST_FLUX_GODUNOV) return godunov(ph, st, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
     return hll(ph, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
+}
+
+/* a face of the passive-scalar step: the gas flux as ora_flux gives it and
+   the scalar's flux *PQ (flux HLLC or HLLCQ) */
+static double ora_flux_q(int flux, const ora_phys* ph, ora_stats* st, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double QL,
+                         double QR, double n1, double n2, d2* Ps, d2* Pu, double* PQ, double rad)
+{
+    (void)st;
+#ifdef ORA_WITH_REF
+    (void)ph;
+    double sl[2] = {Ls.x, Ls.y}, ul[2] = {Lu.x, Lu.y}, sr[2] = {Rs.x, Rs.y}, ur[2] = {Ru.x, Ru.y}, out[5];
+    double t = ref_face_q(REF_WHICH(flux), sl, ul, sr, ur, QL, QR, n1, n2, rad, out);
+    Ps->x = out[0]; Pu->x = out[1]; Pu->y = out[2]; Ps->y = out[3]; *PQ = out[4];
+    return t;
+#endif
+    if (flux == AST_FLUX_HLLCQ) return hllcq(ph, Ls, Lu, Rs, Ru, QL, QR, n1, n2, Ps, Pu, PQ, rad);
+    return hllc_q(ph, Ls, Lu, Rs, Ru, QL, QR, n1, n2, Ps, Pu, PQ, rad, 0);
 }
 
 /* neighbour-side face value with the positivity rule (kernel.cu:2801-2850) */
@@ -737,6 +874,51 @@ static double* g_pmargin = NULL;
    pattern under rounding of its inputs) */
 void ora_set_margin(double* per_cell, double* pattern) { g_margin = per_cell; g_pmargin = pattern; }
 
+/* The passive scalar the steps carry (ora_set_scalar): Q of the old state,
+   Q of the new, and its value in FIXED ghost cells; NULL for none.  Its
+   ghost rules are the state's (mirror, copy of the boundary cell, fixed
+   value); its face values are reconstructed with the density's rule. */
+static const double* g_q = NULL;
+static double* g_q2 = NULL;
+static double g_q_fixed = 0.0;
+
+void ora_set_scalar(const double* q, double* q2, double q_fixed)
+{
+    g_q = q;
+    g_q2 = q2;
+    g_q_fixed = q_fixed;
+}
+
+static double ora_get_q(const ora_grid* g, const ast_config* c, int n, int m)
+{
+    const int N = g->N, M = g->M;
+    if (n >= 0 && n < N && m >= 0 && m < M) return g_q[m * N + n];
+    int side, j, b0, mir;
+    if (n < 0)       { side = AST_Z_LO; j = -1 - n; b0 = m * N + 0;       mir = m * N + j; }
+    else if (n >= N) { side = AST_Z_HI; j = n - N;  b0 = m * N + N - 1;   mir = m * N + (N - 1 - j); }
+    else if (m < 0)  { side = AST_R_LO; j = -1 - m; b0 = 0 * N + n;       mir = j * N + n; }
+    else             { side = AST_R_HI; j = m - M;  b0 = (M - 1) * N + n; mir = (M - 1 - j) * N + n; }
+    if (c->bc[side].kind == AST_BC_REFLECT) return g_q[mir];
+    if (c->bc[side].kind == AST_BC_FIXED) return g_q_fixed;
+    return g_q[b0];
+}
+
+/* neighbour-side face value of the scalar (the density's rule) */
+static double nb_q(double c0, double h, double hh, double q1, double qn, double qn2)
+{
+    double r = ora_linear(c0, q1, c0 + h, qn, c0 + 2.0 * h, qn2, c0 + hh);
+    return (r <= 0) ? qn : r;
+}
+
+/* a high-order face: with the scalar, its flux *PQ beside the gas flux */
+static double face_call(int flux, const ora_phys* ph, ora_stats* st, d2 Ls, d2 Lu, d2 Rs, d2 Ru, double ql,
+                        double qr, double n1, double n2, d2* Ps, d2* Pu, double* PQ, double rad)
+{
+    if (g_q) return ora_flux_q(flux, ph, st, Ls, Lu, Rs, Ru, ql, qr, n1, n2, Ps, Pu, PQ, rad);
+    *PQ = 0.0;
+    return ora_flux(flux, ph, st, Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad);
+}
+
 /* One cell of one step.  Returns the cell's tmin; a cell held fixed returns
    1e7, the reset value of T, because the reference's fixed cells never
    touch T (kernel.cu:2318-2324). */
@@ -759,9 +941,21 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
         double dist2 = (xz * xz) / (c->fixed_az * c->fixed_az) + (y * y) / (c->fixed_ar * c->fixed_ar);
         if (dist2 < 1.0) {
             s2[index] = s_1; u2[index] = u_1;
+            if (g_q) g_q2[index] = g_q[index];
             return 10000000;
         }
     }
+    /* the scalar's stencil and its cell-side face values */
+    double q_1 = 0, q_2 = 0, q_3 = 0, q_4 = 0, q_5 = 0, q21 = 0, q31 = 0, q41 = 0, q51 = 0;
+    double PQ12 = 0, PQ13 = 0, PQ14 = 0, PQ15 = 0;
+    if (g_q) {
+        q_1 = g_q[index];
+        q_2 = ora_get_q(g, c, n + 1, m); q_3 = ora_get_q(g, c, n, m - 1);
+        q_4 = ora_get_q(g, c, n - 1, m); q_5 = ora_get_q(g, c, n, m + 1);
+        q21 = ora_get_q(g, c, n + 2, m); q31 = ora_get_q(g, c, n, m - 2);
+        q41 = ora_get_q(g, c, n - 2, m); q51 = ora_get_q(g, c, n, m + 2);
+    }
+    double q12 = q_1, q13 = q_1, q14 = q_1, q15 = q_1;
 
     d2 s_2, s_3, s_4, s_5, u_2, u_3, u_4, u_5;
     ora_get(g, c, s, u, n + 1, m, &s_2, &u_2);
@@ -803,6 +997,14 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
         u15.x = B; u13.x = A;
         ora_linear2(y - dy, u_3.y, y, u_1.y, y + dy, u_5.y, y - dy / 2.0, y + dy / 2.0, &A, &B);
         u15.y = B; u13.y = A;
+        if (g_q) {
+            ora_linear2(x - dx, q_4, x, q_1, x + dx, q_2, x - dx / 2.0, x + dx / 2.0, &A, &B);
+            q12 = (B <= 0) ? q_1 : B;
+            q14 = (A <= 0) ? q_1 : A;
+            ora_linear2(y - dy, q_3, y, q_1, y + dy, q_5, y - dy / 2.0, y + dy / 2.0, &A, &B);
+            q15 = (B <= 0) ? q_1 : B;
+            q13 = (A <= 0) ? q_1 : A;
+        }
     }
 
     double t;
@@ -810,9 +1012,10 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
     if (in_region(c, x + dx / 2.0)) {
         if (recon) {
             d2 rs = nb_s(x, dx, dx / 2.0, s_1, s_2, s21, gp), ru = nb_u(x, dx, dx / 2.0, u_1, u_2, u21);
-            t = ora_flux(c->flux, ph, st, s12, u12, rs, ru, 1, 0, &Ps12, &Pu12, dx);
+            double rq = g_q ? nb_q(x, dx, dx / 2.0, q_1, q_2, q21) : 0.0;
+            t = face_call(c->flux, ph, st, s12, u12, rs, ru, q12, rq, 1, 0, &Ps12, &Pu12, &PQ12, dx);
         } else {
-            t = ora_flux(c->flux, ph, st, s_1, u_1, s_2, u_2, 1, 0, &Ps12, &Pu12, dx);
+            t = face_call(c->flux, ph, st, s_1, u_1, s_2, u_2, q_1, q_2, 1, 0, &Ps12, &Pu12, &PQ12, dx);
         }
     } else {
         t = ora_flux(AST_FLUX_HLL, ph, st, s_1, u_1, s_2, u_2, 1, 0, &Ps12, &Pu12, dx);
@@ -822,15 +1025,17 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
     if (in_region(c, x)) {
         if (recon) {
             d2 rs = nb_s(y, -dy, -dy / 2.0, s_1, s_3, s31, gp), ru = nb_u(y, -dy, -dy / 2.0, u_1, u_3, u31);
-            t = ora_flux(c->flux, ph, st, s13, u13, rs, ru, 0, -1, &Ps13, &Pu13, dy);
+            double rq = g_q ? nb_q(y, -dy, -dy / 2.0, q_1, q_3, q31) : 0.0;
+            t = face_call(c->flux, ph, st, s13, u13, rs, ru, q13, rq, 0, -1, &Ps13, &Pu13, &PQ13, dy);
             tmin = fmin(tmin, t);
             rs = nb_s(y, dy, dy / 2.0, s_1, s_5, s51, gp); ru = nb_u(y, dy, dy / 2.0, u_1, u_5, u51);
-            t = ora_flux(c->flux, ph, st, s15, u15, rs, ru, 0, 1, &Ps15, &Pu15, dy);
+            rq = g_q ? nb_q(y, dy, dy / 2.0, q_1, q_5, q51) : 0.0;
+            t = face_call(c->flux, ph, st, s15, u15, rs, ru, q15, rq, 0, 1, &Ps15, &Pu15, &PQ15, dy);
             tmin = fmin(tmin, t);
         } else {
-            t = ora_flux(c->flux, ph, st, s_1, u_1, s_3, u_3, 0, -1, &Ps13, &Pu13, dy);
+            t = face_call(c->flux, ph, st, s_1, u_1, s_3, u_3, q_1, q_3, 0, -1, &Ps13, &Pu13, &PQ13, dy);
             tmin = fmin(tmin, t);
-            t = ora_flux(c->flux, ph, st, s_1, u_1, s_5, u_5, 0, 1, &Ps15, &Pu15, dy);
+            t = face_call(c->flux, ph, st, s_1, u_1, s_5, u_5, q_1, q_5, 0, 1, &Ps15, &Pu15, &PQ15, dy);
             tmin = fmin(tmin, t);
         }
     } else {
@@ -843,9 +1048,10 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
     if (in_region(c, x - dx / 2.0)) {
         if (recon) {
             d2 rs = nb_s(x, -dx, -dx / 2.0, s_1, s_4, s41, gp), ru = nb_u(x, -dx, -dx / 2.0, u_1, u_4, u41);
-            t = ora_flux(c->flux, ph, st, s14, u14, rs, ru, -1, 0, &Ps14, &Pu14, dx);
+            double rq = g_q ? nb_q(x, -dx, -dx / 2.0, q_1, q_4, q41) : 0.0;
+            t = face_call(c->flux, ph, st, s14, u14, rs, ru, q14, rq, -1, 0, &Ps14, &Pu14, &PQ14, dx);
         } else {
-            t = ora_flux(c->flux, ph, st, s_1, u_1, s_4, u_4, -1, 0, &Ps14, &Pu14, dx);
+            t = face_call(c->flux, ph, st, s_1, u_1, s_4, u_4, q_1, q_4, -1, 0, &Ps14, &Pu14, &PQ14, dx);
         }
     } else {
         t = ora_flux(AST_FLUX_HLL, ph, st, s_1, u_1, s_4, u_4, -1, 0, &Ps14, &Pu14, dx);
@@ -899,6 +1105,17 @@ static double ora_cell(const ora_grid* g, const ast_config* c, const ora_phys* p
     if (rs2.y <= 0.0) { st->p_floor++; rs2.y = c->p_floor; }
     s2[index] = rs2;
     u2[index] = ru2;
+    if (g_q) {
+        /* the scalar in the density's update form */
+        double PQS;
+        if (c->geom == AST_GEOM_AXISYM) {
+            PQS = (PQ12 + PQ14) * dy + (PQ13 + PQ15) * dx;
+            g_q2[index] = q_1 - (T_do / dV) * PQS - (T_do / y) * q_1 * u_1.y;
+        } else {
+            PQS = PQ12 * dy + PQ13 * dx + PQ14 * dy + PQ15 * dx;
+            g_q2[index] = q_1 - (T_do / dV) * PQS;
+        }
+    }
     return tmin;
 }
 

@@ -35,6 +35,7 @@ DEFAULT_SRC = os.environ.get("ASTERIY_REF_SRC") or "/root/reference"
 
 # (file, first line, last line, text the first line must contain)
 RANGES = [
+    ("Gas_Dinamic.cu", 249, 353, "double HLLCQ_Korolkov_2D("),
     ("Gas_Dinamic.cu", 858, 872, "int sign(double& x)"),
     ("kernel.cu", 22, 75, "double minmod(double x, double y)"),
     ("kernel.cu", 77, 86, "void lev("),

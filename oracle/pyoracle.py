@@ -60,6 +60,9 @@ def lib():
         L.ora_set_margin.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_inflow.restype = None
         L.ora_inflow.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        _scalar_api(L)
+        L.ora_face_q.restype = C.c_double
+        L.ora_face_q.argtypes = [C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, _dp] + [C.c_double] * 5 + [_dp]
         _lib = L
     return _lib
 
@@ -100,8 +103,22 @@ def ref():
             R.ref_end_of_run.restype = None
             R.ref_end_of_run.argtypes = [_dp, _dp, C.c_double, C.c_int, C.c_double, C.c_double, C.c_char_p]
         R.ref_max_threads.restype = C.c_int
+        _scalar_api(R)
+        R.ref_face_q.restype = C.c_double
+        R.ref_face_q.argtypes = [C.c_int, _dp, _dp, _dp, _dp] + [C.c_double] * 5 + [_dp]
         _ref = R
     return _ref
+
+
+def _scalar_api(L):
+    """The step loop's entry points (in both libraries: libastref.so carries
+    the oracle's loop with the reference's face functions)."""
+    L.ora_step.restype = C.c_double
+    L.ora_step.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_int, _i64p]
+    L.ora_set_scalar.restype = None
+    L.ora_set_scalar.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+    L.ora_inflow.restype = None
+    L.ora_inflow.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
 
 
 # ---------------------------------------------------------------- oracle
@@ -117,6 +134,49 @@ def face(flux, sL, uL, sR, uR, n1, n2, rad, gamma=5.0 / 3.0, cfl=0.05, tol=10e-1
     t = lib().ora_face(flux, gamma, cfl, tol, max_iter, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(a[3]),
                        n1, n2, rad, _ptr(out), cnt.ctypes.data_as(_i64p))
     return t, out, cnt
+
+
+def face_q(flux, sL, uL, sR, uR, QL, QR, n1, n2, rad, gamma=5.0 / 3.0, cfl=0.05):
+    """One face of a passive-scalar solver (flux 1: HLLC, 4: HLLCQ).
+    Returns (dt, out[5] = mass, mom_z, mom_r, energy, scalar)."""
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (sL, uL, sR, uR)]
+    out = np.zeros(5)
+    t = lib().ora_face_q(flux, gamma, cfl, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(a[3]), QL, QR, n1, n2, rad,
+                         _ptr(out))
+    return t, out
+
+
+def run_scalar(cfg, s, u, q, nsteps, nthreads=1, T_do=None, TT=0.0, step_no=0, use_ref=False):
+    """nsteps steps carrying the passive scalar q (K values, index m*N + n),
+    with the lagged-dt protocol (and the characteristic inflow after each
+    step when cfg.inflow_p > 0).  use_ref: the faces evaluated by the
+    reference's own functions (libastref.so).  Returns (s, u, q, T_do, TT,
+    step)."""
+    L = ref() if use_ref else lib()
+    if use_ref:
+        ref_set(cfg)
+    s = np.array(s, dtype=np.float64, order="C")
+    u = np.array(u, dtype=np.float64, order="C")
+    q = np.array(q, dtype=np.float64, order="C").reshape(-1)
+    s2, u2, q2 = np.empty_like(s), np.empty_like(u), np.empty_like(q)
+    tdo = cfg.dt_first if T_do is None else T_do
+    cnt = np.zeros(10, dtype=np.int64)
+    for _ in range(nsteps):
+        L.ora_set_scalar(q.ctypes.data, q2.ctypes.data, cfg.scalar_in)
+        try:
+            T = L.ora_step(C.byref(cfg), _ptr(s), _ptr(u), _ptr(s2), _ptr(u2), tdo, nthreads,
+                           cnt.ctypes.data_as(_i64p))
+        finally:
+            L.ora_set_scalar(None, None, 0.0)
+        if cfg.inflow_p > 0.0:
+            L.ora_inflow(C.byref(cfg), _ptr(s), _ptr(u), _ptr(s2), _ptr(u2))
+        tdo = T
+        TT = TT + tdo
+        step_no += 1
+        s, s2 = s2, s
+        u, u2 = u2, u
+        q, q2 = q2, q
+    return s, u, q, tdo, TT, step_no
 
 
 def step(cfg, s, u, T_do, nthreads=1):
@@ -186,6 +246,15 @@ def ref_face(which, sL, uL, sR, uR, n1, n2, rad):
     a = [np.ascontiguousarray(v, dtype=np.float64) for v in (sL, uL, sR, uR)]
     out = np.zeros(4)
     t = ref().ref_face(which, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(a[3]), n1, n2, rad, _ptr(out))
+    return t, out
+
+
+def ref_face_q(which, sL, uL, sR, uR, QL, QR, n1, n2, rad):
+    """The reference's face with a passive scalar: which 1 HLLC_2d_Korolkov_b_s
+    (metod 2, its PQ), 5 HLLCQ_Korolkov_2D.  Returns (dt, out[5])."""
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (sL, uL, sR, uR)]
+    out = np.zeros(5)
+    t = ref().ref_face_q(which, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(a[3]), QL, QR, n1, n2, rad, _ptr(out))
     return t, out
 
 

@@ -61,7 +61,8 @@ void ref_linear2(double x1, double t1, double x2, double t2, double x3, double t
 }
 
 /* which: 0 HLL, 1 HLLC (nul_potok=false), 2 exact Godunov,
-          3 HLLC_Aleksashov, 4 HLLC (nul_potok=true).
+          3 HLLC_Aleksashov, 4 HLLC (nul_potok=true), 5 HLLCQ_Korolkov_2D
+          (its passive scalar zero).
    out[4] = (mass, mom_z, mom_r, energy); returns the face dt. */
 double ref_face(int which, const double* sL, const double* uL, const double* sR, const double* uR,
                 double n1, double n2, double rad, double* out)
@@ -75,9 +76,39 @@ double ref_face(int which, const double* sL, const double* uL, const double* sR,
     case 2: t = Godunov_Solver_Alexashov(Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad); break;
     case 3: t = HLLC_Aleksashov(Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad); break;
     case 4: t = HLLC_2d_Korolkov(Ls, Lu, Rs, Ru, n1, n2, Ps, Pu, rad, true); break;
+    case 5: {
+        double PQ = 0.0;
+        t = HLLCQ_Korolkov_2D(Ls, Lu, Rs, Ru, 0.0, 0.0, n1, n2, Ps, Pu, PQ, rad);
+        break;
+    }
     default: return -1.0;
     }
     out[0] = Ps.x; out[1] = Pu.x; out[2] = Pu.y; out[3] = Ps.y;
+    return t;
+}
+
+/* A face with a passive scalar Q (QL, QR on the two sides).  which: 1 HLLC
+   (HLLC_2d_Korolkov_b_s, metod 2, W = 0, nul_potok = false, its PQ), 5
+   HLLCQ_Korolkov_2D.  out[5] = (mass, mom_z, mom_r, energy, PQ); returns the
+   face dt. */
+double ref_face_q(int which, const double* sL, const double* uL, const double* sR, const double* uR, double QL,
+                  double QR, double n1, double n2, double rad, double* out)
+{
+    double2 Ls = {sL[0], sL[1]}, Lu = {uL[0], uL[1]}, Rs = {sR[0], sR[1]}, Ru = {uR[0], uR[1]};
+    double2 Ps = {0, 0}, Pu = {0, 0};
+    double PQ = 0.0, t = 0.0;
+    if (which == 5) {
+        t = HLLCQ_Korolkov_2D(Ls, Lu, Rs, Ru, QL, QR, n1, n2, Ps, Pu, PQ, rad);
+        out[0] = Ps.x; out[1] = Pu.x; out[2] = Pu.y; out[3] = Ps.y;
+    } else if (which == 1) {
+        double P[4] = {0, 0, 0, 0}, Vl, Vc, Vp;
+        t = HLLC_2d_Korolkov_b_s(Ls.x, QL, Ls.y, Lu.x, Lu.y, Rs.x, QR, Rs.y, Ru.x, Ru.y, 0.0, P, PQ, n1, n2, rad, 2,
+                                 Vl, Vc, Vp, false);
+        out[0] = P[0]; out[1] = P[1]; out[2] = P[2]; out[3] = P[3];
+    } else {
+        return -1.0;
+    }
+    out[4] = PQ;
     return t;
 }
 

@@ -90,3 +90,22 @@ def add2_config(N=96, M=12):
     A.set_bc(c, A.R_HI, A.BC_REFLECT)
     c.body_force, c.body_lo, c.body_hi, c.body_rsplit, c.body_amp = 1, 20.000001, 30.000001, 0.5, 2.5
     return c
+
+
+def scalar_config(flux, N=48, M=24):
+    """A passive scalar carried by the HLLC (flux 1) or HLLCQ (flux 4) solver
+    on an axisymmetric 48x24 grid, z in [-1, 1], r in [0, 1], minmod: fixed
+    inflow (1, 1) (V_inf, 0) with scalar 2 at n = N-1, outflow at n = 0 and
+    r = y_max, axis reflection, cells inside z^2/0.04 + r^2/0.04 < 1 held
+    fixed; FP64."""
+    c = A.default_config()
+    c.N, c.M = N, M
+    c.x_min, c.x_max, c.y_max = -1.0, 1.0, 1.0
+    c.flux, c.recon, c.geom = flux, A.RECON_MINMOD, A.GEOM_AXISYM
+    A.set_bc(c, A.Z_HI, A.BC_FIXED, 1.0, 1.0, V_INF, 0.0)
+    A.set_bc(c, A.Z_LO, A.BC_OUTFLOW)
+    A.set_bc(c, A.R_HI, A.BC_OUTFLOW)
+    A.set_bc(c, A.R_LO, A.BC_REFLECT)
+    c.fixed_region, c.fixed_zc, c.fixed_az, c.fixed_ar = 1, 0.0, 0.2, 0.2
+    c.scalar_in = 2.0
+    return c

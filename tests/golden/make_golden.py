@@ -25,6 +25,17 @@ records their outputs on seeded inputs:
                  20 launches of add2 (kernel.cu:1928) + funk_time, method 0
                  and method 1 (the time-dependent inflow density), on a
                  96x12 grid with a random state;
+  faces_scalar.npz
+                 the passive-scalar solvers' fluxes (mass, momentum, energy,
+                 scalar) + dt on the face states of faces.npz with random
+                 scalars: the Q channel of HLLC_2d_Korolkov_b_s
+                 (Gas_Dinamic.cu:1604-1811, metod 2) and HLLCQ_Korolkov_2D
+                 (Gas_Dinamic.cu:249-353);
+  step_scalar_hllc.npz, step_scalar_hllcq.npz
+                 20 steps carrying a passive scalar on a 48x24 axisymmetric
+                 blast-like grid, every face evaluated by those reference
+                 functions (the reference's steps carry no scalar: the step
+                 loop and the update are the oracle's);
   writers.npz    the bytes of the files the reference's writers produce for a
                  random 24x12 state: print_file_mini (kernel.cu:3109-3173)
                  with every 2nd and every 3rd cell, and the end-of-run block of
@@ -32,7 +43,8 @@ records their outputs on seeded inputs:
                  file with T and Zav, the axis line, the run summary).
 
 The configurations that reproduce those kernels live in golden_configs.py so
-the tests use exactly the same ones.  Usage:  python tests/golden/make_golden.py [writers | add2]   (that fixture only)
+the tests use exactly the same ones.  Usage:
+python tests/golden/make_golden.py [writers | add2 | scalar]   (that fixture only)
 """
 import os
 import sys
@@ -125,6 +137,35 @@ def make_add2():
         make_step(f"step_add2_m{method}.npz", G.add2_config(), O.REF_ADD2, method, 20, rng)
 
 
+def make_scalar(rng):
+    cfg = G.face_config()
+    O.ref_set(cfg)
+    X = face_cases(rng)
+    Q = rng.uniform(0.0, 3.0, (len(X), 2))
+    normals = [(1.0, 0.0), (-1.0, 0.0), (0.0, 1.0), (0.0, -1.0)]
+    n = np.array([normals[i % 4] for i in range(len(X))])
+    rad = np.where(n[:, 0] != 0, 0.01, 0.02)
+    out = {}
+    for name, which in (("hllc", 1), ("hllcq", 5)):
+        F = np.zeros((len(X), 5))
+        T = np.zeros(len(X))
+        for i, row in enumerate(X):
+            T[i], F[i] = O.ref_face_q(which, row[0:2], row[2:4], row[4:6], row[6:8], Q[i, 0], Q[i, 1], n[i, 0],
+                                      n[i, 1], rad[i])
+        out[name + "_flux"] = F
+        out[name + "_dt"] = T
+    np.savez_compressed(os.path.join(HERE, "faces_scalar.npz"), states=X, scalars=Q, normals=n, rad=rad,
+                        gamma=cfg.gamma, cfl=cfg.cfl, **out)
+    for name, flux in (("hllc", 1), ("hllcq", 4)):
+        cfg = G.scalar_config(flux)
+        K = cfg.N * cfg.M
+        s, u = G.random_state(K, rng)
+        q = s[:, 0] * rng.uniform(0.5, 1.5, K)
+        s1, u1, q1, tdo, tt, st = O.run_scalar(cfg, s, u, q, 20, use_ref=True)
+        np.savez_compressed(os.path.join(HERE, f"step_scalar_{name}.npz"), s0=s, u0=u, q0=q, s=s1, u=u1, q=q1,
+                            T_do=tdo, TT=tt, steps=st, nsteps=20)
+
+
 def make_writers(rng):
     import tempfile
     cfg = G.writer_config()
@@ -159,6 +200,10 @@ def main():
         make_add2()
         print("add2 fixtures written to", HERE)
         return
+    if sys.argv[1:] == ["scalar"]:
+        make_scalar(np.random.default_rng(249))
+        print("scalar fixtures written to", HERE)
+        return
     rng = np.random.default_rng(20261203)
     make_faces(rng)
     make_step("step_tvd.npz", G.tvd_config(), O.REF_KERNEL_TVD, 1, 20, rng)
@@ -169,6 +214,7 @@ def main():
     make_neutral(np.random.default_rng(2495))
     make_writers(np.random.default_rng(3109))
     make_add2()
+    make_scalar(np.random.default_rng(249))
     print("golden vectors written to", HERE)
 
 
