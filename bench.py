@@ -452,7 +452,51 @@ def time_e2e(form, start, steps, torch, params=None, mode="chain"):
     return dt, 2 * K * 16, 2 * K * 16
 
 
-def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32, tune_at=200):
+def batch_modes(torch, nprob=64, seed=64, steps=96, pre=16):
+    """The batch's schedules side by side, each from the initial states after
+    `pre` steps, CUDA events over `steps` steps: each class's problems alone
+    with one CTA per 32x16 tile, with the persistent class kernel and with the
+    persistent one-launch kernel; all problems as two launches (both
+    schedules) and as one launch (modes 1 and 2).  ms per step."""
+    from asteriy_2d_gb300 import abi as A
+    from asteriy_2d_gb300 import solver
+    probs = solver.problem_set(seed, nprob, A.PREC_FP32)
+    init = [solver.problem_fill(p) for p in probs]
+
+    def run(idx, sched=None, mixed=0):
+        stream = torch.cuda.Stream()
+        with solver.Batch([probs[i].cfg for i in idx], stream=stream.cuda_stream) as B:
+            for k, i in enumerate(idx):
+                B.set_state(k, *init[i])
+            if mixed:
+                B.set_mixed(mixed)
+            else:
+                for c in range(B.info()["launches_per_step"]):
+                    B.set_schedule(c, sched)
+            B.step(pre)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            B.step(steps, sync=False)
+            e1.record(stream)
+            B.synchronize()
+            return round(e0.elapsed_time(e1) / steps, 4)
+
+    out = {}
+    for name, flux in (("hllc", A.FLUX_HLLC), ("godunov", A.FLUX_GODUNOV)):
+        idx = [i for i, p in enumerate(probs) if p.cfg.flux == flux]
+        out[name] = {"problems": len(idx), "cells": sum(probs[i].cfg.N * probs[i].cfg.M for i in idx),
+                     "per_tile_32x16_ms": run(idx, sched=0), "persistent_ms": run(idx, sched=solver.PERSISTENT),
+                     "one_launch_persistent_ms": run(idx, mixed=2)}
+    idx = list(range(nprob))
+    out["all"] = {"two_launches_per_tile_32x16_ms": run(idx, sched=0),
+                  "two_launches_persistent_ms": run(idx, sched=solver.PERSISTENT),
+                  "one_launch_per_tile_ms": run(idx, mixed=1), "one_launch_persistent_ms": run(idx, mixed=2)}
+    out["note"] = "ms per step over %d steps after %d, from the seeded initial states" % (steps, pre)
+    return out
+
+
+def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32, tune_at=200, mixed=None):
     """The batched form: the seeded set of nprob problems (ast_problem_set:
     128x64 .. 1024x512, blast or wind, HLLC or exact Godunov, gamma 5/3 or
     1.4, Mach 1.5-6), FP32, all advanced together by ast_batch_step.  The
@@ -476,6 +520,9 @@ def time_batch(steps, warmup, torch, nprob=64, seed=64, solo_steps=32, tune_at=2
         # tune_at steps (the tuner leaves the state and clocks as they were)
         B.step(tune_at)
         classes = B.autotune(10)
+        if mixed is not None:
+            # a one-launch mode forced over the tuner's choice (profiling)
+            B.set_mixed(mixed)
         one_launch = B.mixed()
         info = B.info()
         B.step(warmup)
@@ -782,6 +829,10 @@ def main():
     ap.add_argument("--per-tile", action="store_true", help="FP32 forms with one CTA per tile, not the persistent kernel")
     ap.add_argument("--fp32-kernel", type=int, default=1, choices=[0, 1, 2],
                     help="FP32 step kernel: 1 persistent tile kernel, 0 one CTA per tile, 2 strip kernel")
+    ap.add_argument("--batch-modes", action="store_true",
+                    help="time the batch's schedules and one-launch modes side by side")
+    ap.add_argument("--batch-mixed", type=int, default=None, choices=[0, 1, 2],
+                    help="force the batch leg's one-launch mode (0 two launches, 1 a CTA per tile, 2 persistent)")
     ap.add_argument("--phase-clocks", action="store_true",
                     help="report the persistent kernel's cycles per phase (library built with AST_PHASE_CLOCKS=1)")
     args = ap.parse_args()
@@ -914,8 +965,10 @@ def main():
     if PHASES:
         line["phase_clocks"] = phase_breakdown(PHASES)
     if rank == 0 and args.batch_steps:
-        line["batch"] = time_batch(args.batch_steps, args.warmup, torch)
+        line["batch"] = time_batch(args.batch_steps, args.warmup, torch, mixed=args.batch_mixed)
         line["gpu_launches_batch_step"] = line["batch"]["launches_per_step"]
+    if rank == 0 and args.batch_modes:
+        line["batch_modes"] = batch_modes(torch)
     if rank == 0 and args.accuracy_steps:
         acc = accuracy(args.accuracy_steps, params, torch)
         line["accuracy_vs_fp64"] = acc
