@@ -1711,6 +1711,7 @@ struct __align__(16) BatchTile {
     DevClock* clock;
     long long rsv2_;
 };
+static_assert(sizeof(BatchTile) == 32, "a work-list entry is two 16-byte copies");
 
 // One run of consecutive tiles of one problem, reported by every warp
 // without a barrier: the warp's wave-speed maxima (atomic maxima on the

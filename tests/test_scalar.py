@@ -196,3 +196,4 @@ def test_scalar_rejections():
         assert e.value.code == A.AST_ERR_UNSUPPORTED
         S.set_scalar(None)
         S.step_host(*args)
+
