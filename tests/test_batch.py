@@ -360,3 +360,29 @@ def test_one_launch_mode_with_learned_guess():
             (s, u), clk, st = run[i]
             (rs, ru), rclk, rst = out[2][i]
             assert np.array_equal(s, rs) and np.array_equal(u, ru) and clk == rclk and st == rst, i
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["persistent", "one_launch"])
+def test_persistent_batch_single_and_tiny_problems(mode):
+    """The persistent batch kernel on edge cases of its work list: a batch of
+    one problem, and a problem of a single tile beside a larger one (more
+    CTAs claim than there are tiles; the last CTA to leave shifts every
+    clock and rewinds the counter), stepped over several graph blocks."""
+    probs = small_set(A.PREC_FP32, n=2)
+    probs[1].cfg.N, probs[1].cfg.M = 20, 10        # one 32x16 tile
+    for cfgs_idx in ([0], [0, 1], [1]):
+        cfgs = [probs[i].cfg for i in cfgs_idx]
+        init = [solver.problem_fill(probs[i]) for i in cfgs_idx]
+        with solver.Batch(cfgs) as B:
+            if mode == "persistent":
+                for k in range(B.info()["launches_per_step"]):
+                    B.set_schedule(k, solver.PERSISTENT)
+            else:
+                B.set_mixed(2)
+            for i, (s0, u0) in enumerate(init):
+                B.set_state(i, s0, u0)
+            B.step(37)
+            for i, c in enumerate(cfgs):
+                rs, ru, rclock = single_run(c, *init[i], 37)
+                assert_agree(A.PREC_FP32, B.get_state(i), (rs, ru), B.clock(i), rclock, (mode, cfgs_idx, i))
