@@ -446,7 +446,8 @@ int ast_batch_num_classes(ast_batch* batch);
  * tile with tiles of 32x16, 16x16 or 64x8 (z x r) cells; 3 = the persistent
  * batch kernel (FP32 only; the class's tiles of 32x16 staged and stored by
  * bulk-tensor copies, the default for FP32 batches; FP64 batches default to
- * 0); 4 = the single-problem persistent kernel once per problem, each
+ * 0; the last CTA of each launch shifts every problem's dt); 4 = the
+ * single-problem persistent kernel once per problem, each
  * problem its own chain of launches in the step graph (FP32 only).
  * ast_batch_autotune times every schedule on every class, `trials` steps
  * each on the current state (each trial reads the current time level and
