@@ -85,11 +85,15 @@ int ast::encode_planes(CUtensorMap* map, void* base, const ast_config& c, long l
             return fail(AST_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled not available");
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
+    // FP32 or FP64 state planes
+    const bool f64 = c.precision == AST_PREC_FP64;
+    const size_t es = f64 ? sizeof(double) : sizeof(float);
     const cuuint64_t dim[3] = {(cuuint64_t)c.N, (cuuint64_t)c.M, 4};
-    const cuuint64_t stride[2] = {(cuuint64_t)ld * sizeof(float), (cuuint64_t)plane * sizeof(float)};
+    const cuuint64_t stride[2] = {(cuuint64_t)ld * es, (cuuint64_t)plane * es};
     const cuuint32_t box[3] = {bx, by, 4};
     const cuuint32_t estride[3] = {1, 1, 1};
-    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dim, stride, box, estride,
+    CUresult r = encode(map, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dim,
+                        stride, box, estride,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? AST_OK : fail(AST_ERR_CUDA, "cuTensorMapEncodeTiled failed");
@@ -205,15 +209,24 @@ int ast_create(const ast_config* cfg, ast_solver** out)
             S->sweep = true;
         }
     }
-    if (rc == AST_OK && S->elem == 4 && cfg->persistent && !want_sweep) {
+    // FP64: the persistent kernel for the HLL family on grids of at least
+    // two 32x16 tiles per SM (smaller grids step with one CTA per tile of
+    // 16x16).  The exact solver keeps one CTA per tile: with its FP64
+    // bisections the persistent kernel measured 8% slower (11.32 against
+    // 10.44 ms per step at step 1000 of the 4096x2048 blast; HLL 4.79
+    // against 5.20 ms).
+    const long long tiles32 = (long long)((cfg->N + kTZ - 1) / kTZ) * ((cfg->M + kTR - 1) / kTR);
+    const bool tma64 = S->elem == 8 && cfg->flux != AST_FLUX_GODUNOV && tiles32 >= 2LL * sm_count();
+    if (rc == AST_OK && (S->elem == 4 || tma64) && cfg->persistent && !want_sweep) {
         // box loads of tile + halo (TZ+8 x TR+4), stores of the tile (TZ x TR)
         for (int b = 0; b < 2 && rc == AST_OK; b++) {
             rc = encode_planes(&S->tin[b], S->buf[b], *cfg, S->ld, S->plane, kTZ + 8, kTR + 4);
             if (rc == AST_OK) rc = encode_planes(&S->tout[b], S->buf[b], *cfg, S->ld, S->plane, kTZ, kTR);
         }
         int per_sm = 0, dev = 0, sms = 0;
-        if (rc == AST_OK) rc = launch_step_tma(S->P, S->tin[0], S->tout[1], cfg->flux, cfg->recon, 0, nullptr, false,
-                                               &per_sm);
+        if (rc == AST_OK)
+            rc = launch_step_tma_e(S->elem, S->P, S->tin[0], S->tout[1], cfg->flux, cfg->recon, 0, nullptr, false,
+                                   &per_sm);
         if (rc == AST_OK && (e = cudaGetDevice(&dev)) != cudaSuccess) rc = cuda_fail(e, "cudaGetDevice");
         if (rc == AST_OK && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
             rc = cuda_fail(e, "cudaDeviceGetAttribute");
@@ -452,8 +465,8 @@ static int enqueue_one(ast_solver* S)
     if (S->sweep)
         rc = launch_step_sweep(P, S->cfg.flux, S->cfg.recon, S->sweep_grid, S->stream, true, nullptr);
     else if (S->tma)
-        rc = launch_step_tma(P, S->tin[S->cur], S->tout[S->cur ^ 1], S->cfg.flux, S->cfg.recon, S->tma_grid,
-                             S->stream, true, nullptr);
+        rc = launch_step_tma_e(S->elem, P, S->tin[S->cur], S->tout[S->cur ^ 1], S->cfg.flux, S->cfg.recon,
+                               S->tma_grid, S->stream, true, nullptr);
     else
         rc = (S->elem == 8) ? launch_step_r<double, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true)
                             : launch_step_r<float, kSoA>(P, S->cfg.flux, S->cfg.recon, S->stream, true);
@@ -672,8 +685,8 @@ static int host_steps(ast_solver* S, int nsteps, double* s_a, double* u_a, doubl
                 // each band hands out its tiles from a counter set to zero
                 P.units = units;
                 if (b > 0) AST_CUDA(cudaMemsetAsync(&S->clock->next_tile, 0, sizeof(unsigned int), cst));
-                rc = launch_step_tma(P, S->tin[S->cur], S->tout[S->cur ^ 1], S->cfg.flux, S->cfg.recon,
-                                     std::min((bd[b].t1 - bd[b].t0) * tiles_z, S->tma_grid), cst, true, nullptr);
+                rc = launch_step_tma_e(S->elem, P, S->tin[S->cur], S->tout[S->cur ^ 1], S->cfg.flux, S->cfg.recon,
+                                       std::min((bd[b].t1 - bd[b].t0) * tiles_z, S->tma_grid), cst, true, nullptr);
             } else {
                 rc = (S->elem == 8) ? launch_step_r<double, kSoA>(P, S->cfg.flux, S->cfg.recon, cst, true)
                                     : launch_step_r<float, kSoA>(P, S->cfg.flux, S->cfg.recon, cst, true);

@@ -92,18 +92,19 @@ int launch_step_t(const StepParams& P, cudaStream_t st, bool launch)
     return e == cudaSuccess ? AST_OK : cuda_fail(e, "step kernel launch");
 }
 
-// the persistent FP32 kernel over `grid` CTAs; launch=false raises its
-// shared-memory limit and returns the CTAs per SM it reaches in *per_sm
-template <int FLUX, bool RECON>
+// the persistent kernel (FP32 or FP64 state planes) over `grid` CTAs;
+// launch=false raises its shared-memory limit and returns the CTAs per SM it
+// reaches in *per_sm
+template <typename R, int FLUX, bool RECON>
 int launch_tma_t(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int grid, cudaStream_t st,
                  bool launch, int* per_sm)
 {
     // two variants: with the uniform-tile test (skip_uniform) and without it
-    auto k = P.skip_uniform ? step_kernel_tma<FLUX, RECON, true> : step_kernel_tma<FLUX, RECON, false>;
-    constexpr size_t smem = tile_smem_bytes<float, FLUX, 32, 16, 2>();
+    auto k = P.skip_uniform ? step_kernel_tma<R, FLUX, RECON, true> : step_kernel_tma<R, FLUX, RECON, false>;
+    constexpr size_t smem = tile_smem_bytes<R, FLUX, 32, 16, 2>();
     cudaError_t e;
     if (!launch) {
-        for (auto kv : {step_kernel_tma<FLUX, RECON, true>, step_kernel_tma<FLUX, RECON, false>}) {
+        for (auto kv : {step_kernel_tma<R, FLUX, RECON, true>, step_kernel_tma<R, FLUX, RECON, false>}) {
             e = cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
         }
@@ -117,6 +118,16 @@ int launch_tma_t(const StepParams& P, const CUtensorMap& tin, const CUtensorMap&
 
 int launch_step_tma(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int flux, int recon,
                     int grid, cudaStream_t st, bool launch, int* per_sm);
+// the same for FP64 state planes (the FP64 solver on grids of at least two
+// 32x16 tiles per SM)
+int launch_step_tma64(const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout, int flux, int recon,
+                      int grid, cudaStream_t st, bool launch, int* per_sm);
+inline int launch_step_tma_e(size_t elem, const StepParams& P, const CUtensorMap& tin, const CUtensorMap& tout,
+                             int flux, int recon, int grid, cudaStream_t st, bool launch, int* per_sm)
+{
+    return elem == 8 ? launch_step_tma64(P, tin, tout, flux, recon, grid, st, launch, per_sm)
+                     : launch_step_tma(P, tin, tout, flux, recon, grid, st, launch, per_sm);
+}
 
 // the FP32 strip kernel over `grid` CTAs; launch=false returns the CTAs per
 // SM it reaches in *per_sm

@@ -1627,11 +1627,10 @@ __global__ void __launch_bounds__(kThreads, min_ctas<R, 2>())
 // once (one ticket per CTA).  A bulk copy that does not arrive within the
 // wait limit (P.wait_polls) sets AST_ST_TIMEOUT and is waited for with the
 // long limit; one that does not arrive even then ends the CTA's loop.
-template <int FLUX, bool RECON, bool SKIP>
-__global__ void __launch_bounds__(kThreads, 4)
+template <typename R, int FLUX, bool RECON, bool SKIP>
+__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 4 : 2)
     step_kernel_tma(StepParams P, const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout)
 {
-    using R = float;
     constexpr int TZ = 32, TR = 16;
     using S = TileSmem<R, FLUX, TZ, TR, 2>;
     constexpr uint32_t kBoxBytes = 4u * S::HR * S::HZP * sizeof(R);
@@ -1673,7 +1672,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     phase_mark(kPhaseStart);
     TileAcc<R> acc;
     acc.clear();
-    const Gas<R>& g = P.gf;
+    const Gas<R>& g = gas_of<R>(P);
     for (int k = 0;; k++) {
         const int b = k & 1;
         const int t = s_tile[b];

@@ -143,8 +143,10 @@ typedef struct ast_config {
        1 = the persistent tile kernel (tiles staged and stored by
        bulk-tensor copies, double-buffered; the learned start value by f16
        tensor-core tiles); 0 = one CTA per tile.  The same arithmetic per
-       face and cell; the FP64 solver and the raw entry points always use
-       one CTA per tile (default 1)                                          */
+       face and cell.  The FP64 solver with 1 runs the persistent tile
+       kernel for the HLL family on grids of at least two 32x16 tiles per
+       SM, one CTA per tile otherwise (the exact solver: one CTA per tile);
+       the raw entry points always use one CTA per tile (default 1)         */
     int32_t persistent;
     /* 1: tiles whose staged cells (tile and two-cell halo, ghosts included)
        all hold the same four values, bit for bit, skip the face pass: every
