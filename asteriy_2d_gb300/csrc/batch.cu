@@ -166,7 +166,7 @@ int launch_class(ast_batch* B, BatchClass& c, int shape, cudaStream_t st, bool l
             BATCH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
             for (int s = c.first; s < c.first + c.count; s++) {
                 const StepParams& P = B->hPp[0][s];
-                const int tiles = ((P.N + kShapeTZ[0] - 1) / kShapeTZ[0]) * ((P.M + kShapeTR[0] - 1) / kShapeTR[0]);
+                const int tiles = ((P.N + kTmaTZ - 1) / kTmaTZ) * ((P.M + kTmaTR - 1) / kTmaTR);
                 B->pgrid[s] = std::min(tiles, std::max(per_sm, 1) * sms);
             }
             return AST_OK;
@@ -432,10 +432,10 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
                 void* lin = base + (par ? B->level_bytes[i] : 0);
                 void* lout = base + (par ? 0 : B->level_bytes[i]);
                 rc = encode_planes(&maps[(size_t)(2 * par) * nprob + sl], lin, B->cfg[i], B->ld[i], B->plane[i],
-                                   kShapeTZ[0] + 8, kShapeTR[0] + 4);
+                                   kTmaTZ + 8, kTmaTR + 4);
                 if (rc == AST_OK)
                     rc = encode_planes(&maps[(size_t)(2 * par + 1) * nprob + sl], lout, B->cfg[i], B->ld[i],
-                                       B->plane[i], kShapeTZ[0], kShapeTR[0]);
+                                       B->plane[i], kTmaTZ, kTmaTR);
             }
         }
         B->hmaps = maps;
@@ -448,13 +448,14 @@ int ast_batch_create(const ast_config* cfgs, int nprob, ast_batch** out)
                 const ast_config& c = B->cfg[order[s]];
                 const int fk = (c.flux == AST_FLUX_HLL) ? 0 : (c.flux == AST_FLUX_HLLC) ? 1
                                                           : (c.flux == AST_FLUX_HLLC_A) ? 3 : 2;
-                const int tz = (c.N + kShapeTZ[0] - 1) / kShapeTZ[0], nt = tiles_of(c, 0);
+                const int tz = (c.N + kTmaTZ - 1) / kTmaTZ;
+                const int nt = tz * ((c.M + kTmaTR - 1) / kTmaTR);
                 for (int t = 0; t < nt; t++) {
                     BatchTile e;
                     std::memset(&e, 0, sizeof e);
                     e.sf = s | (fk << 24);
-                    e.n0 = (t % tz) * kShapeTZ[0];
-                    e.m0 = (t / tz) * kShapeTR[0];
+                    e.n0 = (t % tz) * kTmaTZ;
+                    e.m0 = (t / tz) * kTmaTR;
                     e.clock = B->clocks + order[s];
                     work.push_back(e);
                 }

@@ -20,6 +20,7 @@
 namespace ast {
 
 constexpr int kTZ = 32, kTR = 16;
+static_assert(kTZ == kTmaTZ && kTR == kTmaTR, "the persistent kernels' tile is the solver's tile");
 
 // records the failure text for ast_last_error() and returns AST_ERR_CUDA
 int cuda_fail(cudaError_t e, const char* what);
@@ -101,7 +102,7 @@ int launch_tma_t(const StepParams& P, const CUtensorMap& tin, const CUtensorMap&
 {
     // two variants: with the uniform-tile test (skip_uniform) and without it
     auto k = P.skip_uniform ? step_kernel_tma<R, FLUX, RECON, true> : step_kernel_tma<R, FLUX, RECON, false>;
-    constexpr size_t smem = tile_smem_bytes<R, FLUX, 32, 16, 2>();
+    constexpr size_t smem = tile_smem_bytes<R, FLUX, kTmaTZ, kTmaTR, 2>();
     cudaError_t e;
     if (!launch) {
         for (auto kv : {step_kernel_tma<R, FLUX, RECON, true>, step_kernel_tma<R, FLUX, RECON, false>}) {
@@ -167,7 +168,7 @@ int launch_batch_tma_t(const StepParams* Ps, const CUtensorMap* tin, const CUten
                        cudaStream_t st, bool launch, int* per_sm)
 {
     auto k = batch_kernel_tma<FLUX, RECON, MIXED>;
-    constexpr size_t smem = tile_smem_bytes<float, MIXED ? 2 : FLUX, 32, 16, 2>();
+    constexpr size_t smem = tile_smem_bytes<float, MIXED ? 2 : FLUX, kTmaTZ, kTmaTR, 2>();
     cudaError_t e;
     if (!launch) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -31,6 +31,10 @@ constexpr int kThreads = 256;
 // of the last warp (in the face pass the first two warps take one face more
 // than the others)
 constexpr int kCopyThread = kThreads - 32;
+// the persistent kernels' tile, z x r cells: their shared-memory buffers are
+// the boxes of the tensor maps the host encodes (TZ + 8 x TR + 4 cells
+// loaded, TZ x TR stored), so every encoder of those maps takes these
+constexpr int kTmaTZ = 32, kTmaTR = 16;
 
 // device-resident clock and counters of a solver (one per solver)
 struct DevClock {
@@ -1631,7 +1635,7 @@ template <typename R, int FLUX, bool RECON, bool SKIP>
 __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 4 : 2)
     step_kernel_tma(StepParams P, const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout)
 {
-    constexpr int TZ = 32, TR = 16;
+    constexpr int TZ = kTmaTZ, TR = kTmaTR;
     using S = TileSmem<R, FLUX, TZ, TR, 2>;
     constexpr uint32_t kBoxBytes = 4u * S::HR * S::HZP * sizeof(R);
     static_assert(sizeof(((S*)nullptr)->qb[0]) == kBoxBytes, "tile buffer is the TMA box");
@@ -1850,7 +1854,7 @@ __global__ void __launch_bounds__(kThreads, 4)
                      int nslots, unsigned int* counter, int wait_polls)
 {
     using R = float;
-    constexpr int TZ = 32, TR = 16;
+    constexpr int TZ = kTmaTZ, TR = kTmaTR;
     using S = TileSmem<R, MIXED ? 2 : FLUX, TZ, TR, 2>;
     constexpr uint32_t kBoxBytes = 4u * S::HR * S::HZP * sizeof(R);
     constexpr uint32_t kParBytes = sizeof(StepParams);
