@@ -314,6 +314,7 @@ struct TileCore {
     unsigned qn;                 // queued faces: above the gate (low 16 bits), others (high 16 bits)
     double ydrow[TR];            // r of the tile's cell rows, y_min + m dy, in FP64
     float yfrow[TR];             // and in FP32
+    double tydrow[TR];           // T_do / r of the rows (axisymmetric grid; FP64 kernels)
 };
 
 // the exact solver's queue: faces as 16-bit codes (face index | active <<
@@ -1238,8 +1239,16 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
     // orders these writes before their use)
     if (threadIdx.x < TR) {
         const int m = m0 + threadIdx.x;
-        sm.ydrow[threadIdx.x] = P.y_min + m * P.dy;
-        sm.yfrow[threadIdx.x] = P.y_minf + (float)m * P.dyf;
+        const double yd = P.y_min + m * P.dy;
+        const float yf = P.y_minf + (float)m * P.dyf;
+        sm.ydrow[threadIdx.x] = yd;
+        sm.yfrow[threadIdx.x] = yf;
+        // FP64 kernels: the axisymmetric source's T_do / r once per row, not
+        // once per cell (the same expression, the same values).  Not in
+        // FP32: there the division per cell is a reciprocal and a multiply,
+        // cheaper than an FP64 division at every tile's start, and the FP32
+        // persistent batch kernel sets K only during the face pass.
+        if constexpr (sizeof(R) == 8) sm.tydrow[threadIdx.x] = (P.geom == 1) ? K.T_do / yd : 0.0;
     }
     // SKIP: the kernel carries the uniform-tile test (skip_uniform); the
     // persistent kernel has a variant without it, so that the default path
@@ -1319,7 +1328,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
             Sz = w * az;
             Sr = w * ar;
         }
-        const double ty = (P.geom == 1) ? T_do / y : 0.0;
+        const double ty = (sizeof(R) == 8) ? sm.tydrow[row] : ((P.geom == 1) ? T_do / y : 0.0);
         update_cell<double>(P, P.gd.ga, P.gd.g1, P.gd.inv_g1, in, f, T_do, tdv_d, ty, P.dx, P.dy, Q2, Sz, Sr,
                             acc.nrho, acc.np, acc.rc.status, o);
     };
