@@ -131,6 +131,26 @@ __device__ __forceinline__ R flux_hll(const Gas<R>& g, R rL, R pL, R unL, R utL,
     return S;
 }
 
+// ------------------------------------------------------------------ identical states
+// The HLL and HLLC fluxes of a face whose two sides hold one state (r, p,
+// un, ut), r > 0, p > 0: the physical flux of that state, which their
+// formulas reach up to rounding (and exactly on supersonic faces, with these
+// expressions), and the wave speed they return, max(|un - c|, |un + c|)
+// with c = sqrt(ga p / r), formed as they form it.
+template <typename R>
+__device__ __forceinline__ R flux_physical(const Gas<R>& g, R r, R p, R un, R ut, R F[4])
+{
+    const R c = sqrt(g.ga * p / r);
+    const R SL = un - c, SR = un + c;
+    const R e = p * g.inv_g1 + r * (un * un + ut * ut) * R(0.5);
+    const R m = r * un;
+    F[0] = m;
+    F[1] = m * un + p;
+    F[2] = m * ut;
+    F[3] = (e + p) * un;
+    return fmax(fabs(SL), fabs(SR));
+}
+
 // ------------------------------------------------------------------ HLL, two faces in packed FP32
 // Two independent HLL faces (.x and .y) with each add, multiply and fused
 // multiply-add on the pair issued as one packed FP32 instruction (FADD2,

@@ -678,7 +678,25 @@ __device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<
     constexpr int TT = ZF ? 3 : 2;           // tangential velocity component
     R F[4];
     R Sp;
-    if constexpr (FLUX == 2) {
+    // FP64, the HLL or HLLC flux, the faces of every active lane of the warp
+    // with one state (one bit pattern, rho > 0, p > 0) on both sides
+    // (undisturbed gas): that state's physical flux (flux_physical; the
+    // solvers' formulas give it up to rounding) for two divisions, two square
+    // roots and the star-state arithmetic.  A warp vote, so that warps with
+    // other faces run as before; bit tests, not FP64 compares (this GPU's
+    // FP64 pipe is slow).
+    bool same = false;
+    if constexpr (sizeof(R) == 8 && FLUX != 2) {
+        const bool eq = (FLUX == 0 || FLUX == 1 || !hi) && same_bits(L[0], U[0]) && same_bits(L[1], U[1]) &&
+                        same_bits(L[2], U[2]) && same_bits(L[3], U[3]) && __double_as_longlong(L[0]) > 0 &&
+                        __double_as_longlong(L[1]) > 0;
+        if (__all_sync(__activemask(), eq)) {
+            Sp = flux_physical(g, L[0], L[1], L[NN], L[TT], F);
+            same = true;
+        }
+    }
+    if (same) {
+    } else if constexpr (FLUX == 2) {
         if (!active) {
             // no updated cell uses this face (both cells outside the grid or
             // held fixed): not solved, so the solver's counters see the same
