@@ -834,11 +834,27 @@ __device__ __forceinline__ void face_two(const StepParams& P, S& sm, int b, cons
         }
     }
     if constexpr (FLUX == 0 && sizeof(R) == 4) {
-        // HLL in FP32: both faces in packed arithmetic
+        // HLL in FP32: both faces in packed arithmetic; or, when both faces
+        // of every active lane of the warp hold one state on all four sides
+        // (one bit pattern, rho > 0, p > 0: undisturbed gas), that state's
+        // physical flux once for both (flux_physical: what the HLL formula
+        // gives up to rounding, its wave speed formed as the formula forms it)
         constexpr int NN = ZF ? 2 : 3, TT = ZF ? 3 : 2;
         float2 F[4], Sp;
-        flux_hll_x2(g, pk(L0[0], L1[0]), pk(L0[1], L1[1]), pk(L0[NN], L1[NN]), pk(L0[TT], L1[TT]), pk(U0[0], U1[0]),
-                    pk(U0[1], U1[1]), pk(U0[NN], U1[NN]), pk(U0[TT], U1[TT]), F, Sp);
+        bool one = two && __float_as_int(L0[0]) > 0 && __float_as_int(L0[1]) > 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            one = one && same_bits(L0[k], U0[k]) && same_bits(L0[k], L1[k]) && same_bits(L0[k], U1[k]);
+        if (__all_sync(__activemask(), one)) {
+            float f[4];
+            const float s = flux_physical(g, L0[0], L0[1], L0[NN], L0[TT], f);
+#pragma unroll
+            for (int k = 0; k < 4; k++) F[k] = pk(f[k], f[k]);
+            Sp = pk(s, s);
+        } else {
+            flux_hll_x2(g, pk(L0[0], L1[0]), pk(L0[1], L1[1]), pk(L0[NN], L1[NN]), pk(L0[TT], L1[TT]),
+                        pk(U0[0], U1[0]), pk(U0[1], U1[1]), pk(U0[NN], U1[NN]), pk(U0[TT], U1[TT]), F, Sp);
+        }
         auto store = [&](int fa, int fc, bool act, float f0, float f1, float f2, float f3, float sp) {
             if (!(sp == sp)) { rc.status |= 0x10u; sp = 0.0f; }
             if (ZF) put4(sm.Fz[fa][fc], f0, f1, f2, f3);
