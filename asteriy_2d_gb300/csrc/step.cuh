@@ -586,9 +586,10 @@ __device__ __forceinline__ bool same_bits(double a, double b)
 // the minmod arithmetic, the same bits.  (At step 1000 of the 4096x2048
 // blast about nine faces in ten are such: the exact-solver step 0.189 ->
 // 0.175 ms in FP32, 11.45 -> 10.44 ms in FP64; where the gas is disturbed
-// everywhere the test costs about 5%.)
+// everywhere the test costs about 5%.)  Returns whether the warp took
+// that path (then the two sides of every lane's face are equal).
 template <typename R, bool RECON, bool ZF, typename S>
-__device__ __forceinline__ void face_states(const StepParams& P, const S& sm, int b, int a, int c, bool hi, R L[4],
+__device__ __forceinline__ bool face_states(const StepParams& P, const S& sm, int b, int a, int c, bool hi, R L[4],
                                             R U[4])
 {
     constexpr int DJ = ZF ? 0 : 1, DI = ZF ? 1 : 0, QX = S::QX;
@@ -616,6 +617,10 @@ __device__ __forceinline__ void face_states(const StepParams& P, const S& sm, in
         if (__all_sync(__activemask(), flat)) {
 #pragma unroll
             for (int k = 0; k < 4; k++) L[k] = tl[k] + R(0);
+            // (the positivity rule below leaves equal sides equal)
+            if (L[0] <= R(0)) L[0] = tl[0];
+            if (L[1] <= R(0) || !P.grad_p) L[1] = tl[1];
+            return true;
         } else {
 #pragma unroll
             for (int k = 0; k < 4; k++) {
@@ -632,6 +637,7 @@ __device__ __forceinline__ void face_states(const StepParams& P, const S& sm, in
         if (L[1] <= R(0) || !P.grad_p) L[1] = tl[1];
         if (U[1] <= R(0) || !P.grad_p) U[1] = tu[1];
     }
+    return false;
 }
 
 // Whether face (a, c) of orientation ZF belongs to an updated cell
@@ -670,7 +676,8 @@ __device__ __forceinline__ void face_meta(const StepParams& P, const S& sm, int 
 // Exact-solver faces of patterns 2 and 3 go to the queue instead.
 template <typename R, int FLUX, int TZ, int TR, bool ZF, typename S>
 __device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<R>& g, int a, int c, bool active,
-                                          bool hi, const R L[4], const R U[4], RiemannCount& rc, R& smax)
+                                          bool hi, const R L[4], const R U[4], RiemannCount& rc, R& smax,
+                                          bool same_sides = false)
 {
     constexpr int NFZ = TR * (TZ + 1);
     constexpr int W = ZF ? TZ + 1 : TZ;      // faces per row of the face array
@@ -703,7 +710,7 @@ __device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<
             // faces however the tile was staged
             F[0] = F[1] = F[2] = F[3] = R(0);
             Sp = R(0);
-        } else if (hi && L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]) {
+        } else if (hi && (same_sides || (L[0] == U[0] && L[1] == U[1] && L[2] == U[2] && L[3] == U[3]))) {
             // identical states: the exact solution is that state (the
             // reference reaches it through the two-rarefaction branch with
             // p* = p, u* = u_n, up to rounding), its flux the physical flux
@@ -888,8 +895,8 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
     bool active, hi;
     face_meta<TZ, TR, ZF>(P, sm, n0, m0, interior, a, c, active, hi);
     R L[4], U[4];
-    face_states<R, RECON, ZF>(P, sm, b, a, c, hi, L, U);
-    face_flux<R, FLUX, TZ, TR, ZF>(P, sm, g, a, c, active, hi, L, U, rc, smax);
+    const bool same = face_states<R, RECON, ZF>(P, sm, b, a, c, hi, L, U);
+    face_flux<R, FLUX, TZ, TR, ZF>(P, sm, g, a, c, active, hi, L, U, rc, smax, same);
 }
 
 // every face of the tile once, in one loop over the CTA's threads.
