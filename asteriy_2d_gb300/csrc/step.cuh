@@ -571,6 +571,9 @@ __device__ __forceinline__ void record_face(const StepParams& P, const Gas<R>& g
 // ------------------------------------------------------------------ face passes
 // bitwise equality of two staged values
 __device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
+// a > 0 or a positive NaN, on the bit pattern
+__device__ __forceinline__ bool positive_bits(float a) { return __float_as_int(a) > 0; }
+__device__ __forceinline__ bool positive_bits(double a) { return __double_as_longlong(a) > 0; }
 __device__ __forceinline__ bool same_bits(double a, double b)
 {
     return __double_as_longlong(a) == __double_as_longlong(b);
@@ -695,8 +698,8 @@ __device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<
     bool same = false;
     if constexpr (sizeof(R) == 8 && FLUX != 2) {
         const bool eq = (FLUX == 0 || FLUX == 1 || !hi) && same_bits(L[0], U[0]) && same_bits(L[1], U[1]) &&
-                        same_bits(L[2], U[2]) && same_bits(L[3], U[3]) && __double_as_longlong(L[0]) > 0 &&
-                        __double_as_longlong(L[1]) > 0;
+                        same_bits(L[2], U[2]) && same_bits(L[3], U[3]) && positive_bits(L[0]) &&
+                        positive_bits(L[1]);
         if (__all_sync(__activemask(), eq)) {
             Sp = flux_physical(g, L[0], L[1], L[NN], L[TT], F);
             same = true;
@@ -771,7 +774,7 @@ __device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<
 // once, so the cell between the two faces is reconstructed once for both
 // (minmod, linear2 and the positivity rule as face_states applies them, the
 // same values).  Z faces take c even and load the cells as aligned pairs.
-template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF, typename S>
+template <typename R, int FLUX, bool RECON, int TZ, int TR, bool ZF, bool FF = false, typename S>
 __device__ __forceinline__ void face_two(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
                                          bool interior, RiemannCount& rc, R& smax, int a, int c, bool two)
 {
@@ -783,9 +786,8 @@ __device__ __forceinline__ void face_two(const StepParams& P, S& sm, int b, cons
     if (two) face_meta<TZ, TR, ZF>(P, sm, n0, m0, interior, a1, c1, act1, hi1);
     R L0[4], U0[4], L1[4], U1[4];
     const auto& q = sm.qb[b];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        R v[5];
+    // the five staged cells of variable k along the normal
+    auto load5 = [&](int k, R v[5]) {
         if constexpr (ZF) {
             // row a, columns c-2 .. c+2 (smem columns c+QX .. c+QX+4, c+QX even)
             const R2 p0 = *reinterpret_cast<const R2*>(&q[k][a + 2][c + QX]);
@@ -801,6 +803,59 @@ __device__ __forceinline__ void face_two(const StepParams& P, S& sm, int b, cons
             v[3] = q[k][a + 3][c + 2 + QX];
             v[4] = q[k][min(a + 4, HR - 1)][c + 2 + QX];
         }
+    };
+    auto store = [&](int fa, int fc, bool act, R f0, R f1, R f2, R f3, R sp) {
+        if (!(sp == sp)) { rc.status |= 0x10u; sp = R(0); }
+        if (ZF) put4(sm.Fz[fa][fc], f0, f1, f2, f3);
+        else put4(sm.Fr[fa][fc], f0, f2, f1, f3);
+        if (act) smax = fmax(smax, sp);
+    };
+    // FF (kernels with the skip_uniform code, when it is set): HLL in FP32,
+    // a face pair in the high-order region.  When the five staged cells of
+    // every variable hold one bit pattern (rho, p > 0, velocities not -0) in
+    // every active lane of the warp (undisturbed gas), every limited slope is
+    // +0 and all four face values are the middle cell's value plus +0, so
+    // both faces take that state's physical flux (as below, where the four
+    // sides are found equal after the reconstruction: the same bits), with no
+    // reconstruction.  The density is voted on first, the other variables
+    // only when it is flat in the whole warp.  Measured at 4096x2048: the
+    // blast at step 1000 0.1414 -> 0.1229 ms per step, but the wind problem
+    // with HLL (its seeded noise disturbs every face) 0.0555 -> 0.0599 ms, so
+    // it goes with the opt-in skip_uniform and not into the default kernel.
+    constexpr bool kFlatFirst = FF && FLUX == 0 && sizeof(R) == 4 && RECON;
+    R rho5[5];
+    const bool ff = kFlatFirst && P.skip_uniform;
+    if (kFlatFirst && ff) {
+        constexpr int NN = ZF ? 2 : 3, TT = ZF ? 3 : 2;
+        load5(0, rho5);
+        bool flat = two && hi0 && hi1 && same_bits(rho5[0], rho5[1]) && same_bits(rho5[1], rho5[2]) &&
+                    same_bits(rho5[2], rho5[3]) && same_bits(rho5[3], rho5[4]) && positive_bits(rho5[2]);
+        if (__all_sync(__activemask(), flat)) {
+            R st[4];
+            st[0] = rho5[2];
+#pragma unroll
+            for (int k = 1; k < 4; k++) {
+                R v[5];
+                load5(k, v);
+                flat = flat && same_bits(v[0], v[1]) && same_bits(v[1], v[2]) && same_bits(v[2], v[3]) &&
+                       same_bits(v[3], v[4]);
+                st[k] = v[2];
+            }
+            flat = flat && positive_bits(st[1]) && __float_as_uint(st[2]) != 0x80000000u &&
+                   __float_as_uint(st[3]) != 0x80000000u;
+            if (__all_sync(__activemask(), flat)) {
+                R f[4];
+                const R sp = flux_physical(g, st[0], st[1], st[NN], st[TT], f);
+                store(a, c, act0, f[0], f[1], f[2], f[3], sp);
+                store(a1, c1, act1, f[0], f[1], f[2], f[3], sp);
+                return;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        R v[5];
+        load5(k, v);
         L0[k] = v[1]; U0[k] = v[2]; L1[k] = v[2]; U1[k] = v[3];
         if (RECON) {
             R x0, x1, y0, y1, z0, z1;
@@ -848,7 +903,7 @@ __device__ __forceinline__ void face_two(const StepParams& P, S& sm, int b, cons
         // gives up to rounding, its wave speed formed as the formula forms it)
         constexpr int NN = ZF ? 2 : 3, TT = ZF ? 3 : 2;
         float2 F[4], Sp;
-        bool one = two && __float_as_int(L0[0]) > 0 && __float_as_int(L0[1]) > 0;
+        bool one = two && positive_bits(L0[0]) && positive_bits(L0[1]);
 #pragma unroll
         for (int k = 0; k < 4; k++)
             one = one && same_bits(L0[k], U0[k]) && same_bits(L0[k], L1[k]) && same_bits(L0[k], U1[k]);
@@ -862,12 +917,6 @@ __device__ __forceinline__ void face_two(const StepParams& P, S& sm, int b, cons
             flux_hll_x2(g, pk(L0[0], L1[0]), pk(L0[1], L1[1]), pk(L0[NN], L1[NN]), pk(L0[TT], L1[TT]),
                         pk(U0[0], U1[0]), pk(U0[1], U1[1]), pk(U0[NN], U1[NN]), pk(U0[TT], U1[TT]), F, Sp);
         }
-        auto store = [&](int fa, int fc, bool act, float f0, float f1, float f2, float f3, float sp) {
-            if (!(sp == sp)) { rc.status |= 0x10u; sp = 0.0f; }
-            if (ZF) put4(sm.Fz[fa][fc], f0, f1, f2, f3);
-            else put4(sm.Fr[fa][fc], f0, f2, f1, f3);
-            if (act) smax = fmax(smax, (R)sp);
-        };
         store(a, c, act0, F[0].x, F[1].x, F[2].x, F[3].x, Sp.x);
         if (two) store(a1, c1, act1, F[0].y, F[1].y, F[2].y, F[3].y, Sp.y);
     } else {
@@ -909,7 +958,7 @@ __device__ __forceinline__ void face_one(const StepParams& P, S& sm, int b, cons
 // per row when TZ = 32, so the warp's staged-cell loads hit distinct
 // banks), then the last z face (c = TZ) of every row, then the r faces; each
 // group padded to whole warps so that no warp mixes groups.
-template <typename R, int FLUX, bool RECON, int TZ, int TR, typename S>
+template <typename R, int FLUX, bool RECON, int TZ, int TR, bool FF = false, typename S>
 __device__ __forceinline__ void face_pass(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
                                           int step, RiemannCount& rc, int& fallback, R& smz, R& smr)
 {
@@ -924,16 +973,16 @@ __device__ __forceinline__ void face_pass(const StepParams& P, S& sm, int b, con
         for (int t = threadIdx.x; t < NP + TZP + TR; t += kThreads) {
             if (t < NZP) {
                 const int a = t / (TZ / 2);
-                face_two<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, interior, rc, smz, a,
+                face_two<R, FLUX, RECON, TZ, TR, true, FF>(P, sm, b, g, n0, m0, interior, rc, smz, a,
                                                        2 * (t - a * (TZ / 2)), true);
             } else if (t < NP) {
                 const int u = t - NZP, a = u / TZ;
-                face_two<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, interior, rc, smr, 2 * a, u - a * TZ,
+                face_two<R, FLUX, RECON, TZ, TR, false, FF>(P, sm, b, g, n0, m0, interior, rc, smr, 2 * a, u - a * TZ,
                                                         true);
             } else if (t < NP + TZ) {
-                face_two<R, FLUX, RECON, TZ, TR, false>(P, sm, b, g, n0, m0, interior, rc, smr, TR, t - NP, false);
+                face_two<R, FLUX, RECON, TZ, TR, false, FF>(P, sm, b, g, n0, m0, interior, rc, smr, TR, t - NP, false);
             } else if (t >= NP + TZP) {
-                face_two<R, FLUX, RECON, TZ, TR, true>(P, sm, b, g, n0, m0, interior, rc, smz, t - NP - TZP, TZ,
+                face_two<R, FLUX, RECON, TZ, TR, true, FF>(P, sm, b, g, n0, m0, interior, rc, smz, t - NP - TZP, TZ,
                                                        false);
             }
         }
@@ -1314,7 +1363,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
         }
     }
     if (!skipped)
-        face_pass<R, FLUX, RECON, TZ, TR>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
+        face_pass<R, FLUX, RECON, TZ, TR, SKIP>(P, sm, b, g, n0, m0, K.step, acc.rc, acc.fallback, acc.smz, acc.smr);
     // persistent kernel: the previous tile's bulk store, issued by the copy
     // thread at the start of this face pass, has read sm.out before anything
     // overwrites it (the network's space in the queue phase, then the update)

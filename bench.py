@@ -13,6 +13,10 @@ Forms measured (each from the same initial state, warm-up steps first):
   fp32_learned_skip  the same with skip_uniform = 1: tiles whose staged cells are
                  all bit-identical skip the face pass (identical results, checked
                  bit for bit against fp32_learned; not the headline)
+  fp64_hll, fp32_hll  the HLL flux in FP64 and in the FP32 form
+  fp32_hll_skip  fp32_hll with skip_uniform = 1 (uniform tiles skip the face
+                 pass; face pairs of undisturbed gas skip the reconstruction),
+                 checked bit for bit against fp32_hll
 The FP32 forms report their density and pressure L1 error against the FP64
 run after the same steps, and Newton statistics (mean/max iterations,
 fallback rate).  The headline `value` is the form named in config.form.
@@ -141,14 +145,14 @@ class ClockSampler:
 # cycles per phase
 PHASES = None
 
-FORMS = ("fp64_godunov", "fp32_pvrs", "fp32_learned", "fp32_learned_skip", "fp64_hll", "fp32_hll")
+FORMS = ("fp64_godunov", "fp32_pvrs", "fp32_learned", "fp32_learned_skip", "fp64_hll", "fp32_hll", "fp32_hll_skip")
 
 
 def make_config(form):
     from asteriy_2d_gb300 import abi as A
     from asteriy_2d_gb300 import problems
     prec = A.PREC_FP64 if form.startswith("fp64") else A.PREC_FP32
-    flux = A.FLUX_HLL if form.endswith("_hll") else A.FLUX_GODUNOV
+    flux = A.FLUX_HLL if "_hll" in form else A.FLUX_GODUNOV
     cfg = problems.blast_config(N_Z, M_R, flux=flux, precision=prec)
     cfg.persistent = PERSISTENT
     if prec == A.PREC_FP32:
@@ -900,7 +904,7 @@ def main():
     # density / pressure L1 error of the FP32 forms against the FP64 run over
     # the timed window (same start, same steps)
     for ref_form, pair in (("fp64_godunov", ("fp32_pvrs", "fp32_learned", "fp32_learned_skip")),
-                           ("fp64_hll", ("fp32_hll",))):
+                           ("fp64_hll", ("fp32_hll", "fp32_hll_skip"))):
         if ref_form not in finals:
             continue
         ref = finals[ref_form]
@@ -918,9 +922,9 @@ def main():
     # few milliseconds is at the mercy of a single host hiccup), the median
     # of three calls
     e2e_steps = max(10, min(args.steps, 50))
-    if "fp32_learned_skip" in finals and "fp32_learned" in finals:
-        forms["fp32_learned_skip"]["bitwise_equal_to_fp32_learned"] = bool(
-            np.array_equal(finals["fp32_learned_skip"], finals["fp32_learned"]))
+    for skip_form, plain in (("fp32_learned_skip", "fp32_learned"), ("fp32_hll_skip", "fp32_hll")):
+        if skip_form in finals and plain in finals:
+            forms[skip_form]["bitwise_equal_to_" + plain] = bool(np.array_equal(finals[skip_form], finals[plain]))
     eparams = params if args.form.startswith("fp32_learned") else None
     def median_e2e(mode):
         runs = [time_e2e(args.form, start, e2e_steps, torch, eparams, mode=mode) for _ in range(3)]
