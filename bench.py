@@ -48,10 +48,10 @@ REF_BUDGET_S = 150.0    # reference arm: seconds of timed host work
 # 4096x2048 from the state at step 1000, from one ncu capture of
 #   bench.py --steps 2 --warmup 1 --no-forms --no-stats --no-cpu --accuracy-steps 0 --batch-steps 0 [--form F]
 # (dram__bytes_read.sum + dram__bytes_write.sum); the default grid only
-MEASURED_TRAFFIC = {"fp32_learned": 134.34e6 + 94.09e6, "fp32_hll": 134.36e6 + 93.17e6}
+MEASURED_TRAFFIC = {"fp32_learned": 134.40e6 + 94.28e6, "fp32_hll": 134.29e6 + 93.31e6}
 MEASURED_TRAFFIC_SOURCE = ("a constant, not measured in this run: ncu dram__bytes_read.sum + dram__bytes_write.sum "
-                           "of one launch (profiles/step_kernel_tma_fp32_learned_godunov_4096x2048.md, the later "
-                           "capture)")
+                           "of one launch (profiles/step_kernel_tma_fp32_learned_godunov_4096x2048.md, the capture "
+                           "of the current kernel)")
 
 
 def peaks():
