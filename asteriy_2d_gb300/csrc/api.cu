@@ -803,8 +803,11 @@ static void drop_graph(ast_solver* S)
 int ast_set_mlp(ast_solver* S, const float* params)
 {
     if (!S || !params) return fail(AST_ERR_INVALID, "null argument");
-    if (!S->mlp) AST_CUDA(cudaMalloc(&S->mlp, sizeof(float) * AST_MLP_NPARAM));
+    // the parameter block and, after it, its packed form for the step kernels
+    if (!S->mlp) AST_CUDA(cudaMalloc(&S->mlp, sizeof(float) * kMlpDevFloats));
     AST_CUDA(cudaMemcpyAsync(S->mlp, params, sizeof(float) * AST_MLP_NPARAM, cudaMemcpyHostToDevice, S->stream));
+    const int rc = launch_mlp_pack(S->mlp, S->stream);
+    if (rc != AST_OK) return rc;
     AST_CUDA(cudaStreamSynchronize(S->stream));
     S->P.mlp = S->mlp;
     drop_graph(S);

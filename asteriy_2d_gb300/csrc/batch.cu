@@ -739,8 +739,12 @@ int ast_batch_set_mlp(ast_batch* B, const float* params)
     if (!B || !params) return set_error(AST_ERR_INVALID, "null argument");
     // the parameter arrays may be in use by queued steps
     BATCH_CUDA(cudaStreamSynchronize(B->stream));
-    if (!B->mlp) BATCH_CUDA(cudaMalloc(&B->mlp, sizeof(float) * AST_MLP_NPARAM));
+    // the parameter block and, after it, its packed form for the step kernels
+    if (!B->mlp) BATCH_CUDA(cudaMalloc(&B->mlp, sizeof(float) * kMlpDevFloats));
     BATCH_CUDA(cudaMemcpy(B->mlp, params, sizeof(float) * AST_MLP_NPARAM, cudaMemcpyHostToDevice));
+    const int rc = launch_mlp_pack(B->mlp, B->stream);
+    if (rc != AST_OK) return rc;
+    BATCH_CUDA(cudaStreamSynchronize(B->stream));
     for (StepParams& p : B->hP) p.mlp = B->mlp;
     drop_graph(B);
     return upload_params(B);

@@ -26,6 +26,9 @@ static_assert(kTZ == kTmaTZ && kTR == kTmaTR, "the persistent kernels' tile is t
 int cuda_fail(cudaError_t e, const char* what);
 // records msg for ast_last_error() and returns code
 int set_error(int code, const char* msg);
+// writes the packed network after the parameter block W (device, kMlpDevFloats
+// floats) on stream st
+int launch_mlp_pack(float* W, cudaStream_t st);
 
 // the four FP32 state planes of one time level (base, rows of ld, planes
 // of `plane` elements) as a 3-D tensor map with a box of bx x by x 4

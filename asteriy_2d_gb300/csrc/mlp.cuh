@@ -150,6 +150,29 @@ __device__ __forceinline__ void pack_weights(const float* W, unsigned* B1, unsig
     }
 }
 
+}  // namespace tc
+
+// The packed network: the vector block (kVLen floats), then W1's and W2's
+// B fragments (tc::kL1 + tc::kL2 words), in the order the step kernels hold
+// them in shared memory, written once per upload after the parameter block
+// of the device copy (at a 16-byte boundary), so that a tile copies it with
+// 16-byte asynchronous copies instead of packing it
+constexpr int kMlpPackOff = (kMlpParams + 3) / 4 * 4;
+constexpr int kMlpPackWords = kVLen + tc::kL1 + tc::kL2;
+constexpr int kMlpDevFloats = kMlpPackOff + kMlpPackWords;   // floats of the device copy
+static_assert(kMlpPackWords % 4 == 0, "whole 16-byte copies");
+
+// the packed network of the parameter block W into W + kMlpPackOff (all
+// threads of one block)
+__device__ __forceinline__ void pack_network(float* W)
+{
+    for (int i = threadIdx.x; i < kVLen; i += blockDim.x) W[kMlpPackOff + i] = mlp_vec(W, i);
+    unsigned* B1 = reinterpret_cast<unsigned*>(W + kMlpPackOff + kVLen);
+    tc::pack_weights(W, B1, B1 + tc::kL1);
+}
+
+namespace tc {
+
 // y for 16 faces whose standardised features sit in X[16][8] (f32, cols 6-7
 // zero); result for face r in y[r] (written by the lanes with t == 0).  V:
 // the compact vector block (kV* offsets)

@@ -380,6 +380,20 @@ __global__ void mlp_forward_tc_kernel(const float* __restrict__ W_g, const float
 
 }  // namespace
 
+namespace {
+// the packed network after the parameter block of a device copy
+__global__ void __launch_bounds__(256) mlp_pack_kernel(float* W) { pack_network(W); }
+}  // namespace
+
+namespace ast {
+int launch_mlp_pack(float* W, cudaStream_t st)
+{
+    mlp_pack_kernel<<<1, 256, 0, st>>>(W);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? AST_OK : cuda_fail(e, "network packing kernel launch");
+}
+}  // namespace ast
+
 extern "C" int ast_mlp_forward_tc(const float* params, const float* x, int64_t n, int stride, float* y)
 {
     if (!params || !x || !y || n < 1 || stride < kI) return AST_ERR_INVALID;

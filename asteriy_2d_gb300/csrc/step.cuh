@@ -18,6 +18,7 @@
 // run in full warps instead of in one or two lanes of many warps.
 #pragma once
 
+#include <cstddef>
 #include <type_traits>
 
 #include "mlp.cuh"
@@ -339,6 +340,9 @@ struct NetSmem {
     float X[kThreads / 32][16][8];
     float Y[kThreads / 32][16];
 };
+static_assert(offsetof(NetSmem, B1) == sizeof(float) * kVLen &&
+                  offsetof(NetSmem, B2) == sizeof(float) * (kVLen + tc::kL1),
+              "v, B1 and B2 are the packed network's layout");
 
 // the output tile of the TMA kernel (the updated cells, four dense planes)
 // and the network's space: the network is used in the queue phase, before
@@ -1051,10 +1055,18 @@ __device__ __forceinline__ void queue_pass(const StepParams& P, S& sm, int b, co
     if (P.riemann_newton && P.guess == 1 && P.mlp != nullptr && ns > 0) {
         // phase 1: learned start values of the faces above the gate (queue
         // slots 0..ns-1), 16 per warp tile on the tensor cores.  Only tiles
-        // with such faces stage the network.  A face's start value waits in
-        // its own flux slot (written with the flux in phase 2).
-        for (int i = threadIdx.x; i < kVLen; i += kThreads) sm.net.v[i] = mlp_vec(P.mlp, i);
-        tc::pack_weights(P.mlp, sm.net.B1, sm.net.B2);
+        // with such faces stage the network: its packed form (written after
+        // the parameters on upload) by 16-byte asynchronous copies, no
+        // registers in between.  A face's start value waits in its own flux
+        // slot (written with the flux in phase 2).
+        {
+            const char* src = reinterpret_cast<const char*>(P.mlp + kMlpPackOff);
+            char* dst = reinterpret_cast<char*>(&sm.net.v[0]);
+            for (int i = threadIdx.x; i < kMlpPackWords / 4; i += kThreads)
+                tma::async_copy16(dst + 16 * i, src + 16 * i);
+            tma::async_commit();
+            tma::async_wait_all();
+        }
         __syncthreads();
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         for (int t0 = 16 * w; t0 < ns; t0 += 16 * (kThreads / 32)) {
