@@ -1215,7 +1215,7 @@ __device__ __forceinline__ void stage_tile(const StepParams& P, S& sm, int b, in
 // no updated cell uses) become copies of the boundary cell.  Also sets the
 // fixed-region flags.
 template <typename R, int TZ, int TR, typename S>
-__device__ __forceinline__ void patch_tile(const StepParams& P, S& sm, int b, int n0, int m0)
+__device__ __forceinline__ void patch_tile_body(const StepParams& P, S& sm, int b, int n0, int m0)
 {
     constexpr int HZ = S::HZ, HR = S::HR, QX = S::QX;
     const int N = P.N, M = P.M;
@@ -1264,6 +1264,22 @@ __device__ __forceinline__ void patch_tile(const StepParams& P, S& sm, int b, in
         }
         q[0][j][i + QX] = v[0]; q[1][j][i + QX] = v[1]; q[2][j][i + QX] = v[2]; q[3][j][i + QX] = v[3];
     }
+}
+
+// The FP64 kernels call it out of line (a smaller persistent kernel: the
+// wind problem, whose fixed region sends every tile through here, 1.512 ->
+// 1.480 ms per step in FP64); the FP32 kernels inline it (out of line the
+// call's register saves cost them 4-8%).
+template <typename R, int TZ, int TR, typename S>
+__device__ __noinline__ void patch_tile_out(const StepParams& P, S& sm, int b, int n0, int m0)
+{
+    patch_tile_body<R, TZ, TR>(P, sm, b, n0, m0);
+}
+template <typename R, int TZ, int TR, typename S>
+__device__ __forceinline__ void patch_tile(const StepParams& P, S& sm, int b, int n0, int m0)
+{
+    if constexpr (sizeof(R) == 8) patch_tile_out<R, TZ, TR>(P, sm, b, n0, m0);
+    else patch_tile_body<R, TZ, TR>(P, sm, b, n0, m0);
 }
 
 // The wave speed and flux of a face whose two sides hold the state
