@@ -1,7 +1,10 @@
 """Host-side pieces of bench.py's reference arm (CPU only): the blast's
 initial state by numpy equals ast_fill_blast, and the start state it
 advances on the part of the grid the blast can reach (z >= 0 mirrored)
-equals the oracle's full-grid run."""
+equals the oracle's full-grid run; and each form the bench times is the
+configuration its name states."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -37,3 +40,17 @@ def test_advanced_start_state_matches_full_grid(flux):
     # the mirrored half and the sub-grid's cell size agree with the full
     # grid to rounding (the full-grid run is symmetric to rounding)
     assert np.all(es < 1e-11) and np.all(eu < 1e-11), (es, eu)
+
+
+@pytest.mark.parametrize("form", bench.FORMS)
+def test_bench_forms_map_to_their_configurations(form):
+    # each form's name states its precision, flux, start value and skip flag
+    cfg = bench.make_config(form)
+    assert (cfg.N, cfg.M) == (bench.N_Z, bench.M_R)
+    assert cfg.precision == (A.PREC_FP64 if form.startswith("fp64") else A.PREC_FP32)
+    assert cfg.flux == (A.FLUX_HLL if "_hll" in form else A.FLUX_GODUNOV)
+    assert cfg.recon == A.RECON_MINMOD
+    if cfg.precision == A.PREC_FP32:
+        assert cfg.skip_uniform == (1 if form.endswith("_skip") else 0)
+        assert cfg.guess == (A.GUESS_MLP if form.startswith("fp32_learned") else A.GUESS_PVRS)
+    assert solver.load().ast_config_check(ctypes.byref(cfg)) == A.AST_OK
