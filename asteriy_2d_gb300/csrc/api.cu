@@ -213,7 +213,8 @@ int ast_create(const ast_config* cfg, ast_solver** out)
     // two 32x16 tiles per SM (smaller grids step with one CTA per tile of
     // 16x16).  The exact solver keeps one CTA per tile: for it the
     // persistent kernel measured 8% slower (11.32 against 10.44 ms per step
-    // at step 1000 of the 4096x2048 blast; HLL 4.79 against 5.20 ms).
+    // at step 1000 of the 4096x2048 blast; HLL 4.79 against 5.20 ms), and
+    // 10% slower again with today's face pass (11.02 against 10.03 ms).
     const long long tiles32 = (long long)((cfg->N + kTZ - 1) / kTZ) * ((cfg->M + kTR - 1) / kTR);
     const bool tma64 = S->elem == 8 && cfg->flux != AST_FLUX_GODUNOV && tiles32 >= 2LL * sm_count();
     if (rc == AST_OK && (S->elem == 4 || tma64) && cfg->persistent && !want_sweep) {
