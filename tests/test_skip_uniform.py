@@ -45,6 +45,21 @@ def test_blast_skip_uniform_identical(precision, flux):
 
 
 @pytest.mark.parametrize("persistent", [0, 1])
+@pytest.mark.parametrize("flux", [A.FLUX_HLL, A.FLUX_GODUNOV])
+def test_negative_zero_velocities_skip_uniform_identical(persistent, flux):
+    # every velocity -0: the FP32 HLL face pairs' one-state path must not
+    # take such stencils (the reconstruction gives +0 on one side and -0 on
+    # the other, which the plain path does not find equal), so the results
+    # stay bit-identical to the full computation
+    cfg = problems.blast_config(384, 192, flux=flux, precision=A.PREC_FP32)
+    cfg.persistent = persistent
+    s0, u0 = solver.fill_blast(cfg)
+    u0 = np.full_like(u0, -0.0)
+    s, u, _, _ = assert_identical(cfg, s0, u0, 30)
+    assert np.all(np.isfinite(s)) and np.all(np.isfinite(u))
+
+
+@pytest.mark.parametrize("persistent", [0, 1])
 @pytest.mark.parametrize("grid", [(150, 70), (97, 33), (33, 17)])
 def test_ragged_grids_and_both_fp32_kernels(persistent, grid):
     cfg = problems.blast_config(*grid, flux=A.FLUX_GODUNOV, precision=A.PREC_FP32)
