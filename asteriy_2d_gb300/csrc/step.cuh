@@ -316,6 +316,7 @@ struct TileCore {
     double ydrow[TR];            // r of the tile's cell rows, y_min + m dy, in FP64
     float yfrow[TR];             // and in FP32
     double tydrow[TR];           // T_do / r of the rows (axisymmetric grid; FP64 kernels)
+    float tyfrow[TR];            // and in FP32 (FP32 kernels with the step's constants set before the tile)
 };
 
 // the exact solver's queue: faces as 16-bit codes (face index | active <<
@@ -595,7 +596,7 @@ __device__ __forceinline__ bool same_bits(double a, double b)
 // 0.175 ms in FP32, 11.45 -> 10.44 ms in FP64; where the gas is disturbed
 // everywhere the test costs about 5%.)  Returns whether the warp took
 // that path (then the two sides of every lane's face are equal).
-template <typename R, bool RECON, bool ZF, typename S>
+template <typename R, bool RECON, bool ZF, bool VOTE = true, typename S>
 __device__ __forceinline__ bool face_states(const StepParams& P, const S& sm, int b, int a, int c, bool hi, R L[4],
                                             R U[4])
 {
@@ -621,7 +622,7 @@ __device__ __forceinline__ bool face_states(const StepParams& P, const S& sm, in
             tuu[k] = q[k][ju + DJ][iu + DI];
             flat = flat && same_bits(tll[k], tl[k]) && same_bits(tl[k], tu[k]) && same_bits(tu[k], tuu[k]);
         }
-        if (__all_sync(__activemask(), flat)) {
+        if (VOTE && __all_sync(__activemask(), flat)) {
 #pragma unroll
             for (int k = 0; k < 4; k++) L[k] = tl[k] + R(0);
             // (the positivity rule below leaves equal sides equal)
@@ -1031,11 +1032,11 @@ __device__ __forceinline__ RPre<R> queued_face(const StepParams& P, const S& sm,
     if (zf) {
         a = fc / (TZ + 1);
         c = fc - a * (TZ + 1);
-        face_states<R, RECON, true>(P, sm, b, a, c, true, L, U);
+        face_states<R, RECON, true, false>(P, sm, b, a, c, true, L, U);
     } else {
         a = (fc - NFZ) / TZ;
         c = (fc - NFZ) - a * TZ;
-        face_states<R, RECON, false>(P, sm, b, a, c, true, L, U);
+        face_states<R, RECON, false, false>(P, sm, b, a, c, true, L, U);
     }
     // normal and tangential velocity: (v_z, v_r) on z faces, (v_r, v_z) on r faces
     const R unL = zf ? L[2] : L[3], utL = zf ? L[3] : L[2];
@@ -1347,7 +1348,7 @@ __device__ __forceinline__ bool tile_uniform(const S& sm, int b, const Gas<R>& g
 // buffer b.  TO_SMEM: the updated cells go to sm.out (for a bulk store)
 // instead of global memory.  Ends without a barrier.
 template <typename R, int FLUX, bool RECON, int LAYOUT, int TZ, int TR, bool TO_SMEM, bool SKIP = true,
-          typename S>
+          bool LATE_K = false, typename S>
 __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, const Gas<R>& g, int n0, int m0,
                                           const StepConsts& K, TileAcc<R>& acc)
 {
@@ -1367,6 +1368,7 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
         // cheaper than an FP64 division at every tile's start, and the FP32
         // persistent batch kernel sets K only during the face pass.
         if constexpr (sizeof(R) == 8) sm.tydrow[threadIdx.x] = (P.geom == 1) ? K.T_do / yd : 0.0;
+        if constexpr (sizeof(R) == 4 && !LATE_K) sm.tyfrow[threadIdx.x] = (P.geom == 1) ? K.T_f / yf : 0.0f;
     }
     // SKIP: the kernel carries the uniform-tile test (skip_uniform); the
     // persistent kernel has a variant without it, so that the default path
@@ -1459,7 +1461,8 @@ __device__ __forceinline__ void tile_body(const StepParams& P, S& sm, int b, con
             if (x > P.body_lof && x < P.body_hif)
                 Q2 = (y >= P.body_rsplitf) ? -P.body_ampf * (float)in[0] : P.body_ampf * (float)in[0];
         }
-        ty = (P.geom == 1) ? Tf / y : 0.0f;
+        if constexpr (LATE_K) ty = (P.geom == 1) ? Tf / y : 0.0f;
+        else ty = sm.tyfrow[row];
     };
     auto store_cell = [&](int row, int col, int n, int m, const R o[4], bool p_only) {
         if constexpr (TO_SMEM) {
@@ -2089,13 +2092,13 @@ __global__ void __launch_bounds__(kThreads, 4)
         }
         if constexpr (MIXED) {
             switch (w.x >> 24) {
-            case 0: tile_body<R, 0, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
-            case 1: tile_body<R, 1, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
-            case 3: tile_body<R, 3, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
-            default: tile_body<R, 2, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
+            case 0: tile_body<R, 0, RECON, kSoA, TZ, TR, true, true, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
+            case 1: tile_body<R, 1, RECON, kSoA, TZ, TR, true, true, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
+            case 3: tile_body<R, 3, RECON, kSoA, TZ, TR, true, true, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
+            default: tile_body<R, 2, RECON, kSoA, TZ, TR, true, true, true>(P, sm, b, P.gf, n0, m0, sK[b], acc); break;
             }
         } else {
-            tile_body<R, FLUX, RECON, kSoA, TZ, TR, true>(P, sm, b, P.gf, n0, m0, sK[b], acc);
+            tile_body<R, FLUX, RECON, kSoA, TZ, TR, true, true, true>(P, sm, b, P.gf, n0, m0, sK[b], acc);
         }
         // this thread's shared-memory writes before the bulk copies that
         // read or overwrite them (ordered by the next barrier)
