@@ -310,7 +310,10 @@ int ast_device_state(ast_solver* solver, void** planes, int64_t* ld, int* elem_b
    A solver created with guess == AST_GUESS_MLP and riemann_newton == 1 (or
    FP32 precision) starts every iterative p* solve from the network's
    prediction p_L exp(y) and falls back to the acoustic start value when the
-   prediction lies outside the pattern's bracket (counted in mlp_fallback). */
+   prediction lies outside the pattern's bracket (counted in mlp_fallback).
+   The call copies the parameters to the device, writes beside them the
+   network's packed form that the step kernels copy into shared memory, and
+   waits for the solver's stream.                                          */
 int ast_set_mlp(ast_solver* solver, const float* params);  /* AST_MLP_NPARAM host floats */
 /* Watch cells: the density of the current state at n cells (indices
    k = m*N + n into the state) and the solver's time TT, the reference's
