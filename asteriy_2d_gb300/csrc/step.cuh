@@ -731,6 +731,12 @@ __device__ __forceinline__ void face_flux(const StepParams& P, S& sm, const Gas<
             F[2] = m * ut;
             F[3] = un * (p * g.inv_g1 + R(0.5) * r * (un * un + ut * ut) + p);
             Sp = fmax(fabs(un) + cs, g.eps8);
+            // stored here: fmax drops a NaN, so this wave speed needs no
+            // test for one
+            if (ZF) put4(sm.Fz[a][c], F[0], F[1], F[2], F[3]);
+            else put4(sm.Fr[a][c], F[0], F[2], F[1], F[3]);
+            if (active) smax = fmax(smax, Sp);
+            return;
         } else if (hi) {
             const RPre<R> q = godunov_pre(g, L[0], L[1], L[NN], L[TT], U[0], U[1], U[NN], U[TT]);
             if (q.pattern == 2 || q.pattern == 3) {
